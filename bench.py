@@ -1,0 +1,512 @@
+#!/usr/bin/env python
+"""Gradient-step throughput of the recursive-control-variate step on GB300.
+
+Workload (default ``cfg2``): 64^3 density + 64^3 RGB albedo Gaussian-blob
+medium, 512x512 film, spp = spp_grad = 16, max_depth = rr_depth = 64, cv_ps
+with the two-state tracer, L2 loss against a 256-spp target of the true grid,
+path-replay adjoint into density and albedo, Adam (lr 0.02) with clamping.
+One step = params.update (state rotation) + two-state render + CV blend +
+loss + adjoint + Adam; paths/step = H*W*(spp + spp_grad).
+
+Prints ONE JSON line (rank 0).  ``--impl reference`` times the CPU
+restatement of the same step on the host cores instead (the reference's own
+llvm_ad_rgb path needs Mitsuba 3 / Dr.Jit, which are not available).
+
+Multi-GPU: the step does not shard without an all-reduce of the gradient
+grid, so N>1 runs N independent replicas (one job per rank, weak scaling, no
+collective in the data path); value = all ranks' paths / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "gradient-step paths/s at matched gradient variance; p50/p99 step latency"
+UNIT = "paths/s"
+L2_BYTES = 129 * 2**20
+FLUSH_BYTES = 512 * 2**20
+
+
+# ------------------------------------------------------------------ helpers
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def init_dist(backend: str):
+    import torch.distributed as dist
+
+    rank, world, _ = dist_info()
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist if world > 1 else None
+
+
+def reduce_max(value: float, dist, device=None) -> float:
+    """Max over ranks (identity without a process group)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(value: float, dist, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Per-rank job seed of a replica (rank 0 = the single-GPU job)."""
+    return 1000 * rank
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+        except Exception:
+            pass
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(kernel: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/
+    (a line `traffic_bytes_per_launch[<kernel>]: <bytes>`), else None."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        m = re.search(rf"traffic_bytes_per_launch\[{re.escape(kernel)}\]:\s*([0-9.eE+]+)", f.read_text())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags) if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------- workload
+class Job:
+    """One optimisation job of the configuration, resident on the device."""
+
+    def __init__(self, cfg, device, seed: int):
+        import torch
+
+        import recursive_control_variates_gb300 as rcv
+        from recursive_control_variates_gb300 import scenes
+
+        self.rcv, self.scenes, self.cfg, self.device, self.seed = rcv, scenes, cfg, device, seed
+        dens, alb = scenes.config_grids(cfg)
+        self.true_density, self.true_albedo = dens, alb
+        scene_ref = rcv.load_dict(scenes.scene_dict(dens, alb, res=cfg.res), device=device)
+        base = rcv.load_dict({"type": "prbvolpath", "max_depth": cfg.max_depth, "rr_depth": cfg.max_depth})
+        self.target = base.render(scene_ref, 0, seed=17843, spp=cfg.spp_ref).contiguous()
+        del scene_ref
+        self.init_density = np.full_like(dens, cfg.init)
+        self.has_albedo = not np.isscalar(alb)
+        self.init_albedo = np.full_like(alb, 0.5) if self.has_albedo else alb
+        self.scene = rcv.load_dict(scenes.scene_dict(self.init_density, self.init_albedo, res=cfg.res), device=device)
+        self.params = rcv.traverse(self.scene)
+        self.integrator = rcv.load_dict({
+            "type": "cv",
+            "integrator": {"type": "twostateprbvolpath", "max_depth": cfg.max_depth, "rr_depth": cfg.max_depth},
+        })
+        self.opt = rcv.ad.Adam(lr=cfg.lr)
+        self.opt[scenes.DENSITY_KEY] = self.init_density
+        self.opt.set_bounds(scenes.DENSITY_KEY, *cfg.clamp)
+        if self.has_albedo:
+            self.opt[scenes.ALBEDO_KEY] = self.init_albedo
+            self.opt.set_bounds(scenes.ALBEDO_KEY, 0.0, 1.0)
+        # twice, so that old = new = initial state (utils.py:62-66)
+        self.params.update(self.opt)
+        self.params.update(self.opt)
+        self.it = 0
+        self.torch = torch
+
+    def step(self, target=None):
+        rcv = self.rcv
+        self.params.update(self.opt)
+        img = rcv.render(self.scene, self.params, integrator=self.integrator, seed=self.seed + self.it,
+                         spp=self.cfg.spp, spp_grad=self.cfg.spp_grad)
+        loss = rcv.l2_loss(img, self.target if target is None else target)
+        loss.backward()
+        self.opt.step()
+        self.it += 1
+        return loss
+
+    def counters(self):
+        return self.integrator.integrator.counters(self.device).clone()
+
+    def paths_per_step(self) -> int:
+        return self.cfg.paths_per_step()
+
+
+def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj) -> dict:
+    """Algorithmic bytes per launch of the two tracer kernels from the device
+    counters (lookups, scatters, gradient events) of one step."""
+    lookups2 = float(c_two[1] + c_two[2])
+    scat2 = float(c_two[3])
+    npix = cfg.res * cfg.res
+    two = 64.0 * lookups2 + (192.0 * scat2 if has_albedo else 0.0) + 24.0 * npix
+    lookups_a = float(c_adj[1] + c_adj[2])
+    scat_a = float(c_adj[3])
+    adj = (32.0 * lookups_a + 32.0 * float(c_adj[4]) + (96.0 * scat_a + 96.0 * float(c_adj[5]) if has_albedo else 0.0)
+           + 12.0 * npix)
+    return {"trace_twostate": two, "trace_adjoint": adj}
+
+
+def run_ours(args, cfg):
+    import torch
+
+    import recursive_control_variates_gb300 as rcv
+    from recursive_control_variates_gb300 import profiling
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = init_dist("nccl")
+    lib = rcv.load_library()
+    job = Job(cfg, device, seed=replica_seed(rank))
+    paths = job.paths_per_step()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    for _ in range(args.warmup):
+        job.step()
+    torch.cuda.synchronize()
+
+    # ------------------------------------------------- device-timed region
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    c0 = job.counters()
+    launches0 = lib.rcv_kernel_launches()
+    timer = profiling.KernelTimer()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks, timer:
+        for i in range(args.steps):
+            flush.fill_(float(i))  # evict the previous step from L2 (> 129 MB)
+            starts[i].record(stream)
+            job.step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    launches = lib.rcv_kernel_launches() - launches0
+    c1 = job.counters()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    local_total_s = sum(step_ms) / 1e3
+    total_s = reduce_max(local_total_s, dist, device)
+    ms_per_step = total_s * 1e3 / args.steps
+    value = paths * world * args.steps / total_s
+    kern = timer.summary()
+
+    # roofline of the dominant kernel
+    delta = (c1 - c0).cpu().numpy().astype(np.float64) / args.steps
+    # the counters mix both tracers; split with a separate 1-step measurement
+    c_two, c_adj = split_counters(job)
+    algo = algorithmic_bytes(cfg, job.has_albedo, c_two, c_adj)
+    dom = max(("trace_twostate", "trace_adjoint"), key=lambda k: kern.get(k, {}).get("total_ms", 0.0))
+    peaks = measured_peaks()
+    dur_s = kern[dom]["mean_ms"] / 1e3
+    achieved = algo[dom] / dur_s / 1e9
+    traffic = ncu_traffic(dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+            "peak_source": peaks["source"], "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+            "traffic": traffic, "algorithmic_bytes_per_launch": algo[dom], "mean_launch_ms": kern[dom]["mean_ms"],
+            "share_of_step": round(kern[dom]["total_ms"] / sum(step_ms), 4)}
+
+    # --------------------------------------------------- end-to-end (API)
+    e2e = None
+    if not args.no_e2e:
+        target_host = job.target.cpu().pin_memory()
+        for _ in range(2):
+            job.step(target_host.to(device, non_blocking=True)).item()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tgt = target_host.to(device, non_blocking=True)
+            loss = job.step(tgt)
+            loss.item()
+        torch.cuda.synchronize()
+        el = reduce_max(time.perf_counter() - t0, dist, device)
+        e2e = {"value": paths * world * args.steps / el, "unit": UNIT,
+               "h2d_bytes_per_step": int(target_host.numel() * 4), "d2h_bytes_per_step": 4,
+               "ms_per_step": el * 1e3 / args.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(cfg, job, target_seconds=args.cpu_seconds)
+
+    ms_sorted = sorted(step_ms)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian-blob medium; no public dataset)",
+        "config": {"workload": f"{cfg.name}: {cfg.grid}^3 density" + (f" + {cfg.grid}^3 RGB albedo" if job.has_albedo
+                   else f", albedo {cfg.albedo}") + f", {cfg.res}x{cfg.res}, spp={cfg.spp}, spp_grad={cfg.spp_grad}, "
+                   f"max_depth={cfg.max_depth}, cv_ps + path-replay adjoint + Adam",
+                   "paths_per_step": paths, "parallelism": f"replicas x{world}",
+                   "l2": "flushed between timed steps (512 MB write)"},
+        "p50_ms": ms_sorted[len(ms_sorted) // 2],
+        "p99_ms": ms_sorted[min(len(ms_sorted) - 1, int(math.ceil(0.99 * len(ms_sorted))) - 1)],
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+        "kernels": {k: {"launches": v["launches"], "mean_ms": round(v["mean_ms"], 4)} for k, v in kern.items()},
+        "counters_per_step": {"paths": float(delta[0]), "lookups": float(delta[1]), "nee_lookups": float(delta[2]),
+                              "scatters": float(delta[3]), "grad_events": float(delta[4])},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def split_counters(job):
+    """Per-kernel counters of one extra (untimed) step."""
+    import torch
+
+    integ = job.integrator.integrator
+    cnt = integ.counters(job.device)
+    job.params.update(job.opt)
+    before = cnt.clone()
+    H, F = integ.render_twostates(job.scene, 0, seed=job.seed + 10**6, spp=job.cfg.spp)
+    mid = cnt.clone()
+    g = torch.ones_like(job.target) / job.target.numel()
+    integ.render_backward(job.scene, job.params, g, 0, seed=job.seed + 2 * 10**6, spp=job.cfg.spp_grad)
+    after = cnt.clone()
+    torch.cuda.synchronize()
+    return (mid - before).cpu().numpy(), (after - mid).cpu().numpy()
+
+
+# ------------------------------------------------------------ CPU baseline
+def oracle_step_factory(cfg, density_old, density_new, albedo_old, albedo_new, target, threads):
+    """One CPU gradient step (two-state render + CV + loss + adjoint) on a
+    band of image rows, with the C++ restatement of the path."""
+    from oracle import oracle as O
+
+    cam = O.camera_basis(cfg.res, cfg.res)
+    has_alb = albedo_new is not None and not np.isscalar(albedo_new)
+    sc = O.Scene(cam, density_old, density_new, albedo_old=albedo_old if has_alb else None,
+                 albedo_new=albedo_new if has_alb else None,
+                 albedo_const=albedo_new if not has_alb else 0.8, max_depth=cfg.max_depth)
+    cv = O.CVOracle()
+
+    def step(seed, rows):
+        """rows = (first, end, stride): every stride-th row is traced."""
+        H, F = O.render_twostates(sc, seed, cfg.spp, threads=threads, rows=rows)
+        sel = slice(*rows)
+        img = cv.step(H[sel], F[sel])
+        g = np.zeros_like(H)
+        g[sel] = 2.0 * (img - target[sel]) / target.size
+        O.backward(sc, seed + 7, cfg.spp_grad, g, threads=threads, rows=rows)
+        return len(range(*rows)) * cfg.res * (cfg.spp + cfg.spp_grad)
+
+    return step, sc
+
+
+def row_sample(res: int, step_fn, seconds: float):
+    """Every-k-th-row sample of the image sized so that one step takes about
+    `seconds` (rows spread over the whole image keep it representative)."""
+    probe = (0, res, max(1, res // 8))
+    t0 = time.perf_counter()
+    step_fn(1, probe)
+    per_row = (time.perf_counter() - t0) / len(range(*probe))
+    nrows = int(min(res, max(4, seconds / max(per_row, 1e-6))))
+    stride = max(1, res // nrows)
+    return (stride // 2, res, stride)
+
+
+def cpu_baseline(cfg, job, target_seconds: float = 15.0):
+    """Oracle timed on a bounded band of rows of the same workload."""
+    from oracle import oracle as O
+
+    threads = O.default_threads()
+    dens_new = job.scene.named_shapes()["object"].interior_medium().new.density.cpu().numpy()[..., 0]
+    dens_old = job.scene.named_shapes()["object"].interior_medium().old.density.cpu().numpy()[..., 0]
+    med = job.scene.named_shapes()["object"].interior_medium()
+    alb_new = med.new.albedo_grid.cpu().numpy() if job.has_albedo else cfg.albedo
+    alb_old = med.old.albedo_grid.cpu().numpy() if job.has_albedo else cfg.albedo
+    target = job.target.cpu().numpy()
+    step, _ = oracle_step_factory(cfg, dens_old, dens_new, alb_old, alb_new, target, threads)
+    rows = row_sample(cfg.res, step, target_seconds)
+    step, _ = oracle_step_factory(cfg, dens_old, dens_new, alb_old, alb_new, target, threads)
+    t0 = time.perf_counter()
+    n = step(2, rows)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"every {rows[2]}th row ({len(range(*rows))} rows) x {cfg.res} px x (spp {cfg.spp} + spp_grad "
+                      f"{cfg.spp_grad}) of {cfg.name} at the job's current state, one CPU gradient step ({n} paths, "
+                      f"{dt:.1f} s), C++ restatement, {threads} threads",
+            "cpu": cpu_model()}
+
+
+def cpu_model() -> str:
+    try:
+        txt = Path("/proc/cpuinfo").read_text()
+        for key in ("model name", "Model", "CPU part"):
+            m = re.search(rf"^{key}\s*:\s*(.+)$", txt, re.M)
+            if m:
+                return m.group(1).strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def run_reference(args, cfg):
+    """CPU arm: the C++ restatement of the step on the host cores (the
+    reference's own llvm_ad_rgb path needs Mitsuba 3 / Dr.Jit, absent here)."""
+    from oracle import oracle as O
+    from recursive_control_variates_gb300 import scenes
+
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    threads = O.default_threads()
+    dens, alb = scenes.config_grids(cfg)
+    has_alb = not np.isscalar(alb)
+    init_d = np.full_like(dens, cfg.init)[..., 0]
+    init_a = np.full_like(alb, 0.5) if has_alb else alb
+    cam = O.camera_basis(cfg.res, cfg.res)
+    ref_sc = O.Scene(cam, dens[..., 0], dens[..., 0], albedo_old=alb if has_alb else None,
+                     albedo_new=alb if has_alb else None, albedo_const=alb if not has_alb else 0.8,
+                     max_depth=cfg.max_depth)
+    # every k-th row, k chosen so that one step takes ~args.cpu_step_seconds;
+    # the states are the initial grid and the grid one Adam step later
+    new_d = init_d + np.float32(cfg.lr)
+    probe_target = O.render(ref_sc, 17843, cfg.spp, threads=threads, rows=(0, cfg.res, max(1, cfg.res // 8)))
+    step, _ = oracle_step_factory(cfg, init_d, new_d, init_a, init_a, probe_target, threads)
+    band = row_sample(cfg.res, step, args.cpu_step_seconds)
+    target = O.render(ref_sc, 17843, cfg.spp_ref, threads=threads, rows=band)
+    step, _ = oracle_step_factory(cfg, init_d, new_d, init_a, init_a, target, threads)
+    times, npaths = [], 0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        n = step(100 + i, band)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            npaths = n
+    total = sum(times)
+    value = npaths * len(times) / total
+    ts = sorted(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total * 1e3 / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded Gaussian-blob medium; no public dataset)", "impl": "reference",
+        "config": {"workload": f"{cfg.name} (CPU sample: every {band[2]}th row of {cfg.res})",
+                   "paths_per_step": npaths},
+        "p50_ms": ts[len(ts) // 2] * 1e3, "p99_ms": ts[-1] * 1e3,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{len(range(*band))} rows x {cfg.res} px x (spp {cfg.spp} + spp_grad "
+                                   f"{cfg.spp_grad}) per step; C++ restatement of the reference's path (its "
+                                   f"llvm_ad_rgb path needs Mitsuba 3 / Dr.Jit, not installable offline)",
+                         "cpu": cpu_model()},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="cfg2")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-step-seconds", type=float, default=4.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    from recursive_control_variates_gb300 import scenes
+
+    cfg = scenes.CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

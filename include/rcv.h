@@ -1,0 +1,204 @@
+/*
+ * librcv — GB300 (sm_103a) implementation of the recursive-control-variate
+ * gradient step of "Recursive Control Variates for Inverse Rendering"
+ * (Nicolet et al. 2023).  C ABI: plain pointers and sizes, no exceptions.
+ *
+ * Memory: every pointer documented as "device" is memory the caller allocated
+ * on the current CUDA device (e.g. a torch tensor); the library never frees
+ * caller memory and, apart from the entry points that say otherwise, never
+ * allocates.  `stream` is a cudaStream_t (NULL = legacy default stream); all
+ * calls are stream-ordered and return before the GPU work completes.
+ *
+ * Return codes: RCV_OK (0) or a negative RCV_ERR_* code; rcv_last_error()
+ * returns a message for the calling thread's last failure.
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the rgl-epfl/recursive_control_variates repository).
+ */
+#ifndef RCV_H
+#define RCV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RCV_OK 0
+#define RCV_ERR_INVALID (-1)     /* bad argument: maps to ValueError      */
+#define RCV_ERR_CUDA (-2)        /* CUDA launch / runtime failure         */
+#define RCV_ERR_UNSUPPORTED (-3) /* configuration not supported           */
+
+/* Counters written by the tracers (optional, may be NULL): 64-bit device
+ * array of RCV_COUNTER_COUNT entries, accumulated with atomics. */
+#define RCV_COUNTER_PATHS 0       /* paths traced                               */
+#define RCV_COUNTER_LOOKUPS 1     /* density lookups on the main path           */
+#define RCV_COUNTER_NEE_LOOKUPS 2 /* density lookups inside ratio tracking      */
+#define RCV_COUNTER_SCATTERS 3    /* real scattering events                     */
+#define RCV_COUNTER_GRAD_EVENTS 4 /* adjoint: density gradient scatters         */
+#define RCV_COUNTER_ALBEDO_EVENTS 5 /* adjoint: albedo gradient scatters        */
+#define RCV_COUNTER_COUNT 8
+
+/* Perspective pinhole sensor.  `right` / `up` are the camera basis vectors
+ * already scaled by tan(fov_x/2) and tan(fov_x/2)*height/width; pixel (x, y)
+ * with film offset (u, v) maps to the direction
+ * forward + (2(x+u)/width - 1) right + (1 - 2(y+v)/height) up. */
+typedef struct rcv_sensor {
+  int32_t width;
+  int32_t height;
+  float origin[3];
+  float forward[3];
+  float right[3];
+  float up[3];
+} rcv_sensor;
+
+/* Two-state heterogeneous medium filling the unit cube [0,1]^3 behind a null
+ * boundary.  Grids are x-fastest float32 arrays of shape [Dz][Dy][Dx] (density)
+ * and [Dz][Dy][Dx][3] (albedo), sampled trilinearly at voxel centres with
+ * clamp-to-edge.  sigma_t = scale * density, sigma_s = albedo * sigma_t. */
+typedef struct rcv_medium {
+  int32_t dims[3]; /* Dx, Dy, Dz */
+  float scale;
+  const float* density_old; /* device, state theta_{i-1}                    */
+  const float* density_new; /* device, state theta_i                        */
+  const float* albedo_old;  /* device or NULL (then albedo_value is used)   */
+  const float* albedo_new;  /* device or NULL                               */
+  float albedo_value[3];
+  void* workspace; /* device, rcv_medium_workspace_bytes(), 256-B aligned  */
+} rcv_medium;
+
+typedef struct rcv_volpath_options {
+  int32_t max_depth;          /* path length limit (real scattering events)  */
+  int32_t rr_depth;           /* Russian roulette applies when depth > this  */
+  int32_t hide_emitters;      /* skip directly visible environment           */
+  int32_t samples_per_thread; /* 0 = automatic; must divide spp              */
+} rcv_volpath_options;
+
+/* ---------------------------------------------------------------- errors */
+const char* rcv_last_error(void);
+/* Number of kernels librcv has launched in this process (all streams). */
+uint64_t rcv_kernel_launches(void);
+/* Compute capability and SM count of the current device (no allocation). */
+int rcv_device_info(int32_t* major, int32_t* minor, int32_t* sm_count);
+
+/* -------------------------------------------------------------- sampling */
+/* TEA hash (4 rounds); out[0] is what the reference uses as the default
+ * gradient seed `mi.sample_tea_32(seed, 1)[0]`
+ * (plugins/twostatepath.py:87-89). */
+void rcv_sample_tea_32(uint32_t v0, uint32_t v1, uint32_t out[2]);
+
+/* --------------------------------------------------------------- medium  */
+/* Bytes of device workspace a medium needs (packed lookup cells, majorants,
+ * gradient accumulators). */
+uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid);
+
+/* Packs the old/new grids into the lookup workspace and computes both
+ * majorants (scale * max density).  Call after every state rotation.
+ * Replaces the grid preparation Mitsuba performs in
+ * TwoStateMedium.parameters_changed (plugins/twostatemedium.py:189-200) and
+ * the majorant queries of sample_interaction_twostates
+ * (plugins/twostatemedium.py:72-78). */
+int rcv_medium_prepare(const rcv_medium* medium, void* stream);
+
+/* ------------------------------------------------------------- tracers  */
+/* Two-state primal: renders the previous (img_old = H) and current
+ * (img_new = F) parameters with shared random numbers.  Images are
+ * [height][width][3] float32 device arrays.
+ * Replaces TwoStatePRBVolpathIntegrator.render_twostates /
+ * sample_twostates / sample_emitter_twostates
+ * (plugins/twostatevolpath.py:91-138, 141-385, 387-479). */
+int rcv_render_twostates_volume(const rcv_medium* medium, const rcv_sensor* sensor,
+                                const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                                float* img_old, float* img_new, uint64_t* counters,
+                                void* stream);
+
+/* Single-state primal on the current (new) parameters; the render that
+ * `integrator.render(...)` of a two-state integrator performs (it delegates
+ * every medium query to `new`, plugins/twostatemedium.py:125-151) and that
+ * MetaIntegrator uses for force_baseline (plugins/metaintegrator.py:124-128). */
+int rcv_render_volume(const rcv_medium* medium, const rcv_sensor* sensor,
+                      const rcv_volpath_options* opts, uint32_t seed, int32_t spp, float* img,
+                      uint64_t* counters, void* stream);
+
+/* Seed-replay adjoint on the current parameters: traces `spp` paths per
+ * pixel from `seed`, first to obtain each path's radiance and then again to
+ * back-propagate grad_img (dLoss/dimage, [height][width][3]) into the density
+ * grid (and the albedo grid when the medium has one).  Gradients are ADDED to
+ * grad_density ([Dz][Dy][Dx]) and grad_albedo ([Dz][Dy][Dx][3] or NULL).
+ * Replaces CVIntegrator.render_backward / MetaIntegrator.render_backward
+ * (plugins/cv_integrator.py:87-94, plugins/metaintegrator.py:140-147), i.e.
+ * the path-replay adjoint of the wrapped two-state integrator. */
+int rcv_render_backward_volume(const rcv_medium* medium, const rcv_sensor* sensor,
+                               const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                               const float* grad_img, float* grad_density, float* grad_albedo,
+                               uint64_t* counters, void* stream);
+
+/* ------------------------------------------------- control variate state */
+/* Per-element state of the recursive control variate; every array holds
+ * `n` float32 device values (n = height*width*3), zero-initialised. */
+typedef struct rcv_cv_state {
+  float* img;    /* G_{i-1} -> G_i                                        */
+  float* w_s;    /* control weight alpha                                  */
+  float* v_n;    /* variance of the previous estimate                     */
+  float* mean_x; /* EMA-Welford statistics of H (x) and F (y)             */
+  float* mean_y;
+  float* var_x;
+  float* var_y;
+  float* cov;
+} rcv_cv_state;
+
+/* One control-variate step: optional statistics update (pre_update), weight
+ * update when it > warmup, the blend img = w_s (img - H) + F, then the
+ * statistics update when it > 0.  *welford_count (host memory) is the
+ * estimator's sample count n and is incremented by every update.
+ * Replaces CVIntegrator.render (plugins/cv_integrator.py:58-77), the cv_ps
+ * branch of MetaIntegrator.render (plugins/metaintegrator.py:93-113) and
+ * StatisticsEstimator.update / get (plugins/welford.py:59-78). */
+int rcv_cv_step(const rcv_cv_state* state, int64_t n, const float* H, const float* F,
+                int32_t it, int32_t warmup, int32_t* welford_count, float beta1, float beta2,
+                int32_t pre_update, void* stream);
+
+/* StatisticsEstimator.get (plugins/welford.py:77-78): bias-corrected
+ * (var_x, var_y, cov) written to out_vx / out_vy / out_cov. */
+int rcv_statistics_get(const rcv_cv_state* state, int64_t n, int32_t welford_count, float beta2,
+                       float* out_vx, float* out_vy, float* out_cov, void* stream);
+
+/* StatisticsEstimator.update (plugins/welford.py:59-75) on its own: updates
+ * mean_x/mean_y/var_x/var_y/cov of `state` from x (= H) and y (= F) and
+ * increments *welford_count; img / w_s / v_n are untouched. */
+int rcv_statistics_update(const rcv_cv_state* state, int64_t n, const float* x, const float* y,
+                          int32_t* welford_count, float beta1, float beta2, void* stream);
+
+/* WelfordVarianceEstimator.update / get (plugins/welford.py:25-36). */
+int rcv_welford_update(float* mean, float* var, int64_t n, const float* x, int32_t* count,
+                       float beta1, float beta2, void* stream);
+int rcv_welford_get(const float* var, int64_t n, int32_t count, float beta2, float* out,
+                    void* stream);
+
+/* --------------------------------------------------------- step harness */
+#define RCV_LOSS_L2 0
+#define RCV_LOSS_L1 1
+/* Workspace bytes rcv_loss needs for a deterministic two-stage reduction. */
+uint64_t rcv_loss_workspace_bytes(int64_t n);
+/* loss = mean((img-ref)^2) or mean(|img-ref|) into *loss (device float);
+ * grad (device, n, or NULL) = dloss/dimg.  Replaces utils.l2_loss / l1_loss
+ * (utils.py:21-25) and their derivative d_l (utils.py:90-96). */
+int rcv_loss(int32_t kind, const float* img, const float* ref, int64_t n, float* loss, float* grad,
+             void* workspace, void* stream);
+
+/* Adam step with the bias correction folded into the step size, followed by
+ * clamping to [lo, hi] and (optionally) zeroing grad.  `t` is the 1-based
+ * step count.  Replaces mi.ad.Adam.step (optimize.py:90,127) and
+ * utils.clamp (utils.py:172-175). */
+int rcv_adam_step(float* param, float* grad, float* m, float* v, int64_t n, int32_t t, float lr,
+                  float beta1, float beta2, float eps, float lo, float hi, int32_t zero_grad,
+                  void* stream);
+
+/* x = min(max(x, lo), hi) elementwise (utils.clamp, utils.py:172-175). */
+int rcv_clamp(float* x, int64_t n, float lo, float hi, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RCV_H */

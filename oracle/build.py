@@ -1,0 +1,43 @@
+"""Build recipe for the CPU oracle (test infrastructure, not product code).
+
+Compiles ``oracle/rcv_oracle.cpp`` into ``oracle/_build/liboracle.so`` with
+``-ffp-contract=off`` so that float operations are rounded one at a time, the
+same way the GPU library (built with ``-fmad=false``) rounds them.
+
+The reference itself (rgl-epfl/recursive_control_variates) is pure Python on
+top of Mitsuba 3 / Dr.Jit, which are not vendored and not installed, so there
+is no reference source to compile here: this recipe builds only the
+restatement.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import subprocess
+from pathlib import Path
+
+ORACLE_DIR = Path(__file__).resolve().parent
+BUILD_DIR = ORACLE_DIR / "_build"
+SRC = ORACLE_DIR / "rcv_oracle.cpp"
+LIB = BUILD_DIR / "liboracle.so"
+FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread"]
+
+
+def build(force: bool = False) -> Path:
+    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    h = hashlib.sha256(SRC.read_bytes() + " ".join(FLAGS).encode() + os.uname().machine.encode())
+    stamp = BUILD_DIR / "stamp.txt"
+    if not force and LIB.exists() and stamp.exists() and stamp.read_text() == h.hexdigest():
+        return LIB
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [os.environ.get("CXX", "g++"), *FLAGS, str(SRC), "-o", str(tmp)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    stamp.write_text(h.hexdigest())
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True))

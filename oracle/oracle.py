@@ -1,0 +1,327 @@
+"""CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this module; the product never does.
+
+Two parts:
+  * ctypes access to ``rcv_oracle.cpp`` (the sequential C++ restatement of the
+    two-state tracer, the single-state tracer and the path-replay adjoint);
+  * a float32-faithful numpy restatement of the control-variate blend and the
+    EMA-Welford statistics, following
+        plugins/cv_integrator.py:58-77      CVIntegrator.render
+        plugins/metaintegrator.py:93-113    MetaIntegrator.render (cv_ps)
+        plugins/welford.py:4-78             Welford estimators
+    and of the Adam step (Kingma & Ba 2015) used by optimize.py:90,127.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class OracleScene(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("cam_o", C.c_float * 3),
+        ("cam_f", C.c_float * 3),
+        ("cam_r", C.c_float * 3),
+        ("cam_u", C.c_float * 3),
+        ("max_depth", C.c_int32),
+        ("rr_depth", C.c_int32),
+        ("hide_emitters", C.c_int32),
+        ("dx", C.c_int32),
+        ("dy", C.c_int32),
+        ("dz", C.c_int32),
+        ("scale", C.c_float),
+        ("dens_old", C.c_void_p),
+        ("dens_new", C.c_void_p),
+        ("alb_old", C.c_void_p),
+        ("alb_new", C.c_void_p),
+        ("albedo_const", C.c_float * 3),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        vp = C.c_void_p
+        L.oracle_render.argtypes = [C.POINTER(OracleScene), C.c_int, C.c_uint32, C.c_int, C.c_int, vp, vp, vp, C.c_int,
+                                    C.c_int, C.c_int, C.c_int]
+        L.oracle_render.restype = C.c_int
+        L.oracle_backward.argtypes = [C.POINTER(OracleScene), C.c_uint32, C.c_int, vp, vp, vp, C.c_int, C.c_int,
+                                      C.c_int, C.c_int]
+        L.oracle_backward.restype = C.c_int
+        L.oracle_sample_tea_32.argtypes = [C.c_uint32, C.c_uint32]
+        L.oracle_sample_tea_32.restype = C.c_uint32
+        L.oracle_pcg32.argtypes = [C.c_uint64, C.c_uint64, C.c_int, vp]
+        L.oracle_pcg32.restype = None
+        L.oracle_rng_stream.argtypes = [C.c_uint32, C.c_uint32, C.c_int, vp]
+        L.oracle_rng_stream.restype = None
+        L.oracle_log_unit.argtypes = [vp, C.c_int, vp]
+        L.oracle_log_unit.restype = None
+        L.oracle_uniform_sphere.argtypes = [vp, C.c_int, vp]
+        L.oracle_uniform_sphere.restype = None
+        _lib = L
+    return _lib
+
+
+def default_threads() -> int:
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:  # pragma: no cover
+        return max(1, os.cpu_count() or 1)
+
+
+@dataclass
+class Camera:
+    width: int
+    height: int
+    origin: tuple
+    forward: tuple
+    right: tuple
+    up: tuple
+
+
+def camera_basis(width, height, origin=(0.5, 0.5, 3.5), target=(0.5, 0.5, 0.5), up=(0.0, 1.0, 0.0), fov=45.0):
+    """Pinhole basis (float32) for a look-at camera with horizontal fov."""
+    o = np.array(origin, np.float64)
+    f = np.array(target, np.float64) - o
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.array(up, np.float64))
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    tx = np.tan(np.radians(fov) * 0.5)
+    ty = tx * height / width
+    as32 = lambda v: tuple(float(np.float32(x)) for x in v)  # noqa: E731
+    return Camera(width, height, as32(o), as32(f), as32(r * tx), as32(u * ty))
+
+
+class Scene:
+    """Keeps the numpy grids alive while the C structure points at them."""
+
+    def __init__(self, cam: Camera, dens_old, dens_new, albedo_old=None, albedo_new=None, albedo_const=0.8,
+                 max_depth=16, rr_depth=None, hide_emitters=False, scale=1.0):
+        self.dens_old = np.ascontiguousarray(dens_old, np.float32)
+        self.dens_new = np.ascontiguousarray(dens_new, np.float32)
+        dz, dy, dx = self.dens_new.shape[:3]
+        self.alb_old = None if albedo_old is None else np.ascontiguousarray(albedo_old, np.float32)
+        self.alb_new = None if albedo_new is None else np.ascontiguousarray(albedo_new, np.float32)
+        s = OracleScene()
+        s.width, s.height = cam.width, cam.height
+        s.cam_o[:], s.cam_f[:], s.cam_r[:], s.cam_u[:] = cam.origin, cam.forward, cam.right, cam.up
+        s.max_depth = max_depth if max_depth >= 0 else 0x7FFFFFFF
+        s.rr_depth = max_depth if rr_depth is None else rr_depth
+        s.hide_emitters = int(hide_emitters)
+        s.dx, s.dy, s.dz = dx, dy, dz
+        s.scale = scale
+        s.dens_old = self.dens_old.ctypes.data
+        s.dens_new = self.dens_new.ctypes.data
+        s.alb_old = None if self.alb_old is None else self.alb_old.ctypes.data
+        s.alb_new = None if self.alb_new is None else self.alb_new.ctypes.data
+        ac = np.broadcast_to(np.asarray(albedo_const, np.float32), (3,))
+        s.albedo_const[:] = [float(v) for v in ac]
+        self.c = s
+        self.width, self.height = cam.width, cam.height
+
+
+def _rows(rows):
+    """(first, end[, stride]) row selection; end 0 = all rows."""
+    r = tuple(int(v) for v in rows)
+    return (r[0], r[1], r[2] if len(r) > 2 else 1)
+
+
+def render_twostates(scene: Scene, seed: int, spp: int, chunk: int | None = None, threads: int | None = None,
+                     counters=None, rows: tuple = (0, 0, 1)):
+    """(H, F) float32 images.  `chunk` = samples per GPU thread (summation
+    order); `rows` = (first, end) row band to render (0, 0 = all)."""
+    chunk = spp if chunk is None else chunk
+    H = np.zeros((scene.height, scene.width, 3), np.float32)
+    F = np.zeros_like(H)
+    cnt = np.zeros(4, np.uint64) if counters is None else counters
+    rc = lib().oracle_render(C.byref(scene.c), 0, seed & 0xFFFFFFFF, spp, chunk, H.ctypes.data, F.ctypes.data,
+                             cnt.ctypes.data, threads or default_threads(), *_rows(rows))
+    if rc:
+        raise ValueError("oracle_render: invalid arguments")
+    return H, F
+
+
+def render(scene: Scene, seed: int, spp: int, chunk: int | None = None, threads: int | None = None, counters=None,
+           rows: tuple = (0, 0, 1)):
+    """Single-state image of the `new` parameters."""
+    chunk = spp if chunk is None else chunk
+    img = np.zeros((scene.height, scene.width, 3), np.float32)
+    cnt = np.zeros(4, np.uint64) if counters is None else counters
+    rc = lib().oracle_render(C.byref(scene.c), 1, seed & 0xFFFFFFFF, spp, chunk, None, img.ctypes.data,
+                             cnt.ctypes.data, threads or default_threads(), *_rows(rows))
+    if rc:
+        raise ValueError("oracle_render: invalid arguments")
+    return img
+
+
+def backward(scene: Scene, seed: int, spp: int, grad_img, threads: int | None = None, rows: tuple = (0, 0, 1)):
+    """(grad_density [dz,dy,dx] float64, grad_albedo [dz,dy,dx,3] or None)."""
+    g = np.ascontiguousarray(grad_img, np.float32)
+    gd = np.zeros(scene.dens_new.shape[:3], np.float64)
+    ga = None if scene.alb_new is None else np.zeros(scene.dens_new.shape[:3] + (3,), np.float64)
+    rc = lib().oracle_backward(C.byref(scene.c), seed & 0xFFFFFFFF, spp, g.ctypes.data, gd.ctypes.data,
+                               None if ga is None else ga.ctypes.data, threads or default_threads(), *_rows(rows))
+    if rc:
+        raise ValueError("oracle_backward: invalid arguments")
+    return gd, ga
+
+
+def sample_tea_32(v0: int, v1: int) -> int:
+    return int(lib().oracle_sample_tea_32(v0 & 0xFFFFFFFF, v1 & 0xFFFFFFFF))
+
+
+def pcg32(initstate: int, initseq: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().oracle_pcg32(initstate, initseq, n, out.ctypes.data)
+    return out
+
+
+def rng_stream(seed: int, lane: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    lib().oracle_rng_stream(seed & 0xFFFFFFFF, lane & 0xFFFFFFFF, n, out.ctypes.data)
+    return out
+
+
+def log_unit(x) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    lib().oracle_log_unit(x.ctypes.data, x.size, out.ctypes.data)
+    return out
+
+
+def uniform_sphere(u) -> np.ndarray:
+    u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+    out = np.zeros((u.shape[0], 3), np.float32)
+    lib().oracle_uniform_sphere(u.ctypes.data, u.shape[0], out.ctypes.data)
+    return out
+
+
+# --------------------------------------------------------------------------
+# float32-faithful restatement of the control variate and Welford statistics
+f32 = np.float32
+
+
+def pow_f32(b: float, n: int) -> np.float32:
+    """beta^n of a float32 beta, rounded to float32."""
+    return f32(float(f32(b)) ** n)
+
+
+class StatisticsOracle:
+    """plugins/welford.py:38-78 in numpy float32."""
+
+    def __init__(self, beta1=0.9, beta2=0.999):
+        self.n = 0
+        self.b1 = f32(beta1)
+        self.b2 = f32(beta2)
+        self.mean_x = self.mean_y = self.var_x = self.var_y = self.cov = f32(0.0)
+
+    def update(self, x, y):
+        x = np.asarray(x, f32)
+        y = np.asarray(y, f32)
+        one = f32(1.0)
+        if self.n > 0:
+            d = one - pow_f32(self.b1, self.n)
+            dx1 = x - (self.mean_x / d).astype(f32)
+            dy1 = y - (self.mean_y / d).astype(f32)
+        else:
+            dx1, dy1 = x, y
+        omb1 = one - self.b1
+        omb2 = one - self.b2
+        self.mean_y = (self.b1 * self.mean_y + omb1 * y).astype(f32)
+        self.mean_x = (self.b1 * self.mean_x + omb1 * x).astype(f32)
+        self.n += 1
+        d = one - pow_f32(self.b1, self.n)
+        dx2 = (x - self.mean_x / d).astype(f32)
+        dy2 = (y - self.mean_y / d).astype(f32)
+        self.var_x = (self.b2 * self.var_x + (omb2 * dx1) * dx2).astype(f32)
+        self.var_y = (self.b2 * self.var_y + (omb2 * dy1) * dy2).astype(f32)
+        self.cov = (self.b2 * self.cov + (omb2 * dx1) * dy2).astype(f32)
+
+    def get(self):
+        d = f32(1.0) - pow_f32(self.b2, self.n)
+        return (np.asarray(self.var_x / d, f32), np.asarray(self.var_y / d, f32), np.asarray(self.cov / d, f32))
+
+
+class WelfordOracle:
+    """plugins/welford.py:4-36 in numpy float32."""
+
+    def __init__(self, beta1=0.9, beta2=0.999):
+        self.n = 0
+        self.b1 = f32(beta1)
+        self.b2 = f32(beta2)
+        self.mean = f32(0.0)
+        self.var = f32(0.0)
+
+    def update(self, x):
+        x = np.asarray(x, f32)
+        one = f32(1.0)
+        if self.n > 0:
+            dx1 = (x - self.mean / (one - pow_f32(self.b1, self.n))).astype(f32)
+        else:
+            dx1 = x
+        self.mean = (self.b1 * self.mean + (one - self.b1) * x).astype(f32)
+        self.n += 1
+        dx2 = (x - self.mean / (one - pow_f32(self.b1, self.n))).astype(f32)
+        self.var = (self.b2 * self.var + ((one - self.b2) * dx1) * dx2).astype(f32)
+
+    def get(self):
+        return np.asarray(self.var / (f32(1.0) - pow_f32(self.b2, self.n)), f32)
+
+
+class CVOracle:
+    """CVIntegrator.render minus the tracer (plugins/cv_integrator.py:58-77),
+    with MetaIntegrator's pre_update option (plugins/metaintegrator.py:95-111)."""
+
+    def __init__(self, warmup=1, beta1=0.9, beta2=0.999, pre_update=False):
+        self.warmup = warmup
+        self.pre_update = pre_update
+        self.stats = StatisticsOracle(beta1, beta2)
+        self.img = f32(0.0)
+        self.v_n = f32(0.0)
+        self.w_s = f32(0.0)
+        self.it = 0
+
+    def step(self, H, F):
+        H = np.asarray(H, f32)
+        F = np.asarray(F, f32)
+        if self.it > 0 and self.pre_update:
+            self.stats.update(H, F)
+        if self.it > self.warmup:
+            v0, v1, cov = self.stats.get()
+            w = np.asarray(self.w_s, f32)
+            self.v_n = ((w * w) * (self.v_n + v0) + v1 - (f32(2.0) * w) * cov).astype(f32)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                ws = (cov / (v0 + self.v_n)).astype(f32)
+            ws = np.where(np.isnan(ws) | np.isinf(ws), f32(0.0), ws).astype(f32)
+            self.w_s = np.clip(ws, f32(0.0), f32(1.0)).astype(f32)
+        self.img = (self.w_s * (self.img - H) + F).astype(f32)
+        if self.it > 0 and not self.pre_update:
+            self.stats.update(H, F)
+        self.it += 1
+        return self.img
+
+
+def adam_step(p, g, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8, lo=-np.inf, hi=np.inf):
+    """One Adam step in float32 arithmetic (bias correction in the step size)."""
+    p, g, m, v = (np.asarray(a, f32) for a in (p, g, m, v))
+    lr_t = f32(lr * np.sqrt(1.0 - float(f32(b2)) ** t) / (1.0 - float(f32(b1)) ** t))
+    b1f, b2f = f32(b1), f32(b2)
+    m = (b1f * m + (f32(1.0) - b1f) * g).astype(f32)
+    v = (b2f * v + (f32(1.0) - b2f) * (g * g)).astype(f32)
+    p = (p - (lr_t * m) / (np.sqrt(v) + f32(eps))).astype(f32)
+    p = np.clip(p, f32(lo), f32(hi)).astype(f32)
+    return p, m, v

@@ -1,0 +1,654 @@
+// CPU oracle for the recursive-control-variate gradient step — TEST
+// INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file; the
+// tests, the smoke check and the CPU-baseline leg of bench.py load it as the
+// checker.
+//
+// It restates, as plain sequential C++ (one path at a time, nested loops),
+// the per-path algorithm of the reference for the synthetic scene family
+// (unit-cube heterogeneous medium behind a null boundary, constant white
+// environment, isotropic phase function, box film):
+//   plugins/twostatevolpath.py:141-385  TwoStatePRBVolpathIntegrator.sample_twostates
+//   plugins/twostatevolpath.py:387-479  sample_emitter_twostates
+//   plugins/twostatemedium.py:15-107    TwoStateMedium.sample_interaction_twostates
+//   plugins/twostatevolpath.py:80-138   render_twostates + develop (box filter)
+// plus the single-state estimator a two-state integrator renders on `new`
+// (plugins/twostatemedium.py:125-151) and its path-replay adjoint (the
+// default adjoint of the cv integrator, plugins/cv_integrator.py:87-94).
+// Mitsuba primitives the reference calls (sampler, gridvolume, warps) are
+// restated from their documented behaviour.
+//
+// Floating point: every float32 operation is written out in the same order
+// as the GPU kernels, compiled with -ffp-contract=off, so that paths agree
+// bit for bit; gradients accumulate in double.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr float kInvFourPi = 0.0795774715459476678844f;
+constexpr float kHalfPi = 1.57079632679489661923f;
+constexpr float kInf = __builtin_huge_valf();
+
+// ------------------------------------------------------------ sampler
+// TEA with the GPU-random-number key schedule (Zafar, Olano, Curtis 2010).
+void tea(uint32_t v0, uint32_t v1, int rounds, uint32_t& o0, uint32_t& o1) {
+  uint32_t sum = 0;
+  for (int i = 0; i < rounds; ++i) {
+    sum += 0x9e3779b9u;
+    v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + sum) ^ ((v1 >> 5) + 0xc8013ea4u);
+    v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + sum) ^ ((v0 >> 5) + 0x7e95761eu);
+  }
+  o0 = v0;
+  o1 = v1;
+}
+
+// PCG32 (O'Neill 2014).
+struct Rng {
+  uint64_t state = 0, inc = 1;
+  uint32_t next() {
+    uint64_t old = state;
+    state = old * 6364136223846793005ull + inc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+  }
+  void seed(uint64_t initstate, uint64_t initseq) {
+    state = 0;
+    inc = (initseq << 1u) | 1u;
+    next();
+    state += initstate;
+    next();
+  }
+  float next1d() {
+    uint32_t bits = (next() >> 9) | 0x3f800000u;
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f - 1.0f;
+  }
+};
+
+Rng lane_rng(uint32_t seed, uint32_t lane) {
+  uint32_t a, b, c, d;
+  tea(seed, lane, 4, a, b);
+  tea(lane, seed, 4, c, d);
+  Rng r;
+  r.seed(((uint64_t)a << 32) | b, ((uint64_t)c << 32) | d);
+  return r;
+}
+
+// ------------------------------------------------------------ float math
+struct V3 {
+  float x, y, z;
+};
+
+// ln(x), x in (0,1]: atanh series of the reduced mantissa (see the GPU notes).
+float log_unit(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  int e = (int)((u >> 23) & 0xffu) - 127;
+  u = (u & 0x007fffffu) | 0x3f800000u;
+  float m;
+  std::memcpy(&m, &u, 4);
+  if (m > 1.41421356237f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float s2 = s * s;
+  float p = std::fmaf(s2, 1.0f / 11.0f, 1.0f / 9.0f);
+  p = std::fmaf(s2, p, 1.0f / 7.0f);
+  p = std::fmaf(s2, p, 1.0f / 5.0f);
+  p = std::fmaf(s2, p, 1.0f / 3.0f);
+  p = std::fmaf(s2, p, 1.0f);
+  const float lm = (2.0f * s) * p;
+  const float fe = (float)e;
+  return std::fmaf(fe, 0.693145751953125f, std::fmaf(fe, 1.4286068203094172e-06f, lm));
+}
+
+void sincos_2pi(float u, float& s, float& c) {
+  const float u4 = u * 4.0f;
+  const float qf = std::floor(u4);
+  const int q = (int)qf & 3;
+  float f = u4 - qf;
+  const bool swap = f > 0.5f;
+  if (swap) f = 1.0f - f;
+  const float x = f * kHalfPi;
+  const float x2 = x * x;
+  float ps = std::fmaf(x2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+  ps = std::fmaf(x2, ps, 1.0f / 120.0f);
+  ps = std::fmaf(x2, ps, -1.0f / 6.0f);
+  const float sn = std::fmaf(x * x2, ps, x);
+  float pc = std::fmaf(x2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+  pc = std::fmaf(x2, pc, -1.0f / 720.0f);
+  pc = std::fmaf(x2, pc, 1.0f / 24.0f);
+  pc = std::fmaf(x2, pc, -0.5f);
+  const float cs = std::fmaf(x2, pc, 1.0f);
+  const float s0 = swap ? cs : sn, c0 = swap ? sn : cs;
+  switch (q) {
+    case 0: s = s0; c = c0; break;
+    case 1: s = c0; c = -s0; break;
+    case 2: s = -s0; c = -c0; break;
+    default: s = -c0; c = s0; break;
+  }
+}
+
+V3 square_to_uniform_sphere(float u0, float u1) {
+  const float z = std::fmaf(-2.0f, u1, 1.0f);
+  const float r = std::sqrt(std::fmax(0.0f, std::fmaf(-z, z, 1.0f)));
+  float s, c;
+  sincos_2pi(u0, s, c);
+  return V3{r * c, r * s, z};
+}
+
+// unit cube [0,1]^3: returns (t_near, t_far)
+void cube_hit(const V3& o, const V3& d, float& tn, float& tf) {
+  const V3 inv{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+  const float ax = (0.0f - o.x) * inv.x, bx = (1.0f - o.x) * inv.x;
+  const float ay = (0.0f - o.y) * inv.y, by = (1.0f - o.y) * inv.y;
+  const float az = (0.0f - o.z) * inv.z, bz = (1.0f - o.z) * inv.z;
+  tn = std::fmax(std::fmax(std::fmin(ax, bx), std::fmin(ay, by)), std::fmin(az, bz));
+  tf = std::fmin(std::fmin(std::fmax(ax, bx), std::fmax(ay, by)), std::fmax(az, bz));
+}
+
+V3 ray_at(const V3& o, float t, const V3& d) { return V3{o.x + t * d.x, o.y + t * d.y, o.z + t * d.z}; }
+
+float lerp(float a, float b, float t) { return std::fmaf(t, b - a, a); }
+
+}  // namespace
+
+extern "C" {
+
+// Scene description shared by every oracle entry point.
+struct oracle_scene {
+  int32_t width, height;
+  float cam_o[3], cam_f[3], cam_r[3], cam_u[3];
+  int32_t max_depth, rr_depth, hide_emitters;
+  int32_t dx, dy, dz;
+  float scale;
+  const float* dens_old;
+  const float* dens_new;
+  const float* alb_old;  // [dz][dy][dx][3] or null
+  const float* alb_new;
+  float albedo_const[3];
+};
+}
+
+namespace {
+
+// Voxel grid corner interpolation of Mitsuba's gridvolume (voxel centres at
+// (i+1/2)/D, clamp to edge).
+struct Corners {
+  int x0, x1, y0, y1, z0, z1;
+  float fx, fy, fz;
+};
+
+void axis(float p, int D, int& i0, int& i1, float& f) {
+  const float g = p * (float)D - 0.5f;
+  const float fl = std::floor(g);
+  f = g - fl;
+  const float flc = std::fmin(std::fmax(fl, -1.0f), (float)D);
+  const int ix = (int)flc;
+  i0 = std::min(std::max(ix, 0), D - 1);
+  i1 = std::min(std::max(ix + 1, 0), D - 1);
+}
+
+Corners corners(const oracle_scene& S, const V3& x) {
+  Corners c;
+  axis(x.x, S.dx, c.x0, c.x1, c.fx);
+  axis(x.y, S.dy, c.y0, c.y1, c.fy);
+  axis(x.z, S.dz, c.z0, c.z1, c.fz);
+  return c;
+}
+
+inline int64_t vidx(const oracle_scene& S, int x, int y, int z) {
+  return ((int64_t)z * S.dy + y) * S.dx + x;
+}
+
+float trilinear(const oracle_scene& S, const float* g, int stride, int ch, const Corners& c) {
+  auto v = [&](int x, int y, int z) { return g[vidx(S, x, y, z) * stride + ch]; };
+  const float c00 = lerp(v(c.x0, c.y0, c.z0), v(c.x1, c.y0, c.z0), c.fx);
+  const float c10 = lerp(v(c.x0, c.y1, c.z0), v(c.x1, c.y1, c.z0), c.fx);
+  const float c01 = lerp(v(c.x0, c.y0, c.z1), v(c.x1, c.y0, c.z1), c.fx);
+  const float c11 = lerp(v(c.x0, c.y1, c.z1), v(c.x1, c.y1, c.z1), c.fx);
+  const float c0 = lerp(c00, c10, c.fy);
+  const float c1 = lerp(c01, c11, c.fy);
+  return lerp(c0, c1, c.fz);
+}
+
+V3 albedo(const oracle_scene& S, const float* grid, const Corners& c) {
+  if (grid == nullptr) return V3{S.albedo_const[0], S.albedo_const[1], S.albedo_const[2]};
+  return V3{trilinear(S, grid, 3, 0, c), trilinear(S, grid, 3, 1, c), trilinear(S, grid, 3, 2, c)};
+}
+
+float grid_max(const oracle_scene& S, const float* g) {
+  float m = 0.0f;
+  const int64_t n = (int64_t)S.dx * S.dy * S.dz;
+  for (int64_t i = 0; i < n; ++i) m = std::fmax(m, g[i]);
+  return m;
+}
+
+// Gradient sink of the adjoint (double accumulators, one per worker).
+struct GradSink {
+  std::vector<double> dens, alb;
+  void density(const oracle_scene& S, const Corners& c, float g) {
+    const float gx0 = 1.0f - c.fx, gy0 = 1.0f - c.fy, gz0 = 1.0f - c.fz;
+    const float a = g * gz0, b = g * c.fz;
+    const float a0 = a * gy0, a1 = a * c.fy, b0 = b * gy0, b1 = b * c.fy;
+    dens[vidx(S, c.x0, c.y0, c.z0)] += a0 * gx0;
+    dens[vidx(S, c.x1, c.y0, c.z0)] += a0 * c.fx;
+    dens[vidx(S, c.x0, c.y1, c.z0)] += a1 * gx0;
+    dens[vidx(S, c.x1, c.y1, c.z0)] += a1 * c.fx;
+    dens[vidx(S, c.x0, c.y0, c.z1)] += b0 * gx0;
+    dens[vidx(S, c.x1, c.y0, c.z1)] += b0 * c.fx;
+    dens[vidx(S, c.x0, c.y1, c.z1)] += b1 * gx0;
+    dens[vidx(S, c.x1, c.y1, c.z1)] += b1 * c.fx;
+  }
+  void albedo(const oracle_scene& S, const Corners& c, const V3& g) {
+    if (alb.empty()) return;
+    const float wx[2] = {1.0f - c.fx, c.fx}, wy[2] = {1.0f - c.fy, c.fy}, wz[2] = {1.0f - c.fz, c.fz};
+    const int xs[2] = {c.x0, c.x1}, ys[2] = {c.y0, c.y1}, zs[2] = {c.z0, c.z1};
+    for (int k = 0; k < 8; ++k) {
+      const int i = k & 1, j = (k >> 1) & 1, m = k >> 2;
+      const float w = (wz[m] * wy[j]) * wx[i];
+      const int64_t v = vidx(S, xs[i], ys[j], zs[m]);
+      alb[v * 3 + 0] += g.x * w;
+      alb[v * 3 + 1] += g.y * w;
+      alb[v * 3 + 2] += g.z * w;
+    }
+  }
+};
+
+enum Mode { kTwoState = 0, kSingle = 1 };
+
+struct PathOut {
+  V3 L_old{0, 0, 0}, L_new{0, 0, 0};
+  uint64_t lookups = 0, nee_lookups = 0, scatters = 0;
+};
+
+struct Tracer {
+  const oracle_scene& S;
+  int mode;         // kTwoState or kSingle
+  float mu;         // majorant used for free-flight sampling
+  GradSink* sink;   // non-null: adjoint replay
+  V3 dL{0, 0, 0};   // adjoint: dLoss/dL for this path
+  V3 Lrem{0, 0, 0}; // adjoint: radiance still to be collected
+
+  float sigma_t(const float* g, const Corners& c) const { return S.scale * trilinear(S, g, 1, 0, c); }
+
+  bool roulette(Rng& rng, int depth, V3& bn, V3& bo) const {
+    bool alive = bn.x != 0.0f || bn.y != 0.0f || bn.z != 0.0f;
+    if (mode == kTwoState) alive = alive || bo.x != 0.0f || bo.y != 0.0f || bo.z != 0.0f;
+    if (!alive) return false;
+    float m = std::fmax(std::fmax(bn.x, bn.y), bn.z);
+    if (mode == kTwoState)
+      m = std::fmax(std::fmax(std::fmax(bn.x, bo.x), std::fmax(bn.y, bo.y)), std::fmax(bn.z, bo.z));
+    const float q = std::fmin(m, 0.99f);
+    const float u = rng.next1d();
+    if (depth > S.rr_depth) {
+      if (!(u < q)) return false;
+      const float inv = 1.0f / q;
+      bn = V3{bn.x * inv, bn.y * inv, bn.z * inv};
+      if (mode == kTwoState) bo = V3{bo.x * inv, bo.y * inv, bo.z * inv};
+    }
+    return true;
+  }
+
+  float free_flight(Rng& rng) const {
+    const float u = rng.next1d();
+    const float tau = -log_unit(1.0f - u);
+    return mu > 0.0f ? tau / mu : kInf;
+  }
+
+  // Ratio-tracking transmittance from p along w to the cube boundary
+  // (plugins/twostatevolpath.py:408-477).  With `grad_scale` set, instead
+  // back-propagates grad_scale * dlog(T) into the density.
+  void transmittance(Rng& rng, const V3& p, const V3& w, float& tro, float& trn, PathOut& out,
+                     const float* grad_scale) const {
+    float tn, tf;
+    cube_hit(p, w, tn, tf);
+    float tr_rem = tf;
+    V3 q = p;
+    tro = 1.0f;
+    trn = 1.0f;
+    for (;;) {
+      const float t = free_flight(rng);
+      if (!(t <= tr_rem)) break;
+      const V3 x = ray_at(q, t, w);
+      const Corners c = corners(S, x);
+      ++out.nee_lookups;
+      const float st_n = sigma_t(S.dens_new, c);
+      if (grad_scale) {
+        const float sn = mu - st_n;
+        if (sn > 0.0f) sink->density(S, c, -(S.scale * *grad_scale) / sn);
+      }
+      trn = trn * ((mu - st_n) / mu);
+      if (mode == kTwoState) {
+        const float st_o = sigma_t(S.dens_old, c);
+        tro = tro * ((mu - st_o) / mu);
+      }
+      q = x;
+      tr_rem = tr_rem - t;
+      const bool dead = mode == kTwoState ? (trn == 0.0f && tro == 0.0f) : trn == 0.0f;
+      if (dead) break;
+    }
+  }
+
+  PathOut trace(uint32_t seed, uint32_t lane, int px, int py) const {
+    PathOut out;
+    Rng rng = lane_rng(seed, lane);
+    // camera ray from the film sample (box filter: the sample stays in its pixel)
+    const float u0 = rng.next1d(), u1 = rng.next1d();
+    const float fx = (float)px + u0, fy = (float)py + u1;
+    const float nx = fx / (float)S.width, ny = fy / (float)S.height;
+    const float a = 2.0f * nx - 1.0f, b = 1.0f - 2.0f * ny;
+    V3 r;
+    r.x = (S.cam_f[0] + a * S.cam_r[0]) + b * S.cam_u[0];
+    r.y = (S.cam_f[1] + a * S.cam_r[1]) + b * S.cam_u[1];
+    r.z = (S.cam_f[2] + a * S.cam_r[2]) + b * S.cam_u[2];
+    const float len = std::sqrt((r.x * r.x + r.y * r.y) + r.z * r.z);
+    V3 d{r.x / len, r.y / len, r.z / len};
+    const V3 o{S.cam_o[0], S.cam_o[1], S.cam_o[2]};
+    (void)rng.next1d();  // colour channel (grey extinction: unused)
+
+    V3 bo{1, 1, 1}, bn{1, 1, 1};
+    V3& Lo = out.L_old;
+    V3& Ln = out.L_new;
+    V3 Lrem_ = Lrem;
+    int depth = 0;
+    const float mis = 0.5f;
+    const float emit_weight = 1.0f / kInvFourPi;
+
+    // camera iteration: Russian roulette draw, then the cube boundary
+    if (!roulette(rng, depth, bn, bo)) return out;
+    float tn, tf;
+    cube_hit(o, d, tn, tf);
+    if (!(tn <= tf && tf > 0.0f)) {
+      if (!S.hide_emitters) {
+        Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
+        if (mode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
+      }
+      return out;
+    }
+    rng.next1d();  // null BSDF sample (1D + 2D)
+    rng.next1d();
+    rng.next1d();
+    V3 p = ray_at(o, std::fmax(tn, 0.0f), d);
+    float t_rem;
+    {
+      float a0, b0;
+      cube_hit(p, d, a0, b0);
+      t_rem = b0;
+    }
+
+    for (;;) {
+      if (!roulette(rng, depth, bn, bo)) return out;
+      const float t = free_flight(rng);
+      if (!(t <= t_rem)) {
+        // leaves the medium through the null boundary, then escapes
+        rng.next1d();
+        rng.next1d();
+        rng.next1d();
+        if (!roulette(rng, depth, bn, bo)) return out;
+        if (!(S.hide_emitters && depth == 0)) {
+          const float k = depth == 0 ? 1.0f : mis;
+          const V3 cn{bn.x * k, bn.y * k, bn.z * k};
+          Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
+          if (mode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
+          Lrem_ = V3{Lrem_.x - cn.x, Lrem_.y - cn.y, Lrem_.z - cn.z};
+        }
+        return out;
+      }
+      const V3 x = ray_at(p, t, d);
+      const Corners c = corners(S, x);
+      ++out.lookups;
+      const float st_n = sigma_t(S.dens_new, c);
+      const float st_o = mode == kTwoState ? sigma_t(S.dens_old, c) : 0.0f;
+      const float ur = rng.next1d();
+      const float prob = mode == kTwoState ? (st_n / mu + st_o / mu) * 0.5f : st_n / mu;
+      if (ur >= prob) {
+        // null collision
+        if (mode == kTwoState) {
+          const float sn_o = mu - st_o, sn_n = mu - st_n;
+          const float den = sn_n + sn_o;
+          const float wn = (2.0f * sn_n) / den, wo = (2.0f * sn_o) / den;
+          bn = V3{bn.x * wn, bn.y * wn, bn.z * wn};
+          bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
+        } else if (sink) {
+          const float sn = mu - st_n;
+          const float sd = (dL.x * Lrem_.x + dL.y * Lrem_.y) + dL.z * Lrem_.z;
+          sink->density(S, c, -(S.scale * sd) / sn);
+        }
+        p = x;
+        t_rem = t_rem - t;
+        continue;
+      }
+      // real scattering
+      depth += 1;
+      if (depth >= S.max_depth) return out;
+      ++out.scatters;
+      const V3 an = albedo(S, S.alb_new, c);
+      const V3 ssn{st_n * an.x, st_n * an.y, st_n * an.z};
+      if (mode == kTwoState) {
+        const V3 ao = albedo(S, S.alb_old, c);
+        const V3 sso{st_o * ao.x, st_o * ao.y, st_o * ao.z};
+        const float den = st_n + st_o;
+        bn = V3{bn.x * ((2.0f * ssn.x) / den), bn.y * ((2.0f * ssn.y) / den), bn.z * ((2.0f * ssn.z) / den)};
+        bo = V3{bo.x * ((2.0f * sso.x) / den), bo.y * ((2.0f * sso.y) / den), bo.z * ((2.0f * sso.z) / den)};
+      } else {
+        bn = V3{bn.x * (ssn.x / st_n), bn.y * (ssn.y / st_n), bn.z * (ssn.z / st_n)};
+        if (sink) {
+          const float sd = (dL.x * Lrem_.x + dL.y * Lrem_.y) + dL.z * Lrem_.z;
+          sink->density(S, c, (S.scale * sd) / st_n);
+          sink->albedo(S, c, V3{(dL.x * Lrem_.x) / std::fmax(an.x, 1e-8f), (dL.y * Lrem_.y) / std::fmax(an.y, 1e-8f),
+                                (dL.z * Lrem_.z) / std::fmax(an.z, 1e-8f)});
+        }
+      }
+      // phase function sample: isotropic, 1D (unused) + 2D
+      rng.next1d();
+      const float pu0 = rng.next1d(), pu1 = rng.next1d();
+      const V3 wo = square_to_uniform_sphere(pu0, pu1);
+      // next event estimation towards the constant environment
+      const float nu0 = rng.next1d(), nu1 = rng.next1d();
+      const V3 w = square_to_uniform_sphere(nu0, nu1);
+      const Rng rng_before = rng;
+      float tro, trn;
+      transmittance(rng, x, w, tro, trn, out, nullptr);
+      const float en = emit_weight * trn;
+      const V3 cn{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
+                  ((bn.z * kInvFourPi) * mis) * en};
+      Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
+      if (mode == kTwoState) {
+        const float eo = emit_weight * tro;
+        Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
+                Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
+      }
+      if (sink) {
+        // replay the shadow walk with the same numbers to differentiate it
+        float gs = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
+        Rng replay = rng_before;
+        float a0, b0;
+        PathOut scratch;
+        transmittance(replay, x, w, a0, b0, scratch, &gs);
+        Lrem_ = V3{Lrem_.x - cn.x, Lrem_.y - cn.y, Lrem_.z - cn.z};
+      }
+      p = x;
+      d = wo;
+      {
+        float a0, b0;
+        cube_hit(p, d, a0, b0);
+        t_rem = b0;
+      }
+    }
+  }
+};
+
+// Butterfly combination of T partial sums (T a power of two), the order in
+// which adjacent GPU lanes combine them with xor-shuffles.
+V3 butterfly(std::vector<V3> v) {
+  const size_t T = v.size();
+  for (size_t off = 1; off < T; off <<= 1) {
+    std::vector<V3> n(T);
+    for (size_t i = 0; i < T; ++i)
+      n[i] = V3{v[i].x + v[i ^ off].x, v[i].y + v[i ^ off].y, v[i].z + v[i ^ off].z};
+    v.swap(n);
+  }
+  return v[0];
+}
+
+// Rows row0, row0 + stride, ... < row1 split over `threads` workers,
+// interleaved for load balance.
+template <class F>
+void parallel_rows(int row0, int row1, int stride, int threads, F&& f) {
+  if (stride < 1) stride = 1;
+  if (threads <= 1) {
+    for (int y = row0; y < row1; y += stride) f(0, y, y + 1);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int k = 0; k < threads; ++k) {
+    pool.emplace_back([&, k] {
+      for (int y = row0 + k * stride; y < row1; y += threads * stride) f(k, y, y + 1);
+    });
+  }
+  for (auto& t : pool) t.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+// Primal render.  mode 0 = two-state (out_old = H, out_new = F), 1 = single
+// state on `new` (out_new).  `chunk` = samples per GPU thread, which fixes the
+// summation order of a pixel's samples (sequential per chunk, butterfly across
+// chunks).  counters (optional) = [paths, lookups, nee lookups, scatters].
+// Rows [row0, row1) of the image only (row1 <= 0: all rows); other pixels of
+// the outputs are left untouched.
+int oracle_render(const oracle_scene* S, int mode, uint32_t seed, int spp, int chunk, float* out_old,
+                  float* out_new, uint64_t* counters, int threads, int row0, int row1, int row_stride) {
+  if (S && row1 <= 0) row1 = S->height;
+  if (!S || row0 < 0 || row1 > S->height || row0 > row1) return -1;
+  if (!S || spp <= 0 || chunk <= 0 || spp % chunk) return -1;
+  const float mu_o = S->scale * grid_max(*S, S->dens_old);
+  const float mu_n = S->scale * grid_max(*S, S->dens_new);
+  const float mu = mode == kTwoState ? std::fmax(mu_o, mu_n) : mu_n;
+  const int T = spp / chunk;
+  std::vector<uint64_t> cnt((size_t)std::max(threads, 1) * 4, 0);
+  parallel_rows(row0, row1, row_stride, threads, [&](int k, int y0, int y1) {
+    Tracer tr{*S, mode, mu, nullptr};
+    for (int py = y0; py < y1; ++py)
+      for (int px = 0; px < S->width; ++px) {
+        const int pix = py * S->width + px;
+        std::vector<V3> so(T), sn(T);
+        for (int g = 0; g < T; ++g) {
+          V3 ao{0, 0, 0}, an{0, 0, 0};
+          for (int s = g * chunk; s < (g + 1) * chunk; ++s) {
+            const PathOut o = tr.trace(seed, (uint32_t)((int64_t)pix * spp + s), px, py);
+            an = V3{an.x + o.L_new.x, an.y + o.L_new.y, an.z + o.L_new.z};
+            ao = V3{ao.x + o.L_old.x, ao.y + o.L_old.y, ao.z + o.L_old.z};
+            cnt[k * 4 + 0] += 1;
+            cnt[k * 4 + 1] += o.lookups;
+            cnt[k * 4 + 2] += o.nee_lookups;
+            cnt[k * 4 + 3] += o.scatters;
+          }
+          so[g] = ao;
+          sn[g] = an;
+        }
+        const V3 Fv = butterfly(sn), Hv = butterfly(so);
+        const float fs = (float)spp;
+        if (out_new) {
+          out_new[pix * 3 + 0] = Fv.x / fs;
+          out_new[pix * 3 + 1] = Fv.y / fs;
+          out_new[pix * 3 + 2] = Fv.z / fs;
+        }
+        if (out_old && mode == kTwoState) {
+          out_old[pix * 3 + 0] = Hv.x / fs;
+          out_old[pix * 3 + 1] = Hv.y / fs;
+          out_old[pix * 3 + 2] = Hv.z / fs;
+        }
+      }
+  });
+  if (counters)
+    for (int k = 0; k < std::max(threads, 1); ++k)
+      for (int j = 0; j < 4; ++j) counters[j] += cnt[k * 4 + j];
+  return 0;
+}
+
+// Path-replay adjoint on `new`: gradients (double) are ADDED to grad_density
+// [dz][dy][dx] and, when the scene has an albedo grid and grad_albedo is not
+// null, to grad_albedo [dz][dy][dx][3].
+int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* grad_img,
+                    double* grad_density, double* grad_albedo, int threads, int row0, int row1,
+                    int row_stride) {
+  if (S && row1 <= 0) row1 = S->height;
+  if (!S || row0 < 0 || row1 > S->height || row0 > row1) return -1;
+  if (!S || spp <= 0 || !grad_img || !grad_density) return -1;
+  const float mu = S->scale * grid_max(*S, S->dens_new);
+  const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
+  const int nt = std::max(threads, 1);
+  std::vector<GradSink> sinks(nt);
+  const bool alb = grad_albedo != nullptr && S->alb_new != nullptr;
+  for (auto& s : sinks) {
+    s.dens.assign(nv, 0.0);
+    if (alb) s.alb.assign(nv * 3, 0.0);
+  }
+  parallel_rows(row0, row1, row_stride, threads, [&](int k, int y0, int y1) {
+    for (int py = y0; py < y1; ++py)
+      for (int px = 0; px < S->width; ++px) {
+        const int pix = py * S->width + px;
+        const float fs = (float)spp;
+        const V3 dL{grad_img[pix * 3 + 0] / fs, grad_img[pix * 3 + 1] / fs, grad_img[pix * 3 + 2] / fs};
+        for (int s = 0; s < spp; ++s) {
+          const uint32_t lane = (uint32_t)((int64_t)pix * spp + s);
+          Tracer primal{*S, kSingle, mu, nullptr};
+          const PathOut o = primal.trace(seed, lane, px, py);
+          Tracer adj{*S, kSingle, mu, &sinks[k], dL, o.L_new};
+          adj.trace(seed, lane, px, py);
+        }
+      }
+  });
+  for (auto& s : sinks) {
+    for (int64_t i = 0; i < nv; ++i) grad_density[i] += s.dens[i];
+    if (alb)
+      for (int64_t i = 0; i < nv * 3; ++i) grad_albedo[i] += s.alb[i];
+  }
+  return 0;
+}
+
+// Default gradient seed of the reference (plugins/twostatepath.py:87-89).
+uint32_t oracle_sample_tea_32(uint32_t v0, uint32_t v1) {
+  uint32_t a, b;
+  tea(v0, v1, 4, a, b);
+  return a;
+}
+
+// Raw PCG32 outputs for (initstate, initseq) (known-answer checks).
+void oracle_pcg32(uint64_t initstate, uint64_t initseq, int n, uint32_t* out) {
+  Rng r;
+  r.seed(initstate, initseq);
+  for (int i = 0; i < n; ++i) out[i] = r.next();
+}
+
+// Draws `n` consecutive uniforms of the stream of (seed, lane).
+void oracle_rng_stream(uint32_t seed, uint32_t lane, int n, float* out) {
+  Rng r = lane_rng(seed, lane);
+  for (int i = 0; i < n; ++i) out[i] = r.next1d();
+}
+
+void oracle_log_unit(const float* x, int n, float* out) {
+  for (int i = 0; i < n; ++i) out[i] = log_unit(x[i]);
+}
+
+void oracle_uniform_sphere(const float* u, int n, float* out) {
+  for (int i = 0; i < n; ++i) {
+    const V3 d = square_to_uniform_sphere(u[2 * i], u[2 * i + 1]);
+    out[3 * i] = d.x;
+    out[3 * i + 1] = d.y;
+    out[3 * i + 2] = d.z;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+"""ctypes binding of librcv (include/rcv.h).
+
+The library is the only compute path of this package: if it cannot be built or
+loaded, every call that needs it raises instead of falling back to anything.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import _build
+
+RCV_OK = 0
+RCV_ERR_INVALID = -1
+RCV_ERR_CUDA = -2
+RCV_ERR_UNSUPPORTED = -3
+
+COUNTER_PATHS = 0
+COUNTER_LOOKUPS = 1
+COUNTER_NEE_LOOKUPS = 2
+COUNTER_SCATTERS = 3
+COUNTER_GRAD_EVENTS = 4
+COUNTER_ALBEDO_EVENTS = 5
+COUNTER_COUNT = 8
+
+LOSS_L2 = 0
+LOSS_L1 = 1
+
+f3 = C.c_float * 3
+i3 = C.c_int32 * 3
+
+
+class Sensor(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("origin", f3),
+        ("forward", f3),
+        ("right", f3),
+        ("up", f3),
+    ]
+
+
+class Medium(C.Structure):
+    _fields_ = [
+        ("dims", i3),
+        ("scale", C.c_float),
+        ("density_old", C.c_void_p),
+        ("density_new", C.c_void_p),
+        ("albedo_old", C.c_void_p),
+        ("albedo_new", C.c_void_p),
+        ("albedo_value", f3),
+        ("workspace", C.c_void_p),
+    ]
+
+
+class VolpathOptions(C.Structure):
+    _fields_ = [
+        ("max_depth", C.c_int32),
+        ("rr_depth", C.c_int32),
+        ("hide_emitters", C.c_int32),
+        ("samples_per_thread", C.c_int32),
+    ]
+
+
+class CvState(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in ("img", "w_s", "v_n", "mean_x", "mean_y", "var_x", "var_y", "cov")]
+
+
+vp = C.c_void_p
+P = C.POINTER
+
+# name -> (restype, argtypes); every symbol of include/rcv.h
+SIGNATURES = {
+    "rcv_last_error": (C.c_char_p, []),
+    "rcv_kernel_launches": (C.c_uint64, []),
+    "rcv_device_info": (C.c_int, [P(C.c_int32), P(C.c_int32), P(C.c_int32)]),
+    "rcv_sample_tea_32": (None, [C.c_uint32, C.c_uint32, P(C.c_uint32)]),
+    "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32]),
+    "rcv_medium_prepare": (C.c_int, [P(Medium), vp]),
+    "rcv_render_twostates_volume": (
+        C.c_int,
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp],
+    ),
+    "rcv_render_volume": (C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp]),
+    "rcv_render_backward_volume": (
+        C.c_int,
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp],
+    ),
+    "rcv_cv_step": (
+        C.c_int,
+        [P(CvState), C.c_int64, vp, vp, C.c_int32, C.c_int32, P(C.c_int32), C.c_float, C.c_float, C.c_int32, vp],
+    ),
+    "rcv_statistics_get": (C.c_int, [P(CvState), C.c_int64, C.c_int32, C.c_float, vp, vp, vp, vp]),
+    "rcv_statistics_update": (C.c_int, [P(CvState), C.c_int64, vp, vp, P(C.c_int32), C.c_float, C.c_float, vp]),
+    "rcv_clamp": (C.c_int, [vp, C.c_int64, C.c_float, C.c_float, vp]),
+    "rcv_welford_update": (C.c_int, [vp, vp, C.c_int64, vp, P(C.c_int32), C.c_float, C.c_float, vp]),
+    "rcv_welford_get": (C.c_int, [vp, C.c_int64, C.c_int32, C.c_float, vp, vp]),
+    "rcv_loss_workspace_bytes": (C.c_uint64, [C.c_int64]),
+    "rcv_loss": (C.c_int, [C.c_int32, vp, vp, C.c_int64, vp, vp, vp, vp]),
+    "rcv_adam_step": (
+        C.c_int,
+        [vp, vp, vp, vp, C.c_int64, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+         C.c_int32, vp],
+    ),
+}
+
+_lock = threading.Lock()
+_lib: C.CDLL | None = None
+
+
+def library_path() -> Path:
+    return _build.lib_path()
+
+
+def load() -> C.CDLL:
+    """Loads librcv, building it first when the sources changed."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.build()
+        lib = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+class RCVError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc == RCV_OK:
+        return
+    msg = load().rcv_last_error().decode(errors="replace")
+    text = f"{what}: {msg}" if what else msg
+    if rc == RCV_ERR_INVALID:
+        raise ValueError(text)
+    raise RCVError(f"{text} (code {rc})")
+
+
+def sample_tea_32(v0: int, v1: int) -> tuple[int, int]:
+    out = (C.c_uint32 * 2)()
+    load().rcv_sample_tea_32(C.c_uint32(v0 & 0xFFFFFFFF), C.c_uint32(v1 & 0xFFFFFFFF), out)
+    return int(out[0]), int(out[1])

@@ -1,0 +1,511 @@
+"""Scene description objects, the plugin registry and scene parameters.
+
+This mirrors the part of Mitsuba's plugin system the reference path uses:
+``mi.load_dict`` over nested ``{'type': name, ...}`` dictionaries
+(optimize.py:66, experiments.py:20-132), ``mi.register_integrator / bsdf /
+medium`` (plugins/__init__.py:11-17), and ``mi.traverse(scene)`` with
+``params.update(opt)`` (optimize.py:41,107).
+
+Supported scene family (the synthetic configurations of this project): one
+unit-cube shape ``[0,1]^3`` with a ``null`` BSDF whose interior is a
+(two-state) heterogeneous medium, a ``constant`` environment emitter of
+radiance 1, a ``perspective`` sensor with an ``hdrfilm`` and a ``box``
+reconstruction filter.  Anything else raises ``ValueError`` at load time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from typing import Any, Callable
+
+import numpy as np
+import torch
+
+from . import _lib
+
+# ----------------------------------------------------------------- registry
+_REGISTRY: dict[str, Callable[["Properties"], Any]] = {}
+_KINDS: dict[str, str] = {}
+
+
+def _register(kind: str, name: str, ctor: Callable[["Properties"], Any]) -> None:
+    _REGISTRY[name] = ctor
+    _KINDS[name] = kind
+
+
+def register_integrator(name: str, ctor) -> None:
+    _register("integrator", name, ctor)
+
+
+def register_bsdf(name: str, ctor) -> None:
+    _register("bsdf", name, ctor)
+
+
+def register_medium(name: str, ctor) -> None:
+    _register("medium", name, ctor)
+
+
+def register_object(kind: str, name: str, ctor) -> None:
+    _register(kind, name, ctor)
+
+
+class Properties(dict):
+    """Plugin properties: a dict with Mitsuba's ``props.get`` / ``props[key]``."""
+
+    def __init__(self, plugin: str, values: dict):
+        super().__init__(values)
+        self.plugin = plugin
+
+    def __getitem__(self, key):
+        if key not in self:
+            raise KeyError(f"plugin '{self.plugin}': required property '{key}' is missing")
+        return super().__getitem__(key)
+
+
+def load_dict(d: dict, device: str | torch.device | None = None) -> Any:
+    """Instantiates a plugin tree (``mi.load_dict`` equivalent)."""
+    if not isinstance(d, dict):
+        raise TypeError("load_dict expects a dictionary")
+    if "type" not in d:
+        raise ValueError("missing 'type' entry")
+    name = d["type"]
+    if name not in _REGISTRY:
+        raise ValueError(f"unknown plugin type '{name}'")
+    values = {}
+    for k, v in d.items():
+        if k == "type":
+            continue
+        if isinstance(v, dict) and "type" in v:
+            v = load_dict(v, device)
+        values[k] = v
+    if device is not None:
+        values.setdefault("device", device)
+    return _REGISTRY[name](Properties(name, values))
+
+
+def _device(props: Properties) -> torch.device:
+    return torch.device(props.get("device", "cuda"))
+
+
+# -------------------------------------------------------------- transforms
+@dataclass
+class LookAt:
+    origin: tuple
+    target: tuple
+    up: tuple
+
+
+def look_at(origin, target, up) -> LookAt:
+    """``T.look_at(origin=..., target=..., up=...)`` of the scene dictionaries."""
+    return LookAt(tuple(map(float, origin)), tuple(map(float, target)), tuple(map(float, up)))
+
+
+# ------------------------------------------------------------------ sensors
+class Film:
+    def __init__(self, props: Properties):
+        self.width = int(props.get("width", 768))
+        self.height = int(props.get("height", 576))
+        rf = props.get("rfilter", None)
+        if rf is not None and not isinstance(rf, BoxFilter):
+            raise ValueError("only the 'box' reconstruction filter is supported")
+        if self.width <= 0 or self.height <= 0:
+            raise ValueError("film size must be positive")
+
+    def size(self):
+        return (self.width, self.height)
+
+
+class BoxFilter:
+    def __init__(self, props: Properties):
+        pass
+
+
+class IndependentSampler:
+    def __init__(self, props: Properties):
+        self.sample_count = int(props.get("sample_count", 4))
+
+
+class PerspectiveSensor:
+    """Pinhole camera; ``fov`` is the horizontal field of view in degrees."""
+
+    def __init__(self, props: Properties):
+        self.fov = float(props.get("fov", 45.0))
+        if props.get("fov_axis", "x") != "x":
+            raise ValueError("only fov_axis='x' is supported")
+        tw = props.get("to_world", look_at((0, 0, 0), (0, 0, 1), (0, 1, 0)))
+        if not isinstance(tw, LookAt):
+            raise ValueError("sensor to_world must be a look_at transform")
+        self.to_world = tw
+        self.film_ = props.get("film", None) or Film(Properties("hdrfilm", {}))
+        self.sampler_ = props.get("sampler", None) or IndependentSampler(Properties("independent", {}))
+
+    def film(self) -> Film:
+        return self.film_
+
+    def sampler(self):
+        return self.sampler_
+
+    def c_struct(self) -> _lib.Sensor:
+        o = np.array(self.to_world.origin, np.float64)
+        t = np.array(self.to_world.target, np.float64)
+        up = np.array(self.to_world.up, np.float64)
+        fwd = t - o
+        fwd /= np.linalg.norm(fwd)
+        right = np.cross(fwd, up)
+        right /= np.linalg.norm(right)
+        cam_up = np.cross(right, fwd)
+        tx = math.tan(math.radians(self.fov) * 0.5)
+        w, h = self.film_.width, self.film_.height
+        ty = tx * h / w
+        s = _lib.Sensor()
+        s.width, s.height = w, h
+        s.origin[:] = [float(np.float32(v)) for v in o]
+        s.forward[:] = [float(np.float32(v)) for v in fwd]
+        s.right[:] = [float(np.float32(v)) for v in right * tx]
+        s.up[:] = [float(np.float32(v)) for v in cam_up * ty]
+        return s
+
+
+# ----------------------------------------------------------------- emitters
+class ConstantEmitter:
+    def __init__(self, props: Properties):
+        rad = props.get("radiance", 1.0)
+        if isinstance(rad, dict):
+            rad = rad.get("value", 1.0)
+        arr = np.broadcast_to(np.asarray(rad, np.float64), (3,))
+        if not np.allclose(arr, 1.0):
+            raise ValueError("the constant emitter supports radiance 1.0 only")
+
+
+# ------------------------------------------------------------------- media
+class Isotropic:
+    def __init__(self, props: Properties):
+        pass
+
+
+def _as_tensor(x, device, channels: int) -> torch.Tensor:
+    t = torch.as_tensor(np.asarray(x) if not isinstance(x, torch.Tensor) else x)
+    # own copy: the states of a two-state object must never alias each other
+    t = t.detach().to(device=device, dtype=torch.float32).clone().contiguous()
+    if t.dim() == 3:
+        t = t.unsqueeze(-1)
+    if t.dim() != 4 or t.shape[-1] != channels:
+        raise ValueError(f"grid data must have shape (Dz, Dy, Dx, {channels}), got {tuple(t.shape)}")
+    return t
+
+
+class GridVolume:
+    """``gridvolume`` with in-memory ``data`` of shape (Dz, Dy, Dx, C)."""
+
+    def __init__(self, props: Properties):
+        if "filename" in props:
+            raise ValueError("gridvolume from .vol files is not supported; pass 'data'")
+        self.raw = props["data"]
+        self.device = _device(props)
+
+
+class _PackedMedium:
+    """Device workspace (packed lookup cells, majorants, gradient
+    accumulators) shared by single- and two-state media."""
+
+    _workspace: torch.Tensor | None = None
+    _dirty: bool = True
+
+    def _states(self):
+        raise NotImplementedError
+
+    def workspace(self) -> torch.Tensor:
+        if self._workspace is None:
+            lib = _lib.load()
+            dims = (C.c_int32 * 3)(*self.dims)
+            nbytes = int(lib.rcv_medium_workspace_bytes(dims, int(self.has_albedo_grid)))
+            self._workspace = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
+        return self._workspace
+
+    def c_struct(self) -> _lib.Medium:
+        old, new = self._states()
+        ws = self.workspace()
+        aligned = (ws.data_ptr() + 255) & ~255
+        m = _lib.Medium()
+        m.dims[:] = list(self.dims)
+        m.scale = new.scale
+        m.density_old = old.density.data_ptr()
+        m.density_new = new.density.data_ptr()
+        if self.has_albedo_grid:
+            m.albedo_old = old.albedo_grid.data_ptr()
+            m.albedo_new = new.albedo_grid.data_ptr()
+        m.albedo_value[:] = list(new.albedo_value)
+        m.workspace = aligned
+        return m
+
+    def prepare(self, stream) -> _lib.Medium:
+        """Packs the grids for the tracers when a state changed."""
+        if self.device.type != "cuda":
+            raise RuntimeError("rendering requires the medium on a CUDA device")
+        m = self.c_struct()
+        if self._dirty:
+            _lib.check(_lib.load().rcv_medium_prepare(C.byref(m), stream), "rcv_medium_prepare")
+            self._dirty = False
+        return m
+
+
+class HeterogeneousMedium(_PackedMedium):
+    """Heterogeneous medium: sigma_t = scale * density grid, albedo constant,
+    RGB or grid, isotropic phase function.  Used on its own (single state,
+    old = new) or as a state of a ``twostatemedium``."""
+
+    def __init__(self, props: Properties):
+        self.device = _device(props)
+        st = props["sigma_t"]
+        if not isinstance(st, GridVolume):
+            raise ValueError("sigma_t must be a gridvolume")
+        self.density = _as_tensor(st.raw, self.device, 1)
+        alb = props.get("albedo", 0.75)
+        self.albedo_grid = None
+        self.albedo_value = (0.75, 0.75, 0.75)
+        if isinstance(alb, GridVolume):
+            self.albedo_grid = _as_tensor(alb.raw, self.device, 3)
+            if self.albedo_grid.shape[:3] != self.density.shape[:3]:
+                raise ValueError("albedo and sigma_t grids must have the same resolution")
+        else:
+            if isinstance(alb, dict):
+                alb = alb.get("value", 0.75)
+            a = np.broadcast_to(np.asarray(alb, np.float64), (3,))
+            self.albedo_value = tuple(float(np.float32(v)) for v in a)
+        self.scale = float(props.get("scale", 1.0))
+        if self.scale < 0:
+            raise ValueError("scale must be non-negative")
+        ph = props.get("phase", None)
+        if ph is not None and not isinstance(ph, Isotropic):
+            raise ValueError("only the isotropic phase function is supported")
+        if props.get("has_spectral_extinction", False):
+            raise ValueError("spectrally varying extinction is not supported")
+        if int(props.get("majorant_resolution_factor", 0)) != 0:
+            raise ValueError("majorant supergrids are not supported")
+        self._workspace = None
+        self._dirty = True
+
+    def _states(self):
+        return self, self
+
+    @property
+    def dims(self):
+        dz, dy, dx, _ = self.density.shape
+        return (dx, dy, dz)
+
+    @property
+    def has_albedo_grid(self) -> bool:
+        return self.albedo_grid is not None
+
+    def param_tensors(self) -> dict[str, torch.Tensor]:
+        out = {"sigma_t.data": self.density}
+        if self.albedo_grid is not None:
+            out["albedo.data"] = self.albedo_grid
+        return out
+
+    def traverse(self) -> dict[str, torch.Tensor]:
+        return self.param_tensors()
+
+    def parameters_changed(self, keys=None) -> None:
+        self._dirty = True
+
+
+class TwoStateMedium(_PackedMedium):
+    """Old / new / incoming copies of a heterogeneous medium
+    (plugins/twostatemedium.py:5-13).  ``traverse`` exposes ``incoming`` only
+    (:186-187); ``parameters_changed`` rotates old <- new <- incoming
+    (:189-200) by swapping buffers plus one device copy, then marks the
+    lookup workspace for repacking."""
+
+    def __init__(self, props: Properties):
+        self.old = props["old"]
+        self.new = props["new"]
+        self.incoming = props["incoming"]
+        for m in (self.old, self.new, self.incoming):
+            if not isinstance(m, HeterogeneousMedium):
+                raise ValueError("twostatemedium expects heterogeneous media for old/new/incoming")
+        if not (self.old.dims == self.new.dims == self.incoming.dims):
+            raise ValueError("old/new/incoming grids must have the same resolution")
+        if (self.old.albedo_grid is None) != (self.new.albedo_grid is None) or (
+            self.new.albedo_grid is None
+        ) != (self.incoming.albedo_grid is None):
+            raise ValueError("old/new/incoming must all have, or all lack, an albedo grid")
+        self.device = self.new.device
+        self._workspace = None
+        self._dirty = True
+
+    def _states(self):
+        return self.old, self.new
+
+    @property
+    def dims(self):
+        return self.new.dims
+
+    @property
+    def has_albedo_grid(self) -> bool:
+        return self.new.albedo_grid is not None
+
+    def traverse(self) -> dict[str, torch.Tensor]:
+        return self.incoming.param_tensors()
+
+    def parameters_changed(self, keys=None) -> None:
+        o, n, i = self.old, self.new, self.incoming
+        o.density, n.density = n.density, o.density
+        n.density.copy_(i.density)
+        if n.albedo_grid is not None:
+            o.albedo_grid, n.albedo_grid = n.albedo_grid, o.albedo_grid
+            n.albedo_grid.copy_(i.albedo_grid)
+        o.albedo_value, n.albedo_value = n.albedo_value, i.albedo_value
+        self._dirty = True
+
+
+class NullBSDF:
+    def __init__(self, props: Properties):
+        pass
+
+
+class CubeShape:
+    """Unit cube [0,1]^3 (the 'cube_unit' mesh of the reference scenes)."""
+
+    def __init__(self, props: Properties):
+        bsdf = props.get("bsdf", None)
+        if bsdf is not None and not isinstance(bsdf, NullBSDF):
+            raise ValueError("the medium boundary must use a 'null' BSDF")
+        if "to_world" in props:
+            raise ValueError("the medium boundary is the unit cube; to_world is not supported")
+        self.interior = props.get("interior", None)
+
+    def interior_medium(self):
+        return self.interior
+
+    def exterior_medium(self):
+        return None
+
+
+class Scene:
+    def __init__(self, props: Properties):
+        self.sensors_ = []
+        self.emitters_ = []
+        self.shapes_ = {}
+        for k, v in props.items():
+            if k == "device":
+                continue
+            if isinstance(v, PerspectiveSensor):
+                self.sensors_.append(v)
+            elif isinstance(v, ConstantEmitter):
+                self.emitters_.append(v)
+            elif isinstance(v, CubeShape) or hasattr(v, "is_surface_shape"):
+                self.shapes_[k] = v
+            else:
+                raise ValueError(f"unsupported scene element '{k}' ({type(v).__name__})")
+
+    def sensors(self):
+        return self.sensors_
+
+    def emitters(self):
+        return self.emitters_
+
+    def shapes(self):
+        return list(self.shapes_.values())
+
+    def named_shapes(self):
+        return dict(self.shapes_)
+
+
+# ------------------------------------------------------- scene parameters
+class SceneParameters:
+    """``mi.traverse(scene)``: differentiable parameters by key.
+
+    ``params[key] = value`` stages a new value; ``params.update(opt)`` takes
+    every key the optimizer holds, copies the values into the scene
+    (``incoming`` of a two-state object) and notifies the owners, which
+    rotates their states."""
+
+    def __init__(self, scene: Scene):
+        self._owners: dict[str, tuple[Any, str]] = {}
+        self._values: dict[str, torch.Tensor] = {}
+        self._pending: set[str] = set()
+        for name, shape in scene.named_shapes().items():
+            owners = []
+            med = shape.interior_medium() if hasattr(shape, "interior_medium") else None
+            if med is not None and hasattr(med, "traverse"):
+                owners.append(("interior_medium", med))
+            bsdf = getattr(shape, "bsdf", None)
+            if bsdf is not None and hasattr(bsdf, "traverse"):
+                owners.append(("bsdf", bsdf))
+            for prefix, owner in owners:
+                for sub, t in owner.traverse().items():
+                    key = f"{name}.{prefix}.{sub}"
+                    self._owners[key] = (owner, sub)
+                    self._values[key] = t
+
+    def keys(self):
+        return self._values.keys()
+
+    def items(self):
+        return self._values.items()
+
+    def __contains__(self, key):
+        return key in self._values
+
+    def __getitem__(self, key):
+        return self._values[key]
+
+    def __setitem__(self, key, value):
+        if key not in self._owners:
+            raise KeyError(f"unknown scene parameter '{key}'")
+        owner, sub = self._owners[key]
+        cur = owner.traverse()[sub] if hasattr(owner, "traverse") else None
+        v = value if isinstance(value, torch.Tensor) else torch.as_tensor(np.asarray(value, np.float32))
+        if cur is not None and tuple(v.shape) != tuple(cur.shape):
+            if v.numel() == 1:
+                v = v.reshape(()).expand(cur.shape)
+            else:
+                raise ValueError(f"parameter '{key}' has shape {tuple(cur.shape)}, got {tuple(v.shape)}")
+        self._values[key] = v
+        self._pending.add(key)
+
+    def update(self, opt=None):
+        if opt is not None:
+            for key in opt.keys():
+                if key in self._owners:
+                    self[key] = opt[key]
+        owners = {}
+        for key in self._pending:
+            owner, sub = self._owners[key]
+            dst = owner.traverse()[sub]
+            with torch.no_grad():
+                dst.copy_(self._values[key].detach().to(dst.device, torch.float32).reshape(dst.shape))
+            owners[id(owner)] = owner
+        self._pending.clear()
+        for owner in owners.values():
+            owner.parameters_changed()
+        return self
+
+    def differentiable(self) -> dict[str, torch.Tensor]:
+        return {k: v for k, v in self._values.items() if isinstance(v, torch.Tensor) and v.requires_grad}
+
+    def owner_of(self, key):
+        return self._owners[key]
+
+
+def traverse(scene: Scene) -> SceneParameters:
+    return SceneParameters(scene)
+
+
+for _name, _ctor, _kind in [
+    ("scene", Scene, "scene"),
+    ("perspective", PerspectiveSensor, "sensor"),
+    ("hdrfilm", Film, "film"),
+    ("box", BoxFilter, "rfilter"),
+    ("independent", IndependentSampler, "sampler"),
+    ("constant", ConstantEmitter, "emitter"),
+    ("gridvolume", GridVolume, "volume"),
+    ("isotropic", Isotropic, "phase"),
+    ("heterogeneous", HeterogeneousMedium, "medium"),
+    ("null", NullBSDF, "bsdf"),
+    ("cube", CubeShape, "shape"),
+]:
+    register_object(_kind, _name, _ctor)
+register_medium("twostatemedium", TwoStateMedium)

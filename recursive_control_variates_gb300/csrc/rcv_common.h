@@ -1,0 +1,78 @@
+// Host-side helpers shared by the librcv translation units: error reporting
+// and workspace layout.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/rcv.h"
+
+namespace rcv {
+
+void set_error(const char* fmt, ...);
+
+inline int cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return RCV_ERR_CUDA;
+  }
+  return RCV_OK;
+}
+
+// Counts one kernel launch of librcv (see rcv_kernel_launches) and reports a
+// launch failure.
+void count_launch();
+inline int launched(const char* what) {
+  count_launch();
+  return cuda_check(cudaGetLastError(), what);
+}
+
+#define RCV_TRY_CUDA(expr, what)                       \
+  do {                                                   \
+    int _rc = ::rcv::cuda_check((expr), (what));         \
+    if (_rc != RCV_OK) return _rc;                       \
+  } while (0)
+
+#define RCV_REQUIRE(cond, ...)        \
+  do {                                \
+    if (!(cond)) {                    \
+      ::rcv::set_error(__VA_ARGS__);  \
+      return RCV_ERR_INVALID;         \
+    }                                 \
+  } while (0)
+
+inline uint64_t align256(uint64_t v) { return (v + 255u) & ~uint64_t(255u); }
+
+// Layout of the medium workspace (all sections 256-byte aligned).
+struct MediumLayout {
+  uint64_t cells, albedo, maxbits, grad_cells, grad_albedo, total;
+};
+
+inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo) {
+  const uint64_t nc = uint64_t(dims[0] + 1) * uint64_t(dims[1] + 1) * uint64_t(dims[2] + 1);
+  const uint64_t nv = uint64_t(dims[0]) * uint64_t(dims[1]) * uint64_t(dims[2]);
+  MediumLayout l;
+  uint64_t off = 0;
+  l.cells = off;
+  off = align256(off + nc * 64u);
+  l.albedo = off;
+  off = align256(off + (has_albedo ? nv * 32u : 0u));
+  l.maxbits = off;
+  off = align256(off + 16u);
+  l.grad_cells = off;
+  off = align256(off + nc * 32u);
+  l.grad_albedo = off;
+  off = align256(off + (has_albedo ? nv * 16u : 0u));
+  l.total = off;
+  return l;
+}
+
+inline unsigned grid_for(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+}  // namespace rcv

@@ -1,0 +1,215 @@
+"""Two-state volumetric path-replay integrator (``twostateprbvolpath``) and
+its single-state counterpart (``prbvolpath``).
+
+Interface of plugins/twostatevolpath.py:11-138 of the reference:
+``render_twostates(scene, sensor, seed, spp) -> (H, F)`` renders the previous
+and current medium parameters with shared random numbers; ``render`` renders
+the current parameters only; ``render_backward`` back-propagates an image
+gradient into the current parameters by path replay.  All three run on the
+GPU through librcv.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from .. import _lib, profiling
+from ..core import CubeShape, HeterogeneousMedium, Properties, TwoStateMedium
+from ..utils import stream_handle
+
+# linear sRGB -> CIE XYZ (D65), for the `xyz` option
+_SRGB_TO_XYZ = torch.tensor(
+    [[0.412453, 0.357580, 0.180423], [0.212671, 0.715160, 0.072169], [0.019334, 0.119193, 0.950227]],
+    dtype=torch.float32,
+)
+
+
+class _VolumeIntegratorBase:
+    two_state = False
+
+    def __init__(self, props: Properties):
+        self.max_depth = int(props.get("max_depth", 6))
+        self.rr_depth = int(props.get("rr_depth", 5))
+        self.hide_emitters = bool(props.get("hide_emitters", False))
+        self.xyz = bool(props.get("xyz", False))
+        self.samples_per_thread = int(props.get("samples_per_thread", 0))
+        if self.max_depth < -1:
+            raise ValueError("max_depth must be -1 (infinite) or non-negative")
+        self.is_checked = False
+        self._counters: dict[torch.device, torch.Tensor] = {}
+
+    # ------------------------------------------------------------- helpers
+    def options(self) -> _lib.VolpathOptions:
+        o = _lib.VolpathOptions()
+        o.max_depth = self.max_depth
+        o.rr_depth = self.rr_depth
+        o.hide_emitters = int(self.hide_emitters)
+        o.samples_per_thread = self.samples_per_thread
+        return o
+
+    def counters(self, device) -> torch.Tensor:
+        device = torch.device(device)
+        if device not in self._counters:
+            self._counters[device] = torch.zeros(_lib.COUNTER_COUNT, dtype=torch.int64, device=device)
+        return self._counters[device]
+
+    @staticmethod
+    def medium_of(scene):
+        for shape in scene.shapes():
+            if isinstance(shape, CubeShape):
+                m = shape.interior_medium()
+                if m is not None:
+                    return m
+        return None
+
+    @staticmethod
+    def sensor_of(scene, sensor):
+        if isinstance(sensor, int):
+            if len(scene.sensors()) == 0:
+                raise Exception("No sensor specified! Add a sensor in the scene description.")
+            return scene.sensors()[sensor]
+        return sensor
+
+    @staticmethod
+    def resolve_spp(sensor, spp: int) -> int:
+        return int(spp) if spp and spp > 0 else int(sensor.sampler().sample_count)
+
+    def _post(self, img: torch.Tensor) -> torch.Tensor:
+        if not self.xyz:
+            return img
+        m = _SRGB_TO_XYZ.to(img.device)
+        return img @ m.T
+
+    def _image(self, sensor, device) -> torch.Tensor:
+        f = sensor.film()
+        return torch.empty((f.height, f.width, 3), dtype=torch.float32, device=device)
+
+    # --------------------------------------------------------------- render
+    def render(self, scene, sensor=0, seed: int = 0, spp: int = 0, develop: bool = True, evaluate: bool = True):
+        """Single-state render of the current parameters."""
+        medium = self._checked_medium(scene)
+        sensor = self.sensor_of(scene, sensor)
+        spp = self.resolve_spp(sensor, spp)
+        st = stream_handle(medium.device)
+        m = medium.prepare(st)
+        s = sensor.c_struct()
+        o = self.options()
+        img = self._image(sensor, medium.device)
+        with profiling.region("trace_single", medium.device):
+            _lib.check(
+                _lib.load().rcv_render_volume(
+                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, img.data_ptr(),
+                    self.counters(medium.device).data_ptr(), st,
+                ),
+                "rcv_render_volume",
+            )
+        return self._post(img)
+
+    def render_backward(self, scene, params, grad_in: torch.Tensor, sensor=0, seed: int = 0, spp: int = 0):
+        """Path-replay adjoint on the current parameters.
+
+        Returns ``{key: gradient}`` for the differentiable medium parameters
+        present in ``params`` (density ``...sigma_t.data`` and, when the
+        medium has an albedo grid, ``...albedo.data``)."""
+        medium = self._checked_medium(scene)
+        sensor = self.sensor_of(scene, sensor)
+        spp = self.resolve_spp(sensor, spp)
+        if self.xyz:
+            grad_in = grad_in @ _SRGB_TO_XYZ.to(grad_in.device)
+        g = grad_in.detach().to(medium.device, torch.float32).contiguous()
+        f = sensor.film()
+        if tuple(g.shape) != (f.height, f.width, 3):
+            raise ValueError(f"grad_in has shape {tuple(g.shape)}, expected {(f.height, f.width, 3)}")
+        st = stream_handle(medium.device)
+        m = medium.prepare(st)
+        s = sensor.c_struct()
+        o = self.options()
+        dx, dy, dz = medium.dims
+        gd = torch.zeros((dz, dy, dx, 1), dtype=torch.float32, device=medium.device)
+        ga = torch.zeros((dz, dy, dx, 3), dtype=torch.float32, device=medium.device) if medium.has_albedo_grid else None
+        with profiling.region("trace_adjoint", medium.device):
+            _lib.check(
+                _lib.load().rcv_render_backward_volume(
+                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, g.data_ptr(), gd.data_ptr(),
+                    ga.data_ptr() if ga is not None else None, self.counters(medium.device).data_ptr(), st,
+                ),
+                "rcv_render_backward_volume",
+            )
+        out = {}
+        keys = list(params.keys()) if params is not None else []
+        for key in keys:
+            owner, sub = params.owner_of(key)
+            if owner is not medium:
+                continue
+            if sub == "sigma_t.data":
+                out[key] = gd
+            elif sub == "albedo.data" and ga is not None:
+                out[key] = ga
+        return out
+
+    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0):
+        raise NotImplementedError("forward-mode derivatives are not provided; use render_backward")
+
+    def _checked_medium(self, scene):
+        raise NotImplementedError
+
+
+class TwoStatePRBVolpathIntegrator(_VolumeIntegratorBase):
+    """``twostateprbvolpath`` (plugins/twostatevolpath.py:11-482)."""
+
+    two_state = True
+
+    def check_scene(self, scene):
+        # plugins/twostatevolpath.py:67-78
+        if self.is_checked:
+            return
+        self.is_checked = True
+        if not isinstance(self.medium_of(scene), TwoStateMedium):
+            self.is_checked = False
+            raise RuntimeError("No TwoStateMedium found in the scene!")
+
+    def _checked_medium(self, scene):
+        self.check_scene(scene)
+        return self.medium_of(scene)
+
+    def render_twostates(self, scene, sensor=0, seed: int = 0, spp: int = 1):
+        """Returns (H, F): images of the previous and current parameters
+        rendered with the same random numbers (plugins/twostatevolpath.py:91-138)."""
+        medium = self._checked_medium(scene)
+        sensor = self.sensor_of(scene, sensor)
+        spp = self.resolve_spp(sensor, spp)
+        st = stream_handle(medium.device)
+        m = medium.prepare(st)
+        s = sensor.c_struct()
+        o = self.options()
+        H = self._image(sensor, medium.device)
+        F = self._image(sensor, medium.device)
+        with profiling.region("trace_twostate", medium.device):
+            _lib.check(
+                _lib.load().rcv_render_twostates_volume(
+                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, H.data_ptr(), F.data_ptr(),
+                    self.counters(medium.device).data_ptr(), st,
+                ),
+                "rcv_render_twostates_volume",
+            )
+        self.primal_image_old, self.primal_image_new = self._post(H), self._post(F)
+        return self.primal_image_old, self.primal_image_new
+
+    def to_string(self):
+        return f"TwoStatePRBVolpathIntegrator[max_depth = {self.max_depth}]"
+
+
+class PRBVolpathIntegrator(_VolumeIntegratorBase):
+    """Single-state volumetric path replay (``prbvolpath``): the integrator the
+    reference pairs with the baseline method (experiments.py:131).  Accepts a
+    plain heterogeneous medium or a two-state one (then renders ``new``)."""
+
+    def _checked_medium(self, scene):
+        m = self.medium_of(scene)
+        if not isinstance(m, (HeterogeneousMedium, TwoStateMedium)):
+            raise RuntimeError("No heterogeneous medium found in the scene!")
+        return m
+
+    def to_string(self):
+        return f"PRBVolpathIntegrator[max_depth = {self.max_depth}]"

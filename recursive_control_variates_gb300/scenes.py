@@ -1,0 +1,128 @@
+"""Synthetic scenes of the benchmark configurations.
+
+The reference's own scenes (janga, dust_devil, rover, ...) are separate
+downloads that are not available; these seeded generators stand in for them
+with the same structure as the reference's grid scenes (experiments.py:20-132):
+a unit cube with a null BSDF holding a heterogeneous medium, seen by a
+perspective camera, lit by a constant environment.
+
+Density at voxel centres (i+1/2)/D:
+    rho(x) = sum_{k<8} a_k exp(-|x - c_k|^2 / (2 s_k^2)),
+    c_k ~ U[0.2, 0.8]^3, s_k ~ U[0.05, 0.15], a_k ~ U[5, 20]
+drawn from numpy.random.default_rng(seed).  RGB albedo grids are U[0.3, 0.95]
+per voxel smoothed by a Gaussian of 2 voxels.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .core import look_at
+
+CAMERA_ORIGIN = (0.5, 0.5, 3.5)
+CAMERA_TARGET = (0.5, 0.5, 0.5)
+CAMERA_UP = (0.0, 1.0, 0.0)
+
+
+def blob_density(D: int, seed: int, n_blobs: int = 8) -> np.ndarray:
+    """(D, D, D, 1) float32 sum of isotropic Gaussian blobs."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.2, 0.8, size=(n_blobs, 3))
+    sigmas = rng.uniform(0.05, 0.15, size=n_blobs)
+    amps = rng.uniform(5.0, 20.0, size=n_blobs)
+    c = (np.arange(D, dtype=np.float64) + 0.5) / D
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    rho = np.zeros((D, D, D), np.float64)
+    for k in range(n_blobs):
+        d2 = (x - centres[k, 0]) ** 2 + (y - centres[k, 1]) ** 2 + (z - centres[k, 2]) ** 2
+        rho += amps[k] * np.exp(-d2 / (2.0 * sigmas[k] ** 2))
+    return rho.astype(np.float32)[..., None]
+
+
+def albedo_grid(D: int, seed: int, lo: float = 0.3, hi: float = 0.95, smooth: float = 2.0) -> np.ndarray:
+    """(D, D, D, 3) float32 smoothed uniform RGB albedo."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed + 7919)
+    a = rng.uniform(lo, hi, size=(D, D, D, 3))
+    for ch in range(3):
+        a[..., ch] = gaussian_filter(a[..., ch], sigma=smooth, mode="nearest")
+    return np.clip(a, lo, hi).astype(np.float32)
+
+
+@dataclass
+class VolumeConfig:
+    name: str
+    grid: int
+    res: int
+    spp: int
+    max_depth: int
+    steps: int
+    lr: float = 0.02
+    albedo: float | None = 0.8  # None -> RGB albedo grid
+    spp_ref: int = 256
+    init: float = 1.0
+    seed: int = 0
+    clamp: tuple = (0.0, 250.0)
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def spp_grad(self) -> int:
+        return self.spp
+
+    def paths_per_step(self) -> int:
+        return self.res * self.res * (self.spp + self.spp_grad)
+
+
+CONFIGS = {
+    # 32^3 density, constant albedo, 128^2, spp 4, depth 16, 50 Adam steps
+    "cfg1": VolumeConfig("cfg1", grid=32, res=128, spp=4, max_depth=16, steps=50),
+    # 64^3 density + 64^3 RGB albedo, 512^2, spp 16, depth 64, 200 steps
+    "cfg2": VolumeConfig("cfg2", grid=64, res=512, spp=16, max_depth=64, steps=200, albedo=None),
+}
+
+
+def medium_dict(density, albedo) -> dict:
+    m = {
+        "type": "heterogeneous",
+        "sigma_t": {"type": "gridvolume", "data": density},
+        "scale": 1.0,
+        "phase": {"type": "isotropic"},
+    }
+    if albedo is None or np.isscalar(albedo) or np.asarray(albedo).ndim <= 1:
+        m["albedo"] = albedo if albedo is not None else 0.8
+    else:
+        m["albedo"] = {"type": "gridvolume", "data": albedo}
+    return m
+
+
+def scene_dict(density, albedo, res: int, two_state: bool = True, spp: int = 4) -> dict:
+    """Scene dictionary for ``load_dict`` (reference layout: a cube 'object'
+    whose interior is a (two-state) medium, experiments.py:72-95)."""
+    med = medium_dict(density, albedo)
+    interior = {"type": "twostatemedium", "old": med, "new": med, "incoming": med} if two_state else med
+    return {
+        "type": "scene",
+        "sensor": {
+            "type": "perspective",
+            "fov": 45.0,
+            "to_world": look_at(CAMERA_ORIGIN, CAMERA_TARGET, CAMERA_UP),
+            "film": {"type": "hdrfilm", "width": res, "height": res, "rfilter": {"type": "box"}},
+            "sampler": {"type": "independent", "sample_count": spp},
+        },
+        "emitter": {"type": "constant", "radiance": 1.0},
+        "object": {"type": "cube", "bsdf": {"type": "null"}, "interior": interior},
+    }
+
+
+def config_grids(cfg: VolumeConfig, seed: int | None = None):
+    """True density / albedo of a configuration (albedo is a float when constant)."""
+    s = cfg.seed if seed is None else seed
+    dens = blob_density(cfg.grid, s)
+    alb = cfg.albedo if cfg.albedo is not None else albedo_grid(cfg.grid, s)
+    return dens, alb
+
+
+DENSITY_KEY = "object.interior_medium.sigma_t.data"
+ALBEDO_KEY = "object.interior_medium.albedo.data"

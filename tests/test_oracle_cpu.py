@@ -1,0 +1,182 @@
+"""CPU checks of the oracle itself: known-answer vectors, golden fixtures made
+by running the reference's own control-variate code, closed forms and
+finite-difference consistency of its adjoint."""
+import numpy as np
+import pytest
+
+from recursive_control_variates_gb300.scenes import blob_density
+
+
+def test_pcg32_known_answer(oracle):
+    # pcg32_srandom_r(42, 54): first outputs of O'Neill's reference demo
+    expect = [0xA15C02B7, 0x7B47F409, 0xBA1D3330, 0x83D2F293, 0xBFA4784B, 0xCBED606E]
+    assert [int(v) for v in oracle.pcg32(42, 54, 6)] == expect
+
+
+def test_tea_matches_library(oracle, rcvlib):
+    from recursive_control_variates_gb300 import _lib
+
+    rng = np.random.default_rng(1)
+    for v0, v1 in rng.integers(0, 2**32, size=(200, 2), dtype=np.uint64):
+        assert oracle.sample_tea_32(int(v0), int(v1)) == _lib.sample_tea_32(int(v0), int(v1))[0]
+
+
+def test_uniform_stream_range(oracle):
+    u = np.concatenate([oracle.rng_stream(7, lane, 64) for lane in range(64)])
+    assert u.min() >= 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 0.01
+    # 23-bit grid
+    assert np.all((u * 2**23) == np.floor(u * 2**23))
+
+
+def test_log_accuracy(oracle):
+    rng = np.random.default_rng(2)
+    x = np.concatenate([rng.uniform(0, 1, 200000), 2.0 ** -np.arange(0, 24), [1.0]]).astype(np.float32)
+    x = x[x > 0]
+    got = oracle.log_unit(x).astype(np.float64)
+    ref = np.log(x.astype(np.float64))
+    err = np.abs(got - ref)
+    assert np.all(err <= 2.5e-7 * np.maximum(1.0, np.abs(ref)))
+
+
+def test_uniform_sphere(oracle):
+    rng = np.random.default_rng(3)
+    u = rng.uniform(0, 1, (50000, 2)).astype(np.float32)
+    d = oracle.uniform_sphere(u).astype(np.float64)
+    assert np.all(np.abs(np.linalg.norm(d, axis=1) - 1.0) < 2e-6)
+    assert np.all(np.abs(d.mean(axis=0)) < 0.02)
+    # azimuth follows the first sample, z the second
+    np.testing.assert_allclose(d[:, 2], 1.0 - 2.0 * u[:, 1].astype(np.float64), atol=1e-6)
+    phi = np.arctan2(d[:, 1], d[:, 0]) % (2 * np.pi)
+    dphi = np.abs(phi - 2 * np.pi * u[:, 0])
+    dphi = np.minimum(dphi, 2 * np.pi - dphi)
+    assert np.all(dphi[np.linalg.norm(d[:, :2], axis=1) > 1e-3] < 2e-5)
+
+
+def _scene(oracle, res=24, D=16, seeds=(1, 1), albedo=None, max_depth=8, rr_depth=None):
+    cam = oracle.camera_basis(res, res)
+    old = blob_density(D, seeds[0])
+    new = blob_density(D, seeds[1])
+    kw = {}
+    if albedo is not None:
+        kw = dict(albedo_old=albedo[0], albedo_new=albedo[1])
+    return oracle.Scene(cam, old, new, max_depth=max_depth, rr_depth=rr_depth, **kw)
+
+
+def test_two_state_equal_states_bitwise(oracle):
+    """old == new: the two-state weights are exactly 1 and H == F == single
+    (plugins/twostatevolpath.py:230-231, 259-260)."""
+    sc = _scene(oracle)
+    H, F = oracle.render_twostates(sc, seed=5, spp=8)
+    S = oracle.render(sc, seed=5, spp=8)
+    assert np.array_equal(H, F)
+    assert np.array_equal(F, S)
+    assert F.mean() > 0.05
+
+
+def test_chunking_changes_only_summation_order(oracle):
+    sc = _scene(oracle, seeds=(1, 2))
+    H1, F1 = oracle.render_twostates(sc, seed=9, spp=8, chunk=8)
+    H2, F2 = oracle.render_twostates(sc, seed=9, spp=8, chunk=1)
+    np.testing.assert_allclose(F1, F2, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(H1, H2, rtol=1e-6, atol=1e-7)
+
+
+def test_closed_form_transmittance(oracle):
+    """Albedo 0, constant density: a pixel's expectation is the footprint
+    average of exp(-sigma * chord)."""
+    res, sigma = 16, 3.0
+    cam = oracle.camera_basis(res, res)
+    dens = np.full((8, 8, 8), sigma, np.float32)
+    sc = oracle.Scene(cam, dens, dens, albedo_const=0.0, max_depth=16)
+    spp = 1024
+    img = oracle.render(sc, seed=3, spp=spp)[..., 0].astype(np.float64)
+    o, f, r, u = (np.array(v, np.float64) for v in (cam.origin, cam.forward, cam.right, cam.up))
+    sub = (np.arange(16) + 0.5) / 16
+    expect = np.zeros((res, res))
+    for py in range(res):
+        for px in range(res):
+            fx = px + sub[None, :]
+            fy = py + sub[:, None]
+            a = 2 * fx / res - 1
+            b = 1 - 2 * fy / res
+            d = f[None, None] + a[..., None] * r + b[..., None] * u
+            d = d / np.linalg.norm(d, axis=-1, keepdims=True)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                t0 = (0 - o) / d
+                t1 = (1 - o) / d
+            tn = np.max(np.minimum(t0, t1), -1)
+            tf = np.min(np.maximum(t0, t1), -1)
+            chord = np.where(tn <= tf, np.maximum(tf - np.maximum(tn, 0), 0), 0)
+            expect[py, px] = np.exp(-sigma * chord).mean()
+    sd = np.sqrt(np.maximum(expect * (1 - expect), 1e-4) / spp)
+    z = np.abs(img - expect) / sd
+    assert np.mean(z < 3) > 0.98
+    assert abs(img.mean() - expect.mean()) < 4 * np.sqrt((sd**2).sum()) / img.size + 2e-3
+
+
+def test_cv_welford_golden(oracle, golden_cv):
+    """The numpy restatement reproduces the reference's own CVIntegrator /
+    MetaIntegrator / StatisticsEstimator code bit for bit."""
+    g = golden_cv
+    for name in g["cases"]:
+        cv = oracle.CVOracle(
+            warmup=int(g[f"{name}/warmup"]),
+            beta1=float(g[f"{name}/beta1"]),
+            beta2=float(g[f"{name}/beta2"]),
+            pre_update=bool(g[f"{name}/pre_update"]),
+        )
+        H, F = g[f"{name}/H"], g[f"{name}/F"]
+        for i in range(len(H)):
+            with np.errstate(all="ignore"):
+                img = cv.step(H[i], F[i])
+            np.testing.assert_array_equal(np.broadcast_to(img, H[i].shape), g[f"{name}/img"][i], err_msg=str(name))
+            np.testing.assert_array_equal(np.broadcast_to(cv.w_s, H[i].shape), g[f"{name}/w_s"][i])
+            np.testing.assert_array_equal(np.broadcast_to(cv.stats.cov, H[i].shape), g[f"{name}/cov"][i])
+            assert cv.stats.n == int(g[f"{name}/n"][i])
+
+
+def test_welford1_golden(oracle, golden_cv):
+    g = golden_cv
+    est = oracle.WelfordOracle()
+    for i, x in enumerate(g["welford1/x"]):
+        est.update(x)
+        np.testing.assert_array_equal(est.mean, g["welford1/mean"][i])
+        np.testing.assert_array_equal(est.var, g["welford1/var"][i])
+        np.testing.assert_array_equal(est.get(), g["welford1/get"][i])
+
+
+def test_adjoint_matches_two_state_finite_differences(oracle):
+    """The path-replay adjoint against central differences of the expected
+    image, estimated with the two-state tracer (old = theta - h e_v,
+    new = theta + h e_v share random numbers, so F - H has low variance)."""
+    res, D = 20, 8
+    cam = oracle.camera_basis(res, res)
+    theta = blob_density(D, 4)[..., 0] * 0.5
+    rng = np.random.default_rng(0)
+    dLdimg = rng.normal(0, 1, (res, res, 3)).astype(np.float32)
+    sc = oracle.Scene(cam, theta, theta, albedo_const=0.8, max_depth=6)
+    runs = np.array([oracle.backward(sc, seed=100 + s, spp=64, grad_img=dLdimg)[0] for s in range(16)])
+
+    def fd_estimate(delta, h, n=12):
+        s2 = oracle.Scene(cam, theta - h * delta, theta + h * delta, albedo_const=0.8, max_depth=6)
+        est = []
+        for seed in range(n):
+            H, F = oracle.render_twostates(s2, seed=7 + seed, spp=64)
+            est.append(float(((F.astype(np.float64) - H) * dLdimg).sum() / (2 * h)))
+        return np.mean(est), np.std(est) / np.sqrt(n)
+
+    def check(delta, h):
+        proj = (runs * delta).sum(axis=(1, 2, 3))
+        adj, adj_sem = proj.mean(), proj.std() / np.sqrt(len(proj))
+        fd, fd_sem = fd_estimate(delta, h)
+        assert abs(fd - adj) < 4 * np.hypot(adj_sem, fd_sem) + 1e-4, (adj, adj_sem, fd, fd_sem)
+
+    # density-weighted direction: path replay's 1/sigma_t terms are heavy
+    # tailed in near-empty voxels, so weight the perturbation by the density
+    check(theta / theta.max(), 0.02)
+    # single voxels where the medium is dense
+    for flat in np.argsort(-theta.ravel())[:3]:
+        delta = np.zeros_like(theta)
+        delta[np.unravel_index(flat, theta.shape)] = 1.0
+        check(delta, 0.05)
