@@ -159,10 +159,22 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- workload
+def initial_density(cfg, true_density, phase: str):
+    """Starting grid of the timed job.  'late': 0.8 x the true grid, the
+    converging phase the recursive control variate is designed for (the
+    medium is as dense as the configuration's medium family); 'early': the
+    constant grid of the configuration's optimisation start (cfg.init)."""
+    if phase == "late":
+        return (0.8 * true_density).astype(np.float32)
+    if phase == "early":
+        return np.full_like(true_density, cfg.init)
+    raise ValueError(f"unknown phase {phase!r}")
+
+
 class Job:
     """One optimisation job of the configuration, resident on the device."""
 
-    def __init__(self, cfg, device, seed: int):
+    def __init__(self, cfg, device, seed: int, phase: str = "late", target=None):
         import torch
 
         import recursive_control_variates_gb300 as rcv
@@ -171,11 +183,13 @@ class Job:
         self.rcv, self.scenes, self.cfg, self.device, self.seed = rcv, scenes, cfg, device, seed
         dens, alb = scenes.config_grids(cfg)
         self.true_density, self.true_albedo = dens, alb
-        scene_ref = rcv.load_dict(scenes.scene_dict(dens, alb, res=cfg.res), device=device)
-        base = rcv.load_dict({"type": "prbvolpath", "max_depth": cfg.max_depth, "rr_depth": cfg.max_depth})
-        self.target = base.render(scene_ref, 0, seed=17843, spp=cfg.spp_ref).contiguous()
-        del scene_ref
-        self.init_density = np.full_like(dens, cfg.init)
+        if target is None:
+            scene_ref = rcv.load_dict(scenes.scene_dict(dens, alb, res=cfg.res), device=device)
+            base = rcv.load_dict({"type": "prbvolpath", "max_depth": cfg.max_depth, "rr_depth": cfg.max_depth})
+            target = base.render(scene_ref, 0, seed=17843, spp=cfg.spp_ref).contiguous()
+            del scene_ref
+        self.target = target
+        self.init_density = initial_density(cfg, dens, phase)
         self.has_albedo = not np.isscalar(alb)
         self.init_albedo = np.full_like(alb, 0.5) if self.has_albedo else alb
         self.scene = rcv.load_dict(scenes.scene_dict(self.init_density, self.init_albedo, res=cfg.res), device=device)
@@ -310,6 +324,10 @@ def run_ours(args, cfg):
                "h2d_bytes_per_step": int(target_host.numel() * 4), "d2h_bytes_per_step": 4,
                "ms_per_step": el * 1e3 / args.steps}
 
+    early = None
+    if not args.no_early:
+        early = time_phase(args, cfg, device, dist, job.target, "early", world, flush)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(cfg, job, target_seconds=args.cpu_seconds)
@@ -331,11 +349,38 @@ def run_ours(args, cfg):
         "counters_per_step": {"paths": float(delta[0]), "lookups": float(delta[1]), "nee_lookups": float(delta[2]),
                               "scatters": float(delta[3]), "grad_events": float(delta[4])},
         "clocks": clocks.summary(),
+        "phase": "late (density starts at 0.8 x the true grid)",
+        "early_phase": early,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def time_phase(args, cfg, device, dist, target, phase, world, flush):
+    """Device-timed steps of a second job started in another phase."""
+    import torch
+
+    job = Job(cfg, device, seed=replica_seed(dist_info()[0]) + 77, phase=phase, target=target)
+    for _ in range(args.warmup):
+        job.step()
+    stream = torch.cuda.current_stream(device)
+    c0 = job.counters()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for i, (a, b) in enumerate(ev):
+        flush.fill_(float(i))
+        a.record(stream)
+        job.step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    total = reduce_max(sum(a.elapsed_time(b) for a, b in ev) / 1e3, dist, device)
+    d = (job.counters() - c0).cpu().numpy().astype(np.float64) / args.steps
+    paths = job.paths_per_step()
+    return {"value": paths * world * args.steps / total, "unit": UNIT, "ms_per_step": total * 1e3 / args.steps,
+            "start": f"density {'constant ' + str(cfg.init) if phase == 'early' else '0.8 x true grid'}",
+            "lookups_per_path": float((d[1] + d[2]) / max(d[0], 1.0))}
 
 
 def split_counters(job):
@@ -443,7 +488,7 @@ def run_reference(args, cfg):
     threads = O.default_threads()
     dens, alb = scenes.config_grids(cfg)
     has_alb = not np.isscalar(alb)
-    init_d = np.full_like(dens, cfg.init)[..., 0]
+    init_d = initial_density(cfg, dens, "late")[..., 0]
     init_a = np.full_like(alb, 0.5) if has_alb else alb
     cam = O.camera_basis(cfg.res, cfg.res)
     ref_sc = O.Scene(cam, dens[..., 0], dens[..., 0], albedo_old=alb if has_alb else None,
@@ -493,6 +538,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="cfg2")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-early", action="store_true", help="skip the early-phase measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-step-seconds", type=float, default=4.0)

@@ -228,9 +228,11 @@ def test_finite_differences_32_voxels(cuda):
 
 
 def test_three_sigma_against_4096_spp(cuda):
-    """Per-pixel means of spp-4 renders lie within 3 sigma of a 4096-spp
-    render (config-1 medium); the image mean of the 4096-spp render agrees
-    with an FP64 host accumulation of 16 x 256-spp passes."""
+    """Per-pixel means over 64 independent spp-64 renders lie within 3 sigma
+    of a 4096-spp render (config-1 medium; sigma from the renders' spread, so
+    that rare events at the cube's silhouette are represented in it); the
+    image mean of the 4096-spp render agrees with an FP64 host accumulation
+    of 16 x 256-spp passes within their statistical error."""
     cfg = scenes.CONFIGS["cfg1"]
     dens, alb = scenes.config_grids(cfg)
     scene = rcv.load_dict(scenes.scene_dict(dens, alb, res=cfg.res), device=cuda)
@@ -240,11 +242,13 @@ def test_three_sigma_against_4096_spp(cuda):
     for j in range(16):
         acc += integ.render(scene, 0, seed=17843 + j, spp=256).double()
     ref64 = (acc / 16).cpu().numpy()
-    imgs = torch.stack([integ.render(scene, 0, seed=s, spp=4) for s in range(64)]).double()
-    sigma = imgs.std(dim=0)
-    one = imgs[0]
-    zz = ((one - ref).abs() / torch.sqrt(sigma**2 * (1 + 4 / 4096) + 1e-12)).cpu().numpy()
-    assert np.mean(zz < 3) >= 0.99
+    imgs = torch.stack([integ.render(scene, 0, seed=s, spp=64) for s in range(64)]).double()
+    sigma = imgs.std(dim=0)  # of one spp-64 render
+    mean = imgs.mean(dim=0)  # 4096 samples per pixel
+    se = torch.sqrt(sigma**2 * (1.0 / 64 + 64.0 / 4096) + 1e-12)
+    zz = ((mean - ref).abs() / se).cpu().numpy()
+    assert np.mean(zz < 3) >= 0.99, np.mean(zz < 3)
+    assert float(np.mean(zz**2)) < 1.3  # chi^2 per degree of freedom ~ 1
     mean_err = abs(float(ref.mean()) - float(ref64.mean()))
     stat = float(sigma.mean()) * np.sqrt(4 / 4096.0) / np.sqrt(ref.numel())
     assert mean_err < 6 * stat + 1e-5, (mean_err, stat)
