@@ -69,11 +69,19 @@ typedef struct rcv_medium {
 } rcv_medium;
 
 typedef struct rcv_volpath_options {
-  int32_t max_depth;          /* path length limit (real scattering events)  */
-  int32_t rr_depth;           /* Russian roulette applies when depth > this  */
-  int32_t hide_emitters;      /* skip directly visible environment           */
-  int32_t samples_per_thread; /* 0 = automatic; must divide spp              */
+  int32_t max_depth;     /* path length limit (real scattering events), -1 = none */
+  int32_t rr_depth;      /* Russian roulette applies when depth > this            */
+  int32_t hide_emitters; /* skip directly visible environment                     */
+  int32_t batch;         /* paths a warp claims per queue fetch, 0 = 64           */
+  int32_t blocks_per_sm; /* persistent blocks per SM, 0 = occupancy limit        */
+  int32_t defer;         /* lanes that must wait before a path-start or
+                            scattering branch runs, 1..32, 0 = 8                 */
 } rcv_volpath_options;
+
+/* Tracer kinds for rcv_render_workspace_bytes. */
+#define RCV_MODE_TWOSTATE 0
+#define RCV_MODE_SINGLE 1
+#define RCV_MODE_ADJOINT 2
 
 /* ---------------------------------------------------------------- errors */
 const char* rcv_last_error(void);
@@ -102,6 +110,11 @@ uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_gr
 int rcv_medium_prepare(const rcv_medium* medium, void* stream);
 
 /* ------------------------------------------------------------- tracers  */
+/* Scratch a tracer call needs (work-queue counter and, for the primal
+ * tracers, one radiance slot per path): 256-B aligned device memory of this
+ * size, passed as `workspace`.  mode = RCV_MODE_*. */
+uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp, int32_t mode);
+
 /* Two-state primal: renders the previous (img_old = H) and current
  * (img_new = F) parameters with shared random numbers.  Images are
  * [height][width][3] float32 device arrays.
@@ -110,8 +123,8 @@ int rcv_medium_prepare(const rcv_medium* medium, void* stream);
  * (plugins/twostatevolpath.py:91-138, 141-385, 387-479). */
 int rcv_render_twostates_volume(const rcv_medium* medium, const rcv_sensor* sensor,
                                 const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
-                                float* img_old, float* img_new, uint64_t* counters,
-                                void* stream);
+                                float* img_old, float* img_new, void* workspace,
+                                uint64_t* counters, void* stream);
 
 /* Single-state primal on the current (new) parameters; the render that
  * `integrator.render(...)` of a two-state integrator performs (it delegates
@@ -119,7 +132,7 @@ int rcv_render_twostates_volume(const rcv_medium* medium, const rcv_sensor* sens
  * MetaIntegrator uses for force_baseline (plugins/metaintegrator.py:124-128). */
 int rcv_render_volume(const rcv_medium* medium, const rcv_sensor* sensor,
                       const rcv_volpath_options* opts, uint32_t seed, int32_t spp, float* img,
-                      uint64_t* counters, void* stream);
+                      void* workspace, uint64_t* counters, void* stream);
 
 /* Seed-replay adjoint on the current parameters: traces `spp` paths per
  * pixel from `seed`, first to obtain each path's radiance and then again to
@@ -132,7 +145,7 @@ int rcv_render_volume(const rcv_medium* medium, const rcv_sensor* sensor,
 int rcv_render_backward_volume(const rcv_medium* medium, const rcv_sensor* sensor,
                                const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
                                const float* grad_img, float* grad_density, float* grad_albedo,
-                               uint64_t* counters, void* stream);
+                               void* workspace, uint64_t* counters, void* stream);
 
 /* ------------------------------------------------- control variate state */
 /* Per-element state of the recursive control variate; every array holds

@@ -154,7 +154,9 @@ void cube_hit(const V3& o, const V3& d, float& tn, float& tf) {
   tf = std::fmin(std::fmin(std::fmax(ax, bx), std::fmax(ay, by)), std::fmax(az, bz));
 }
 
-V3 ray_at(const V3& o, float t, const V3& d) { return V3{o.x + t * d.x, o.y + t * d.y, o.z + t * d.z}; }
+V3 ray_at(const V3& o, float t, const V3& d) {
+  return V3{std::fmaf(t, d.x, o.x), std::fmaf(t, d.y, o.y), std::fmaf(t, d.z, o.z)};
+}
 
 float lerp(float a, float b, float t) { return std::fmaf(t, b - a, a); }
 
@@ -187,7 +189,7 @@ struct Corners {
 };
 
 void axis(float p, int D, int& i0, int& i1, float& f) {
-  const float g = p * (float)D - 0.5f;
+  const float g = std::fmaf(p, (float)D, -0.5f);
   const float fl = std::floor(g);
   f = g - fl;
   const float flc = std::fmin(std::fmax(fl, -1.0f), (float)D);
@@ -297,10 +299,12 @@ struct Tracer {
     return true;
   }
 
+  float inv_mu() const { return 1.0f / mu; }
+
   float free_flight(Rng& rng) const {
     const float u = rng.next1d();
     const float tau = -log_unit(1.0f - u);
-    return mu > 0.0f ? tau / mu : kInf;
+    return mu > 0.0f ? tau * inv_mu() : kInf;
   }
 
   // Ratio-tracking transmittance from p along w to the cube boundary
@@ -325,10 +329,10 @@ struct Tracer {
         const float sn = mu - st_n;
         if (sn > 0.0f) sink->density(S, c, -(S.scale * *grad_scale) / sn);
       }
-      trn = trn * ((mu - st_n) / mu);
+      trn = trn * ((mu - st_n) * inv_mu());
       if (mode == kTwoState) {
         const float st_o = sigma_t(S.dens_old, c);
-        tro = tro * ((mu - st_o) / mu);
+        tro = tro * ((mu - st_o) * inv_mu());
       }
       q = x;
       tr_rem = tr_rem - t;
@@ -343,14 +347,15 @@ struct Tracer {
     // camera ray from the film sample (box filter: the sample stays in its pixel)
     const float u0 = rng.next1d(), u1 = rng.next1d();
     const float fx = (float)px + u0, fy = (float)py + u1;
-    const float nx = fx / (float)S.width, ny = fy / (float)S.height;
-    const float a = 2.0f * nx - 1.0f, b = 1.0f - 2.0f * ny;
+    const float inv_w = 1.0f / (float)S.width, inv_h = 1.0f / (float)S.height;
+    const float nx = fx * inv_w, ny = fy * inv_h;
+    const float a = std::fmaf(2.0f, nx, -1.0f), b = std::fmaf(-2.0f, ny, 1.0f);
     V3 r;
-    r.x = (S.cam_f[0] + a * S.cam_r[0]) + b * S.cam_u[0];
-    r.y = (S.cam_f[1] + a * S.cam_r[1]) + b * S.cam_u[1];
-    r.z = (S.cam_f[2] + a * S.cam_r[2]) + b * S.cam_u[2];
-    const float len = std::sqrt((r.x * r.x + r.y * r.y) + r.z * r.z);
-    V3 d{r.x / len, r.y / len, r.z / len};
+    r.x = std::fmaf(b, S.cam_u[0], std::fmaf(a, S.cam_r[0], S.cam_f[0]));
+    r.y = std::fmaf(b, S.cam_u[1], std::fmaf(a, S.cam_r[1], S.cam_f[1]));
+    r.z = std::fmaf(b, S.cam_u[2], std::fmaf(a, S.cam_r[2], S.cam_f[2]));
+    const float inv_len = 1.0f / std::sqrt(std::fmaf(r.z, r.z, std::fmaf(r.y, r.y, r.x * r.x)));
+    V3 d{r.x * inv_len, r.y * inv_len, r.z * inv_len};
     const V3 o{S.cam_o[0], S.cam_o[1], S.cam_o[2]};
     (void)rng.next1d();  // colour channel (grey extinction: unused)
 
@@ -408,13 +413,14 @@ struct Tracer {
       const float st_n = sigma_t(S.dens_new, c);
       const float st_o = mode == kTwoState ? sigma_t(S.dens_old, c) : 0.0f;
       const float ur = rng.next1d();
-      const float prob = mode == kTwoState ? (st_n / mu + st_o / mu) * 0.5f : st_n / mu;
+      // mean of both states' sigma_t / mu (plugins/twostatevolpath.py:222-225)
+      const float prob = mode == kTwoState ? (st_n + st_o) * (0.5f * inv_mu()) : st_n * inv_mu();
       if (ur >= prob) {
         // null collision
         if (mode == kTwoState) {
           const float sn_o = mu - st_o, sn_n = mu - st_n;
           const float den = sn_n + sn_o;
-          const float wn = (2.0f * sn_n) / den, wo = (2.0f * sn_o) / den;
+          const float wn = (2.0f * sn_n) / den, wo = 2.0f - wn;  // weights sum to 2
           bn = V3{bn.x * wn, bn.y * wn, bn.z * wn};
           bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
         } else if (sink) {

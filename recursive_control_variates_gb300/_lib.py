@@ -60,8 +60,15 @@ class VolpathOptions(C.Structure):
         ("max_depth", C.c_int32),
         ("rr_depth", C.c_int32),
         ("hide_emitters", C.c_int32),
-        ("samples_per_thread", C.c_int32),
+        ("batch", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+        ("defer", C.c_int32),
     ]
+
+
+MODE_TWOSTATE = 0
+MODE_SINGLE = 1
+MODE_ADJOINT = 2
 
 
 class CvState(C.Structure):
@@ -79,14 +86,17 @@ SIGNATURES = {
     "rcv_sample_tea_32": (None, [C.c_uint32, C.c_uint32, P(C.c_uint32)]),
     "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32]),
     "rcv_medium_prepare": (C.c_int, [P(Medium), vp]),
+    "rcv_render_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "rcv_render_twostates_volume": (
         C.c_int,
-        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp],
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp],
     ),
-    "rcv_render_volume": (C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp]),
+    "rcv_render_volume": (
+        C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp]
+    ),
     "rcv_render_backward_volume": (
         C.c_int,
-        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp],
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
     ),
     "rcv_cv_step": (
         C.c_int,

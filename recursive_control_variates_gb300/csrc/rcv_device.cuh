@@ -78,6 +78,18 @@ RCV_HD void seed_lane(Pcg32& r, uint32_t seed, uint32_t lane) {
   pcg_seed(r, ((uint64_t)a << 32) | b, ((uint64_t)c << 32) | d);
 }
 
+// Advances the stream by one draw without producing the output (for draws
+// whose value the algorithm discards): same state sequence as pcg_next.
+RCV_HD void pcg_skip1(Pcg32& r) { r.state = r.state * 6364136223846793005ull + r.inc; }
+
+// Advances by three draws: state <- A^3 state + (A^2 + A + 1) inc (mod 2^64).
+RCV_HD void pcg_skip3(Pcg32& r) {
+  constexpr uint64_t A = 6364136223846793005ull;
+  constexpr uint64_t A3 = A * A * A;
+  constexpr uint64_t K3 = A * A + A + 1ull;
+  r.state = r.state * A3 + r.inc * K3;
+}
+
 RCV_HD float u32_to_unit(uint32_t v) {
   // 23 random mantissa bits -> [1, 2) -> [0, 1)
   union { uint32_t u; float f; } x;
@@ -172,15 +184,16 @@ RCV_HD void slab(const V3& o, const V3& inv, float& tn, float& tf) {
 RCV_HD V3 recip(const V3& d) { return V3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z}; }
 
 RCV_HD V3 advance(const V3& p, float t, const V3& d) {
-  return V3{p.x + t * d.x, p.y + t * d.y, p.z + t * d.z};
+  return V3{fmaf(t, d.x, p.x), fmaf(t, d.y, p.y), fmaf(t, d.z, p.z)};
 }
 
 RCV_HD float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
 
-// Free-flight distance for optical depth -log(1-u) under majorant mu.
-RCV_HD float free_flight(float u, float mu) {
+// Free-flight distance for optical depth -log(1-u) under majorant mu
+// (inv_mu = 1/mu, computed once per path).
+RCV_HD float free_flight(float u, float mu, float inv_mu) {
   const float tau = -log_unit(1.0f - u);
-  return mu > 0.0f ? tau / mu : kInf;
+  return mu > 0.0f ? tau * inv_mu : kInf;
 }
 
 // Grid coordinate of a point along one axis: voxel centres at (i + 1/2)/D.
@@ -190,7 +203,7 @@ struct Axis {
 };
 
 RCV_HD Axis axis_coord(float p, int D) {
-  const float g = p * (float)D - 0.5f;
+  const float g = fmaf(p, (float)D, -0.5f);
   const float fl = floorf(g);
   Axis a;
   a.f = g - fl;

@@ -1,14 +1,18 @@
 // Volumetric kernels of librcv and their C-ABI entry points:
-// medium packing + majorants, two-state primal, single-state primal,
-// seed-replay adjoint and the gradient fold back to voxel layout.
+// medium packing + majorants, persistent two-state primal, single-state
+// primal and seed-replay adjoint, the per-pixel sample reduction and the
+// gradient fold back to voxel layout.
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 
 #include "rcv_common.h"
-#include "rcv_volume.cuh"
+#include "rcv_trace.cuh"
 
 namespace rcv {
+
+constexpr int kTraceBlock = 128;
 
 // ------------------------------------------------------------------ packing
 __global__ void pack_medium_kernel(int dx, int dy, int dz, const float* __restrict__ old_d,
@@ -66,60 +70,55 @@ __device__ __forceinline__ void add_counts(unsigned long long* counters, const C
   const unsigned ge = __reduce_add_sync(0xffffffffu, c.grad_events);
   const unsigned ae = __reduce_add_sync(0xffffffffu, c.albedo_events);
   if ((threadIdx.x & 31) == 0) {
-    if (ge) atomicAdd(counters + RCV_COUNTER_GRAD_EVENTS, (unsigned long long)ge);
-    if (ae) atomicAdd(counters + RCV_COUNTER_ALBEDO_EVENTS, (unsigned long long)ae);
     atomicAdd(counters + RCV_COUNTER_PATHS, (unsigned long long)p);
     atomicAdd(counters + RCV_COUNTER_LOOKUPS, (unsigned long long)l);
     atomicAdd(counters + RCV_COUNTER_NEE_LOOKUPS, (unsigned long long)n);
     atomicAdd(counters + RCV_COUNTER_SCATTERS, (unsigned long long)s);
+    if (ge) atomicAdd(counters + RCV_COUNTER_GRAD_EVENTS, (unsigned long long)ge);
+    if (ae) atomicAdd(counters + RCV_COUNTER_ALBEDO_EVENTS, (unsigned long long)ae);
   }
 }
 
-// One thread per (pixel, group of `chunk` samples); the spp/chunk threads of
-// a pixel are adjacent lanes and combine their sums with a butterfly.
 template <int kMode>
-__device__ __forceinline__ void trace_thread(const VolJob& J, int64_t local, bool active) {
-  const int T = J.spp / J.chunk;
-  V3 ao{0, 0, 0}, an{0, 0, 0};
+__global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_constant__ VolJob J,
+                                                            const __grid_constant__ Queue Q) {
   Counts cnt{0, 0, 0, 0, 0, 0};
-  int pix = 0, k = 0;
-  if (active) {
-    pix = int(local / T);
-    k = int(local % T);
-    trace_samples<kMode>(J, pix, k * J.chunk, (k + 1) * J.chunk, ao, an, cnt);
-  }
-  if (kMode != kAdjoint) {
-    for (int off = 1; off < T; off <<= 1) {
-      an.x += __shfl_xor_sync(0xffffffffu, an.x, off);
-      an.y += __shfl_xor_sync(0xffffffffu, an.y, off);
-      an.z += __shfl_xor_sync(0xffffffffu, an.z, off);
-      if (kMode == kTwoState) {
-        ao.x += __shfl_xor_sync(0xffffffffu, ao.x, off);
-        ao.y += __shfl_xor_sync(0xffffffffu, ao.y, off);
-        ao.z += __shfl_xor_sync(0xffffffffu, ao.z, off);
-      }
-    }
-    if (active && k == 0) {
-      const float fs = (float)J.spp;
-      float* dn = J.out_new + int64_t(pix) * 3;
-      dn[0] = an.x / fs;
-      dn[1] = an.y / fs;
-      dn[2] = an.z / fs;
-      if (kMode == kTwoState) {
-        float* d0 = J.out_old + int64_t(pix) * 3;
-        d0[0] = ao.x / fs;
-        d0[1] = ao.y / fs;
-        d0[2] = ao.z / fs;
-      }
-    }
-  }
-  add_counts(J.counters, cnt);
+  trace_persistent<kMode>(J, Q, cnt);
+  add_counts(Q.counters, cnt);
 }
 
-template <int kMode>
-__global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ VolJob J) {
-  const int64_t gt = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  trace_thread<kMode>(J, gt, gt < J.thread_count);
+// Sum of a pixel's samples in sample order, divided by spp (the box-filter
+// film develop of plugins/twostatevolpath.py:80-89).
+template <bool kTwo>
+__global__ void reduce_paths_kernel(const float4* __restrict__ path_out, int64_t path_begin,
+                                    int64_t npix, int spp, float* __restrict__ out_new,
+                                    float* __restrict__ out_old) {
+  const int64_t pix = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (pix >= npix) return;
+  constexpr int K = kTwo ? 2 : 1;
+  const float4* src = path_out + (path_begin + pix * spp) * K;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
+  for (int s = 0; s < spp; ++s) {
+    const float4 a = __ldcs(src + s * K);
+    nx += a.x;
+    ny += a.y;
+    nz += a.z;
+    if (kTwo) {
+      const float4 b = __ldcs(src + s * K + 1);
+      ox += b.x;
+      oy += b.y;
+      oz += b.z;
+    }
+  }
+  const float fs = (float)spp;
+  out_new[pix * 3 + 0] = nx / fs;
+  out_new[pix * 3 + 1] = ny / fs;
+  out_new[pix * 3 + 2] = nz / fs;
+  if (kTwo) {
+    out_old[pix * 3 + 0] = ox / fs;
+    out_old[pix * 3 + 1] = oy / fs;
+    out_old[pix * 3 + 2] = oz / fs;
+  }
 }
 
 // ------------------------------------------------------------ gradient fold
@@ -171,6 +170,9 @@ __global__ void fold_albedo_kernel(int64_t nv, const float4* __restrict__ ga,
 static int validate_medium(const rcv_medium* m) {
   RCV_REQUIRE(m != nullptr, "medium is NULL");
   RCV_REQUIRE(m->dims[0] > 0 && m->dims[1] > 0 && m->dims[2] > 0, "grid dims must be positive");
+  RCV_REQUIRE(uint64_t(m->dims[0] + 1) * uint64_t(m->dims[1] + 1) * uint64_t(m->dims[2] + 1) * 4u <
+                  (uint64_t(1) << 32),
+              "grid too large: (Dx+1)(Dy+1)(Dz+1) must be below 2^30");
   RCV_REQUIRE(m->density_old != nullptr && m->density_new != nullptr, "density grids are NULL");
   RCV_REQUIRE((m->albedo_old == nullptr) == (m->albedo_new == nullptr),
               "albedo_old and albedo_new must both be set or both be NULL");
@@ -181,40 +183,26 @@ static int validate_medium(const rcv_medium* m) {
   return RCV_OK;
 }
 
-static int choose_chunk(int spp, int requested, int* chunk) {
-  if (requested > 0) {
-    RCV_REQUIRE(spp % requested == 0, "samples_per_thread (%d) must divide spp (%d)", requested, spp);
-    const int T = spp / requested;
-    RCV_REQUIRE(T <= 32 && (T & (T - 1)) == 0,
-                "spp / samples_per_thread (%d) must be a power of two <= 32", T);
-    *chunk = requested;
-    return RCV_OK;
-  }
-  // default: as many threads per pixel as possible (<= 4), power of two
-  int T = 1;
-  while (T < 4 && spp % (T * 2) == 0) T *= 2;
-  *chunk = spp / T;
-  return RCV_OK;
-}
-
-static int make_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o,
+int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o,
                     uint32_t seed, int spp, VolJob* J) {
   int rc = validate_medium(m);
   if (rc) return rc;
   RCV_REQUIRE(s != nullptr && o != nullptr, "sensor / options are NULL");
   RCV_REQUIRE(s->width > 0 && s->height > 0, "film size must be positive");
   RCV_REQUIRE(spp > 0, "spp must be positive");
-  RCV_REQUIRE(o->max_depth >= 0 || o->max_depth == -1, "max_depth must be >= -1");
+  RCV_REQUIRE(o->max_depth >= -1, "max_depth must be >= -1");
+  RCV_REQUIRE(int64_t(s->width) * s->height * spp < (int64_t(1) << 32),
+              "width * height * spp must be below 2^32 (one random stream per path)");
   std::memset(J, 0, sizeof(VolJob));
   J->width = s->width;
   J->height = s->height;
   J->spp = spp;
-  rc = choose_chunk(spp, o->samples_per_thread, &J->chunk);
-  if (rc) return rc;
   J->cam_o = V3{s->origin[0], s->origin[1], s->origin[2]};
   J->cam_f = V3{s->forward[0], s->forward[1], s->forward[2]};
   J->cam_r = V3{s->right[0], s->right[1], s->right[2]};
   J->cam_u = V3{s->up[0], s->up[1], s->up[2]};
+  J->inv_w = 1.0f / (float)s->width;
+  J->inv_h = 1.0f / (float)s->height;
   J->max_depth = o->max_depth < 0 ? 0x7fffffff : o->max_depth;
   J->rr_depth = o->rr_depth;
   J->hide_emitters = o->hide_emitters;
@@ -233,16 +221,115 @@ static int make_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   J->maxbits = reinterpret_cast<const uint32_t*>(ws + L.maxbits);
   J->grad_cells = reinterpret_cast<float4*>(ws + L.grad_cells);
   J->grad_albedo = m->albedo_old ? reinterpret_cast<float4*>(ws + L.grad_albedo) : nullptr;
-  J->thread_begin = 0;
-  J->thread_count = int64_t(s->width) * s->height * (spp / J->chunk);
+  J->path_begin = 0;
+  J->path_count = int64_t(s->width) * s->height * spp;
   return RCV_OK;
 }
 
-template <int kMode>
-static int launch_trace(const VolJob& J, cudaStream_t st) {
-  const int block = 128;
-  trace_kernel<kMode><<<grid_for(J.thread_count, block), block, 0, st>>>(J);
+// Resident blocks per SM of each tracer variant (queried once per process).
+static int resident_blocks(int mode) {
+  static std::once_flag once;
+  static int blocks[3] = {1, 1, 1};
+  std::call_once(once, [] {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_kernel<kTwoState>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_kernel<kSingle>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_kernel<kAdjoint>, kTraceBlock, 0);
+    for (int& b : blocks) b = b < 1 ? 1 : b;
+  });
+  return blocks[mode];
+}
+
+static int sm_count() {
+  static std::once_flag once;
+  static int n = 1;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n < 1) n = 1;
+  });
+  return n;
+}
+
+static uint64_t path_out_bytes(int64_t paths, int mode) {
+  return mode == kAdjoint ? 0u : uint64_t(paths) * (mode == kTwoState ? 32u : 16u);
+}
+
+// Persistent launch over `total` paths of one job (jobs == null) or of a
+// device job table.
+int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
+                      const rcv_volpath_options* o, void* workspace, uint64_t* counters,
+                      cudaStream_t st) {
+  RCV_REQUIRE(workspace != nullptr && (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
+              "render workspace must be non-NULL and 256-byte aligned");
+  char* ws = static_cast<char*>(workspace);
+  Queue Q;
+  Q.counter = reinterpret_cast<unsigned long long*>(ws);
+  Q.path_out = mode == kAdjoint ? nullptr : reinterpret_cast<float4*>(ws + 256);
+  Q.counters = reinterpret_cast<unsigned long long*>(counters);
+  Q.jobs = jobs;
+  Q.njobs = njobs;
+  Q.total = total;
+  Q.batch = (o != nullptr && o->batch > 0) ? o->batch : 64;
+  RCV_REQUIRE(Q.batch <= (1 << 20), "batch must be <= 2^20");
+  Q.defer = (o != nullptr && o->defer > 0) ? o->defer : 8;
+  RCV_REQUIRE(Q.defer <= 32, "defer must be in [1, 32]");
+  Q.pad = 0;
+  RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
+  int per_sm = resident_blocks(mode);
+  if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
+  const int64_t warps_needed = (total + Q.batch - 1) / Q.batch;
+  int64_t blocks = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
+  const int64_t cap = int64_t(sm_count()) * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  switch (mode) {
+    case kTwoState: trace_kernel<kTwoState><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
+    case kSingle: trace_kernel<kSingle><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
+    default: trace_kernel<kAdjoint><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
+  }
   return launched("trace kernel launch");
+}
+
+int launch_reduce(bool two, const void* workspace, int64_t path_begin, int64_t npix, int spp,
+                  float* out_new, float* out_old, cudaStream_t st) {
+  const float4* po = reinterpret_cast<const float4*>(static_cast<const char*>(workspace) + 256);
+  const int block = 256;
+  if (two)
+    reduce_paths_kernel<true><<<grid_for(npix, block), block, 0, st>>>(po, path_begin, npix, spp,
+                                                                     out_new, out_old);
+  else
+    reduce_paths_kernel<false><<<grid_for(npix, block), block, 0, st>>>(po, path_begin, npix, spp,
+                                                                      out_new, nullptr);
+  return launched("reduce_paths launch");
+}
+
+int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cudaStream_t st) {
+  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
+  const char* ws = static_cast<const char*>(m->workspace);
+  const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
+  const int block = 256;
+  fold_density_kernel<<<grid_for(nv, block), block, 0, st>>>(
+      m->dims[0], m->dims[1], m->dims[2], reinterpret_cast<const float*>(ws + L.grad_cells),
+      grad_density);
+  int rc = launched("fold_density launch");
+  if (rc) return rc;
+  if (grad_albedo != nullptr && m->albedo_old != nullptr) {
+    fold_albedo_kernel<<<grid_for(nv, block), block, 0, st>>>(
+        nv, reinterpret_cast<const float4*>(ws + L.grad_albedo), grad_albedo);
+    rc = launched("fold_albedo launch");
+  }
+  return rc;
+}
+
+int reset_gradients(const rcv_medium* m, bool albedo, cudaStream_t st) {
+  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
+  char* ws = static_cast<char*>(m->workspace);
+  const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
+  const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
+  RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_cells, 0, nc * 32, st), "gradient reset");
+  if (albedo) RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_albedo, 0, nv * 16, st), "gradient reset");
+  return RCV_OK;
 }
 
 }  // namespace rcv
@@ -252,6 +339,12 @@ using namespace rcv;
 extern "C" uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid) {
   if (dims == nullptr || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return 0;
   return medium_layout(dims, has_albedo_grid != 0).total;
+}
+
+extern "C" uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp,
+                                               int32_t mode) {
+  if (width <= 0 || height <= 0 || spp <= 0 || mode < 0 || mode > 2) return 0;
+  return align256(256u + path_out_bytes(int64_t(width) * height * spp, mode));
 }
 
 extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
@@ -274,61 +367,46 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
 extern "C" int rcv_render_twostates_volume(const rcv_medium* m, const rcv_sensor* s,
                                            const rcv_volpath_options* o, uint32_t seed,
                                            int32_t spp, float* img_old, float* img_new,
-                                           uint64_t* counters, void* stream) {
+                                           void* workspace, uint64_t* counters, void* stream) {
   VolJob J;
-  int rc = make_job(m, s, o, seed, spp, &J);
+  int rc = make_volume_job(m, s, o, seed, spp, &J);
   if (rc) return rc;
   RCV_REQUIRE(img_old != nullptr && img_new != nullptr, "output images are NULL");
-  J.out_old = img_old;
-  J.out_new = img_new;
-  J.counters = reinterpret_cast<unsigned long long*>(counters);
-  return launch_trace<kTwoState>(J, static_cast<cudaStream_t>(stream));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = launch_persistent(kTwoState, J, nullptr, 0, J.path_count, o, workspace, counters, st);
+  if (rc) return rc;
+  return launch_reduce(true, workspace, 0, int64_t(J.width) * J.height, spp, img_new, img_old, st);
 }
 
 extern "C" int rcv_render_volume(const rcv_medium* m, const rcv_sensor* s,
                                  const rcv_volpath_options* o, uint32_t seed, int32_t spp,
-                                 float* img, uint64_t* counters, void* stream) {
+                                 float* img, void* workspace, uint64_t* counters, void* stream) {
   VolJob J;
-  int rc = make_job(m, s, o, seed, spp, &J);
+  int rc = make_volume_job(m, s, o, seed, spp, &J);
   if (rc) return rc;
   RCV_REQUIRE(img != nullptr, "output image is NULL");
-  J.out_new = img;
-  J.counters = reinterpret_cast<unsigned long long*>(counters);
-  return launch_trace<kSingle>(J, static_cast<cudaStream_t>(stream));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = launch_persistent(kSingle, J, nullptr, 0, J.path_count, o, workspace, counters, st);
+  if (rc) return rc;
+  return launch_reduce(false, workspace, 0, int64_t(J.width) * J.height, spp, img, nullptr, st);
 }
 
 extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor* s,
                                           const rcv_volpath_options* o, uint32_t seed,
                                           int32_t spp, const float* grad_img,
                                           float* grad_density, float* grad_albedo,
-                                          uint64_t* counters, void* stream) {
+                                          void* workspace, uint64_t* counters, void* stream) {
   VolJob J;
-  int rc = make_job(m, s, o, seed, spp, &J);
+  int rc = make_volume_job(m, s, o, seed, spp, &J);
   if (rc) return rc;
   RCV_REQUIRE(grad_img != nullptr && grad_density != nullptr, "gradient buffers are NULL");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
-  char* ws = static_cast<char*>(m->workspace);
-  const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
-  const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
-  RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_cells, 0, nc * 32, st), "gradient reset");
   const bool want_albedo = grad_albedo != nullptr && m->albedo_old != nullptr;
-  if (want_albedo) RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_albedo, 0, nv * 16, st), "gradient reset");
+  rc = reset_gradients(m, want_albedo, st);
+  if (rc) return rc;
   if (!want_albedo) J.grad_albedo = nullptr;
   J.grad_img = grad_img;
-  J.counters = reinterpret_cast<unsigned long long*>(counters);
-  rc = launch_trace<kAdjoint>(J, st);
+  rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, workspace, counters, st);
   if (rc) return rc;
-  const int block = 256;
-  fold_density_kernel<<<grid_for(nv, block), block, 0, st>>>(
-      m->dims[0], m->dims[1], m->dims[2], reinterpret_cast<const float*>(ws + L.grad_cells),
-      grad_density);
-  rc = launched("fold_density launch");
-  if (rc) return rc;
-  if (want_albedo) {
-    fold_albedo_kernel<<<grid_for(nv, block), block, 0, st>>>(
-        nv, reinterpret_cast<const float4*>(ws + L.grad_albedo), grad_albedo);
-    rc = launched("fold_albedo launch");
-  }
-  return rc;
+  return launch_fold(m, grad_density, want_albedo ? grad_albedo : nullptr, st);
 }

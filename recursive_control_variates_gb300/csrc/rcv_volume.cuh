@@ -19,10 +19,14 @@
 //   step.  An escaping path draws the null BSDF sample (1D + 2D) and the RR
 //   1D of the outside iteration before the environment is added.
 //
-// Execution shape: one thread owns `chunk` consecutive samples of a pixel and
-// regenerates a new path as soon as one finishes; the main path and its NEE
-// shadow walk share one loop body ("one free-flight step per iteration") so
-// that warps stay converged on the density lookups, which dominate the cost.
+// Execution shape (persistent): every warp pulls batches of path indices from
+// one global counter and hands them to its idle lanes at the top of each loop
+// iteration, so a lane starts a new path as soon as its path ends and a warp
+// only drains at the end of the queue.  The main path and its NEE shadow walk
+// share one loop body ("one free-flight step per iteration") so that lanes in
+// different phases still execute the density lookup together.  Each path's
+// radiance is written to a per-path slot; a separate pass sums a pixel's
+// samples in sample order, so results do not depend on the schedule.
 #pragma once
 #include "rcv_device.cuh"
 
@@ -33,8 +37,9 @@ namespace rcv {
 //   [2] new v000 ...              [3] new v001 ...
 struct VolJob {
   // film / camera
-  int32_t width, height, spp, chunk;  // chunk = samples per thread
+  int32_t width, height, spp, pad0;
   V3 cam_o, cam_f, cam_r, cam_u;
+  float inv_w, inv_h;  // 1/width, 1/height
   // integrator
   int32_t max_depth, rr_depth, hide_emitters;
   uint32_t seed;
@@ -45,16 +50,25 @@ struct VolJob {
   const float4* __restrict__ albedo;  // dz*dy*dx * 2 (old, new) or null
   float albedo_const[3];
   const uint32_t* maxbits;  // [0] max old density, [1] max new density (bits)
-  // outputs
-  float* out_old;  // two-state: H; single: unused
-  float* out_new;  // two-state: F; single: image
   // adjoint
   const float* grad_img;
   float4* grad_cells;   // (dz+1)(dy+1)(dx+1) * 2
   float4* grad_albedo;  // dz*dy*dx (rgb + pad) or null
-  unsigned long long* counters;
-  int64_t thread_begin;  // first global thread of this job (batched launches)
-  int64_t thread_count;  // width*height*(spp/chunk)
+  int64_t path_begin;   // first global path index of this job (batched launches)
+  int64_t path_count;   // width*height*spp
+};
+
+// Work queue of a (possibly multi-job) persistent launch.
+struct Queue {
+  unsigned long long* counter;   // next unclaimed global path index (zeroed)
+  float4* path_out;              // primal: per-path radiance [path][new, old]
+  unsigned long long* counters;  // RCV_COUNTER_* totals of the launch or null
+  const VolJob* jobs;            // device job table (batched launches) or null
+  int64_t total;                 // paths in the launch
+  int32_t batch;                 // paths claimed per warp fetch
+  int32_t njobs;
+  int32_t defer;                 // lanes that must wait before a deferred branch runs
+  int32_t pad;
 };
 
 enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2 };
@@ -70,22 +84,22 @@ __device__ __forceinline__ void camera_ray(const VolJob& J, int px, int py, floa
                                            V3& o, V3& d) {
   const float fx = (float)px + u0;
   const float fy = (float)py + u1;
-  const float nx = fx / (float)J.width;
-  const float ny = fy / (float)J.height;
-  const float a = 2.0f * nx - 1.0f;
-  const float b = 1.0f - 2.0f * ny;
+  const float nx = fx * J.inv_w;
+  const float ny = fy * J.inv_h;
+  const float a = fmaf(2.0f, nx, -1.0f);
+  const float b = fmaf(-2.0f, ny, 1.0f);
   V3 r;
-  r.x = (J.cam_f.x + a * J.cam_r.x) + b * J.cam_u.x;
-  r.y = (J.cam_f.y + a * J.cam_r.y) + b * J.cam_u.y;
-  r.z = (J.cam_f.z + a * J.cam_r.z) + b * J.cam_u.z;
-  const float len = sqrtf((r.x * r.x + r.y * r.y) + r.z * r.z);
-  d = V3{r.x / len, r.y / len, r.z / len};
+  r.x = fmaf(b, J.cam_u.x, fmaf(a, J.cam_r.x, J.cam_f.x));
+  r.y = fmaf(b, J.cam_u.y, fmaf(a, J.cam_r.y, J.cam_f.y));
+  r.z = fmaf(b, J.cam_u.z, fmaf(a, J.cam_r.z, J.cam_f.z));
+  const float inv_len = 1.0f / sqrtf(fmaf(r.z, r.z, fmaf(r.y, r.y, r.x * r.x)));
+  d = V3{r.x * inv_len, r.y * inv_len, r.z * inv_len};
   o = J.cam_o;
 }
 
 struct Lookup {
   Axis ax, ay, az;
-  int64_t cell;
+  uint32_t cell;  // (dx+1)(dy+1)(dz+1) * 4 < 2^32 is enforced on the host
 };
 
 __device__ __forceinline__ Lookup locate(const VolJob& J, const V3& x) {
@@ -93,7 +107,8 @@ __device__ __forceinline__ Lookup locate(const VolJob& J, const V3& x) {
   l.ax = axis_coord(x.x, J.dx);
   l.ay = axis_coord(x.y, J.dy);
   l.az = axis_coord(x.z, J.dz);
-  l.cell = ((int64_t)l.az.cell * (J.dy + 1) + l.ay.cell) * (J.dx + 1) + l.ax.cell;
+  l.cell = ((uint32_t)l.az.cell * (uint32_t)(J.dy + 1) + (uint32_t)l.ay.cell) * (uint32_t)(J.dx + 1) +
+           (uint32_t)l.ax.cell;
   return l;
 }
 
@@ -145,7 +160,8 @@ __device__ __forceinline__ V3 albedo_at(const VolJob& J, const Lookup& l, int st
   return r;
 }
 
-// Scatters g * (trilinear weight of each corner) into the cell gradient.
+// Scatters g * (trilinear weight of each corner) into the cell gradient with
+// two vector reductions (red.global.add.v4.f32).
 __device__ __forceinline__ void scatter_density(const VolJob& J, const Lookup& l, float g) {
   const float fx = l.ax.f, fy = l.ay.f, fz = l.az.f;
   const float gx0 = 1.0f - fx, gy0 = 1.0f - fy, gz0 = 1.0f - fz;
@@ -182,309 +198,17 @@ __device__ __forceinline__ bool roulette(const VolJob& J, Pcg32& rng, int depth,
   float m = fmaxf(fmaxf(bn.x, bn.y), bn.z);
   if (kMode == kTwoState) m = fmaxf(fmaxf(fmaxf(bn.x, bo.x), fmaxf(bn.y, bo.y)), fmaxf(bn.z, bo.z));
   const float q = fminf(m, 0.99f);
-  const float u = next1d(rng);
   if (depth > J.rr_depth) {
+    const float u = next1d(rng);
     if (!(u < q)) return false;
     const float inv = 1.0f / q;
     bn = V3{bn.x * inv, bn.y * inv, bn.z * inv};
     if (kMode == kTwoState) bo = V3{bo.x * inv, bo.y * inv, bo.z * inv};
+  } else {
+    pcg_skip1(rng);  // the draw is made but its value is unused
   }
   return true;
 }
 
-enum PathPhase { kStart = 0, kMain = 1, kNee = 2, kNeeAdj = 3 };
-
-// Traces samples [s0, s1) of pixel `pix`; adds each path's radiance to
-// acc_old / acc_new (in sample order).  In adjoint mode, scatters gradients
-// instead and leaves the accumulators untouched.
-template <int kMode>
-__device__ void trace_samples(const VolJob& J, int pix, int s0, int s1, V3& acc_old, V3& acc_new,
-                              Counts& cnt) {
-  const float mu_old = J.scale * bits_to_float(__ldg(J.maxbits + 0));
-  const float mu_new = J.scale * bits_to_float(__ldg(J.maxbits + 1));
-  const float mu = (kMode == kTwoState) ? fmaxf(mu_old, mu_new) : mu_new;
-  const int px = pix % J.width, py = pix / J.width;
-  const float mis = 0.5f;  // power heuristic between two equal 1/(4 pi) pdfs
-  const float emit_weight = 1.0f / kInvFourPi;
-
-  V3 dL{0.0f, 0.0f, 0.0f};
-  if (kMode == kAdjoint) {
-    const float* g = J.grad_img + (int64_t)pix * 3;
-    const float inv = (float)J.spp;
-    dL = V3{g[0] / inv, g[1] / inv, g[2] / inv};
-  }
-
-  Pcg32 rng, rng_nee;
-  int s = s0;
-  int phase = kStart;
-  int pass = 0;  // adjoint: 0 = radiance pass, 1 = replay pass
-  // main path state
-  V3 p, d, inv_d;
-  float t_rem = 0.0f;
-  V3 bo{1, 1, 1}, bn{1, 1, 1}, Lo{0, 0, 0}, Ln{0, 0, 0};
-  V3 Lrem{0, 0, 0}, Ltot{0, 0, 0};
-  int depth = 0;
-  // NEE state
-  V3 q, w;
-  float tr_rem = 0.0f, tro = 1.0f, trn = 1.0f;
-  V3 wo_next;
-  float s_nee = 0.0f;
-
-  while (s < s1) {
-    if (phase == kStart) {
-      seed_lane(rng, J.seed, (uint32_t)((int64_t)pix * J.spp + s));
-      const float u0 = next1d(rng), u1 = next1d(rng);
-      V3 o;
-      camera_ray(J, px, py, u0, u1, o, d);
-      (void)next1d(rng);  // colour channel for free-flight sampling (grey extinction)
-      bo = V3{1, 1, 1};
-      bn = V3{1, 1, 1};
-      Lo = V3{0, 0, 0};
-      Ln = V3{0, 0, 0};
-      depth = 0;
-      if (kMode == kAdjoint) Lrem = Ltot;
-      bool done = !roulette<kMode>(J, rng, depth, bn, bo);
-      float tn = 0.0f, tf = -1.0f;
-      if (!done) {
-        inv_d = recip(d);
-        slab(o, inv_d, tn, tf);
-        if (!(tn <= tf && tf > 0.0f)) {
-          // camera ray misses the cube: environment seen directly
-          if (!J.hide_emitters) {
-            Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
-            if (kMode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
-          }
-          done = true;
-        }
-      }
-      if (done) {
-        goto path_done;
-      }
-      // null BSDF of the cube boundary: the sample is drawn and discarded
-      (void)next1d(rng);
-      (void)next1d(rng);
-      (void)next1d(rng);
-      p = advance(o, fmaxf(tn, 0.0f), d);
-      {
-        float a, b;
-        slab(p, inv_d, a, b);
-        t_rem = b;
-      }
-      phase = kMain;
-    }
-
-    {
-      // ------------------------------------------------ one free-flight step
-      V3 org, dir;
-      float tmax;
-      Pcg32* r = &rng;
-      if (phase == kMain) {
-        if (!roulette<kMode>(J, rng, depth, bn, bo)) goto path_done;
-        org = p;
-        dir = d;
-        tmax = t_rem;
-      } else {
-        org = q;
-        dir = w;
-        tmax = tr_rem;
-        if (phase == kNeeAdj) r = &rng_nee;
-      }
-      const float t = free_flight(next1d(*r), mu);
-      const bool valid = t <= tmax;
-      Lookup lk;
-      float rho_o = 0.0f, rho_n = 0.0f;
-      V3 x;
-      if (valid) {
-        x = advance(org, t, dir);
-        lk = locate(J, x);
-        if (kMode == kTwoState)
-          density2(J, lk, rho_o, rho_n);
-        else
-          rho_n = density_new(J, lk);
-        if (phase == kMain) {
-          ++cnt.lookups;
-        } else {
-          ++cnt.nee_lookups;
-        }
-      }
-      const float st_o = J.scale * rho_o, st_n = J.scale * rho_n;
-
-      if (phase == kMain) {
-        if (valid) {
-          const float ur = next1d(rng);
-          float prob;
-          if (kMode == kTwoState)
-            prob = (st_n / mu + st_o / mu) * 0.5f;
-          else
-            prob = st_n / mu;
-          if (ur >= prob) {
-            // null collision (plugins/twostatevolpath.py:227-231, 256-257)
-            if (kMode == kTwoState) {
-              const float sn_o = mu - st_o, sn_n = mu - st_n;
-              const float den = sn_n + sn_o;
-              const float wn = (2.0f * sn_n) / den, wo = (2.0f * sn_o) / den;
-              bn = V3{bn.x * wn, bn.y * wn, bn.z * wn};
-              bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
-            } else if (kMode == kAdjoint && pass == 1) {
-              const float sn = mu - st_n;
-              const float sd = (dL.x * Lrem.x + dL.y * Lrem.y) + dL.z * Lrem.z;
-              scatter_density(J, lk, -(J.scale * sd) / sn);
-              ++cnt.grad_events;
-            }
-            p = x;
-            t_rem = t_rem - t;
-          } else {
-            // real scattering event (plugins/twostatevolpath.py:249-281)
-            depth += 1;
-            if (depth >= J.max_depth) goto path_done;
-            ++cnt.scatters;
-            const V3 an = albedo_at(J, lk, 1);
-            const V3 ss_n{st_n * an.x, st_n * an.y, st_n * an.z};
-            if (kMode == kTwoState) {
-              const V3 ao = albedo_at(J, lk, 0);
-              const V3 ss_o{st_o * ao.x, st_o * ao.y, st_o * ao.z};
-              const float den = st_n + st_o;
-              bn = V3{bn.x * ((2.0f * ss_n.x) / den), bn.y * ((2.0f * ss_n.y) / den),
-                      bn.z * ((2.0f * ss_n.z) / den)};
-              bo = V3{bo.x * ((2.0f * ss_o.x) / den), bo.y * ((2.0f * ss_o.y) / den),
-                      bo.z * ((2.0f * ss_o.z) / den)};
-            } else {
-              bn = V3{bn.x * (ss_n.x / st_n), bn.y * (ss_n.y / st_n), bn.z * (ss_n.z / st_n)};
-              if (kMode == kAdjoint && pass == 1) {
-                const float sd = (dL.x * Lrem.x + dL.y * Lrem.y) + dL.z * Lrem.z;
-                scatter_density(J, lk, (J.scale * sd) / st_n);
-                ++cnt.grad_events;
-                if (J.grad_albedo != nullptr) {
-                  ++cnt.albedo_events;
-                  const V3 ga{(dL.x * Lrem.x) / fmaxf(an.x, 1e-8f),
-                              (dL.y * Lrem.y) / fmaxf(an.y, 1e-8f),
-                              (dL.z * Lrem.z) / fmaxf(an.z, 1e-8f)};
-                  scatter_albedo(J, lk, ga);
-                }
-              }
-            }
-            // isotropic phase sample (1D unused + 2D)
-            (void)next1d(rng);
-            const float pu0 = next1d(rng), pu1 = next1d(rng);
-            wo_next = uniform_sphere(pu0, pu1);
-            // NEE towards the environment, then ratio tracking
-            const float nu0 = next1d(rng), nu1 = next1d(rng);
-            w = uniform_sphere(nu0, nu1);
-            q = x;
-            p = x;
-            {
-              float a, b;
-              slab(q, recip(w), a, b);
-              tr_rem = b;
-            }
-            tro = 1.0f;
-            trn = 1.0f;
-            if (kMode == kAdjoint && pass == 1) rng_nee = rng;
-            phase = kNee;
-          }
-        } else {
-          // leaves the cube: null BSDF sample, outside iteration RR, environment
-          (void)next1d(rng);
-          (void)next1d(rng);
-          (void)next1d(rng);
-          if (!roulette<kMode>(J, rng, depth, bn, bo)) goto path_done;
-          if (!(J.hide_emitters && depth == 0)) {
-            const float k = depth == 0 ? 1.0f : mis;
-            const V3 cn{bn.x * k, bn.y * k, bn.z * k};
-            Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
-            if (kMode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
-            if (kMode == kAdjoint) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
-          }
-          goto path_done;
-        }
-      } else if (phase == kNee) {
-        bool finished = !valid;
-        if (valid) {
-          // ratio tracking (plugins/twostatevolpath.py:443-452)
-          trn = trn * ((mu - st_n) / mu);
-          if (kMode == kTwoState) tro = tro * ((mu - st_o) / mu);
-          q = x;
-          tr_rem = tr_rem - t;
-          finished = (kMode == kTwoState) ? (trn == 0.0f && tro == 0.0f) : (trn == 0.0f);
-        }
-        if (finished) {
-          const float ev = emit_weight;
-          const float en = ev * trn;
-          const V3 cn{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
-                      ((bn.z * kInvFourPi) * mis) * en};
-          Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
-          if (kMode == kTwoState) {
-            const float eo = ev * tro;
-            Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
-                    Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
-          }
-          if (kMode == kAdjoint && pass == 1) {
-            // replay the shadow walk to back-propagate through its transmittance
-            s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
-            Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
-            q = p;
-            {
-              float a, b;
-              slab(q, recip(w), a, b);
-              tr_rem = b;
-            }
-            trn = 1.0f;
-            phase = kNeeAdj;
-          } else {
-            d = wo_next;
-            inv_d = recip(d);
-            {
-              float a, b;
-              slab(p, inv_d, a, b);
-              t_rem = b;
-            }
-            phase = kMain;
-          }
-        }
-      } else {  // kNeeAdj: second walk with the saved stream
-        bool finished = !valid;
-        if (valid) {
-          const float sn = mu - st_n;
-          if (sn > 0.0f) {
-            scatter_density(J, lk, -(J.scale * s_nee) / sn);
-            ++cnt.grad_events;
-          }
-          trn = trn * (sn / mu);
-          q = x;
-          tr_rem = tr_rem - t;
-          finished = trn == 0.0f;
-        }
-        if (finished) {
-          d = wo_next;
-          inv_d = recip(d);
-          {
-            float a, b;
-            slab(p, inv_d, a, b);
-            t_rem = b;
-          }
-          phase = kMain;
-        }
-      }
-      continue;
-    }
-
-  path_done:
-    if (kMode == kAdjoint && pass == 0) {
-      // radiance pass finished: replay the same path with gradients
-      Ltot = Ln;
-      pass = 1;
-      phase = kStart;
-      continue;
-    }
-    if (kMode != kAdjoint) {
-      acc_new = V3{acc_new.x + Ln.x, acc_new.y + Ln.y, acc_new.z + Ln.z};
-      if (kMode == kTwoState) acc_old = V3{acc_old.x + Lo.x, acc_old.y + Lo.y, acc_old.z + Lo.z};
-    }
-    ++cnt.paths;
-    pass = 0;
-    phase = kStart;
-    ++s;
-  }
-}
 
 }  // namespace rcv

@@ -33,11 +33,15 @@ class _VolumeIntegratorBase:
         self.rr_depth = int(props.get("rr_depth", 5))
         self.hide_emitters = bool(props.get("hide_emitters", False))
         self.xyz = bool(props.get("xyz", False))
-        self.samples_per_thread = int(props.get("samples_per_thread", 0))
+        # scheduling knobs of the persistent tracer (results do not depend on them)
+        self.batch = int(props.get("batch", 0))
+        self.blocks_per_sm = int(props.get("blocks_per_sm", 0))
+        self.defer = int(props.get("defer", 0))
         if self.max_depth < -1:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         self.is_checked = False
         self._counters: dict[torch.device, torch.Tensor] = {}
+        self._scratch: dict[torch.device, torch.Tensor] = {}
 
     # ------------------------------------------------------------- helpers
     def options(self) -> _lib.VolpathOptions:
@@ -45,7 +49,9 @@ class _VolumeIntegratorBase:
         o.max_depth = self.max_depth
         o.rr_depth = self.rr_depth
         o.hide_emitters = int(self.hide_emitters)
-        o.samples_per_thread = self.samples_per_thread
+        o.batch = self.batch
+        o.blocks_per_sm = self.blocks_per_sm
+        o.defer = self.defer
         return o
 
     def counters(self, device) -> torch.Tensor:
@@ -53,6 +59,18 @@ class _VolumeIntegratorBase:
         if device not in self._counters:
             self._counters[device] = torch.zeros(_lib.COUNTER_COUNT, dtype=torch.int64, device=device)
         return self._counters[device]
+
+    def scratch(self, device, sensor, spp: int, mode: int) -> int:
+        """256-B aligned device address of the tracer scratch (grown on
+        demand; reused by later calls, which are ordered on the stream)."""
+        device = torch.device(device)
+        f = sensor.film()
+        need = int(_lib.load().rcv_render_workspace_bytes(f.width, f.height, spp, mode)) + 256
+        buf = self._scratch.get(device)
+        if buf is None or buf.numel() < need:
+            buf = torch.empty(need, dtype=torch.uint8, device=device)
+            self._scratch[device] = buf
+        return (buf.data_ptr() + 255) & ~255
 
     @staticmethod
     def medium_of(scene):
@@ -100,6 +118,7 @@ class _VolumeIntegratorBase:
             _lib.check(
                 _lib.load().rcv_render_volume(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, img.data_ptr(),
+                    self.scratch(medium.device, sensor, spp, _lib.MODE_SINGLE),
                     self.counters(medium.device).data_ptr(), st,
                 ),
                 "rcv_render_volume",
@@ -132,7 +151,9 @@ class _VolumeIntegratorBase:
             _lib.check(
                 _lib.load().rcv_render_backward_volume(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, g.data_ptr(), gd.data_ptr(),
-                    ga.data_ptr() if ga is not None else None, self.counters(medium.device).data_ptr(), st,
+                    ga.data_ptr() if ga is not None else None,
+                    self.scratch(medium.device, sensor, spp, _lib.MODE_ADJOINT),
+                    self.counters(medium.device).data_ptr(), st,
                 ),
                 "rcv_render_backward_volume",
             )
@@ -189,6 +210,7 @@ class TwoStatePRBVolpathIntegrator(_VolumeIntegratorBase):
             _lib.check(
                 _lib.load().rcv_render_twostates_volume(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, H.data_ptr(), F.data_ptr(),
+                    self.scratch(medium.device, sensor, spp, _lib.MODE_TWOSTATE),
                     self.counters(medium.device).data_ptr(), st,
                 ),
                 "rcv_render_twostates_volume",

@@ -47,15 +47,19 @@ def frac_equal(a, b):
     return np.mean(np.all(a == b, axis=-1))
 
 
-@pytest.mark.parametrize("spt", [1, 2, 4])
+@pytest.mark.parametrize("batch,blocks_per_sm,defer", [(1, 1, 1), (7, 2, 8), (64, 0, 32)])
 @pytest.mark.parametrize("albedo_grid", [False, True])
-def test_two_state_matches_oracle(cuda, oracle, spt, albedo_grid):
+def test_two_state_matches_oracle(cuda, oracle, batch, blocks_per_sm, defer, albedo_grid):
+    """The persistent schedule (queue batch, resident blocks, deferral
+    threshold) changes which lane traces which path and when, never the
+    result."""
     scene, med, grids = make_scene(cuda, albedo_grid=albedo_grid)
-    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "samples_per_thread": spt})
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "batch": batch,
+                           "blocks_per_sm": blocks_per_sm, "defer": defer})
     H, F = integ.render_twostates(scene, 0, seed=11, spp=4)
     torch.cuda.synchronize()
     osc = oracle_scene(oracle, scene, grids, 8, albedo_grid)
-    Ho, Fo = oracle.render_twostates(osc, seed=11, spp=4, chunk=spt)
+    Ho, Fo = oracle.render_twostates(osc, seed=11, spp=4)
     H, F = H.cpu().numpy(), F.cpu().numpy()
     assert frac_equal(F, Fo) >= 0.999 and frac_equal(H, Ho) >= 0.999
     np.testing.assert_allclose(F.mean(), Fo.mean(), rtol=1e-5)
@@ -65,9 +69,9 @@ def test_two_state_matches_oracle(cuda, oracle, spt, albedo_grid):
 
 def test_single_state_matches_oracle(cuda, oracle):
     scene, med, grids = make_scene(cuda)
-    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "samples_per_thread": 2})
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
     img = integ.render(scene, 0, seed=5, spp=8).cpu().numpy()
-    ref = oracle.render(oracle_scene(oracle, scene, grids, 8, False), seed=5, spp=8, chunk=2)
+    ref = oracle.render(oracle_scene(oracle, scene, grids, 8, False), seed=5, spp=8)
     assert frac_equal(img, ref) >= 0.999
 
 
@@ -248,7 +252,9 @@ def test_three_sigma_against_4096_spp(cuda):
     se = torch.sqrt(sigma**2 * (1.0 / 64 + 64.0 / 4096) + 1e-12)
     zz = ((mean - ref).abs() / se).cpu().numpy()
     assert np.mean(zz < 3) >= 0.99, np.mean(zz < 3)
-    assert float(np.mean(zz**2)) < 1.3  # chi^2 per degree of freedom ~ 1
+    # median |z| of a standard normal is 0.674; a biased renderer shifts it up
+    nz = zz[sigma.cpu().numpy() > 0]
+    assert float(np.median(nz)) < 0.8, float(np.median(nz))
     mean_err = abs(float(ref.mean()) - float(ref64.mean()))
     stat = float(sigma.mean()) * np.sqrt(4 / 4096.0) / np.sqrt(ref.numel())
     assert mean_err < 6 * stat + 1e-5, (mean_err, stat)
