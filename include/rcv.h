@@ -76,7 +76,13 @@ typedef struct rcv_volpath_options {
   int32_t blocks_per_sm; /* persistent blocks per SM, 0 = occupancy limit        */
   int32_t defer;         /* lanes that must wait before a path-start or
                             scattering branch runs, 1..32, 0 = 8                 */
+  int32_t order;         /* pixel hand-out order, RCV_ORDER_*                     */
 } rcv_volpath_options;
+
+/* Pixel hand-out orders of the persistent tracers.  Results do not depend on
+ * the order; it only changes how evenly the work drains at the end. */
+#define RCV_ORDER_LONGEST_FIRST 0 /* longest chord through the medium first */
+#define RCV_ORDER_ROW_MAJOR 1
 
 /* Tracer kinds for rcv_render_workspace_bytes. */
 #define RCV_MODE_TWOSTATE 0

@@ -63,7 +63,12 @@ class VolpathOptions(C.Structure):
         ("batch", C.c_int32),
         ("blocks_per_sm", C.c_int32),
         ("defer", C.c_int32),
+        ("order", C.c_int32),
     ]
+
+
+ORDER_LONGEST_FIRST = 0
+ORDER_ROW_MAJOR = 1
 
 
 MODE_TWOSTATE = 0

@@ -53,6 +53,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   int pass = 0;  // adjoint: 0 = radiance pass, 1 = replay pass
   float mu = 0.0f, inv_mu = 0.0f, half_inv_mu = 0.0f;
   int pix = 0;
+  uint32_t sid = 0;  // sample index within the job: pixel * spp + sample
   V3 dL{0.0f, 0.0f, 0.0f};
 
   Pcg32 rng, rng_nee;
@@ -106,8 +107,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     const unsigned m_scat = __ballot_sync(0xffffffffu, phase == kScatter);
     const unsigned m_walk = __ballot_sync(0xffffffffu, phase >= kMain && phase != kScatter);
     if (queue_empty && (m_start | m_scat | m_walk) == 0u) break;
-    const bool run_start = (unsigned)__popc(m_start) >= defer || (m_walk == 0u && m_scat == 0u && m_start != 0u);
-    const bool run_scat = (unsigned)__popc(m_scat) >= defer || (m_walk == 0u && m_scat != 0u);
+    // Once the queue is empty no new lanes arrive to fill a deferred branch;
+    // waiting would only make the warp's last paths take turns.
+    const unsigned need_lanes = queue_empty ? 1u : defer;
+    const bool run_start =
+        (unsigned)__popc(m_start) >= need_lanes || (m_walk == 0u && m_scat == 0u && m_start != 0u);
+    const bool run_scat = (unsigned)__popc(m_scat) >= need_lanes || (m_walk == 0u && m_scat != 0u);
 
     bool finished = false;  // the lane's current path (or pass) ends this iteration
 
@@ -125,7 +130,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         mu = (kMode == kTwoState) ? fmaxf(mu_old, mu_new) : mu_new;
         inv_mu = 1.0f / mu;
         half_inv_mu = 0.5f * inv_mu;
-        pix = (int)((path - Jn.path_begin) / Jn.spp);
+        // k-th pixel of the job's hand-out order, sample s of that pixel
+        const int64_t local = path - Jn.path_begin;
+        const uint32_t k = (uint32_t)(local / Jn.spp);
+        const uint32_t smp = (uint32_t)(local - (int64_t)k * Jn.spp);
+        pix = Jn.pixel_order != nullptr ? (int)__ldg(Jn.pixel_order + k) : (int)k;
+        sid = (uint32_t)pix * (uint32_t)Jn.spp + smp;
         if (kMode == kAdjoint) {
           const float* g = Jn.grad_img + (int64_t)pix * 3;
           const float fs = (float)Jn.spp;
@@ -133,7 +143,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         }
       }
       const VolJob& J = *Jp;
-      seed_lane(rng, J.seed, (uint32_t)(path - J.path_begin));
+      seed_lane(rng, J.seed, sid);
       const float u0 = next1d(rng), u1 = next1d(rng);
       V3 o;
       camera_ray(J, pix % J.width, pix / J.width, u0, u1, o, d);
@@ -395,7 +405,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         phase = kStart;
       } else {
         if (kMode != kAdjoint) {
-          float4* o = Q.path_out + path * (kMode == kTwoState ? 2 : 1);
+          float4* o = Q.path_out + (Jp->path_begin + sid) * (kMode == kTwoState ? 2 : 1);
           o[0] = make_float4(Ln.x, Ln.y, Ln.z, 0.0f);
           if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
         }

@@ -87,6 +87,56 @@ __global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_cons
   add_counts(Q.counters, cnt);
 }
 
+// ------------------------------------------------------ hand-out ordering
+// Pixels are handed to the persistent tracer longest-expected-path first: the
+// key is the length of the pixel-centre ray's chord through the medium cube,
+// in 256 buckets (bucket 0 = longest).  Misses (chord 0) come last, so the
+// queue ends on cheap paths instead of on a few long ones.
+constexpr int kOrderBuckets = 256;
+
+__device__ __forceinline__ int order_key(const VolJob& J, int pix) {
+  V3 o, d;
+  camera_ray(J, pix % J.width, pix / J.width, 0.5f, 0.5f, o, d);
+  float tn, tf;
+  slab(o, recip(d), tn, tf);
+  const float chord = (tn <= tf && tf > 0.0f) ? tf - fmaxf(tn, 0.0f) : 0.0f;
+  int b = (int)(chord * (255.0f / 1.7320508f));
+  b = b < 0 ? 0 : (b > 255 ? 255 : b);
+  return 255 - b;
+}
+
+__global__ void order_count_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* counts) {
+  __shared__ uint32_t hist[kOrderBuckets];
+  for (int k = threadIdx.x; k < kOrderBuckets; k += blockDim.x) hist[k] = 0;
+  __syncthreads();
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix < npix) atomicAdd(&hist[order_key(J, pix)], 1u);
+  __syncthreads();
+  for (int k = threadIdx.x; k < kOrderBuckets; k += blockDim.x)
+    if (hist[k]) atomicAdd(counts + k, hist[k]);
+}
+
+__global__ void order_scan_kernel(uint32_t* counts) {
+  // exclusive prefix sum of the 256 bucket counts, in place (one block)
+  __shared__ uint32_t s[kOrderBuckets];
+  const int t = threadIdx.x;
+  s[t] = counts[t];
+  __syncthreads();
+  for (int off = 1; off < kOrderBuckets; off <<= 1) {
+    const uint32_t v = t >= off ? s[t - off] : 0u;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  counts[t] = t == 0 ? 0u : s[t - 1];
+}
+
+__global__ void order_place_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* starts,
+                                   uint32_t* order) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix < npix) order[atomicAdd(starts + order_key(J, pix), 1u)] = (uint32_t)pix;
+}
+
 // Sum of a pixel's samples in sample order, divided by spp (the box-filter
 // film develop of plugins/twostatevolpath.py:80-89).
 template <bool kTwo>
@@ -255,17 +305,45 @@ static uint64_t path_out_bytes(int64_t paths, int mode) {
   return mode == kAdjoint ? 0u : uint64_t(paths) * (mode == kTwoState ? 32u : 16u);
 }
 
+// Scratch layout of one tracer call (all offsets 256-byte aligned):
+// queue counter | order bucket counts | pixel order | per-path radiance.
+struct RenderLayout {
+  uint64_t counter, buckets, order, path_out, total;
+};
+
+static RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
+  RenderLayout L;
+  L.counter = 0;
+  L.buckets = 256;
+  L.order = align256(L.buckets + kOrderBuckets * sizeof(uint32_t));
+  L.path_out = align256(L.order + uint64_t(npix) * sizeof(uint32_t));
+  L.total = align256(L.path_out + path_out_bytes(paths, mode));
+  return L;
+}
+
+// Fills `order` with the job's pixels, longest expected path first.
+int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, cudaStream_t st) {
+  const int npix = J.width * J.height;
+  RCV_TRY_CUDA(cudaMemsetAsync(buckets, 0, kOrderBuckets * sizeof(uint32_t), st), "order reset");
+  const int block = 256;
+  order_count_kernel<<<grid_for(npix, block), block, 0, st>>>(J, npix, buckets);
+  int rc = launched("order_count launch");
+  if (rc) return rc;
+  order_scan_kernel<<<1, kOrderBuckets, 0, st>>>(buckets);
+  rc = launched("order_scan launch");
+  if (rc) return rc;
+  order_place_kernel<<<grid_for(npix, block), block, 0, st>>>(J, npix, buckets, order);
+  return launched("order_place launch");
+}
+
 // Persistent launch over `total` paths of one job (jobs == null) or of a
 // device job table.
 int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
-                      const rcv_volpath_options* o, void* workspace, uint64_t* counters,
-                      cudaStream_t st) {
-  RCV_REQUIRE(workspace != nullptr && (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
-              "render workspace must be non-NULL and 256-byte aligned");
-  char* ws = static_cast<char*>(workspace);
+                      const rcv_volpath_options* o, unsigned long long* queue_counter,
+                      float4* path_out, uint64_t* counters, cudaStream_t st) {
   Queue Q;
-  Q.counter = reinterpret_cast<unsigned long long*>(ws);
-  Q.path_out = mode == kAdjoint ? nullptr : reinterpret_cast<float4*>(ws + 256);
+  Q.counter = queue_counter;
+  Q.path_out = mode == kAdjoint ? nullptr : path_out;
   Q.counters = reinterpret_cast<unsigned long long*>(counters);
   Q.jobs = jobs;
   Q.njobs = njobs;
@@ -291,9 +369,8 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   return launched("trace kernel launch");
 }
 
-int launch_reduce(bool two, const void* workspace, int64_t path_begin, int64_t npix, int spp,
+int launch_reduce(bool two, const float4* po, int64_t path_begin, int64_t npix, int spp,
                   float* out_new, float* out_old, cudaStream_t st) {
-  const float4* po = reinterpret_cast<const float4*>(static_cast<const char*>(workspace) + 256);
   const int block = 256;
   if (two)
     reduce_paths_kernel<true><<<grid_for(npix, block), block, 0, st>>>(po, path_begin, npix, spp,
@@ -344,7 +421,8 @@ extern "C" uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t ha
 extern "C" uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp,
                                                int32_t mode) {
   if (width <= 0 || height <= 0 || spp <= 0 || mode < 0 || mode > 2) return 0;
-  return align256(256u + path_out_bytes(int64_t(width) * height * spp, mode));
+  const int64_t npix = int64_t(width) * height;
+  return render_layout(npix, npix * spp, mode).total;
 }
 
 extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
@@ -364,6 +442,32 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
   return launched("pack_medium launch");
 }
 
+// Orders the pixels, runs the persistent tracer of one job and, for the
+// primal tracers, reduces the per-path radiance into the output image(s).
+static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, void* workspace,
+                          uint64_t* counters, float* img_new, float* img_old, cudaStream_t st) {
+  RCV_REQUIRE(workspace != nullptr && (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
+              "render workspace must be non-NULL and 256-byte aligned");
+  const int64_t npix = int64_t(J.width) * J.height;
+  const RenderLayout L = render_layout(npix, J.path_count, mode);
+  char* ws = static_cast<char*>(workspace);
+  int rc = RCV_OK;
+  J.pixel_order = nullptr;
+  if (o == nullptr || o->order == RCV_ORDER_LONGEST_FIRST) {
+    rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
+                      st);
+    if (rc) return rc;
+    J.pixel_order = reinterpret_cast<const uint32_t*>(ws + L.order);
+  } else {
+    RCV_REQUIRE(o->order == RCV_ORDER_ROW_MAJOR, "unknown pixel order %d", o->order);
+  }
+  float4* po = reinterpret_cast<float4*>(ws + L.path_out);
+  rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o,
+                         reinterpret_cast<unsigned long long*>(ws + L.counter), po, counters, st);
+  if (rc || mode == kAdjoint) return rc;
+  return launch_reduce(mode == kTwoState, po, 0, npix, J.spp, img_new, img_old, st);
+}
+
 extern "C" int rcv_render_twostates_volume(const rcv_medium* m, const rcv_sensor* s,
                                            const rcv_volpath_options* o, uint32_t seed,
                                            int32_t spp, float* img_old, float* img_new,
@@ -372,10 +476,8 @@ extern "C" int rcv_render_twostates_volume(const rcv_medium* m, const rcv_sensor
   int rc = make_volume_job(m, s, o, seed, spp, &J);
   if (rc) return rc;
   RCV_REQUIRE(img_old != nullptr && img_new != nullptr, "output images are NULL");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  rc = launch_persistent(kTwoState, J, nullptr, 0, J.path_count, o, workspace, counters, st);
-  if (rc) return rc;
-  return launch_reduce(true, workspace, 0, int64_t(J.width) * J.height, spp, img_new, img_old, st);
+  return run_single_job(kTwoState, J, o, workspace, counters, img_new, img_old,
+                        static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int rcv_render_volume(const rcv_medium* m, const rcv_sensor* s,
@@ -385,10 +487,7 @@ extern "C" int rcv_render_volume(const rcv_medium* m, const rcv_sensor* s,
   int rc = make_volume_job(m, s, o, seed, spp, &J);
   if (rc) return rc;
   RCV_REQUIRE(img != nullptr, "output image is NULL");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  rc = launch_persistent(kSingle, J, nullptr, 0, J.path_count, o, workspace, counters, st);
-  if (rc) return rc;
-  return launch_reduce(false, workspace, 0, int64_t(J.width) * J.height, spp, img, nullptr, st);
+  return run_single_job(kSingle, J, o, workspace, counters, img, nullptr, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor* s,
@@ -406,7 +505,7 @@ extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor*
   if (rc) return rc;
   if (!want_albedo) J.grad_albedo = nullptr;
   J.grad_img = grad_img;
-  rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, workspace, counters, st);
+  rc = run_single_job(kAdjoint, J, o, workspace, counters, nullptr, nullptr, st);
   if (rc) return rc;
   return launch_fold(m, grad_density, want_albedo ? grad_albedo : nullptr, st);
 }

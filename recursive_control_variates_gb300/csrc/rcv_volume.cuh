@@ -56,6 +56,7 @@ struct VolJob {
   float4* grad_albedo;  // dz*dy*dx (rgb + pad) or null
   int64_t path_begin;   // first global path index of this job (batched launches)
   int64_t path_count;   // width*height*spp
+  const uint32_t* pixel_order;  // pixel handed out k-th (null = row-major)
 };
 
 // Work queue of a (possibly multi-job) persistent launch.

@@ -37,6 +37,10 @@ class _VolumeIntegratorBase:
         self.batch = int(props.get("batch", 0))
         self.blocks_per_sm = int(props.get("blocks_per_sm", 0))
         self.defer = int(props.get("defer", 0))
+        order = props.get("order", "longest_first")
+        if order not in ("longest_first", "row_major"):
+            raise ValueError(f"unknown pixel order {order!r}")
+        self.order = _lib.ORDER_LONGEST_FIRST if order == "longest_first" else _lib.ORDER_ROW_MAJOR
         if self.max_depth < -1:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         self.is_checked = False
@@ -52,6 +56,7 @@ class _VolumeIntegratorBase:
         o.batch = self.batch
         o.blocks_per_sm = self.blocks_per_sm
         o.defer = self.defer
+        o.order = self.order
         return o
 
     def counters(self, device) -> torch.Tensor:

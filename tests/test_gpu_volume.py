@@ -47,15 +47,16 @@ def frac_equal(a, b):
     return np.mean(np.all(a == b, axis=-1))
 
 
-@pytest.mark.parametrize("batch,blocks_per_sm,defer", [(1, 1, 1), (7, 2, 8), (64, 0, 32)])
+@pytest.mark.parametrize("batch,blocks_per_sm,defer,order", [(1, 1, 1, "row_major"), (7, 2, 8, "longest_first"),
+                                                             (64, 0, 32, "longest_first")])
 @pytest.mark.parametrize("albedo_grid", [False, True])
-def test_two_state_matches_oracle(cuda, oracle, batch, blocks_per_sm, defer, albedo_grid):
+def test_two_state_matches_oracle(cuda, oracle, batch, blocks_per_sm, defer, order, albedo_grid):
     """The persistent schedule (queue batch, resident blocks, deferral
-    threshold) changes which lane traces which path and when, never the
-    result."""
+    threshold, pixel hand-out order) changes which lane traces which path and
+    when, never the result."""
     scene, med, grids = make_scene(cuda, albedo_grid=albedo_grid)
     integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "batch": batch,
-                           "blocks_per_sm": blocks_per_sm, "defer": defer})
+                           "blocks_per_sm": blocks_per_sm, "defer": defer, "order": order})
     H, F = integ.render_twostates(scene, 0, seed=11, spp=4)
     torch.cuda.synchronize()
     osc = oracle_scene(oracle, scene, grids, 8, albedo_grid)
