@@ -140,6 +140,26 @@ int rcv_render_volume(const rcv_medium* medium, const rcv_sensor* sensor,
                       const rcv_volpath_options* opts, uint32_t seed, int32_t spp, float* img,
                       void* workspace, uint64_t* counters, void* stream);
 
+/* rcv_render_volume without caller scratch.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory — for example code
+ * that runs where cudaMalloc is unavailable or forbidden, or a host that owns
+ * a fixed memory pool and gives this library only its inputs and outputs.
+ * Its scratch (work-queue counter, pixel order, per-path radiance) is a
+ * file-scope static __device__ array of 16 MiB that every GPU loading the
+ * library holds until exit, so width * height * spp is limited to about
+ * 16 MiB / (16 B per path + 4 B per pixel); larger requests return
+ * RCV_ERR_INVALID with the needed size.  It calls no allocator.  The first
+ * call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls on one device share that device's copy of the array and find
+ * the previous call's contents in it (the call resets what must start at
+ * zero): calls that can overlap on the GPU, e.g. issued on two streams,
+ * race and must be serialised by the caller.  The medium and its workspace
+ * are inputs, as for rcv_render_volume. */
+int rcv_render_volume_noalloc(const rcv_medium* medium, const rcv_sensor* sensor,
+                              const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                              float* img, uint64_t* counters, void* stream);
+
 /* Seed-replay adjoint on the current parameters: traces `spp` paths per
  * pixel from `seed`, first to obtain each path's radiance and then again to
  * back-propagate grad_img (dLoss/dimage, [height][width][3]) into the density

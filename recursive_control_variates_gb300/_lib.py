@@ -99,6 +99,9 @@ SIGNATURES = {
     "rcv_render_volume": (
         C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp]
     ),
+    "rcv_render_volume_noalloc": (
+        C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp]
+    ),
     "rcv_render_backward_volume": (
         C.c_int,
         [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],

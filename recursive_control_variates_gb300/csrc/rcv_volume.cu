@@ -509,3 +509,58 @@ extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor*
   if (rc) return rc;
   return launch_fold(m, grad_density, want_albedo ? grad_albedo : nullptr, st);
 }
+
+// ------------------------------------------------- allocation-free render
+// Single-state render for callers that cannot allocate device memory: code
+// running where cudaMalloc is unavailable or forbidden, such as a host that
+// owns a fixed memory pool and hands this library only its inputs and
+// outputs, or a real-time loop that may not allocate between frames.  Its
+// scratch (work-queue counter, pixel order, per-path radiance) lives in this
+// file-scope array instead of a caller buffer.  Every GPU that loads librcv
+// holds the array until the process exits.
+namespace rcv {
+
+constexpr uint64_t kNoAllocScratchBytes = uint64_t(16) << 20;  // 16 MiB
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch on the current device.  In host code the
+// symbol is only a host-side stand-in, so the address is looked up once per
+// device (with that device current) and cached.
+static int noalloc_scratch(void** out) {
+  static std::mutex mu;
+  static void* addr[kNoAllocMaxDevices] = {};
+  int dev = 0;
+  RCV_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  RCV_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal %d is not supported", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    RCV_TRY_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return RCV_OK;
+}
+
+}  // namespace rcv
+
+extern "C" int rcv_render_volume_noalloc(const rcv_medium* m, const rcv_sensor* s,
+                                         const rcv_volpath_options* o, uint32_t seed, int32_t spp,
+                                         float* img, uint64_t* counters, void* stream) {
+  VolJob J;
+  int rc = make_volume_job(m, s, o, seed, spp, &J);
+  if (rc) return rc;
+  RCV_REQUIRE(img != nullptr, "output image is NULL");
+  const uint64_t need = render_layout(int64_t(J.width) * J.height, J.path_count, kSingle).total;
+  RCV_REQUIRE(need <= kNoAllocScratchBytes,
+              "rcv_render_volume_noalloc: width*height*spp = %lld needs %llu bytes of scratch, "
+              "more than its static %llu bytes (16 MiB); use rcv_render_volume with caller scratch",
+              (long long)J.path_count, (unsigned long long)need,
+              (unsigned long long)kNoAllocScratchBytes);
+  void* ws = nullptr;
+  rc = noalloc_scratch(&ws);
+  if (rc) return rc;
+  return run_single_job(kSingle, J, o, ws, counters, img, nullptr, static_cast<cudaStream_t>(stream));
+}
