@@ -173,6 +173,63 @@ int rcv_render_backward_volume(const rcv_medium* medium, const rcv_sensor* senso
                                const float* grad_img, float* grad_density, float* grad_albedo,
                                void* workspace, uint64_t* counters, void* stream);
 
+/* ------------------------------------------------------- surface scenes */
+#define RCV_MAX_SPHERES 8
+
+typedef struct rcv_sphere {
+  float center[3];
+  float radius;
+  float albedo[3]; /* diffuse reflectance (equal in both states) */
+} rcv_sphere;
+
+/* Ground rectangle y = 0, |x|,|z| <= plane_half, with a two-state diffuse
+ * RGB texture (u along x, v along z, bilinear, repeat wrap), diffuse spheres
+ * and one rectangular area light at y = light_center[1] facing -y. */
+typedef struct rcv_surface_scene {
+  float plane_half;
+  int32_t tex_width;
+  int32_t tex_height;
+  const float* tex_old; /* device [tex_height][tex_width][3], state theta_{i-1} */
+  const float* tex_new; /* device, state theta_i                              */
+  int32_t num_spheres;  /* <= RCV_MAX_SPHERES */
+  rcv_sphere spheres[RCV_MAX_SPHERES];
+  float light_center[3];
+  float light_half[2]; /* half extents along x and z */
+  float light_radiance[3];
+  void* workspace; /* device, rcv_surface_workspace_bytes(), 256-B aligned */
+} rcv_surface_scene;
+
+/* Workspace of a surface scene: texture state pairs and gradient. */
+uint64_t rcv_surface_workspace_bytes(int32_t tex_width, int32_t tex_height);
+
+/* Packs the old / new textures after a state rotation
+ * (TwoStateBSDF.parameters_changed, plugins/twostatebsdf.py:46-56). */
+int rcv_surface_prepare(const rcv_surface_scene* scene, void* stream);
+
+/* Two-state surface primal (H = old, F = new), replacing
+ * TwoStatePRBIntegrator.render_twostates / sample_twostates
+ * (plugins/twostatepath.py:179-223, 225-364) with the two-state BSDF of
+ * plugins/twostatebsdf.py:25-38.  Scratch: rcv_render_workspace_bytes(...,
+ * RCV_MODE_TWOSTATE). */
+int rcv_render_twostates_surface(const rcv_surface_scene* scene, const rcv_sensor* sensor,
+                                 const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                                 float* img_old, float* img_new, void* workspace,
+                                 uint64_t* counters, void* stream);
+
+/* Single-state surface render of `new` (TwoStatePRBIntegrator.render). */
+int rcv_render_surface(const rcv_surface_scene* scene, const rcv_sensor* sensor,
+                       const rcv_volpath_options* opts, uint32_t seed, int32_t spp, float* img,
+                       void* workspace, uint64_t* counters, void* stream);
+
+/* Path-replay adjoint of the surface render on `new`: ADDS dLoss/dtexture to
+ * grad_texture ([tex_height][tex_width][3]); replaces
+ * CVIntegrator.render_backward with a twostateprb integrator
+ * (plugins/cv_integrator.py:87-94, Mitsuba PRBIntegrator.render_backward). */
+int rcv_render_backward_surface(const rcv_surface_scene* scene, const rcv_sensor* sensor,
+                                const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                                const float* grad_img, float* grad_texture, void* workspace,
+                                uint64_t* counters, void* stream);
+
 /* ------------------------------------------------- control variate state */
 /* Per-element state of the recursive control variate; every array holds
  * `n` float32 device values (n = height*width*3), zero-initialised. */

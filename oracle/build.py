@@ -18,19 +18,19 @@ from pathlib import Path
 
 ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
-SRC = ORACLE_DIR / "rcv_oracle.cpp"
+SRCS = [ORACLE_DIR / "rcv_oracle.cpp", ORACLE_DIR / "rcv_oracle_surface.cpp"]
 LIB = BUILD_DIR / "liboracle.so"
 FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread"]
 
 
 def build(force: bool = False) -> Path:
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
-    h = hashlib.sha256(SRC.read_bytes() + " ".join(FLAGS).encode() + os.uname().machine.encode())
+    h = hashlib.sha256(b"".join(s.read_bytes() for s in SRCS) + " ".join(FLAGS).encode() + os.uname().machine.encode())
     stamp = BUILD_DIR / "stamp.txt"
     if not force and LIB.exists() and stamp.exists() and stamp.read_text() == h.hexdigest():
         return LIB
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [os.environ.get("CXX", "g++"), *FLAGS, str(SRC), "-o", str(tmp)]
+    cmd = [os.environ.get("CXX", "g++"), *FLAGS, *map(str, SRCS), "-o", str(tmp)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")

@@ -49,6 +49,83 @@ class OracleScene(C.Structure):
     ]
 
 
+class OracleSurface(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("cam_o", C.c_float * 3),
+        ("cam_f", C.c_float * 3),
+        ("cam_r", C.c_float * 3),
+        ("cam_u", C.c_float * 3),
+        ("max_depth", C.c_int32),
+        ("rr_depth", C.c_int32),
+        ("hide_emitters", C.c_int32),
+        ("plane_half", C.c_float),
+        ("tex_w", C.c_int32),
+        ("tex_h", C.c_int32),
+        ("tex_old", C.c_void_p),
+        ("tex_new", C.c_void_p),
+        ("nspheres", C.c_int32),
+        ("spheres", (C.c_float * 7) * 8),
+        ("light_c", C.c_float * 3),
+        ("light_h", C.c_float * 2),
+        ("light_le", C.c_float * 3),
+    ]
+
+
+class SurfaceScene:
+    """Surface scene for the oracle; keeps the numpy textures alive."""
+
+    def __init__(self, cam: "Camera", tex_old, tex_new, spheres, light_c, light_h, light_le, plane_half=2.0,
+                 max_depth=8, rr_depth=5, hide_emitters=False):
+        self.tex_old = np.ascontiguousarray(tex_old, np.float32)
+        self.tex_new = np.ascontiguousarray(tex_new, np.float32)
+        s = OracleSurface()
+        s.width, s.height = cam.width, cam.height
+        s.cam_o[:], s.cam_f[:], s.cam_r[:], s.cam_u[:] = cam.origin, cam.forward, cam.right, cam.up
+        s.max_depth = max_depth if max_depth >= 0 else 0x7FFFFFFF
+        s.rr_depth = rr_depth
+        s.hide_emitters = int(hide_emitters)
+        s.plane_half = plane_half
+        s.tex_h, s.tex_w = self.tex_new.shape[:2]
+        s.tex_old = self.tex_old.ctypes.data
+        s.tex_new = self.tex_new.ctypes.data
+        s.nspheres = len(spheres)
+        for k, (c, r, a) in enumerate(spheres):
+            s.spheres[k][:] = [float(np.float32(v)) for v in (*c, r, *a)]
+        s.light_c[:] = [float(np.float32(v)) for v in light_c]
+        s.light_h[:] = [float(np.float32(v)) for v in light_h]
+        s.light_le[:] = [float(np.float32(v)) for v in light_le]
+        self.c = s
+        self.width, self.height = cam.width, cam.height
+
+
+def surface_render_twostates(scene: SurfaceScene, seed: int, spp: int, threads: int | None = None):
+    H = np.zeros((scene.height, scene.width, 3), np.float32)
+    F = np.zeros_like(H)
+    if lib().oracle_surface_render(C.byref(scene.c), 0, seed & 0xFFFFFFFF, spp, H.ctypes.data, F.ctypes.data,
+                                   threads or default_threads()):
+        raise ValueError("oracle_surface_render: invalid arguments")
+    return H, F
+
+
+def surface_render(scene: SurfaceScene, seed: int, spp: int, threads: int | None = None):
+    img = np.zeros((scene.height, scene.width, 3), np.float32)
+    if lib().oracle_surface_render(C.byref(scene.c), 1, seed & 0xFFFFFFFF, spp, None, img.ctypes.data,
+                                   threads or default_threads()):
+        raise ValueError("oracle_surface_render: invalid arguments")
+    return img
+
+
+def surface_backward(scene: SurfaceScene, seed: int, spp: int, grad_img, threads: int | None = None):
+    g = np.ascontiguousarray(grad_img, np.float32)
+    out = np.zeros(scene.tex_new.shape, np.float64)
+    if lib().oracle_surface_backward(C.byref(scene.c), seed & 0xFFFFFFFF, spp, g.ctypes.data, out.ctypes.data,
+                                     threads or default_threads()):
+        raise ValueError("oracle_surface_backward: invalid arguments")
+    return out
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -61,6 +138,10 @@ def lib():
         L.oracle_backward.argtypes = [C.POINTER(OracleScene), C.c_uint32, C.c_int, vp, vp, vp, C.c_int, C.c_int,
                                       C.c_int, C.c_int]
         L.oracle_backward.restype = C.c_int
+        L.oracle_surface_render.argtypes = [C.POINTER(OracleSurface), C.c_int, C.c_uint32, C.c_int, vp, vp, C.c_int]
+        L.oracle_surface_render.restype = C.c_int
+        L.oracle_surface_backward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int]
+        L.oracle_surface_backward.restype = C.c_int
         L.oracle_sample_tea_32.argtypes = [C.c_uint32, C.c_uint32]
         L.oracle_sample_tea_32.restype = C.c_uint32
         L.oracle_pcg32.argtypes = [C.c_uint64, C.c_uint64, C.c_int, vp]

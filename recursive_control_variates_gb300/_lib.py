@@ -76,6 +76,29 @@ MODE_SINGLE = 1
 MODE_ADJOINT = 2
 
 
+class SphereDesc(C.Structure):
+    _fields_ = [("center", f3), ("radius", C.c_float), ("albedo", f3)]
+
+
+MAX_SPHERES = 8
+
+
+class SurfaceScene(C.Structure):
+    _fields_ = [
+        ("plane_half", C.c_float),
+        ("tex_width", C.c_int32),
+        ("tex_height", C.c_int32),
+        ("tex_old", C.c_void_p),
+        ("tex_new", C.c_void_p),
+        ("num_spheres", C.c_int32),
+        ("spheres", SphereDesc * MAX_SPHERES),
+        ("light_center", f3),
+        ("light_half", C.c_float * 2),
+        ("light_radiance", f3),
+        ("workspace", C.c_void_p),
+    ]
+
+
 class CvState(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in ("img", "w_s", "v_n", "mean_x", "mean_y", "var_x", "var_y", "cov")]
 
@@ -105,6 +128,17 @@ SIGNATURES = {
     "rcv_render_backward_volume": (
         C.c_int,
         [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
+    ),
+    "rcv_surface_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32]),
+    "rcv_surface_prepare": (C.c_int, [P(SurfaceScene), vp]),
+    "rcv_render_twostates_surface": (
+        C.c_int, [P(SurfaceScene), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp]
+    ),
+    "rcv_render_surface": (
+        C.c_int, [P(SurfaceScene), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp]
+    ),
+    "rcv_render_backward_surface": (
+        C.c_int, [P(SurfaceScene), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp]
     ),
     "rcv_cv_step": (
         C.c_int,

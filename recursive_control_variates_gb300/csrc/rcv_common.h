@@ -69,6 +69,33 @@ inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo) {
   return l;
 }
 
+// Scratch layout of one tracer call (all offsets 256-byte aligned):
+// queue counter | order bucket counts | pixel order | per-path radiance
+// (32 B per path for two-state, 16 B single-state, none for adjoints).
+constexpr int kRenderOrderBuckets = 256;
+
+struct RenderLayout {
+  uint64_t counter, buckets, order, path_out, total;
+};
+
+inline uint64_t path_out_bytes(int64_t paths, int mode) {
+  return mode == RCV_MODE_ADJOINT ? 0u : uint64_t(paths) * (mode == RCV_MODE_TWOSTATE ? 32u : 16u);
+}
+
+inline RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
+  RenderLayout L;
+  L.counter = 0;
+  L.buckets = 256;
+  L.order = align256(L.buckets + kRenderOrderBuckets * sizeof(uint32_t));
+  L.path_out = align256(L.order + uint64_t(npix) * sizeof(uint32_t));
+  L.total = align256(L.path_out + path_out_bytes(paths, mode));
+  return L;
+}
+
+// Per-pixel sum of per-path radiance slots in sample order (rcv_volume.cu).
+int launch_reduce(bool two, const float4* po, int64_t path_begin, int64_t npix, int spp,
+                  float* out_new, float* out_old, cudaStream_t st);
+
 inline unsigned grid_for(int64_t n, int block) {
   int64_t g = (n + block - 1) / block;
   if (g < 1) g = 1;

@@ -301,25 +301,7 @@ static int sm_count() {
   return n;
 }
 
-static uint64_t path_out_bytes(int64_t paths, int mode) {
-  return mode == kAdjoint ? 0u : uint64_t(paths) * (mode == kTwoState ? 32u : 16u);
-}
-
-// Scratch layout of one tracer call (all offsets 256-byte aligned):
-// queue counter | order bucket counts | pixel order | per-path radiance.
-struct RenderLayout {
-  uint64_t counter, buckets, order, path_out, total;
-};
-
-static RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
-  RenderLayout L;
-  L.counter = 0;
-  L.buckets = 256;
-  L.order = align256(L.buckets + kOrderBuckets * sizeof(uint32_t));
-  L.path_out = align256(L.order + uint64_t(npix) * sizeof(uint32_t));
-  L.total = align256(L.path_out + path_out_bytes(paths, mode));
-  return L;
-}
+static_assert(kOrderBuckets == kRenderOrderBuckets, "order bucket count mismatch");
 
 // Fills `order` with the job's pixels, longest expected path first.
 int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, cudaStream_t st) {

@@ -128,3 +128,97 @@ def config_grids(cfg: VolumeConfig, seed: int | None = None):
 
 DENSITY_KEY = "object.interior_medium.sigma_t.data"
 ALBEDO_KEY = "object.interior_medium.albedo.data"
+
+# ------------------------------------------------------------ surface scenes
+TEXTURE_KEY = "plane.bsdf.reflectance.data"
+SURFACE_CAMERA = ((0.0, 2.5, 4.5), (0.0, 0.3, 0.0), (0.0, 1.0, 0.0))
+
+
+def value_noise(res: int, seed: int, octaves: int = 4, base: int = 4) -> np.ndarray:
+    """(res, res, 3) float32 RGB value noise in [0.05, 0.95]: `octaves`
+    lattices of seeded uniform values (base, 2 base, ... cells per side),
+    smoothstep-interpolated, amplitudes halving per octave."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(res) + 0.5) / res
+    out = np.zeros((res, res, 3))
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = base * 2**o
+        lat = rng.uniform(0.0, 1.0, size=(cells + 1, cells + 1, 3))
+        g = x * cells
+        i0 = np.floor(g).astype(int)
+        f = g - i0
+        s = f * f * (3.0 - 2.0 * f)
+        v = (lat[i0][:, i0] * (1 - s)[:, None, None] * (1 - s)[None, :, None]
+             + lat[i0 + 1][:, i0] * s[:, None, None] * (1 - s)[None, :, None]
+             + lat[i0][:, i0 + 1] * (1 - s)[:, None, None] * s[None, :, None]
+             + lat[i0 + 1][:, i0 + 1] * s[:, None, None] * s[None, :, None])
+        out += amp * v
+        total += amp
+        amp *= 0.5
+    out /= total
+    return (0.05 + 0.9 * out).astype(np.float32)
+
+
+def surface_spheres(seed: int, n: int = 3):
+    """n spheres with radii U[0.2, 0.5] resting on the ground, seeded colours."""
+    rng = np.random.default_rng(seed + 104729)
+    out = []
+    for _ in range(n):
+        r = float(rng.uniform(0.2, 0.5))
+        cx, cz = rng.uniform(-1.2, 1.2, size=2)
+        alb = tuple(float(v) for v in rng.uniform(0.3, 0.9, size=3))
+        out.append(((float(cx), r, float(cz)), r, alb))
+    return out
+
+
+def surface_scene_dict(texture, res: int, seed: int = 0, spp: int = 8, light_radiance: float = 15.0) -> dict:
+    """Ground plane ([-2, 2]^2 at y = 0, two-state textured diffuse), three
+    diffuse spheres and one 1 x 1 area light at y = 3 (config 3)."""
+    tex_bsdf = {"type": "diffuse", "reflectance": {"type": "bitmap", "data": texture}}
+    d = {
+        "type": "scene",
+        "sensor": {
+            "type": "perspective",
+            "fov": 45.0,
+            "to_world": look_at(*SURFACE_CAMERA),
+            "film": {"type": "hdrfilm", "width": res, "height": res, "rfilter": {"type": "box"}},
+            "sampler": {"type": "independent", "sample_count": spp},
+        },
+        "plane": {"type": "rectangle", "ground": True, "half_size": 2.0,
+                  "bsdf": {"type": "twostate", "old": tex_bsdf, "new": tex_bsdf, "incoming": tex_bsdf}},
+        "light": {"type": "rectangle", "center": (0.0, 3.0, 0.0), "half_size": (0.5, 0.5),
+                  "emitter": {"type": "area", "radiance": light_radiance}},
+    }
+    for k, (c, r, alb) in enumerate(surface_spheres(seed)):
+        sb = {"type": "diffuse", "reflectance": alb}
+        d[f"sphere{k}"] = {"type": "sphere", "center": c, "radius": r,
+                           "bsdf": {"type": "twostate", "old": sb, "new": sb, "incoming": sb}}
+    return d
+
+
+@dataclass
+class SurfaceConfig:
+    name: str
+    res: int
+    tex_res: int
+    spp: int
+    max_depth: int
+    rr_depth: int
+    steps: int
+    lr: float = 0.02
+    init: float = 0.5
+    seed: int = 0
+
+    @property
+    def spp_grad(self) -> int:
+        return self.spp
+
+    def paths_per_step(self) -> int:
+        return self.res * self.res * (self.spp + self.spp_grad)
+
+
+SURFACE_CONFIGS = {
+    # 1024^2, 512^2 RGB texture from 0.5 grey, spp 8, depth 8, 300 steps
+    "cfg3": SurfaceConfig("cfg3", res=1024, tex_res=512, spp=8, max_depth=8, rr_depth=5, steps=300),
+}
