@@ -11,6 +11,7 @@
 #include <cstring>
 
 #include "rcv_common.h"
+#include "rcv_cvmath.cuh"
 #include "rcv_device.cuh"
 
 namespace rcv {
@@ -27,65 +28,13 @@ void set_error(const char* fmt, ...) {
   va_end(ap);
 }
 
-// Scalars of one control-variate step.  Bias corrections are computed on the
-// host the way float32 tensors of the reference produce them: beta^n rounded
-// to float32, then 1 - that in float32.
-struct CvScalars {
-  float b1, b2, omb1, omb2;  // beta1, beta2, 1-beta1, 1-beta2 (float32)
-  float d1_prev;             // 1 - beta1^n       (n = count before the update)
-  float d1_next;             // 1 - beta1^(n+1)
-  float d2_get;              // 1 - beta2^n_get   (count seen by get())
-  int32_t has_prev;          // n > 0
-  int32_t do_pre, do_weight, do_post;
-};
-
 static float pow_f32(float b, int n) { return (float)std::pow((double)b, (double)n); }
-
-struct WelfordOut {
-  float mean_x, mean_y, var_x, var_y, cov;
-};
-
-__device__ __forceinline__ void welford2(const CvScalars& S, float x, float y, float& mean_x,
-                                         float& mean_y, float& var_x, float& var_y, float& cov) {
-  // plugins/welford.py:59-75
-  const float dx1 = S.has_prev ? x - mean_x / S.d1_prev : x;
-  const float dy1 = S.has_prev ? y - mean_y / S.d1_prev : y;
-  mean_y = S.b1 * mean_y + S.omb1 * y;
-  mean_x = S.b1 * mean_x + S.omb1 * x;
-  const float dx2 = x - mean_x / S.d1_next;
-  const float dy2 = y - mean_y / S.d1_next;
-  var_x = S.b2 * var_x + (S.omb2 * dx1) * dx2;
-  var_y = S.b2 * var_y + (S.omb2 * dy1) * dy2;
-  cov = S.b2 * cov + (S.omb2 * dx1) * dy2;
-}
 
 __global__ void cv_step_kernel(rcv_cv_state st, int64_t n, const float* __restrict__ H,
                                const float* __restrict__ F, CvScalars S) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float x = H[i], y = F[i];
-  float img = st.img[i], w = st.w_s[i], vn = st.v_n[i];
-  float mx = st.mean_x[i], my = st.mean_y[i], vx = st.var_x[i], vy = st.var_y[i],
-        cv = st.cov[i];
-  if (S.do_pre) welford2(S, x, y, mx, my, vx, vy, cv);
-  if (S.do_weight) {
-    // plugins/cv_integrator.py:60-67
-    const float v0 = vx / S.d2_get, v1 = vy / S.d2_get, c = cv / S.d2_get;
-    vn = ((w * w) * (vn + v0) + v1) - (2.0f * w) * c;
-    w = c / (v0 + vn);
-    if (isnan(w) || isinf(w)) w = 0.0f;
-    w = fminf(fmaxf(w, 0.0f), 1.0f);
-  }
-  img = w * (img - x) + y;  // plugins/cv_integrator.py:69
-  if (S.do_post) welford2(S, x, y, mx, my, vx, vy, cv);
-  st.img[i] = img;
-  st.w_s[i] = w;
-  st.v_n[i] = vn;
-  st.mean_x[i] = mx;
-  st.mean_y[i] = my;
-  st.var_x[i] = vx;
-  st.var_y[i] = vy;
-  st.cov[i] = cv;
+  cv_element(st, i, H[i], F[i], S);
 }
 
 __global__ void stats_update_kernel(rcv_cv_state st, int64_t n, const float* __restrict__ X,
@@ -185,15 +134,7 @@ __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float*
                             float omb1, float omb2, float eps, float lo, float hi, int zero_grad) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float gi = g[i];
-  const float mi = b1 * m[i] + omb1 * gi;
-  const float vi = b2 * v[i] + omb2 * (gi * gi);
-  float pi = p[i] - (lr_t * mi) / (sqrtf(vi) + eps);
-  pi = fminf(fmaxf(pi, lo), hi);
-  m[i] = mi;
-  v[i] = vi;
-  p[i] = pi;
-  if (zero_grad) g[i] = 0.0f;
+  adam_element(p, g, m, v, i, lr_t, b1, b2, omb1, omb2, eps, lo, hi, zero_grad != 0);
 }
 
 static CvScalars make_scalars(float beta1, float beta2, int n) {

@@ -1,0 +1,106 @@
+// Element functions of the medium packing (grids -> 64-byte lookup cells,
+// albedo state pairs, majorants), of the per-pixel sample reduction and of
+// the gradient fold (cell gradients -> voxel gradients), shared by the
+// single-job and the batched kernels.
+#pragma once
+#include "rcv_volume.cuh"
+
+namespace rcv {
+
+// Cell i of a (dx+1)(dy+1)(dz+1) lattice: the 8 clamped corner voxels of the
+// old and the new density.
+__device__ __forceinline__ void pack_cell(int64_t i, int dx, int dy, int dz, const float* __restrict__ old_d,
+                                          const float* __restrict__ new_d, float4* __restrict__ cells) {
+  const int cx = int(i % (dx + 1));
+  const int cy = int((i / (dx + 1)) % (dy + 1));
+  const int cz = int(i / (int64_t(dx + 1) * (dy + 1)));
+  const int x0 = clampi(cx - 1, dx - 1), x1 = clampi(cx, dx - 1);
+  const int y0 = clampi(cy - 1, dy - 1), y1 = clampi(cy, dy - 1);
+  const int z0 = clampi(cz - 1, dz - 1), z1 = clampi(cz, dz - 1);
+  auto idx = [&](int x, int y, int z) { return (int64_t(z) * dy + y) * dx + x; };
+  const int64_t i000 = idx(x0, y0, z0), i100 = idx(x1, y0, z0), i010 = idx(x0, y1, z0), i110 = idx(x1, y1, z0),
+                i001 = idx(x0, y0, z1), i101 = idx(x1, y0, z1), i011 = idx(x0, y1, z1), i111 = idx(x1, y1, z1);
+  float4* c = cells + i * 4;
+  c[0] = make_float4(old_d[i000], old_d[i100], old_d[i010], old_d[i110]);
+  c[1] = make_float4(old_d[i001], old_d[i101], old_d[i011], old_d[i111]);
+  c[2] = make_float4(new_d[i000], new_d[i100], new_d[i010], new_d[i110]);
+  c[3] = make_float4(new_d[i001], new_d[i101], new_d[i011], new_d[i111]);
+}
+
+// Voxel i of the old and the new RGB albedo as one 32-byte pair.
+__device__ __forceinline__ void pack_albedo(int64_t i, const float* __restrict__ old_a,
+                                            const float* __restrict__ new_a, float4* __restrict__ albedo) {
+  albedo[i * 2 + 0] = make_float4(old_a[i * 3 + 0], old_a[i * 3 + 1], old_a[i * 3 + 2], 0.0f);
+  albedo[i * 2 + 1] = make_float4(new_a[i * 3 + 0], new_a[i * 3 + 1], new_a[i * 3 + 2], 0.0f);
+}
+
+// Sum of a pixel's per-path radiance slots in sample order, divided by spp
+// (the box-filter film develop of plugins/twostatevolpath.py:80-89).  Slots
+// are [path][new, old] for two-state launches and [path] otherwise.
+template <bool kTwo>
+__device__ __forceinline__ void reduce_pixel(const float4* __restrict__ path_out, int64_t path_begin, int64_t pix,
+                                             int spp, V3& out_new, V3& out_old) {
+  constexpr int K = kTwo ? 2 : 1;
+  const float4* src = path_out + (path_begin + pix * spp) * K;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
+  for (int s = 0; s < spp; ++s) {
+    const float4 a = __ldcs(src + s * K);
+    nx += a.x;
+    ny += a.y;
+    nz += a.z;
+    if (kTwo) {
+      const float4 b = __ldcs(src + s * K + 1);
+      ox += b.x;
+      oy += b.y;
+      oz += b.z;
+    }
+  }
+  const float fs = (float)spp;
+  out_new = V3{nx / fs, ny / fs, nz / fs};
+  out_old = V3{ox / fs, oy / fs, oz / fs};
+}
+
+// Warp-wide max of the voxel densities into maxbits[0] (old), [1] (new);
+// every lane of the warp must call it.
+__device__ __forceinline__ void reduce_majorants(float mo, float mn, uint32_t* maxbits) {
+  uint32_t bo = __float_as_uint(fmaxf(mo, 0.0f)), bn = __float_as_uint(fmaxf(mn, 0.0f));
+  bo = __reduce_max_sync(0xffffffffu, bo);
+  bn = __reduce_max_sync(0xffffffffu, bn);
+  if ((threadIdx.x & 31) == 0) {
+    if (bo) atomicMax(maxbits + 0, bo);
+    if (bn) atomicMax(maxbits + 1, bn);
+  }
+}
+
+__device__ __forceinline__ int fold_candidates(int i, int D, int* cell, int* bit) {
+  int n = 0;
+  for (int c = i; c <= i + 1 && c <= D; ++c)
+    for (int b = 0; b < 2; ++b) {
+      const int v = clampi(c - 1 + b, D - 1);
+      if (v == i) {
+        cell[n] = c;
+        bit[n] = b;
+        ++n;
+      }
+    }
+  return n;
+}
+
+// Gradient of voxel i: the sum of its corner entries in every cell that uses it.
+__device__ __forceinline__ float fold_voxel(int64_t i, int dx, int dy, int dz, const float* __restrict__ gcells) {
+  const int x = int(i % dx), y = int((i / dx) % dy), z = int(i / (int64_t(dx) * dy));
+  int cxs[4], bxs[4], cys[4], bys[4], czs[4], bzs[4];
+  const int nx = fold_candidates(x, dx, cxs, bxs);
+  const int ny = fold_candidates(y, dy, cys, bys);
+  const int nz = fold_candidates(z, dz, czs, bzs);
+  float g = 0.0f;
+  for (int a = 0; a < nz; ++a)
+    for (int b = 0; b < ny; ++b)
+      for (int c = 0; c < nx; ++c) {
+        const int64_t cell = (int64_t(czs[a]) * (dy + 1) + cys[b]) * (dx + 1) + cxs[c];
+        g += gcells[cell * 8 + bxs[c] + 2 * bys[b] + 4 * bzs[a]];
+      }
+  return g;
+}
+
+}  // namespace rcv

@@ -8,6 +8,7 @@
 #include <mutex>
 
 #include "rcv_common.h"
+#include "rcv_pack.cuh"
 #include "rcv_trace.cuh"
 
 namespace rcv {
@@ -23,41 +24,14 @@ __global__ void pack_medium_kernel(int dx, int dy, int dz, const float* __restri
   const int64_t nv = int64_t(dx) * dy * dz;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   float mo = 0.0f, mn = 0.0f;
-  if (i < nc) {
-    const int cx = int(i % (dx + 1));
-    const int cy = int((i / (dx + 1)) % (dy + 1));
-    const int cz = int(i / (int64_t(dx + 1) * (dy + 1)));
-    const int x0 = clampi(cx - 1, dx - 1), x1 = clampi(cx, dx - 1);
-    const int y0 = clampi(cy - 1, dy - 1), y1 = clampi(cy, dy - 1);
-    const int z0 = clampi(cz - 1, dz - 1), z1 = clampi(cz, dz - 1);
-    auto idx = [&](int x, int y, int z) { return (int64_t(z) * dy + y) * dx + x; };
-    const int64_t i000 = idx(x0, y0, z0), i100 = idx(x1, y0, z0), i010 = idx(x0, y1, z0),
-                  i110 = idx(x1, y1, z0), i001 = idx(x0, y0, z1), i101 = idx(x1, y0, z1),
-                  i011 = idx(x0, y1, z1), i111 = idx(x1, y1, z1);
-    float4* c = cells + i * 4;
-    c[0] = make_float4(old_d[i000], old_d[i100], old_d[i010], old_d[i110]);
-    c[1] = make_float4(old_d[i001], old_d[i101], old_d[i011], old_d[i111]);
-    c[2] = make_float4(new_d[i000], new_d[i100], new_d[i010], new_d[i110]);
-    c[3] = make_float4(new_d[i001], new_d[i101], new_d[i011], new_d[i111]);
-  }
+  if (i < nc) pack_cell(i, dx, dy, dz, old_d, new_d, cells);
   if (i < nv) {
     mo = old_d[i];
     mn = new_d[i];
-    if (albedo != nullptr) {
-      albedo[i * 2 + 0] = make_float4(old_a[i * 3 + 0], old_a[i * 3 + 1], old_a[i * 3 + 2], 0.0f);
-      albedo[i * 2 + 1] = make_float4(new_a[i * 3 + 0], new_a[i * 3 + 1], new_a[i * 3 + 2], 0.0f);
-    }
+    if (albedo != nullptr) pack_albedo(i, old_a, new_a, albedo);
   }
   // majorant: maximum density of each state (non-negative part)
-  mo = fmaxf(mo, 0.0f);
-  mn = fmaxf(mn, 0.0f);
-  uint32_t bo = __float_as_uint(mo), bn = __float_as_uint(mn);
-  bo = __reduce_max_sync(0xffffffffu, bo);
-  bn = __reduce_max_sync(0xffffffffu, bn);
-  if ((threadIdx.x & 31) == 0) {
-    if (bo) atomicMax(maxbits + 0, bo);
-    if (bn) atomicMax(maxbits + 1, bn);
-  }
+  reduce_majorants(mo, mn, maxbits);
 }
 
 // ----------------------------------------------------------------- tracing
@@ -145,65 +119,25 @@ __global__ void reduce_paths_kernel(const float4* __restrict__ path_out, int64_t
                                     float* __restrict__ out_old) {
   const int64_t pix = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (pix >= npix) return;
-  constexpr int K = kTwo ? 2 : 1;
-  const float4* src = path_out + (path_begin + pix * spp) * K;
-  float nx = 0.0f, ny = 0.0f, nz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
-  for (int s = 0; s < spp; ++s) {
-    const float4 a = __ldcs(src + s * K);
-    nx += a.x;
-    ny += a.y;
-    nz += a.z;
-    if (kTwo) {
-      const float4 b = __ldcs(src + s * K + 1);
-      ox += b.x;
-      oy += b.y;
-      oz += b.z;
-    }
-  }
-  const float fs = (float)spp;
-  out_new[pix * 3 + 0] = nx / fs;
-  out_new[pix * 3 + 1] = ny / fs;
-  out_new[pix * 3 + 2] = nz / fs;
+  V3 n, o;
+  reduce_pixel<kTwo>(path_out, path_begin, pix, spp, n, o);
+  out_new[pix * 3 + 0] = n.x;
+  out_new[pix * 3 + 1] = n.y;
+  out_new[pix * 3 + 2] = n.z;
   if (kTwo) {
-    out_old[pix * 3 + 0] = ox / fs;
-    out_old[pix * 3 + 1] = oy / fs;
-    out_old[pix * 3 + 2] = oz / fs;
+    out_old[pix * 3 + 0] = o.x;
+    out_old[pix * 3 + 1] = o.y;
+    out_old[pix * 3 + 2] = o.z;
   }
 }
 
 // ------------------------------------------------------------ gradient fold
-__device__ __forceinline__ int fold_candidates(int i, int D, int* cell, int* bit) {
-  int n = 0;
-  for (int c = i; c <= i + 1 && c <= D; ++c)
-    for (int b = 0; b < 2; ++b) {
-      const int v = clampi(c - 1 + b, D - 1);
-      if (v == i) {
-        cell[n] = c;
-        bit[n] = b;
-        ++n;
-      }
-    }
-  return n;
-}
-
 __global__ void fold_density_kernel(int dx, int dy, int dz, const float* __restrict__ gcells,
                                     float* __restrict__ grad) {
   const int64_t nv = int64_t(dx) * dy * dz;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= nv) return;
-  const int x = int(i % dx), y = int((i / dx) % dy), z = int(i / (int64_t(dx) * dy));
-  int cxs[4], bxs[4], cys[4], bys[4], czs[4], bzs[4];
-  const int nx = fold_candidates(x, dx, cxs, bxs);
-  const int ny = fold_candidates(y, dy, cys, bys);
-  const int nz = fold_candidates(z, dz, czs, bzs);
-  float g = 0.0f;
-  for (int a = 0; a < nz; ++a)
-    for (int b = 0; b < ny; ++b)
-      for (int c = 0; c < nx; ++c) {
-        const int64_t cell = (int64_t(czs[a]) * (dy + 1) + cys[b]) * (dx + 1) + cxs[c];
-        g += gcells[cell * 8 + bxs[c] + 2 * bys[b] + 4 * bzs[a]];
-      }
-  grad[i] += g;
+  grad[i] += fold_voxel(i, dx, dy, dz, gcells);
 }
 
 __global__ void fold_albedo_kernel(int64_t nv, const float4* __restrict__ ga,
