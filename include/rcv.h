@@ -294,6 +294,123 @@ int rcv_adam_step(float* param, float* grad, float* m, float* v, int64_t n, int3
 /* x = min(max(x, lo), hi) elementwise (utils.clamp, utils.py:172-175). */
 int rcv_clamp(float* x, int64_t n, float lo, float hi, void* stream);
 
+/* ---------------------------------------------------- bias-correction tables
+ * The batched engine derives every per-step scalar on the device from step
+ * counters, so the powers beta^k that rcv_cv_step and rcv_adam_step compute on
+ * the host come from tables filled here with the same host arithmetic.
+ *
+ * CV table of beta: d[k] = 1 - float32(beta^k), k = 0..len-1, where len-1 is
+ * the first k with d[k] == 1.0f (every later power gives 1.0f as well).
+ * Adam table of (beta1, beta2): two doubles per t = 0..len-1,
+ * (sqrt(1 - beta2^t), 1 - beta1^t), ending at the first t where both are 1.0.
+ * The _len functions return the entry count, or RCV_ERR_UNSUPPORTED when beta
+ * is so close to 1 that the table would exceed 2^22 entries, or
+ * RCV_ERR_INVALID for beta outside [0, 1).  _fill writes `len` entries into
+ * host memory. */
+int64_t rcv_cv_table_len(float beta);
+int rcv_cv_table_fill(float beta, float* out, int64_t len);
+int64_t rcv_adam_table_len(float beta1, float beta2);
+int rcv_adam_table_fill(float beta1, float beta2, double* out, int64_t len);
+
+/* ------------------------------------------------------ batched cv_ps steps
+ * Many independent optimisation jobs (each a cv_ps loop of optimize.py:
+ * params.update, mi.render with the cv integrator around twostateprbvolpath,
+ * l2/l1 loss, dr.backward, Adam + clamp) advanced together: one step of the
+ * batch is one step of every job, in six kernel launches whatever the number
+ * of jobs: a prologue that derives each job's seeds and CV / Adam scalars from
+ * its device counters, the medium packing of all jobs, ONE persistent
+ * two-state tracer launch over the paths of all jobs, one fused
+ * reduce + control-variate + loss kernel, ONE persistent adjoint launch and
+ * one fused gradient fold + Adam + clamp kernel.  No host value changes from
+ * step to step, so the step can be captured once into a CUDA graph and
+ * replayed.  Per job and step the results equal the single-job calls
+ * (rcv_render_twostates_volume, rcv_cv_step, rcv_loss,
+ * rcv_render_backward_volume, rcv_adam_step) with seed = seed_base + it and
+ * seed_grad = sample_tea_32(seed, 1)[0] (plugins/twostatepath.py:84-92); the
+ * images are identical, the gradients agree up to the order of float atomics.
+ * Replaces the per-iteration loop body of optimize.py:105-131 for many jobs;
+ * the reference has no batched form. */
+
+/* One job.  All pointers are device memory owned by the caller. */
+typedef struct rcv_batch_job {
+  rcv_sensor sensor;
+  int32_t dims[3];         /* density grid Dx, Dy, Dz                             */
+  float scale;             /* sigma_t = scale * density                           */
+  float albedo_value[3];   /* constant albedo when albedo[0] is NULL              */
+  int32_t spp, spp_grad;   /* primal / adjoint samples per pixel                  */
+  int32_t max_depth, rr_depth, hide_emitters;
+  uint32_t seed_base;      /* step `it` renders with seed = seed_base + it        */
+  int32_t warmup;          /* cv plugin: weights update when it > warmup          */
+  int32_t pre_update;      /* meta cv_ps: statistics update before the weight     */
+  float cv_beta1, cv_beta2;
+  const float* cv_table1;  /* rcv_cv_table_fill(cv_beta1) copied to the device    */
+  const float* cv_table2;  /* rcv_cv_table_fill(cv_beta2)                         */
+  int32_t cv_table1_len, cv_table2_len;
+  int32_t loss;            /* RCV_LOSS_L2 / RCV_LOSS_L1 against `target`          */
+  float lr, adam_beta1, adam_beta2, adam_eps;
+  float density_lo, density_hi, albedo_lo, albedo_hi; /* clamp ranges             */
+  const double* adam_table; /* rcv_adam_table_fill(adam_beta1, adam_beta2)        */
+  int32_t adam_table_len;
+  int32_t pad0;
+  /* Parameters, double-buffered: before step `it`, density[it & 1] holds
+   * theta_it (the `new` state) and density[(it & 1) ^ 1] holds theta_{it-1}
+   * (`old`); the step writes theta_{it+1} into the latter.  Both buffers hold
+   * the initial grid before the first step (old = new = initial state, as
+   * the reference's double initialize_parameters, utils.py:62-66). */
+  float* density[2];       /* D^3 each                                            */
+  float* albedo[2];        /* D^3 * 3 each, or both NULL                          */
+  float* density_m;        /* Adam moments, zero before the first step            */
+  float* density_v;
+  float* albedo_m;         /* NULL: the albedo is not optimised (then albedo[0]   */
+  float* albedo_v;         /* and albedo[1] hold the same grid, may be one buffer) */
+  const float* target;     /* (H, W, 3) reference image                           */
+  rcv_cv_state cv;         /* (H, W, 3) each, zero before the first step          */
+  float* img_old;          /* optional H output (NULL = not written)              */
+  float* img_new;          /* optional F output                                   */
+  void* workspace;         /* rcv_batch_job_workspace_bytes(), 256-B aligned      */
+} rcv_batch_job;
+
+/* Status at the start of a job workspace (device memory; read it with a
+ * device-to-host copy). */
+typedef struct rcv_batch_job_status {
+  int32_t it;             /* steps taken; density[it & 1] holds theta_it          */
+  int32_t welford_count;  /* the CV statistics' sample count n                    */
+  int32_t adam_t;         /* Adam steps taken                                     */
+  int32_t pad;
+  double loss_sum;        /* sum of the last step's per-element losses            */
+  float loss;             /* mean loss of the last step                           */
+  float pad1;
+} rcv_batch_job_status;
+
+uint64_t rcv_batch_job_workspace_bytes(const rcv_batch_job* job);
+/* Validates the job, zeroes its status and computes its longest-first pixel
+ * order (camera geometry only) into the workspace. */
+int rcv_batch_job_init(const rcv_batch_job* job, void* stream);
+
+typedef struct rcv_batch rcv_batch; /* opaque host handle of a batch plan */
+
+/* Shared device scratch of a batch: job tables and the per-path radiance of
+ * the two-state launch (32 bytes per primal path of all jobs). */
+uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n);
+/* Plans a batch of n initialised jobs with launch options `opts` (batch,
+ * blocks_per_sm, defer, order; max_depth / rr_depth / hide_emitters come from
+ * each job).  Copies the job tables into `workspace` on `stream`; the host
+ * array `jobs` may be freed on return.  *out is released by rcv_batch_destroy.
+ * This is the one entry point group that allocates: host memory for the plan
+ * and, when graphs are used, the CUDA graph. */
+int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_volpath_options* opts,
+                     void* workspace, uint64_t workspace_bytes, rcv_batch** out, void* stream);
+/* One step of every job.  use_graph != 0: the first call captures the six
+ * launches into a CUDA graph (on an internal stream, nothing runs), every
+ * call launches the graph on `stream`. */
+int rcv_batch_step(rcv_batch* batch, int32_t use_graph, void* stream);
+/* Device pointer to 2 * RCV_COUNTER_COUNT uint64 tracer counters accumulated
+ * over all steps: the two-state launch, then the adjoint launch. */
+uint64_t* rcv_batch_counters(rcv_batch* batch);
+/* Kernel launches one step issues (graph replays count the same). */
+int32_t rcv_batch_kernels_per_step(void);
+int rcv_batch_destroy(rcv_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

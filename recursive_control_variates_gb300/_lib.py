@@ -103,6 +103,64 @@ class CvState(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in ("img", "w_s", "v_n", "mean_x", "mean_y", "var_x", "var_y", "cov")]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [
+        ("sensor", Sensor),
+        ("dims", i3),
+        ("scale", C.c_float),
+        ("albedo_value", f3),
+        ("spp", C.c_int32),
+        ("spp_grad", C.c_int32),
+        ("max_depth", C.c_int32),
+        ("rr_depth", C.c_int32),
+        ("hide_emitters", C.c_int32),
+        ("seed_base", C.c_uint32),
+        ("warmup", C.c_int32),
+        ("pre_update", C.c_int32),
+        ("cv_beta1", C.c_float),
+        ("cv_beta2", C.c_float),
+        ("cv_table1", C.c_void_p),
+        ("cv_table2", C.c_void_p),
+        ("cv_table1_len", C.c_int32),
+        ("cv_table2_len", C.c_int32),
+        ("loss", C.c_int32),
+        ("lr", C.c_float),
+        ("adam_beta1", C.c_float),
+        ("adam_beta2", C.c_float),
+        ("adam_eps", C.c_float),
+        ("density_lo", C.c_float),
+        ("density_hi", C.c_float),
+        ("albedo_lo", C.c_float),
+        ("albedo_hi", C.c_float),
+        ("adam_table", C.c_void_p),
+        ("adam_table_len", C.c_int32),
+        ("pad0", C.c_int32),
+        ("density", C.c_void_p * 2),
+        ("albedo", C.c_void_p * 2),
+        ("density_m", C.c_void_p),
+        ("density_v", C.c_void_p),
+        ("albedo_m", C.c_void_p),
+        ("albedo_v", C.c_void_p),
+        ("target", C.c_void_p),
+        ("cv", CvState),
+        ("img_old", C.c_void_p),
+        ("img_new", C.c_void_p),
+        ("workspace", C.c_void_p),
+    ]
+
+
+class BatchJobStatus(C.Structure):
+    _fields_ = [
+        ("it", C.c_int32),
+        ("welford_count", C.c_int32),
+        ("adam_t", C.c_int32),
+        ("pad", C.c_int32),
+        ("loss_sum", C.c_double),
+        ("loss", C.c_float),
+        ("pad1", C.c_float),
+    ]
+
+
 vp = C.c_void_p
 P = C.POINTER
 
@@ -147,6 +205,18 @@ SIGNATURES = {
     "rcv_statistics_get": (C.c_int, [P(CvState), C.c_int64, C.c_int32, C.c_float, vp, vp, vp, vp]),
     "rcv_statistics_update": (C.c_int, [P(CvState), C.c_int64, vp, vp, P(C.c_int32), C.c_float, C.c_float, vp]),
     "rcv_clamp": (C.c_int, [vp, C.c_int64, C.c_float, C.c_float, vp]),
+    "rcv_cv_table_len": (C.c_int64, [C.c_float]),
+    "rcv_cv_table_fill": (C.c_int, [C.c_float, vp, C.c_int64]),
+    "rcv_adam_table_len": (C.c_int64, [C.c_float, C.c_float]),
+    "rcv_adam_table_fill": (C.c_int, [C.c_float, C.c_float, vp, C.c_int64]),
+    "rcv_batch_job_workspace_bytes": (C.c_uint64, [P(BatchJob)]),
+    "rcv_batch_job_init": (C.c_int, [P(BatchJob), vp]),
+    "rcv_batch_workspace_bytes": (C.c_uint64, [P(BatchJob), C.c_int32]),
+    "rcv_batch_create": (C.c_int, [P(BatchJob), C.c_int32, P(VolpathOptions), vp, C.c_uint64, P(vp), vp]),
+    "rcv_batch_step": (C.c_int, [vp, C.c_int32, vp]),
+    "rcv_batch_counters": (vp, [vp]),
+    "rcv_batch_kernels_per_step": (C.c_int32, []),
+    "rcv_batch_destroy": (C.c_int, [vp]),
     "rcv_welford_update": (C.c_int, [vp, vp, C.c_int64, vp, P(C.c_int32), C.c_float, C.c_float, vp]),
     "rcv_welford_get": (C.c_int, [vp, C.c_int64, C.c_int32, C.c_float, vp, vp]),
     "rcv_loss_workspace_bytes": (C.c_uint64, [C.c_int64]),

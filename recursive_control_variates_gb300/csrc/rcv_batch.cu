@@ -1,0 +1,619 @@
+// Batched cv_ps steps: many optimisation jobs of uneven grid, film and
+// sample counts advanced by one step in six kernel launches.
+//
+//   prologue   1 block: per job, seeds, CV scalars and Adam step size from the
+//              job's device counters and bias-correction tables; counters++
+//   pack       medium packing of every job (old = theta_{it-1}, new =
+//              theta_it from the parameter double buffer), majorants, and
+//              zeroed gradient cells
+//   trace 2S   ONE persistent two-state launch over the paths of all jobs
+//   image      per pixel of every job: sample reduction (H, F), control
+//              variate blend + statistics, loss gradient and loss sum
+//   trace adj  ONE persistent adjoint launch over the gradient paths of all jobs
+//   update     per voxel of every job: cell-gradient fold, Adam + clamp into
+//              the other half of the parameter double buffer
+//
+// The elementwise kernels give each job a whole number of blocks (a block
+// never spans two jobs) and find their job by binary search over the block
+// prefix table.  Nothing the host passes changes between steps, so a step can
+// be captured once into a CUDA graph and replayed.
+//
+// Per job, every stage performs the arithmetic of the single-job entry points
+// it replaces (rcv_medium_prepare, rcv_render_twostates_volume, rcv_cv_step,
+// rcv_loss, rcv_render_backward_volume, rcv_adam_step) through the same
+// element functions, so images are identical to the single-job path and
+// gradients differ only by the order of float atomics.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "rcv_common.h"
+#include "rcv_cvmath.cuh"
+#include "rcv_pack.cuh"
+#include "rcv_volume.cuh"
+
+namespace rcv {
+
+constexpr int kBatchBlock = 256;
+constexpr int kBatchKernels = 6;
+constexpr int kMaxBatchJobs = 1 << 16;
+
+// Per-step values of a job, written by the prologue.
+struct StepParams {
+  CvScalars S;
+  float lr_t;        // Adam step size with both bias corrections
+  int32_t cur;       // density[cur] = theta_it (new), density[cur ^ 1] = theta_{it-1}
+  uint32_t seed, seed_grad;
+};
+
+struct JobHeader {
+  rcv_batch_job_status status;
+  StepParams step;
+};
+static_assert(sizeof(rcv_batch_job_status) == 32, "status layout");
+
+// Job workspace: header | medium (cells, albedo pairs, majorants, gradient
+// cells) | order buckets | pixel order | dL/dimage.
+struct JobLayout {
+  uint64_t header, medium, buckets, order, grad_img, total;
+};
+
+static JobLayout job_layout(const rcv_batch_job& j) {
+  JobLayout L;
+  const uint64_t npix = uint64_t(j.sensor.width) * uint64_t(j.sensor.height);
+  uint64_t off = 0;
+  L.header = off;
+  off = align256(off + sizeof(JobHeader));
+  L.medium = off;
+  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr).total);
+  L.buckets = off;
+  off = align256(off + kRenderOrderBuckets * sizeof(uint32_t));
+  L.order = off;
+  off = align256(off + npix * sizeof(uint32_t));
+  L.grad_img = off;
+  off = align256(off + npix * 3 * sizeof(float));
+  L.total = off;
+  return L;
+}
+
+// Device view of one job.
+struct BatchEntry {
+  rcv_batch_job d;
+  JobHeader* hdr;
+  float4* cells;
+  float4* albedo;  // packed (old, new) pairs or null
+  uint32_t* maxbits;
+  float4* grad_cells;
+  float4* grad_albedo;  // or null
+  float* grad_img;
+  int64_t npix, nv, nc;
+  int64_t two_begin;  // first path of the job in the two-state launch
+  double inv_n;       // 1 / (npix * 3)
+  float gscale;       // float32(1 / (npix * 3))
+  int32_t has_albedo;  // albedo grid (else albedo_value)
+  int32_t opt_albedo;  // albedo is optimised (moments given)
+};
+
+__device__ __forceinline__ int job_of_block(const int32_t* __restrict__ bp, int n, int block) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(bp + mid) <= block)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// d[k] = 1 - beta^k from a table that saturates at 1.0f.
+__device__ __forceinline__ float table_d(const float* __restrict__ tab, int len, int k) {
+  return k < len ? __ldg(tab + k) : 1.0f;
+}
+
+__global__ void batch_prologue_kernel(BatchEntry* __restrict__ E, VolJob* __restrict__ two,
+                                      VolJob* __restrict__ adj, int n) {
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const rcv_batch_job& d = E[j].d;
+    JobHeader* h = E[j].hdr;
+    const int it = h->status.it, cnt = h->status.welford_count, t = h->status.adam_t + 1;
+    StepParams P;
+    // seed = seed_base + it; seed_grad = sample_tea_32(seed, 1)[0]
+    // (plugins/twostatepath.py:84-92)
+    P.seed = d.seed_base + (uint32_t)it;
+    uint32_t a, b;
+    tea(P.seed, 1u, 4, a, b);
+    P.seed_grad = a;
+    P.cur = it & 1;
+    // control-variate scalars, as rcv_cv_step derives them on the host
+    CvScalars& S = P.S;
+    S.b1 = d.cv_beta1;
+    S.b2 = d.cv_beta2;
+    S.omb1 = 1.0f - d.cv_beta1;
+    S.omb2 = 1.0f - d.cv_beta2;
+    S.has_prev = cnt > 0;
+    S.d1_prev = cnt > 0 ? table_d(d.cv_table1, d.cv_table1_len, cnt) : 1.0f;
+    S.d1_next = table_d(d.cv_table1, d.cv_table1_len, cnt + 1);
+    const bool update = it > 0;
+    S.do_pre = update && d.pre_update;
+    S.do_post = update && !d.pre_update;
+    S.do_weight = it > d.warmup;
+    S.d2_get = table_d(d.cv_table2, d.cv_table2_len, cnt + (S.do_pre ? 1 : 0));
+    // lr_t = lr * sqrt(1 - beta2^t) / (1 - beta1^t) in double, as rcv_adam_step
+    double s2 = 1.0, bc1 = 1.0;
+    if (t < d.adam_table_len) {
+      s2 = d.adam_table[2 * t];
+      bc1 = d.adam_table[2 * t + 1];
+    }
+    P.lr_t = (float)(((double)d.lr * s2) / bc1);
+    h->step = P;
+    h->status.it = it + 1;
+    h->status.welford_count = cnt + (update ? 1 : 0);
+    h->status.adam_t = t;
+    h->status.loss_sum = 0.0;
+    E[j].maxbits[0] = 0u;
+    E[j].maxbits[1] = 0u;
+    two[j].seed = P.seed;
+    adj[j].seed = P.seed_grad;
+  }
+}
+
+__global__ void batch_pack_kernel(const BatchEntry* __restrict__ E, const int32_t* __restrict__ bp, int n) {
+  const int j = job_of_block(bp, n, blockIdx.x);
+  const BatchEntry& B = E[j];
+  const int64_t i = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  const int cur = B.hdr->step.cur;
+  const float* nd = B.d.density[cur];
+  const float* od = B.d.density[cur ^ 1];
+  const int dx = B.d.dims[0], dy = B.d.dims[1], dz = B.d.dims[2];
+  float mo = 0.0f, mn = 0.0f;
+  if (i < B.nc) {
+    pack_cell(i, dx, dy, dz, od, nd, B.cells);
+    B.grad_cells[i * 2 + 0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    B.grad_cells[i * 2 + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  if (i < B.nv) {
+    mo = od[i];
+    mn = nd[i];
+    if (B.has_albedo) pack_albedo(i, B.d.albedo[cur ^ 1], B.d.albedo[cur], B.albedo);
+    if (B.opt_albedo) B.grad_albedo[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  reduce_majorants(mo, mn, B.maxbits);
+}
+
+__global__ void batch_image_kernel(const BatchEntry* __restrict__ E, const int32_t* __restrict__ bp, int n,
+                                   const float4* __restrict__ path_out) {
+  const int j = job_of_block(bp, n, blockIdx.x);
+  const BatchEntry& B = E[j];
+  const int64_t pix = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (pix < B.npix) {
+    const CvScalars S = B.hdr->step.S;
+    V3 F, H;
+    reduce_pixel<true>(path_out, B.two_begin, pix, B.d.spp, F, H);
+    if (B.d.img_new != nullptr) {
+      B.d.img_new[pix * 3 + 0] = F.x;
+      B.d.img_new[pix * 3 + 1] = F.y;
+      B.d.img_new[pix * 3 + 2] = F.z;
+    }
+    if (B.d.img_old != nullptr) {
+      B.d.img_old[pix * 3 + 0] = H.x;
+      B.d.img_old[pix * 3 + 1] = H.y;
+      B.d.img_old[pix * 3 + 2] = H.z;
+    }
+    const float hs[3] = {H.x, H.y, H.z}, fs[3] = {F.x, F.y, F.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t i = pix * 3 + c;
+      const float g = cv_element(B.d.cv, i, hs[c], fs[c], S);
+      B.grad_img[i] = loss_grad(B.d.loss, g - __ldg(B.d.target + i), B.gscale, acc);
+    }
+  }
+  // block sum of the loss terms, one atomic per block
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  __shared__ double warp_sums[kBatchBlock / 32];
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < kBatchBlock / 32; ++k) s += warp_sums[k];
+    atomicAdd(&B.hdr->status.loss_sum, s);
+  }
+}
+
+__global__ void batch_update_kernel(const BatchEntry* __restrict__ E, const int32_t* __restrict__ bp, int n) {
+  const int j = job_of_block(bp, n, blockIdx.x);
+  const BatchEntry& B = E[j];
+  const int64_t i = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  if (i == 0) B.hdr->status.loss = float(B.hdr->status.loss_sum * B.inv_n);
+  if (i >= B.nv) return;
+  const int cur = B.hdr->step.cur;
+  const float lr_t = B.hdr->step.lr_t;
+  const float b1 = B.d.adam_beta1, b2 = B.d.adam_beta2, eps = B.d.adam_eps;
+  const float omb1 = 1.0f - b1, omb2 = 1.0f - b2;
+  // the single-job path accumulates the fold into a zeroed gradient: 0 + g
+  const float g = 0.0f + fold_voxel(i, B.d.dims[0], B.d.dims[1], B.d.dims[2],
+                                    reinterpret_cast<const float*>(B.grad_cells));
+  {
+    float m = B.d.density_m[i], v = B.d.density_v[i];
+    B.d.density[cur ^ 1][i] =
+        adam_value(B.d.density[cur][i], g, m, v, lr_t, b1, b2, omb1, omb2, eps, B.d.density_lo, B.d.density_hi);
+    B.d.density_m[i] = m;
+    B.d.density_v[i] = v;
+  }
+  if (B.opt_albedo) {
+    const float4 ga = B.grad_albedo[i];
+    const float gs[3] = {0.0f + ga.x, 0.0f + ga.y, 0.0f + ga.z};
+    const float* pin = B.d.albedo[cur];
+    float* pout = B.d.albedo[cur ^ 1];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t k = i * 3 + c;
+      float m = B.d.albedo_m[k], v = B.d.albedo_v[k];
+      pout[k] = adam_value(pin[k], gs[c], m, v, lr_t, b1, b2, omb1, omb2, eps, B.d.albedo_lo, B.d.albedo_hi);
+      B.d.albedo_m[k] = m;
+      B.d.albedo_v[k] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host
+static int validate_job(const rcv_batch_job* j, int idx) {
+  RCV_REQUIRE(j != nullptr, "job %d is NULL", idx);
+  RCV_REQUIRE(j->dims[0] > 0 && j->dims[1] > 0 && j->dims[2] > 0, "job %d: grid dims must be positive", idx);
+  RCV_REQUIRE(uint64_t(j->dims[0] + 1) * uint64_t(j->dims[1] + 1) * uint64_t(j->dims[2] + 1) * 4u <
+                  (uint64_t(1) << 32),
+              "job %d: grid too large: (Dx+1)(Dy+1)(Dz+1) must be below 2^30", idx);
+  RCV_REQUIRE(j->sensor.width > 0 && j->sensor.height > 0, "job %d: film size must be positive", idx);
+  RCV_REQUIRE(j->spp > 0 && j->spp_grad > 0, "job %d: spp and spp_grad must be positive", idx);
+  const int64_t npix = int64_t(j->sensor.width) * j->sensor.height;
+  RCV_REQUIRE(npix * j->spp < (int64_t(1) << 32) && npix * j->spp_grad < (int64_t(1) << 32),
+              "job %d: width * height * spp must be below 2^32", idx);
+  RCV_REQUIRE(j->max_depth >= -1, "job %d: max_depth must be >= -1", idx);
+  RCV_REQUIRE(j->scale >= 0.0f, "job %d: scale must be non-negative", idx);
+  RCV_REQUIRE(j->density[0] && j->density[1] && j->density_m && j->density_v,
+              "job %d: density buffers / moments are NULL", idx);
+  RCV_REQUIRE(j->density[0] != j->density[1], "job %d: the two density buffers must differ", idx);
+  const bool alb = j->albedo[0] != nullptr, opt_alb = j->albedo_m != nullptr;
+  RCV_REQUIRE(alb == (j->albedo[1] != nullptr), "job %d: albedo[0] and albedo[1] must both be set or both be NULL",
+              idx);
+  RCV_REQUIRE(opt_alb == (j->albedo_v != nullptr), "job %d: albedo_m and albedo_v must both be set or both be NULL",
+              idx);
+  RCV_REQUIRE(!opt_alb || alb, "job %d: albedo moments without an albedo grid", idx);
+  RCV_REQUIRE(!opt_alb || j->albedo[0] != j->albedo[1], "job %d: the two albedo buffers must differ", idx);
+  RCV_REQUIRE(j->target != nullptr, "job %d: target is NULL", idx);
+  const rcv_cv_state& s = j->cv;
+  RCV_REQUIRE(s.img && s.w_s && s.v_n && s.mean_x && s.mean_y && s.var_x && s.var_y && s.cov,
+              "job %d: a control-variate state array is NULL", idx);
+  RCV_REQUIRE(j->cv_beta1 >= 0.0f && j->cv_beta1 < 1.0f && j->cv_beta2 >= 0.0f && j->cv_beta2 < 1.0f,
+              "job %d: cv betas must be in [0, 1)", idx);
+  RCV_REQUIRE(j->adam_beta1 >= 0.0f && j->adam_beta1 < 1.0f && j->adam_beta2 >= 0.0f && j->adam_beta2 < 1.0f,
+              "job %d: Adam betas must be in [0, 1)", idx);
+  RCV_REQUIRE(j->cv_table1 && j->cv_table2 && j->cv_table1_len > 0 && j->cv_table2_len > 0,
+              "job %d: CV bias-correction tables are missing", idx);
+  RCV_REQUIRE(j->adam_table && j->adam_table_len > 0, "job %d: Adam bias-correction table is missing", idx);
+  RCV_REQUIRE(j->loss == RCV_LOSS_L2 || j->loss == RCV_LOSS_L1, "job %d: unknown loss kind %d", idx, j->loss);
+  RCV_REQUIRE(j->workspace != nullptr && (reinterpret_cast<uintptr_t>(j->workspace) & 255u) == 0,
+              "job %d: workspace must be non-NULL and 256-byte aligned", idx);
+  return RCV_OK;
+}
+
+// Plan workspace: entries | two-state jobs | adjoint jobs | block prefixes |
+// queue counters | tracer counters | per-path radiance.
+struct PlanLayout {
+  uint64_t entries, two, adj, prefix, queue, counters, path_out, total;
+};
+
+static PlanLayout plan_layout(int n, int64_t total_two_paths) {
+  PlanLayout L;
+  uint64_t off = 0;
+  L.entries = off;
+  off = align256(off + uint64_t(n) * sizeof(BatchEntry));
+  L.two = off;
+  off = align256(off + uint64_t(n) * sizeof(VolJob));
+  L.adj = off;
+  off = align256(off + uint64_t(n) * sizeof(VolJob));
+  L.prefix = off;
+  off = align256(off + 3u * uint64_t(n + 1) * sizeof(int32_t));
+  L.queue = off;
+  off = align256(off + 2u * sizeof(unsigned long long));
+  L.counters = off;
+  off = align256(off + 2u * RCV_COUNTER_COUNT * sizeof(uint64_t));
+  L.path_out = off;
+  off = align256(off + uint64_t(total_two_paths) * 32u);
+  L.total = off;
+  return L;
+}
+
+static int64_t primal_paths(const rcv_batch_job& j) { return int64_t(j.sensor.width) * j.sensor.height * j.spp; }
+
+static rcv_medium job_medium(const rcv_batch_job& j, const JobLayout& L) {
+  rcv_medium m;
+  std::memset(&m, 0, sizeof(m));
+  std::memcpy(m.dims, j.dims, sizeof(m.dims));
+  m.scale = j.scale;
+  m.density_old = j.density[0];
+  m.density_new = j.density[1];
+  m.albedo_old = j.albedo[0];
+  m.albedo_new = j.albedo[1];
+  std::memcpy(m.albedo_value, j.albedo_value, sizeof(m.albedo_value));
+  m.workspace = static_cast<char*>(j.workspace) + L.medium;
+  return m;
+}
+
+static rcv_volpath_options job_options(const rcv_batch_job& j, const rcv_volpath_options* o) {
+  rcv_volpath_options r;
+  std::memset(&r, 0, sizeof(r));
+  if (o != nullptr) r = *o;
+  r.max_depth = j.max_depth;
+  r.rr_depth = j.rr_depth;
+  r.hide_emitters = j.hide_emitters;
+  return r;
+}
+
+}  // namespace rcv
+
+using namespace rcv;
+
+struct rcv_batch {
+  int n = 0;
+  int device = 0;
+  rcv_volpath_options opt{};
+  BatchEntry* entries = nullptr;
+  VolJob* two = nullptr;
+  VolJob* adj = nullptr;
+  int32_t* prefix = nullptr;  // pack | image | update block prefixes, n + 1 each
+  unsigned long long* queue = nullptr;
+  uint64_t* counters = nullptr;
+  float4* path_out = nullptr;
+  int64_t total_two = 0, total_adj = 0;
+  int32_t pack_blocks = 0, pix_blocks = 0, vox_blocks = 0;
+  // host copies of the tables (kept until destroy: the upload reads them)
+  std::vector<BatchEntry> h_entries;
+  std::vector<VolJob> h_two, h_adj;
+  std::vector<int32_t> h_prefix;
+  cudaStream_t capture_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" uint64_t rcv_batch_job_workspace_bytes(const rcv_batch_job* job) {
+  if (job == nullptr || job->dims[0] <= 0 || job->dims[1] <= 0 || job->dims[2] <= 0 || job->sensor.width <= 0 ||
+      job->sensor.height <= 0)
+    return 0;
+  return job_layout(*job).total;
+}
+
+extern "C" int rcv_batch_job_init(const rcv_batch_job* job, void* stream) {
+  int rc = validate_job(job, 0);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const JobLayout L = job_layout(*job);
+  char* ws = static_cast<char*>(job->workspace);
+  RCV_TRY_CUDA(cudaMemsetAsync(ws + L.header, 0, sizeof(JobHeader), st), "job status reset");
+  const rcv_medium m = job_medium(*job, L);
+  const rcv_volpath_options o = job_options(*job, nullptr);
+  VolJob J;
+  rc = make_volume_job(&m, &job->sensor, &o, 0u, job->spp, &J);
+  if (rc) return rc;
+  return order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
+                      st);
+}
+
+extern "C" uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n) {
+  if (jobs == nullptr || n < 1 || n > kMaxBatchJobs) return 0;
+  int64_t total = 0;
+  for (int j = 0; j < n; ++j) {
+    if (jobs[j].sensor.width <= 0 || jobs[j].sensor.height <= 0 || jobs[j].spp <= 0) return 0;
+    total += primal_paths(jobs[j]);
+  }
+  return plan_layout(n, total).total;
+}
+
+extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_volpath_options* opts,
+                                void* workspace, uint64_t workspace_bytes, rcv_batch** out, void* stream) {
+  RCV_REQUIRE(out != nullptr, "out is NULL");
+  *out = nullptr;
+  RCV_REQUIRE(jobs != nullptr && n >= 1 && n <= kMaxBatchJobs, "need 1..%d jobs", kMaxBatchJobs);
+  for (int j = 0; j < n; ++j) {
+    int rc = validate_job(&jobs[j], j);
+    if (rc) return rc;
+  }
+  if (opts != nullptr) {
+    RCV_REQUIRE(opts->order == RCV_ORDER_LONGEST_FIRST || opts->order == RCV_ORDER_ROW_MAJOR,
+                "unknown pixel order %d", opts->order);
+    RCV_REQUIRE(opts->batch >= 0 && opts->batch <= (1 << 20), "batch must be in [0, 2^20]");
+    RCV_REQUIRE(opts->defer >= 0 && opts->defer <= 32, "defer must be in [0, 32]");
+    RCV_REQUIRE(opts->blocks_per_sm >= 0, "blocks_per_sm must be >= 0");
+  }
+  const uint64_t need = rcv_batch_workspace_bytes(jobs, n);
+  RCV_REQUIRE(need > 0 && workspace_bytes >= need, "batch workspace too small: %llu bytes, need %llu",
+              (unsigned long long)workspace_bytes, (unsigned long long)need);
+  RCV_REQUIRE(workspace != nullptr && (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
+              "batch workspace must be non-NULL and 256-byte aligned");
+
+  int device = 0;
+  RCV_TRY_CUDA(cudaGetDevice(&device), "cudaGetDevice");
+  rcv_batch* b = new (std::nothrow) rcv_batch();
+  RCV_REQUIRE(b != nullptr, "out of host memory");
+  b->n = n;
+  b->device = device;
+  if (opts != nullptr) b->opt = *opts;
+  b->h_entries.resize(n);
+  b->h_two.resize(n);
+  b->h_adj.resize(n);
+  b->h_prefix.assign(3 * size_t(n + 1), 0);
+  int32_t* pp = b->h_prefix.data();
+  int32_t* pi = pp + (n + 1);
+  int32_t* pv = pi + (n + 1);
+  int64_t two_total = 0, adj_total = 0, pack_blocks = 0, pix_blocks = 0, vox_blocks = 0;
+  for (int j = 0; j < n; ++j) {
+    const rcv_batch_job& d = jobs[j];
+    const JobLayout L = job_layout(d);
+    char* ws = static_cast<char*>(d.workspace);
+    const rcv_medium m = job_medium(d, L);
+    const rcv_volpath_options o = job_options(d, opts);
+    VolJob T, A;
+    int rc = make_volume_job(&m, &d.sensor, &o, 0u, d.spp, &T);
+    if (rc == RCV_OK) rc = make_volume_job(&m, &d.sensor, &o, 0u, d.spp_grad, &A);
+    if (rc) {
+      delete b;
+      return rc;
+    }
+    const uint32_t* order = reinterpret_cast<const uint32_t*>(ws + L.order);
+    const bool sorted = opts == nullptr || opts->order == RCV_ORDER_LONGEST_FIRST;
+    T.pixel_order = sorted ? order : nullptr;
+    A.pixel_order = sorted ? order : nullptr;
+    T.path_begin = two_total;
+    A.path_begin = adj_total;
+    A.grad_img = reinterpret_cast<const float*>(ws + L.grad_img);
+    if (d.albedo_m == nullptr) A.grad_albedo = nullptr;  // a fixed albedo grid gets no gradient
+    b->h_two[j] = T;
+    b->h_adj[j] = A;
+
+    BatchEntry& e = b->h_entries[j];
+    std::memset(&e, 0, sizeof(e));
+    e.d = d;
+    e.hdr = reinterpret_cast<JobHeader*>(ws + L.header);
+    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr);
+    char* mw = ws + L.medium;
+    e.cells = reinterpret_cast<float4*>(mw + M.cells);
+    e.has_albedo = d.albedo[0] != nullptr;
+    e.albedo = e.has_albedo ? reinterpret_cast<float4*>(mw + M.albedo) : nullptr;
+    e.maxbits = reinterpret_cast<uint32_t*>(mw + M.maxbits);
+    e.grad_cells = reinterpret_cast<float4*>(mw + M.grad_cells);
+    e.opt_albedo = d.albedo_m != nullptr;
+    e.grad_albedo = e.opt_albedo ? reinterpret_cast<float4*>(mw + M.grad_albedo) : nullptr;
+    e.grad_img = reinterpret_cast<float*>(ws + L.grad_img);
+    e.npix = int64_t(d.sensor.width) * d.sensor.height;
+    e.nv = int64_t(d.dims[0]) * d.dims[1] * d.dims[2];
+    e.nc = int64_t(d.dims[0] + 1) * (d.dims[1] + 1) * (d.dims[2] + 1);
+    e.two_begin = two_total;
+    const int64_t nelem = e.npix * 3;
+    e.inv_n = 1.0 / (double)nelem;
+    e.gscale = (float)(1.0 / (double)nelem);
+
+    pp[j] = (int32_t)pack_blocks;
+    pi[j] = (int32_t)pix_blocks;
+    pv[j] = (int32_t)vox_blocks;
+    pack_blocks += grid_for(e.nc, kBatchBlock);
+    pix_blocks += grid_for(e.npix, kBatchBlock);
+    vox_blocks += grid_for(e.nv, kBatchBlock);
+    two_total += T.path_count;
+    adj_total += A.path_count;
+    if (pack_blocks >= INT32_MAX || pix_blocks >= INT32_MAX || vox_blocks >= INT32_MAX) {
+      delete b;
+      set_error("batch too large: more than 2^31 blocks in an elementwise kernel");
+      return RCV_ERR_INVALID;
+    }
+  }
+  pp[n] = (int32_t)pack_blocks;
+  pi[n] = (int32_t)pix_blocks;
+  pv[n] = (int32_t)vox_blocks;
+  b->total_two = two_total;
+  b->total_adj = adj_total;
+  b->pack_blocks = (int32_t)pack_blocks;
+  b->pix_blocks = (int32_t)pix_blocks;
+  b->vox_blocks = (int32_t)vox_blocks;
+
+  const PlanLayout P = plan_layout(n, two_total);
+  char* w = static_cast<char*>(workspace);
+  b->entries = reinterpret_cast<BatchEntry*>(w + P.entries);
+  b->two = reinterpret_cast<VolJob*>(w + P.two);
+  b->adj = reinterpret_cast<VolJob*>(w + P.adj);
+  b->prefix = reinterpret_cast<int32_t*>(w + P.prefix);
+  b->queue = reinterpret_cast<unsigned long long*>(w + P.queue);
+  b->counters = reinterpret_cast<uint64_t*>(w + P.counters);
+  b->path_out = reinterpret_cast<float4*>(w + P.path_out);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(b->entries, b->h_entries.data(), sizeof(BatchEntry) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->two, b->h_two.data(), sizeof(VolJob) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->adj, b->h_adj.data(), sizeof(VolJob) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->prefix, b->h_prefix.data(), sizeof(int32_t) * b->h_prefix.size(),
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 2 * RCV_COUNTER_COUNT * sizeof(uint64_t), st);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_check(e, "batch table upload");
+  }
+  warm_launch_config();
+  *out = b;
+  return RCV_OK;
+}
+
+namespace rcv {
+static int enqueue_step(rcv_batch* b, cudaStream_t st) {
+  const int n = b->n;
+  const int32_t* pp = b->prefix;
+  const int32_t* pi = pp + (n + 1);
+  const int32_t* pv = pi + (n + 1);
+  batch_prologue_kernel<<<1, kBatchBlock, 0, st>>>(b->entries, b->two, b->adj, n);
+  int rc = launched("batch prologue launch");
+  if (rc) return rc;
+  batch_pack_kernel<<<(unsigned)b->pack_blocks, kBatchBlock, 0, st>>>(b->entries, pp, n);
+  rc = launched("batch pack launch");
+  if (rc) return rc;
+  VolJob none;
+  std::memset(&none, 0, sizeof(none));
+  rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out,
+                         b->counters, st);
+  if (rc) return rc;
+  batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
+  rc = launched("batch image launch");
+  if (rc) return rc;
+  rc = launch_persistent(kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr,
+                         b->counters + RCV_COUNTER_COUNT, st);
+  if (rc) return rc;
+  batch_update_kernel<<<(unsigned)b->vox_blocks, kBatchBlock, 0, st>>>(b->entries, pv, n);
+  return launched("batch update launch");
+}
+}  // namespace rcv
+
+extern "C" int rcv_batch_step(rcv_batch* b, int32_t use_graph, void* stream) {
+  RCV_REQUIRE(b != nullptr, "batch is NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!use_graph) return enqueue_step(b, st);
+  if (b->exec == nullptr) {
+    if (b->capture_stream == nullptr)
+      RCV_TRY_CUDA(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking), "capture stream");
+    RCV_TRY_CUDA(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const uint64_t before = rcv_kernel_launches();
+    const int rc = enqueue_step(b, b->capture_stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->capture_stream, &g);
+    // captured launches did not run: take them out of the launch count
+    add_launches(-int64_t(rcv_kernel_launches() - before));
+    if (rc != RCV_OK || e != cudaSuccess) {
+      if (g != nullptr) cudaGraphDestroy(g);
+      return rc != RCV_OK ? rc : cuda_check(e, "end capture");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(g);
+      b->exec = nullptr;
+      return cuda_check(ie, "graph instantiate");
+    }
+    b->graph = g;
+  }
+  RCV_TRY_CUDA(cudaGraphLaunch(b->exec, st), "graph launch");
+  add_launches(kBatchKernels);
+  return RCV_OK;
+}
+
+extern "C" uint64_t* rcv_batch_counters(rcv_batch* b) { return b != nullptr ? b->counters : nullptr; }
+
+extern "C" int32_t rcv_batch_kernels_per_step(void) { return kBatchKernels; }
+
+extern "C" int rcv_batch_destroy(rcv_batch* b) {
+  if (b == nullptr) return RCV_OK;
+  if (b->exec != nullptr) cudaGraphExecDestroy(b->exec);
+  if (b->graph != nullptr) cudaGraphDestroy(b->graph);
+  if (b->capture_stream != nullptr) cudaStreamDestroy(b->capture_stream);
+  delete b;
+  return RCV_OK;
+}

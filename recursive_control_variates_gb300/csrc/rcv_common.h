@@ -24,6 +24,8 @@ inline int cuda_check(cudaError_t e, const char* what) {
 // Counts one kernel launch of librcv (see rcv_kernel_launches) and reports a
 // launch failure.
 void count_launch();
+// Adds delta (may be negative) to the launch count.
+void add_launches(int64_t delta);
 inline int launched(const char* what) {
   count_launch();
   return cuda_check(cudaGetLastError(), what);

@@ -21,6 +21,8 @@ static std::atomic<uint64_t> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+void add_launches(int64_t delta) { g_launches.fetch_add(uint64_t(delta), std::memory_order_relaxed); }
+
 void set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -96,14 +98,8 @@ __global__ void loss_partial_kernel(int kind, const float* __restrict__ img,
   double acc = 0.0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x) {
-    const float diff = img[i] - ref[i];
-    if (kind == RCV_LOSS_L2) {
-      acc += double(diff * diff);
-      if (grad) grad[i] = (2.0f * diff) * gscale;
-    } else {
-      acc += double(fabsf(diff));
-      if (grad) grad[i] = (diff > 0.0f ? 1.0f : (diff < 0.0f ? -1.0f : 0.0f)) * gscale;
-    }
+    const float gi = loss_grad(kind, img[i] - ref[i], gscale, acc);
+    if (grad) grad[i] = gi;
   }
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
   __shared__ double warp_sums[kLossBlock / 32];
@@ -312,4 +308,55 @@ extern "C" int rcv_adam_step(float* param, float* grad, float* m, float* v, int6
   adam_kernel<<<grid_for(n, block), block, 0, static_cast<cudaStream_t>(stream)>>>(
       param, grad, m, v, n, lr_t, beta1, beta2, 1.0f - beta1, 1.0f - beta2, eps, lo, hi, zero_grad);
   return launched("adam launch");
+}
+
+// ------------------------------------------------- bias-correction tables
+namespace rcv {
+constexpr int64_t kMaxPowerTable = int64_t(1) << 22;
+}
+
+extern "C" int64_t rcv_cv_table_len(float beta) {
+  RCV_REQUIRE(beta >= 0.0f && beta < 1.0f, "beta must be in [0, 1), got %g", (double)beta);
+  for (int64_t k = 0; k < kMaxPowerTable; ++k)
+    if (1.0f - pow_f32(beta, (int)k) == 1.0f) return k + 1;
+  set_error("beta = %.9g: 1 - beta^k does not reach 1.0f within %lld steps", (double)beta,
+            (long long)kMaxPowerTable);
+  return RCV_ERR_UNSUPPORTED;
+}
+
+extern "C" int rcv_cv_table_fill(float beta, float* out, int64_t len) {
+  RCV_REQUIRE(beta >= 0.0f && beta < 1.0f, "beta must be in [0, 1), got %g", (double)beta);
+  RCV_REQUIRE(out != nullptr && len > 0 && len <= kMaxPowerTable, "invalid table buffer / length");
+  for (int64_t k = 0; k < len; ++k) out[k] = 1.0f - pow_f32(beta, (int)k);
+  return RCV_OK;
+}
+
+namespace rcv {
+// (sqrt(1 - beta2^t), 1 - beta1^t) with the arithmetic of rcv_adam_step.
+static void adam_corrections(float beta1, float beta2, int64_t t, double& s2, double& bc1) {
+  const double bc2 = 1.0 - std::pow((double)beta2, (double)t);
+  bc1 = 1.0 - std::pow((double)beta1, (double)t);
+  s2 = std::sqrt(bc2);
+}
+}  // namespace rcv
+
+extern "C" int64_t rcv_adam_table_len(float beta1, float beta2) {
+  RCV_REQUIRE(beta1 >= 0.0f && beta1 < 1.0f && beta2 >= 0.0f && beta2 < 1.0f,
+              "Adam betas must be in [0, 1)");
+  for (int64_t t = 0; t < kMaxPowerTable; ++t) {
+    double s2, bc1;
+    adam_corrections(beta1, beta2, t, s2, bc1);
+    if (s2 == 1.0 && bc1 == 1.0) return t + 1;
+  }
+  set_error("Adam betas (%.9g, %.9g): bias corrections do not reach 1.0 within %lld steps", (double)beta1,
+            (double)beta2, (long long)kMaxPowerTable);
+  return RCV_ERR_UNSUPPORTED;
+}
+
+extern "C" int rcv_adam_table_fill(float beta1, float beta2, double* out, int64_t len) {
+  RCV_REQUIRE(beta1 >= 0.0f && beta1 < 1.0f && beta2 >= 0.0f && beta2 < 1.0f,
+              "Adam betas must be in [0, 1)");
+  RCV_REQUIRE(out != nullptr && len > 0 && len <= kMaxPowerTable, "invalid table buffer / length");
+  for (int64_t t = 0; t < len; ++t) adam_corrections(beta1, beta2, t, out[2 * t], out[2 * t + 1]);
+  return RCV_OK;
 }

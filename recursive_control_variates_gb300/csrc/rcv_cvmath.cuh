@@ -34,9 +34,10 @@ __host__ __device__ __forceinline__ void welford2(const CvScalars& S, float x, f
   cov = S.b2 * cov + (S.omb2 * dx1) * dy2;
 }
 
-// One element of a control-variate step, in place on the state arrays.
-__device__ __forceinline__ void cv_element(const rcv_cv_state& st, int64_t i, float x, float y,
-                                           const CvScalars& S) {
+// One element of a control-variate step, in place on the state arrays;
+// returns the blended image value.
+__device__ __forceinline__ float cv_element(const rcv_cv_state& st, int64_t i, float x, float y,
+                                            const CvScalars& S) {
   float img = st.img[i], w = st.w_s[i], vn = st.v_n[i];
   float mx = st.mean_x[i], my = st.mean_y[i], vx = st.var_x[i], vy = st.var_y[i], cv = st.cov[i];
   if (S.do_pre) welford2(S, x, y, mx, my, vx, vy, cv);
@@ -57,21 +58,40 @@ __device__ __forceinline__ void cv_element(const rcv_cv_state& st, int64_t i, fl
   st.var_x[i] = vx;
   st.var_y[i] = vy;
   st.cov[i] = cv;
+  return img;
 }
 
-// Adam update of one parameter (bias correction folded into lr_t) + clamp.
+// Adam update of one parameter value (bias correction folded into lr_t) +
+// clamp; updates the moments in place and returns the new value.
+__device__ __forceinline__ float adam_value(float p, float g, float& m, float& v, float lr_t, float b1, float b2,
+                                            float omb1, float omb2, float eps, float lo, float hi) {
+  m = b1 * m + omb1 * g;
+  v = b2 * v + omb2 * (g * g);
+  const float q = p - (lr_t * m) / (sqrtf(v) + eps);
+  return fminf(fmaxf(q, lo), hi);
+}
+
 __device__ __forceinline__ void adam_element(float* p, float* g, float* m, float* v, int64_t i, float lr_t,
                                              float b1, float b2, float omb1, float omb2, float eps, float lo,
                                              float hi, bool zero_grad) {
-  const float gi = g[i];
-  const float mi = b1 * m[i] + omb1 * gi;
-  const float vi = b2 * v[i] + omb2 * (gi * gi);
-  float pi = p[i] - (lr_t * mi) / (sqrtf(vi) + eps);
-  pi = fminf(fmaxf(pi, lo), hi);
+  float mi = m[i], vi = v[i];
+  const float pi = adam_value(p[i], g[i], mi, vi, lr_t, b1, b2, omb1, omb2, eps, lo, hi);
   m[i] = mi;
   v[i] = vi;
   p[i] = pi;
   if (zero_grad) g[i] = 0.0f;
+}
+
+// Derivative of the image loss for one element (utils.py:21-25): L2
+// 2 diff / n, L1 sign(diff) / n with gscale = float32(1 / n); adds the
+// element's loss term to acc.
+__device__ __forceinline__ float loss_grad(int kind, float diff, float gscale, double& acc) {
+  if (kind == RCV_LOSS_L2) {
+    acc += double(diff * diff);
+    return (2.0f * diff) * gscale;
+  }
+  acc += double(fabsf(diff));
+  return (diff > 0.0f ? 1.0f : (diff < 0.0f ? -1.0f : 0.0f)) * gscale;
 }
 
 }  // namespace rcv

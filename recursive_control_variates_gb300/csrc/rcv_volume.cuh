@@ -28,6 +28,7 @@
 // radiance is written to a per-path slot; a separate pass sums a pixel's
 // samples in sample order, so results do not depend on the schedule.
 #pragma once
+#include "../../include/rcv.h"
 #include "rcv_device.cuh"
 
 namespace rcv {
@@ -211,5 +212,20 @@ __device__ __forceinline__ bool roulette(const VolJob& J, Pcg32& rng, int depth,
   return true;
 }
 
+// ---------------------------------------- host launchers (rcv_volume.cu)
+// Validates a medium + sensor + options and fills a job for one launch.
+int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o, uint32_t seed,
+                    int spp, VolJob* J);
+// Writes the job's pixels, longest expected path first, into `order`
+// (buckets: 256 uint32 of scratch).
+int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, cudaStream_t st);
+// Persistent tracer launch (TraceMode `mode`) over `total` paths of one job
+// (jobs == NULL) or of a device job table of njobs entries.
+int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
+                      const rcv_volpath_options* o, unsigned long long* queue_counter, float4* path_out,
+                      uint64_t* counters, cudaStream_t st);
+// Queries the occupancy and SM count the launchers cache, so that later
+// launches (e.g. under stream capture) make no device queries.
+void warm_launch_config();
 
 }  // namespace rcv
