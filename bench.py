@@ -332,12 +332,19 @@ def run_ours(args, cfg):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(cfg, job, target_seconds=args.cpu_seconds)
 
+    has_albedo = job.has_albedo
+    del job
+    torch.cuda.empty_cache()
+    # the batched and served forms run on a single GPU only (rank 0 of one)
+    batched = None if (args.no_batched or world > 1) else batched_form(args, device, flush)
+    served = None if (args.no_served or world > 1) else served_form(args, device)
+
     ms_sorted = sorted(step_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian-blob medium; no public dataset)",
-        "config": {"workload": f"{cfg.name}: {cfg.grid}^3 density" + (f" + {cfg.grid}^3 RGB albedo" if job.has_albedo
+        "config": {"workload": f"{cfg.name}: {cfg.grid}^3 density" + (f" + {cfg.grid}^3 RGB albedo" if has_albedo
                    else f", albedo {cfg.albedo}") + f", {cfg.res}x{cfg.res}, spp={cfg.spp}, spp_grad={cfg.spp_grad}, "
                    f"max_depth={cfg.max_depth}, cv_ps + path-replay adjoint + Adam",
                    "paths_per_step": paths, "parallelism": f"replicas x{world}",
@@ -351,6 +358,8 @@ def run_ours(args, cfg):
         "clocks": clocks.summary(),
         "phase": "late (density starts at 0.8 x the true grid)",
         "early_phase": early,
+        "batched": batched,
+        "served": served,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -401,6 +410,143 @@ def split_counters(job):
 
 
 # ------------------------------------------------------------ CPU baseline
+# ------------------------------------------------- batched and served forms
+def pctl(values, q):
+    v = sorted(values)
+    return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))]
+
+
+def plain_mix_setup(mix, jobs, device):
+    """The plain single-job API objects of each job of a mix, at the job's
+    current parameters (load_dict / traverse / cv integrator / ad.Adam)."""
+    import recursive_control_variates_gb300 as rcv
+    from recursive_control_variates_gb300 import scenes
+
+    plains = []
+    for m, job in zip(mix, jobs):
+        dens0 = job.params().detach().cpu().numpy()[..., None]
+        scene = rcv.load_dict(scenes.scene_dict(dens0, 0.8, res=m["res"], spp=m["spp"]), device=device)
+        params = rcv.traverse(scene)
+        integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath",
+                                                             "max_depth": m["max_depth"], "rr_depth": m["max_depth"]}})
+        opt = rcv.ad.Adam(lr=0.02)
+        opt[scenes.DENSITY_KEY] = dens0
+        opt.set_bounds(scenes.DENSITY_KEY, 0.0, 250.0)
+        params.update(opt)
+        params.update(opt)
+        plains.append([scene, params, integ, opt, job.target, job.seed, m["spp"], 0])
+    return plains
+
+
+def plain_mix_step(plains):
+    import recursive_control_variates_gb300 as rcv
+
+    for p in plains:
+        scene, params, integ, opt, target, seed, spp, it = p
+        params.update(opt)
+        img = rcv.render(scene, params, integrator=integ, seed=seed + it, spp=spp)
+        rcv.l2_loss(img, target).backward()
+        opt.step()
+        p[7] += 1
+
+
+def batched_form(args, device, flush):
+    """cfg4: 32 uneven cv_ps jobs advanced by one BatchedCV step per
+    iteration (CUDA graph, autotuned launch options), against the plain
+    single-job API stepping the same jobs one after another."""
+    import torch
+
+    from recursive_control_variates_gb300 import batch
+
+    mix = batch.cfg4_mix(32)
+    jobs = batch.make_mix_jobs(mix, device=device, target_spp=args.target_spp)
+    paths = sum(j.paths_per_step() for j in jobs)
+    plains = plain_mix_setup(mix, jobs, device)
+    t0 = time.perf_counter()
+    best = batch.autotune(jobs, steps=2)
+    tune_s = time.perf_counter() - t0
+    b = batch.BatchedCV(jobs, options=best, use_graph=True)
+    stream = torch.cuda.current_stream(device)
+    b.step(args.warmup)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.batched_steps)]
+    c0 = b.counters().clone()
+    for i, (a, e) in enumerate(ev):
+        flush.fill_(float(i))
+        a.record(stream)
+        b.step()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(e) for a, e in ev]
+    dc = (b.counters() - c0).cpu().numpy().astype(np.float64) / len(ms)
+    b.close()
+    # plain single-job form, same jobs, same launch options of the tracers
+    plain_mix_step(plains)
+    torch.cuda.synchronize()
+    rounds = max(1, args.plain_rounds)
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    a.record(stream)
+    for _ in range(rounds):
+        plain_mix_step(plains)
+    e.record(stream)
+    torch.cuda.synchronize()
+    plain_wall = (time.perf_counter() - t0) / rounds
+    plain_ms = a.elapsed_time(e) / rounds
+    total = sum(ms) / 1e3
+    value = paths * len(ms) / total
+    plain_value = paths / (plain_ms / 1e3)
+    return {
+        "workload": "cfg4: 32 cv_ps jobs, grids {16,32,64,128}^3, films {64..512}^2, spp {4,8,16}, depth 32, "
+                    "constant albedo 0.8, one persistent launch per tracer pass, CUDA graph",
+        "value": value, "unit": UNIT, "ms_per_step": total * 1e3 / len(ms), "steps": len(ms),
+        "p50_ms": pctl(ms, 0.5), "p99_ms": pctl(ms, 0.99), "paths_per_step": paths,
+        "launch_options": best.__dict__, "autotune_s": round(tune_s, 2),
+        "gpu_launches_per_step": b.kernels_per_step,
+        "plain_value": plain_value, "plain_ms_per_round": plain_ms, "plain_wall_ms_per_round": plain_wall * 1e3,
+        "speedup_vs_plain": value / plain_value,
+        "lookups_per_path": float((dc[0][1] + dc[0][2] + dc[1][1] + dc[1][2]) / max(dc[0][0] + dc[1][0], 1.0)),
+        "l2": "flushed between timed steps (512 MB write)",
+    }
+
+
+def served_form(args, device):
+    """cfg5: Poisson arrivals (2000 req/s) of gradient-step requests over 64
+    resident cfg4-mix jobs + 8 jobs at 256^3 / 1024^2 / spp 16, continuous
+    batching under a 120 GB HBM budget; p50/p99 request latency and paths/s."""
+    import torch
+
+    from recursive_control_variates_gb300 import batch, serve
+
+    mix = serve.cfg5_mix()
+    jobs = batch.make_mix_jobs(mix, device=device, target_spp=args.target_spp, seed_offset=5000)
+    server = serve.StepServer(120 * 10**9, device=device, options=batch.autotune(jobs[:64], steps=1), pipeline=2)
+    ids = [server.add_job(j) for j in jobs]
+    resident = sum(server.is_resident(i) for i in ids)
+    for i in ids:  # warm-up: one step of every job
+        server.submit(i)
+    server.drain()
+    torch.cuda.synchronize()
+    server.stats = serve.ServerStats()
+    arrivals = serve.poisson_arrivals(2000.0, args.served_requests, ids, seed=11)
+    t0 = time.perf_counter()
+    reqs = server.run_arrivals(arrivals)
+    wall = time.perf_counter() - t0
+    server.close()
+    lat = serve.latency_summary(reqs)
+    paths = server.stats.paths
+    return {
+        "workload": "cfg5: Poisson 2000 req/s over 64 cfg4-mix jobs + 8 jobs (256^3, 1024^2, spp 16, depth 32), "
+                    "continuous batching, 120 GB HBM budget",
+        "requests": len(reqs), "value": paths / wall, "unit": UNIT, "wall_s": wall,
+        "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"], "mean_ms": lat["mean_ms"],
+        "ticks": server.stats.ticks, "mean_jobs_per_tick": float(np.mean(server.stats.jobs_per_tick)),
+        "plan_reuses": server.stats.plan_reuses, "resident_jobs": int(resident),
+        "resident_gb": round(server.resident_bytes() / 1e9, 2),
+        "offered_paths_per_s": 2000.0 * float(np.mean([j.paths_per_step() for j in jobs])),
+    }
+
+
 def oracle_step_factory(cfg, density_old, density_new, albedo_old, albedo_new, target, threads):
     """One CPU gradient step (two-state render + CV + loss + adjoint) on a
     band of image rows, with the C++ restatement of the path."""
@@ -542,6 +688,12 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-step-seconds", type=float, default=4.0)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched (cfg4) form")
+    ap.add_argument("--no-served", action="store_true", help="skip the served (cfg5) form")
+    ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--plain-rounds", type=int, default=2)
+    ap.add_argument("--served-requests", type=int, default=400)
+    ap.add_argument("--target-spp", type=int, default=64, help="spp of the batched/served jobs' target renders")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
