@@ -110,15 +110,16 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, interval_ms: int = 50):
         self.gpu = gpu_index
+        self.interval_ms = int(interval_ms)
         self.proc = None
         self.lines: list[str] = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", str(self.interval_ms),
                  "-i", str(self.gpu)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
@@ -458,12 +459,12 @@ def batched_form(args, device, flush):
 
     from recursive_control_variates_gb300 import batch
 
-    mix = batch.cfg4_mix(32)
+    mix = batch.cfg4_mix(32)[:args.batched_jobs]
     jobs = batch.make_mix_jobs(mix, device=device, target_spp=args.target_spp)
     paths = sum(j.paths_per_step() for j in jobs)
-    plains = plain_mix_setup(mix, jobs, device)
+    plains = plain_mix_setup(mix, jobs, device) if args.plain_rounds > 0 else None
     t0 = time.perf_counter()
-    best = batch.autotune(jobs, steps=2)
+    best = batch.autotune(jobs, steps=2) if not args.no_autotune else batch.LaunchOptions()
     tune_s = time.perf_counter() - t0
     b = batch.BatchedCV(jobs, options=best, use_graph=True)
     stream = torch.cuda.current_stream(device)
@@ -471,40 +472,43 @@ def batched_form(args, device, flush):
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.batched_steps)]
     c0 = b.counters().clone()
-    for i, (a, e) in enumerate(ev):
-        flush.fill_(float(i))
-        a.record(stream)
-        b.step()
-        e.record(stream)
-    torch.cuda.synchronize()
+    with ClockSampler(device.index or 0) as clocks:
+        for i, (a, e) in enumerate(ev):
+            flush.fill_(float(i))
+            a.record(stream)
+            b.step()
+            e.record(stream)
+        torch.cuda.synchronize()
     ms = [a.elapsed_time(e) for a, e in ev]
     dc = (b.counters() - c0).cpu().numpy().astype(np.float64) / len(ms)
     b.close()
-    # plain single-job form, same jobs, same launch options of the tracers
-    plain_mix_step(plains)
-    torch.cuda.synchronize()
-    rounds = max(1, args.plain_rounds)
-    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    a.record(stream)
-    for _ in range(rounds):
-        plain_mix_step(plains)
-    e.record(stream)
-    torch.cuda.synchronize()
-    plain_wall = (time.perf_counter() - t0) / rounds
-    plain_ms = a.elapsed_time(e) / rounds
     total = sum(ms) / 1e3
     value = paths * len(ms) / total
-    plain_value = paths / (plain_ms / 1e3)
+    plain_value = plain_ms = plain_wall = None
+    if plains is not None:
+        # plain single-job form: the same jobs through the single-job API
+        plain_mix_step(plains)
+        torch.cuda.synchronize()
+        rounds = args.plain_rounds
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record(stream)
+        for _ in range(rounds):
+            plain_mix_step(plains)
+        e.record(stream)
+        torch.cuda.synchronize()
+        plain_wall = (time.perf_counter() - t0) / rounds * 1e3
+        plain_ms = a.elapsed_time(e) / rounds
+        plain_value = paths / (plain_ms / 1e3)
     return {
-        "workload": "cfg4: 32 cv_ps jobs, grids {16,32,64,128}^3, films {64..512}^2, spp {4,8,16}, depth 32, "
-                    "constant albedo 0.8, one persistent launch per tracer pass, CUDA graph",
+        "workload": f"cfg4: {len(jobs)} cv_ps jobs, grids {{16,32,64,128}}^3, films {{64..512}}^2, spp {{4,8,16}}, "
+                    "depth 32, constant albedo 0.8, one persistent launch per tracer pass, CUDA graph",
         "value": value, "unit": UNIT, "ms_per_step": total * 1e3 / len(ms), "steps": len(ms),
         "p50_ms": pctl(ms, 0.5), "p99_ms": pctl(ms, 0.99), "paths_per_step": paths,
-        "launch_options": best.__dict__, "autotune_s": round(tune_s, 2),
+        "launch_options": best.__dict__, "autotune_s": round(tune_s, 2), "clocks": clocks.summary(),
         "gpu_launches_per_step": b.kernels_per_step,
-        "plain_value": plain_value, "plain_ms_per_round": plain_ms, "plain_wall_ms_per_round": plain_wall * 1e3,
-        "speedup_vs_plain": value / plain_value,
+        "plain_value": plain_value, "plain_ms_per_round": plain_ms, "plain_wall_ms_per_round": plain_wall,
+        "speedup_vs_plain": value / plain_value if plain_value else None,
         "lookups_per_path": float((dc[0][1] + dc[0][2] + dc[1][1] + dc[1][2]) / max(dc[0][0] + dc[1][0], 1.0)),
         "l2": "flushed between timed steps (512 MB write)",
     }
@@ -690,6 +694,11 @@ def main(argv=None):
     ap.add_argument("--cpu-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (cfg4) form")
     ap.add_argument("--no-served", action="store_true", help="skip the served (cfg5) form")
+    ap.add_argument("--form", choices=["all", "batched", "served"], default="all",
+                    help="all: the headline line (plain cfg2) with the batched and served forms; batched / served: "
+                         "only that form, printed as its own JSON object (profiling runs)")
+    ap.add_argument("--batched-jobs", type=int, default=32)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--plain-rounds", type=int, default=2)
     ap.add_argument("--served-requests", type=int, default=400)
@@ -702,8 +711,21 @@ def main(argv=None):
     cfg = scenes.CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif args.form != "all":
+        run_form(args)
     else:
         run_ours(args, cfg)
+
+
+def run_form(args):
+    """One of the batched / served forms alone (single GPU)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    device = torch.device("cuda", 0)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    out = batched_form(args, device, flush) if args.form == "batched" else served_form(args, device)
+    print(json.dumps({"form": args.form, **out}), flush=True)
 
 
 if __name__ == "__main__":

@@ -80,9 +80,16 @@ typedef struct rcv_volpath_options {
 } rcv_volpath_options;
 
 /* Pixel hand-out orders of the persistent tracers.  Results do not depend on
- * the order; it only changes how evenly the work drains at the end. */
-#define RCV_ORDER_LONGEST_FIRST 0 /* longest chord through the medium first */
+ * the order; it only changes how evenly the work drains at the end.
+ * RCV_ORDER_COST hands out first the pixels whose paths took longest in the
+ * previous call on the same workspace: each tracer call adds every path's
+ * length (loop iterations) to a per-pixel cost array kept in the workspace,
+ * and the next call sorts the pixels by it (then clears it).  A first call
+ * finds whatever the workspace holds there; any content is valid and
+ * changes only the schedule. */
+#define RCV_ORDER_COST 0          /* most expensive pixels of the last call first */
 #define RCV_ORDER_ROW_MAJOR 1
+#define RCV_ORDER_LONGEST_FIRST 2 /* longest chord through the medium first     */
 
 /* Tracer kinds for rcv_render_workspace_bytes. */
 #define RCV_MODE_TWOSTATE 0
@@ -116,9 +123,11 @@ uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_gr
 int rcv_medium_prepare(const rcv_medium* medium, void* stream);
 
 /* ------------------------------------------------------------- tracers  */
-/* Scratch a tracer call needs (work-queue counter and, for the primal
- * tracers, one radiance slot per path): 256-B aligned device memory of this
- * size, passed as `workspace`.  mode = RCV_MODE_*. */
+/* Scratch a tracer call needs (work-queue counter, pixel order, per-pixel
+ * cost and, for the primal tracers, one radiance slot per path): 256-B
+ * aligned device memory of this size, passed as `workspace`.  The per-pixel
+ * cost persists from call to call (RCV_ORDER_COST); pass the same workspace to
+ * the calls of one image size.  mode = RCV_MODE_*. */
 uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp, int32_t mode);
 
 /* Two-state primal: renders the previous (img_old = H) and current
@@ -317,7 +326,8 @@ int rcv_adam_table_fill(float beta1, float beta2, double* out, int64_t len);
  * params.update, mi.render with the cv integrator around twostateprbvolpath,
  * l2/l1 loss, dr.backward, Adam + clamp) advanced together: one step of the
  * batch is one step of every job, in six kernel launches whatever the number
- * of jobs: a prologue that derives each job's seeds and CV / Adam scalars from
+ * of jobs (nine with the per-step pixel sort of RCV_ORDER_COST): a prologue
+ * that derives each job's seeds and CV / Adam scalars from
  * its device counters, the medium packing of all jobs, ONE persistent
  * two-state tracer launch over the paths of all jobs, one fused
  * reduce + control-variate + loss kernel, ONE persistent adjoint launch and
@@ -383,8 +393,8 @@ typedef struct rcv_batch_job_status {
 } rcv_batch_job_status;
 
 uint64_t rcv_batch_job_workspace_bytes(const rcv_batch_job* job);
-/* Validates the job, zeroes its status and computes its longest-first pixel
- * order (camera geometry only) into the workspace. */
+/* Validates the job, zeroes its status, computes its longest-chord-first
+ * pixel order (camera geometry only) and seeds its per-pixel cost with it. */
 int rcv_batch_job_init(const rcv_batch_job* job, void* stream);
 
 typedef struct rcv_batch rcv_batch; /* opaque host handle of a batch plan */
@@ -394,7 +404,8 @@ typedef struct rcv_batch rcv_batch; /* opaque host handle of a batch plan */
 uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n);
 /* Plans a batch of n initialised jobs with launch options `opts` (batch,
  * blocks_per_sm, defer, order; max_depth / rr_depth / hide_emitters come from
- * each job).  Copies the job tables into `workspace` on `stream`; the host
+ * each job; NULL = defaults with RCV_ORDER_COST).  The per-pixel costs and
+ * pixel orders live in the job workspaces.  Copies the job tables into `workspace` on `stream`; the host
  * array `jobs` may be freed on return.  *out is released by rcv_batch_destroy.
  * This is the one entry point group that allocates: host memory for the plan
  * and, when graphs are used, the CUDA graph. */
@@ -407,8 +418,9 @@ int rcv_batch_step(rcv_batch* batch, int32_t use_graph, void* stream);
 /* Device pointer to 2 * RCV_COUNTER_COUNT uint64 tracer counters accumulated
  * over all steps: the two-state launch, then the adjoint launch. */
 uint64_t* rcv_batch_counters(rcv_batch* batch);
-/* Kernel launches one step issues (graph replays count the same). */
-int32_t rcv_batch_kernels_per_step(void);
+/* Kernel launches one step of this batch issues (graph replays count the
+ * same): six, plus three that sort each job's pixels with RCV_ORDER_COST. */
+int32_t rcv_batch_kernels_per_step(const rcv_batch* batch);
 int rcv_batch_destroy(rcv_batch* batch);
 
 #ifdef __cplusplus

@@ -277,7 +277,11 @@ struct Tracer {
   float mu;         // majorant used for free-flight sampling
   GradSink* sink;   // non-null: adjoint replay
   V3 dL{0, 0, 0};   // adjoint: dLoss/dL for this path
-  V3 Lrem{0, 0, 0}; // adjoint: radiance still to be collected
+  V3 Ltot{0, 0, 0}; // adjoint: the path's total radiance (radiance pass)
+
+  // Radiance the path still gathers after the contributions in `got`:
+  // L_rem = L - got, one rounding per channel.
+  V3 remaining(const V3& got) const { return V3{Ltot.x - got.x, Ltot.y - got.y, Ltot.z - got.z}; }
 
   float sigma_t(const float* g, const Corners& c) const { return S.scale * trilinear(S, g, 1, 0, c); }
 
@@ -362,7 +366,6 @@ struct Tracer {
     V3 bo{1, 1, 1}, bn{1, 1, 1};
     V3& Lo = out.L_old;
     V3& Ln = out.L_new;
-    V3 Lrem_ = Lrem;
     int depth = 0;
     const float mis = 0.5f;
     const float emit_weight = 1.0f / kInvFourPi;
@@ -403,7 +406,6 @@ struct Tracer {
           const V3 cn{bn.x * k, bn.y * k, bn.z * k};
           Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
           if (mode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
-          Lrem_ = V3{Lrem_.x - cn.x, Lrem_.y - cn.y, Lrem_.z - cn.z};
         }
         return out;
       }
@@ -425,7 +427,8 @@ struct Tracer {
           bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
         } else if (sink) {
           const float sn = mu - st_n;
-          const float sd = (dL.x * Lrem_.x + dL.y * Lrem_.y) + dL.z * Lrem_.z;
+          const V3 Lr = remaining(Ln);
+          const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
           sink->density(S, c, -(S.scale * sd) / sn);
         }
         p = x;
@@ -447,10 +450,11 @@ struct Tracer {
       } else {
         bn = V3{bn.x * (ssn.x / st_n), bn.y * (ssn.y / st_n), bn.z * (ssn.z / st_n)};
         if (sink) {
-          const float sd = (dL.x * Lrem_.x + dL.y * Lrem_.y) + dL.z * Lrem_.z;
+          const V3 Lr = remaining(Ln);
+          const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
           sink->density(S, c, (S.scale * sd) / st_n);
-          sink->albedo(S, c, V3{(dL.x * Lrem_.x) / std::fmax(an.x, 1e-8f), (dL.y * Lrem_.y) / std::fmax(an.y, 1e-8f),
-                                (dL.z * Lrem_.z) / std::fmax(an.z, 1e-8f)});
+          sink->albedo(S, c, V3{(dL.x * Lr.x) / std::fmax(an.x, 1e-8f), (dL.y * Lr.y) / std::fmax(an.y, 1e-8f),
+                                (dL.z * Lr.z) / std::fmax(an.z, 1e-8f)});
         }
       }
       // phase function sample: isotropic, 1D (unused) + 2D
@@ -479,7 +483,6 @@ struct Tracer {
         float a0, b0;
         PathOut scratch;
         transmittance(replay, x, w, a0, b0, scratch, &gs);
-        Lrem_ = V3{Lrem_.x - cn.x, Lrem_.y - cn.y, Lrem_.z - cn.z};
       }
       p = x;
       d = wo;

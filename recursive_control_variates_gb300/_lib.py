@@ -67,8 +67,10 @@ class VolpathOptions(C.Structure):
     ]
 
 
-ORDER_LONGEST_FIRST = 0
+ORDER_COST = 0
 ORDER_ROW_MAJOR = 1
+ORDER_LONGEST_FIRST = 2
+ORDERS = {"cost": ORDER_COST, "row_major": ORDER_ROW_MAJOR, "longest_first": ORDER_LONGEST_FIRST}
 
 
 MODE_TWOSTATE = 0
@@ -215,7 +217,7 @@ SIGNATURES = {
     "rcv_batch_create": (C.c_int, [P(BatchJob), C.c_int32, P(VolpathOptions), vp, C.c_uint64, P(vp), vp]),
     "rcv_batch_step": (C.c_int, [vp, C.c_int32, vp]),
     "rcv_batch_counters": (vp, [vp]),
-    "rcv_batch_kernels_per_step": (C.c_int32, []),
+    "rcv_batch_kernels_per_step": (C.c_int32, [vp]),
     "rcv_batch_destroy": (C.c_int, [vp]),
     "rcv_welford_update": (C.c_int, [vp, vp, C.c_int64, vp, P(C.c_int32), C.c_float, C.c_float, vp]),
     "rcv_welford_get": (C.c_int, [vp, C.c_int64, C.c_int32, C.c_float, vp, vp]),

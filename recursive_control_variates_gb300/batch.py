@@ -299,14 +299,14 @@ class LaunchOptions:
     batch: int = 64          # paths a warp claims per queue fetch
     blocks_per_sm: int = 0   # resident tracer blocks per SM (0 = occupancy limit)
     defer: int = 8           # lanes that must wait before a deferred branch runs
-    order: str = "longest_first"
+    order: str = "cost"      # pixel hand-out order: cost | longest_first | row_major
 
     def c_struct(self) -> _lib.VolpathOptions:
         o = _lib.VolpathOptions()
         o.batch, o.blocks_per_sm, o.defer = self.batch, self.blocks_per_sm, self.defer
-        if self.order not in ("longest_first", "row_major"):
+        if self.order not in _lib.ORDERS:
             raise ValueError(f"unknown pixel order {self.order!r}")
-        o.order = _lib.ORDER_LONGEST_FIRST if self.order == "longest_first" else _lib.ORDER_ROW_MAJOR
+        o.order = _lib.ORDERS[self.order]
         return o
 
 
@@ -339,7 +339,7 @@ class BatchedCV:
         ptr = int(lib.rcv_batch_counters(self._handle))
         off = ptr - self.workspace.data_ptr()
         self._counters = self.workspace[off:off + 16 * 8].view(torch.int64).view(2, _lib.COUNTER_COUNT)
-        self.kernels_per_step = int(lib.rcv_batch_kernels_per_step())
+        self.kernels_per_step = int(lib.rcv_batch_kernels_per_step(self._handle))
 
     def step(self, steps: int = 1) -> None:
         if self._handle is None:
@@ -390,6 +390,7 @@ def default_candidates():
         out.append(LaunchOptions(defer=d))
     for k in (2, 3, 4):
         out.append(LaunchOptions(blocks_per_sm=k))
+    out.append(LaunchOptions(order="longest_first"))
     out.append(LaunchOptions(order="row_major"))
     return out
 

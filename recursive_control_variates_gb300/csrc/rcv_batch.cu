@@ -37,7 +37,7 @@
 namespace rcv {
 
 constexpr int kBatchBlock = 256;
-constexpr int kBatchKernels = 6;
+constexpr int kBatchKernels = 7;
 constexpr int kMaxBatchJobs = 1 << 16;
 
 // Per-step values of a job, written by the prologue.
@@ -55,9 +55,9 @@ struct JobHeader {
 static_assert(sizeof(rcv_batch_job_status) == 32, "status layout");
 
 // Job workspace: header | medium (cells, albedo pairs, majorants, gradient
-// cells) | order buckets | pixel order | dL/dimage.
+// cells) | order buckets | pixel order | per-pixel cost | dL/dimage.
 struct JobLayout {
-  uint64_t header, medium, buckets, order, grad_img, total;
+  uint64_t header, medium, buckets, order, cost, grad_img, total;
 };
 
 static JobLayout job_layout(const rcv_batch_job& j) {
@@ -71,6 +71,8 @@ static JobLayout job_layout(const rcv_batch_job& j) {
   L.buckets = off;
   off = align256(off + kRenderOrderBuckets * sizeof(uint32_t));
   L.order = off;
+  off = align256(off + npix * sizeof(uint32_t));
+  L.cost = off;
   off = align256(off + npix * sizeof(uint32_t));
   L.grad_img = off;
   off = align256(off + npix * 3 * sizeof(float));
@@ -88,6 +90,9 @@ struct BatchEntry {
   float4* grad_cells;
   float4* grad_albedo;  // or null
   float* grad_img;
+  uint32_t* buckets;  // 256 order buckets
+  uint32_t* order;    // pixel hand-out order
+  uint32_t* cost;     // per-pixel path lengths of the last step
   int64_t npix, nv, nc;
   int64_t two_begin;  // first path of the job in the two-state launch
   double inv_n;       // 1 / (npix * 3)
@@ -164,6 +169,7 @@ __global__ void batch_pack_kernel(const BatchEntry* __restrict__ E, const int32_
   const int j = job_of_block(bp, n, blockIdx.x);
   const BatchEntry& B = E[j];
   const int64_t i = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  if (i < kRenderOrderBuckets) B.buckets[i] = 0u;  // for this step's pixel order
   const int cur = B.hdr->step.cur;
   const float* nd = B.d.density[cur];
   const float* od = B.d.density[cur ^ 1];
@@ -181,6 +187,53 @@ __global__ void batch_pack_kernel(const BatchEntry* __restrict__ E, const int32_
     if (B.opt_albedo) B.grad_albedo[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   reduce_majorants(mo, mn, B.maxbits);
+}
+
+// Pixel order of every job by the path lengths of its last step (most
+// expensive first): bucket counts, per-job exclusive scan, placement.
+__global__ void batch_order_count_kernel(const BatchEntry* __restrict__ E, const int32_t* __restrict__ bp,
+                                         int n) {
+  const int j = job_of_block(bp, n, blockIdx.x);
+  const BatchEntry& B = E[j];
+  const int64_t pix = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  __shared__ uint32_t hist[kRenderOrderBuckets];
+  for (int k = threadIdx.x; k < kRenderOrderBuckets; k += blockDim.x) hist[k] = 0u;
+  __syncthreads();
+  if (pix < B.npix) atomicAdd(&hist[cost_bucket(B.cost[pix])], 1u);
+  __syncthreads();
+  for (int k = threadIdx.x; k < kRenderOrderBuckets; k += blockDim.x)
+    if (hist[k]) atomicAdd(B.buckets + k, hist[k]);
+}
+
+__global__ void batch_order_scan_kernel(const BatchEntry* __restrict__ E) {
+  uint32_t* counts = E[blockIdx.x].buckets;
+  __shared__ uint32_t sh[kRenderOrderBuckets];
+  const int t = threadIdx.x;
+  sh[t] = counts[t];
+  __syncthreads();
+  for (int off = 1; off < kRenderOrderBuckets; off <<= 1) {
+    const uint32_t v = t >= off ? sh[t - off] : 0u;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  counts[t] = t == 0 ? 0u : sh[t - 1];
+}
+
+__global__ void batch_order_place_kernel(const BatchEntry* __restrict__ E, const int32_t* __restrict__ bp,
+                                         int n) {
+  const int j = job_of_block(bp, n, blockIdx.x);
+  const BatchEntry& B = E[j];
+  const int64_t pix = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  if (pix >= B.npix) return;
+  B.order[atomicAdd(B.buckets + cost_bucket(B.cost[pix]), 1u)] = (uint32_t)pix;
+  B.cost[pix] = 0u;
+}
+
+// Initial per-pixel cost of a job: its chord order (longest chord first).
+__global__ void cost_from_chord_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* cost) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix < npix) cost[pix] = 4u * uint32_t(255 - chord_key(J, pix));
 }
 
 __global__ void batch_image_kernel(const BatchEntry* __restrict__ E, const int32_t* __restrict__ bp, int n,
@@ -301,12 +354,14 @@ static int validate_job(const rcv_batch_job* j, int idx) {
 }
 
 // Plan workspace: entries | two-state jobs | adjoint jobs | block prefixes |
-// queue counters | tracer counters | per-path radiance.
+// queue counters (two-state, adjoint radiance, replay, checkpoints) | tracer
+// counters | per-path radiance | adjoint per-path total radiance |
+// scatter checkpoints.
 struct PlanLayout {
-  uint64_t entries, two, adj, prefix, queue, counters, path_out, total;
+  uint64_t entries, two, adj, prefix, queue, counters, path_out, ltot, ckpt, total;
 };
 
-static PlanLayout plan_layout(int n, int64_t total_two_paths) {
+static PlanLayout plan_layout(int n, int64_t total_two_paths, int64_t total_adj_paths) {
   PlanLayout L;
   uint64_t off = 0;
   L.entries = off;
@@ -318,11 +373,15 @@ static PlanLayout plan_layout(int n, int64_t total_two_paths) {
   L.prefix = off;
   off = align256(off + 3u * uint64_t(n + 1) * sizeof(int32_t));
   L.queue = off;
-  off = align256(off + 2u * sizeof(unsigned long long));
+  off = align256(off + 4u * sizeof(unsigned long long));
   L.counters = off;
   off = align256(off + 2u * RCV_COUNTER_COUNT * sizeof(uint64_t));
   L.path_out = off;
   off = align256(off + uint64_t(total_two_paths) * 32u);
+  L.ltot = off;
+  off = align256(off + uint64_t(total_adj_paths) * 16u);
+  L.ckpt = off;
+  off = align256(off + uint64_t(ckpt_capacity(total_adj_paths)) * 64u);
   L.total = off;
   return L;
 }
@@ -368,6 +427,7 @@ struct rcv_batch {
   unsigned long long* queue = nullptr;
   uint64_t* counters = nullptr;
   float4* path_out = nullptr;
+  AdjBuffers adjbuf{};
   int64_t total_two = 0, total_adj = 0;
   int32_t pack_blocks = 0, pix_blocks = 0, vox_blocks = 0;
   // host copies of the tables (kept until destroy: the upload reads them)
@@ -377,6 +437,9 @@ struct rcv_batch {
   cudaStream_t capture_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // the adjoint radiance launch runs beside the two-state launch
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 extern "C" uint64_t rcv_batch_job_workspace_bytes(const rcv_batch_job* job) {
@@ -398,18 +461,25 @@ extern "C" int rcv_batch_job_init(const rcv_batch_job* job, void* stream) {
   VolJob J;
   rc = make_volume_job(&m, &job->sensor, &o, 0u, job->spp, &J);
   if (rc) return rc;
-  return order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
-                      st);
+  rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
+                    nullptr, st);
+  if (rc) return rc;
+  const int npix = J.width * J.height;
+  cost_from_chord_kernel<<<grid_for(npix, kBatchBlock), kBatchBlock, 0, st>>>(
+      J, npix, reinterpret_cast<uint32_t*>(ws + L.cost));
+  return launched("batch cost init launch");
 }
 
 extern "C" uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n) {
   if (jobs == nullptr || n < 1 || n > kMaxBatchJobs) return 0;
-  int64_t total = 0;
+  int64_t total = 0, total_adj = 0;
   for (int j = 0; j < n; ++j) {
-    if (jobs[j].sensor.width <= 0 || jobs[j].sensor.height <= 0 || jobs[j].spp <= 0) return 0;
+    if (jobs[j].sensor.width <= 0 || jobs[j].sensor.height <= 0 || jobs[j].spp <= 0 || jobs[j].spp_grad <= 0)
+      return 0;
     total += primal_paths(jobs[j]);
+    total_adj += int64_t(jobs[j].sensor.width) * jobs[j].sensor.height * jobs[j].spp_grad;
   }
-  return plan_layout(n, total).total;
+  return plan_layout(n, total, total_adj).total;
 }
 
 extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_volpath_options* opts,
@@ -422,7 +492,8 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     if (rc) return rc;
   }
   if (opts != nullptr) {
-    RCV_REQUIRE(opts->order == RCV_ORDER_LONGEST_FIRST || opts->order == RCV_ORDER_ROW_MAJOR,
+    RCV_REQUIRE(opts->order == RCV_ORDER_COST || opts->order == RCV_ORDER_LONGEST_FIRST ||
+                    opts->order == RCV_ORDER_ROW_MAJOR,
                 "unknown pixel order %d", opts->order);
     RCV_REQUIRE(opts->batch >= 0 && opts->batch <= (1 << 20), "batch must be in [0, 2^20]");
     RCV_REQUIRE(opts->defer >= 0 && opts->defer <= 32, "defer must be in [0, 32]");
@@ -463,9 +534,12 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
       return rc;
     }
     const uint32_t* order = reinterpret_cast<const uint32_t*>(ws + L.order);
-    const bool sorted = opts == nullptr || opts->order == RCV_ORDER_LONGEST_FIRST;
-    T.pixel_order = sorted ? order : nullptr;
-    A.pixel_order = sorted ? order : nullptr;
+    const int policy = opts == nullptr ? RCV_ORDER_COST : opts->order;
+    uint32_t* cost = policy == RCV_ORDER_COST ? reinterpret_cast<uint32_t*>(ws + L.cost) : nullptr;
+    T.pixel_order = policy != RCV_ORDER_ROW_MAJOR ? order : nullptr;
+    A.pixel_order = T.pixel_order;
+    T.pixel_cost = cost;
+    A.pixel_cost = cost;
     T.path_begin = two_total;
     A.path_begin = adj_total;
     A.grad_img = reinterpret_cast<const float*>(ws + L.grad_img);
@@ -487,6 +561,9 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     e.opt_albedo = d.albedo_m != nullptr;
     e.grad_albedo = e.opt_albedo ? reinterpret_cast<float4*>(mw + M.grad_albedo) : nullptr;
     e.grad_img = reinterpret_cast<float*>(ws + L.grad_img);
+    e.buckets = reinterpret_cast<uint32_t*>(ws + L.buckets);
+    e.order = reinterpret_cast<uint32_t*>(ws + L.order);
+    e.cost = reinterpret_cast<uint32_t*>(ws + L.cost);
     e.npix = int64_t(d.sensor.width) * d.sensor.height;
     e.nv = int64_t(d.dims[0]) * d.dims[1] * d.dims[2];
     e.nc = int64_t(d.dims[0] + 1) * (d.dims[1] + 1) * (d.dims[2] + 1);
@@ -518,7 +595,8 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->pix_blocks = (int32_t)pix_blocks;
   b->vox_blocks = (int32_t)vox_blocks;
 
-  const PlanLayout P = plan_layout(n, two_total);
+  RCV_REQUIRE(adj_total < (int64_t(1) << 32), "a batch must have fewer than 2^32 gradient paths");
+  const PlanLayout P = plan_layout(n, two_total, adj_total);
   char* w = static_cast<char*>(workspace);
   b->entries = reinterpret_cast<BatchEntry*>(w + P.entries);
   b->two = reinterpret_cast<VolJob*>(w + P.two);
@@ -527,6 +605,10 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->queue = reinterpret_cast<unsigned long long*>(w + P.queue);
   b->counters = reinterpret_cast<uint64_t*>(w + P.counters);
   b->path_out = reinterpret_cast<float4*>(w + P.path_out);
+  b->adjbuf.ckpt = reinterpret_cast<float4*>(w + P.ckpt);
+  b->adjbuf.ckpt_count = b->queue + 3;
+  b->adjbuf.ckpt_cap = ckpt_capacity(adj_total);
+  b->adjbuf.path_ltot = reinterpret_cast<float4*>(w + P.ltot);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemcpyAsync(b->entries, b->h_entries.data(), sizeof(BatchEntry) * n, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
@@ -542,6 +624,12 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     return cuda_check(e, "batch table upload");
   }
   warm_launch_config();
+  if (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+    rcv_batch_destroy(b);
+    return cuda_check(cudaGetLastError(), "batch stream / event creation");
+  }
   *out = b;
   return RCV_OK;
 }
@@ -558,15 +646,36 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   batch_pack_kernel<<<(unsigned)b->pack_blocks, kBatchBlock, 0, st>>>(b->entries, pp, n);
   rc = launched("batch pack launch");
   if (rc) return rc;
+  if (b->opt.order == RCV_ORDER_COST) {
+    batch_order_count_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n);
+    rc = launched("batch order count launch");
+    if (rc) return rc;
+    batch_order_scan_kernel<<<(unsigned)n, kRenderOrderBuckets, 0, st>>>(b->entries);
+    rc = launched("batch order scan launch");
+    if (rc) return rc;
+    batch_order_place_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n);
+    rc = launched("batch order place launch");
+    if (rc) return rc;
+  }
   VolJob none;
   std::memset(&none, 0, sizeof(none));
-  rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out,
+  // the adjoint radiance pass needs no image gradient: it runs on the side
+  // stream beside the two-state pass and the image kernel
+  RCV_TRY_CUDA(cudaEventRecord(b->fork, st), "fork record");
+  RCV_TRY_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "fork wait");
+  RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, sizeof(unsigned long long), b->side), "checkpoint reset");
+  rc = launch_persistent(kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr, &b->adjbuf,
+                         b->counters + RCV_COUNTER_COUNT, b->side);
+  if (rc) return rc;
+  RCV_TRY_CUDA(cudaEventRecord(b->join, b->side), "join record");
+  rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr,
                          b->counters, st);
   if (rc) return rc;
   batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
   rc = launched("batch image launch");
   if (rc) return rc;
-  rc = launch_persistent(kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr,
+  RCV_TRY_CUDA(cudaStreamWaitEvent(st, b->join, 0), "join wait");
+  rc = launch_persistent(kReplay, none, b->adj, n, b->total_adj, &b->opt, b->queue + 2, nullptr, &b->adjbuf,
                          b->counters + RCV_COUNTER_COUNT, st);
   if (rc) return rc;
   batch_update_kernel<<<(unsigned)b->vox_blocks, kBatchBlock, 0, st>>>(b->entries, pv, n);
@@ -601,19 +710,25 @@ extern "C" int rcv_batch_step(rcv_batch* b, int32_t use_graph, void* stream) {
     b->graph = g;
   }
   RCV_TRY_CUDA(cudaGraphLaunch(b->exec, st), "graph launch");
-  add_launches(kBatchKernels);
+  add_launches(rcv_batch_kernels_per_step(b));
   return RCV_OK;
 }
 
 extern "C" uint64_t* rcv_batch_counters(rcv_batch* b) { return b != nullptr ? b->counters : nullptr; }
 
-extern "C" int32_t rcv_batch_kernels_per_step(void) { return kBatchKernels; }
+extern "C" int32_t rcv_batch_kernels_per_step(const rcv_batch* b) {
+  if (b == nullptr) return RCV_ERR_INVALID;
+  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0);
+}
 
 extern "C" int rcv_batch_destroy(rcv_batch* b) {
   if (b == nullptr) return RCV_OK;
   if (b->exec != nullptr) cudaGraphExecDestroy(b->exec);
   if (b->graph != nullptr) cudaGraphDestroy(b->graph);
   if (b->capture_stream != nullptr) cudaStreamDestroy(b->capture_stream);
+  if (b->side != nullptr) cudaStreamDestroy(b->side);
+  if (b->fork != nullptr) cudaEventDestroy(b->fork);
+  if (b->join != nullptr) cudaEventDestroy(b->join);
   delete b;
   return RCV_OK;
 }

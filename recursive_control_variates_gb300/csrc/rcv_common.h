@@ -72,13 +72,18 @@ inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo) {
 }
 
 // Scratch layout of one tracer call (all offsets 256-byte aligned):
-// queue counter | order bucket counts | pixel order | per-path radiance
-// (32 B per path for two-state, 16 B single-state, none for adjoints).
+// queue counter (+ checkpoint counter) | order bucket counts | pixel order |
+// per-pixel cost | per-path radiance (32 B per path for two-state, 16 B
+// single-state) | adjoint: per-path total radiance | scatter checkpoints.
 constexpr int kRenderOrderBuckets = 256;
 
 struct RenderLayout {
-  uint64_t counter, buckets, order, path_out, total;
+  uint64_t counter, buckets, order, cost, path_out, ltot, ckpt, total;
 };
+
+// Adjoint scatter checkpoints: 64 bytes each, room for 2 per path plus a
+// margin; paths whose checkpoints do not fit are replayed whole.
+inline int64_t ckpt_capacity(int64_t paths) { return 2 * paths + 65536; }
 
 inline uint64_t path_out_bytes(int64_t paths, int mode) {
   return mode == RCV_MODE_ADJOINT ? 0u : uint64_t(paths) * (mode == RCV_MODE_TWOSTATE ? 32u : 16u);
@@ -89,8 +94,12 @@ inline RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
   L.counter = 0;
   L.buckets = 256;
   L.order = align256(L.buckets + kRenderOrderBuckets * sizeof(uint32_t));
-  L.path_out = align256(L.order + uint64_t(npix) * sizeof(uint32_t));
-  L.total = align256(L.path_out + path_out_bytes(paths, mode));
+  L.cost = align256(L.order + uint64_t(npix) * sizeof(uint32_t));
+  L.path_out = align256(L.cost + uint64_t(npix) * sizeof(uint32_t));
+  const bool adj = mode == RCV_MODE_ADJOINT;
+  L.ltot = align256(L.path_out + path_out_bytes(paths, mode));
+  L.ckpt = align256(L.ltot + (adj ? uint64_t(paths) * 16u : 0u));
+  L.total = align256(L.ckpt + (adj ? uint64_t(ckpt_capacity(paths)) * 64u : 0u));
   return L;
 }
 

@@ -7,7 +7,8 @@
 //   kScatter  real scattering event waiting to be processed (albedo lookups,
 //             phase and NEE direction sampling, adjoint scatter)
 //   kNee      walking the NEE shadow ray (ratio tracking)
-//   kNeeAdj   adjoint only: replaying the shadow walk to scatter gradients
+//   kNeeAdj   adjoint replay only: walking the shadow ray again to scatter
+//             its gradients
 // Path starts and scattering events cost 100-200 instructions while a
 // free-flight step costs a few dozen; executing them as soon as one lane
 // needs them would leave the other 31 lanes waiting in almost every
@@ -16,12 +17,45 @@
 // so the expensive branches run with many lanes and the free-flight step
 // stays converged.  The per-path random-number order is unchanged, so results
 // do not depend on the schedule.
+//
+// Adjoint (path replay backpropagation, Vicini et al. 2021) in two launches.
+// The gradient of an event is dL . L_rem times a factor of the event, where
+// L_rem = L - (radiance gathered before the event) is only known once the
+// path has ended.
+//   kAdjoint  radiance pass: traces the path on `new`, stores its total
+//             radiance L and, at every real scattering event, a 64-byte
+//             checkpoint (random-number state, position, depth, throughput,
+//             radiance so far, NEE contribution).
+//   kReplay   a queue of replay tasks: the segment of every path from the
+//             camera to its first scattering event, then one task per
+//             checkpoint (that scattering event, its NEE shadow ray and the
+//             segment to the next event).  Each task replays its segment with
+//             the same random numbers and scatters the gradients; a task
+//             stops at the next scattering event, which has its own task.
+// A path whose checkpoints did not fit is replayed whole by its camera task.
+// Replaying segments instead of whole paths keeps every task short, so the
+// launch does not end on a few paths that scatter dozens of times.
 #pragma once
 #include "rcv_volume.cuh"
 
 namespace rcv {
 
 enum PathPhase { kIdle = 0, kStart = 1, kMain = 2, kScatter = 3, kNee = 4, kNeeAdj = 5 };
+
+// Replay task kinds.
+enum TaskKind { kTaskSegment = 0, kTaskWhole = 1, kTaskCheckpoint = 2 };
+
+// Checkpoint record (4 float4): [path, depth, rng.state lo, hi] [p, bn.x]
+// [bn.y, bn.z, Lacc.x, Lacc.y] [Lacc.z, cn]; Lacc = radiance gathered before
+// the event's NEE contribution cn.
+__device__ __forceinline__ void write_checkpoint(float4* rec, uint32_t path, int depth, uint64_t state,
+                                                 const V3& p, const V3& bn, const V3& lacc, const V3& cn) {
+  rec[0] = make_float4(__uint_as_float(path), __int_as_float(depth), __uint_as_float((uint32_t)state),
+                       __uint_as_float((uint32_t)(state >> 32)));
+  rec[1] = make_float4(p.x, p.y, p.z, bn.x);
+  rec[2] = make_float4(bn.y, bn.z, lacc.x, lacc.y);
+  rec[3] = make_float4(lacc.z, cn.x, cn.y, cn.z);
+}
 
 // Job of a global path index: binary search in the launch's job table.
 __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queue& Q, int64_t path) {
@@ -39,45 +73,50 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
 
 template <int kMode>
 __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& cnt) {
+  constexpr bool kAdj = kMode == kAdjoint || kMode == kReplay;  // single-state `new`, gradients
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const float mis = 0.5f;  // power heuristic between two equal 1/(4 pi) pdfs
   const float emit_weight = 1.0f / kInvFourPi;
   const unsigned defer = (unsigned)Q.defer;
+  // replay: camera tasks [0, paths), then the checkpoints that were written
+  const int64_t total =
+      kMode == kReplay ? Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap) : Q.total;
 
   int64_t batch_next = 0, batch_end = 0;
   bool queue_empty = false;
   int64_t path = 0;
   const VolJob* Jp = &single;
   int phase = kIdle;
-  int pass = 0;  // adjoint: 0 = radiance pass, 1 = replay pass
   float mu = 0.0f, inv_mu = 0.0f, half_inv_mu = 0.0f;
   int pix = 0;
   uint32_t sid = 0;  // sample index within the job: pixel * spp + sample
   V3 dL{0.0f, 0.0f, 0.0f};
 
-  Pcg32 rng, rng_nee;
+  Pcg32 rng, rng_nee;  // rng_nee: whole-path replay, stream of the second shadow walk
   // main path state
   V3 p, d;
   float t_rem = 0.0f;
   V3 bo{1, 1, 1}, bn{1, 1, 1}, Lo{0, 0, 0}, Ln{0, 0, 0};
-  V3 Lrem{0, 0, 0}, Ltot{0, 0, 0};
   int depth = 0;
   float sc_n = 0.0f, sc_o = 0.0f;  // sigma_t of both states at a pending scattering event
   // NEE state
   V3 q, w;
   float tr_rem = 0.0f, tro = 1.0f, trn = 1.0f;
   V3 wo_next;
+  // adjoint radiance pass: random-number state at the pending scattering event
+  uint64_t ck_state = 0;
+  bool ck_lost = false;  // a checkpoint of this path did not fit
+  // replay
+  V3 Ltot{0, 0, 0}, cn_task{0, 0, 0};
   float s_nee = 0.0f;
-  // adjoint: NEE transmittances of the radiance pass, reused by the replay
-  // pass (same random numbers, so the same values); the replay then walks
-  // each shadow ray once, on the main stream, instead of twice
-  constexpr int kTrStore = 16;
-  float tr_store[kMode == kAdjoint ? kTrStore : 1];
-  int n_store = 0, i_event = 0;
-  bool nee_saved_rng = false;  // kNeeAdj draws from rng_nee (after a full walk)
+  int task = kTaskSegment;
+  bool own_event = false;  // checkpoint task: its scattering event is still to be processed
+  // loop iterations: a path's length is n_iter - iter0 when it ends
+  uint32_t n_iter = 0, iter0 = 0;
 
   while (true) {
+    ++n_iter;
     // ------------------------------------------- hand new paths to idle lanes
     unsigned need = __ballot_sync(0xffffffffu, phase == kIdle);
     while (need != 0u && !queue_empty) {
@@ -85,12 +124,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         unsigned long long b = 0;
         if (lane == 0) b = atomicAdd(Q.counter, (unsigned long long)Q.batch);
         b = __shfl_sync(0xffffffffu, b, 0);
-        if ((int64_t)b >= Q.total) {
+        if ((int64_t)b >= total) {
           queue_empty = true;
           break;
         }
         batch_next = (int64_t)b;
-        batch_end = min((int64_t)b + Q.batch, Q.total);
+        batch_end = min((int64_t)b + Q.batch, total);
       }
       const unsigned avail = (unsigned)(batch_end - batch_next);
       const unsigned take = min((unsigned)__popc(need), avail);
@@ -98,7 +137,6 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       if (((need >> lane) & 1u) && rank < take) {
         path = batch_next + rank;
         phase = kStart;
-        pass = 0;
       }
       batch_next += take;
       need = __ballot_sync(0xffffffffu, phase == kIdle);
@@ -114,66 +152,90 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         (unsigned)__popc(m_start) >= need_lanes || (m_walk == 0u && m_scat == 0u && m_start != 0u);
     const bool run_scat = (unsigned)__popc(m_scat) >= need_lanes || (m_walk == 0u && m_scat != 0u);
 
-    bool finished = false;  // the lane's current path (or pass) ends this iteration
+    bool finished = false;  // the lane's current path (or task) ends this iteration
 
     // ------------------------------------------------------------ path start
     if (run_start && phase == kStart) {
-      if (kMode == kAdjoint) {
-        if (pass == 0) n_store = 0;
-        i_event = 0;
+      iter0 = n_iter;
+      // replay: a checkpoint task resumes at its scattering event
+      const bool resume = kMode == kReplay && path >= Q.total;
+      float4 r0, r1, r2, r3;
+      if (resume) {
+        const float4* rec = Q.ckpt + (path - Q.total) * 4;
+        r0 = rec[0];
+        r1 = rec[1];
+        r2 = rec[2];
+        r3 = rec[3];
+        path = (int64_t)__float_as_uint(r0.x);
       }
-      if (pass == 0) {
-        Jp = &job_of(single, Q, path);
-        const VolJob& Jn = *Jp;
-        const float mu_old = Jn.scale * bits_to_float(__ldg(Jn.maxbits + 0));
-        const float mu_new = Jn.scale * bits_to_float(__ldg(Jn.maxbits + 1));
-        mu = (kMode == kTwoState) ? fmaxf(mu_old, mu_new) : mu_new;
-        inv_mu = 1.0f / mu;
-        half_inv_mu = 0.5f * inv_mu;
-        // k-th pixel of the job's hand-out order, sample s of that pixel
-        const int64_t local = path - Jn.path_begin;
-        const uint32_t k = (uint32_t)(local / Jn.spp);
-        const uint32_t smp = (uint32_t)(local - (int64_t)k * Jn.spp);
-        pix = Jn.pixel_order != nullptr ? (int)__ldg(Jn.pixel_order + k) : (int)k;
-        sid = (uint32_t)pix * (uint32_t)Jn.spp + smp;
-        if (kMode == kAdjoint) {
-          const float* g = Jn.grad_img + (int64_t)pix * 3;
-          const float fs = (float)Jn.spp;
-          dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
-        }
-      }
+      Jp = &job_of(single, Q, path);
       const VolJob& J = *Jp;
+      const float mu_old = J.scale * bits_to_float(__ldg(J.maxbits + 0));
+      const float mu_new = J.scale * bits_to_float(__ldg(J.maxbits + 1));
+      mu = (kMode == kTwoState) ? fmaxf(mu_old, mu_new) : mu_new;
+      inv_mu = 1.0f / mu;
+      half_inv_mu = 0.5f * inv_mu;
+      // k-th pixel of the job's hand-out order, sample s of that pixel
+      const int64_t local = path - J.path_begin;
+      const uint32_t k = (uint32_t)(local / J.spp);
+      const uint32_t smp = (uint32_t)(local - (int64_t)k * J.spp);
+      pix = J.pixel_order != nullptr ? (int)__ldg(J.pixel_order + k) : (int)k;
+      sid = (uint32_t)pix * (uint32_t)J.spp + smp;
       seed_lane(rng, J.seed, sid);
-      const float u0 = next1d(rng), u1 = next1d(rng);
-      V3 o;
-      camera_ray(J, pix % J.width, pix / J.width, u0, u1, o, d);
-      (void)next1d(rng);  // colour channel for free-flight sampling (grey extinction)
       bo = V3{1, 1, 1};
       bn = V3{1, 1, 1};
       Lo = V3{0, 0, 0};
       Ln = V3{0, 0, 0};
       depth = 0;
-      if (kMode == kAdjoint) Lrem = Ltot;
-      if (!roulette<kMode>(J, rng, depth, bn, bo)) {
-        finished = true;
+      if (kMode == kAdjoint) ck_lost = false;
+      if (kMode == kReplay) {
+        const float* g = J.grad_img + (int64_t)pix * 3;
+        const float fs = (float)J.spp;
+        dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
+        const float4 lt = Q.path_ltot[path];
+        Ltot = V3{lt.x, lt.y, lt.z};
+        task = resume ? kTaskCheckpoint : (lt.w != 0.0f ? kTaskWhole : kTaskSegment);
+      }
+      if (resume) {
+        if (task != kTaskCheckpoint || Q.path_ltot[path].w != 0.0f) {
+          finished = true;  // the path is replayed whole by its camera task
+        } else {
+          depth = __float_as_int(r0.y);
+          rng.state = (uint64_t)__float_as_uint(r0.z) | ((uint64_t)__float_as_uint(r0.w) << 32);
+          p = V3{r1.x, r1.y, r1.z};
+          bn = V3{r1.w, r2.x, r2.y};
+          Ln = V3{r2.z, r2.w, r3.x};
+          cn_task = V3{r3.y, r3.z, r3.w};
+          sc_n = J.scale * density_new(J, locate(J, p));
+          own_event = true;
+          phase = kScatter;
+        }
       } else {
-        const V3 inv_d = recip(d);
-        float tn, tf;
-        slab(o, inv_d, tn, tf);
-        if (!(tn <= tf && tf > 0.0f)) {
-          // camera ray misses the cube: environment seen directly
-          if (!J.hide_emitters) {
-            Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
-            if (kMode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
-          }
+        const float u0 = next1d(rng), u1 = next1d(rng);
+        V3 o;
+        camera_ray(J, pix % J.width, pix / J.width, u0, u1, o, d);
+        (void)next1d(rng);  // colour channel for free-flight sampling (grey extinction)
+        if (!roulette<kMode>(J, rng, depth, bn, bo)) {
           finished = true;
         } else {
-          // null BSDF of the cube boundary: its 1D + 2D sample is drawn and discarded
-          pcg_skip3(rng);
-          p = advance(o, fmaxf(tn, 0.0f), d);
-          float a;
-          slab(p, inv_d, a, t_rem);
-          phase = kMain;
+          const V3 inv_d = recip(d);
+          float tn, tf;
+          slab(o, inv_d, tn, tf);
+          if (!(tn <= tf && tf > 0.0f)) {
+            // camera ray misses the cube: environment seen directly
+            if (!J.hide_emitters) {
+              Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
+              if (kMode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
+            }
+            finished = true;
+          } else {
+            // null BSDF of the cube boundary: its 1D + 2D sample is drawn and discarded
+            pcg_skip3(rng);
+            p = advance(o, fmaxf(tn, 0.0f), d);
+            float a;
+            slab(p, inv_d, a, t_rem);
+            phase = kMain;
+          }
         }
       }
     }
@@ -181,65 +243,70 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     // ------------------------------------------------- real scattering event
     if (run_scat && phase == kScatter) {
       const VolJob& J = *Jp;
-      const Lookup lk = locate(J, p);
-      const float st_n = sc_n, st_o = sc_o;
-      const V3 an = albedo_at(J, lk, 1);
-      const V3 ss_n{st_n * an.x, st_n * an.y, st_n * an.z};
-      if (kMode == kTwoState) {
-        // plugins/twostatevolpath.py:259-260
-        const V3 ao = albedo_at(J, lk, 0);
-        const V3 ss_o{st_o * ao.x, st_o * ao.y, st_o * ao.z};
-        const float den = st_n + st_o;
-        bn = V3{bn.x * ((2.0f * ss_n.x) / den), bn.y * ((2.0f * ss_n.y) / den),
-                bn.z * ((2.0f * ss_n.z) / den)};
-        bo = V3{bo.x * ((2.0f * ss_o.x) / den), bo.y * ((2.0f * ss_o.y) / den),
-                bo.z * ((2.0f * ss_o.z) / den)};
+      if (kMode == kReplay && task == kTaskSegment) {
+        finished = true;  // the event has its own checkpoint task
+      } else if (kMode == kReplay && task == kTaskCheckpoint && !own_event) {
+        finished = true;
       } else {
-        bn = V3{bn.x * (ss_n.x / st_n), bn.y * (ss_n.y / st_n), bn.z * (ss_n.z / st_n)};
-        if (kMode == kAdjoint && pass == 1) {
-          const float sd = (dL.x * Lrem.x + dL.y * Lrem.y) + dL.z * Lrem.z;
-          scatter_density(J, lk, (J.scale * sd) / st_n);
-          ++cnt.grad_events;
-          if (J.grad_albedo != nullptr) {
-            ++cnt.albedo_events;
-            const V3 ga{(dL.x * Lrem.x) / fmaxf(an.x, 1e-8f), (dL.y * Lrem.y) / fmaxf(an.y, 1e-8f),
-                        (dL.z * Lrem.z) / fmaxf(an.z, 1e-8f)};
-            scatter_albedo(J, lk, ga);
+        const Lookup lk = locate(J, p);
+        const float st_n = sc_n, st_o = sc_o;
+        const V3 an = albedo_at(J, lk, 1);
+        const V3 ss_n{st_n * an.x, st_n * an.y, st_n * an.z};
+        if (kMode == kTwoState) {
+          // plugins/twostatevolpath.py:259-260
+          const V3 ao = albedo_at(J, lk, 0);
+          const V3 ss_o{st_o * ao.x, st_o * ao.y, st_o * ao.z};
+          const float den = st_n + st_o;
+          bn = V3{bn.x * ((2.0f * ss_n.x) / den), bn.y * ((2.0f * ss_n.y) / den),
+                  bn.z * ((2.0f * ss_n.z) / den)};
+          bo = V3{bo.x * ((2.0f * ss_o.x) / den), bo.y * ((2.0f * ss_o.y) / den),
+                  bo.z * ((2.0f * ss_o.z) / den)};
+        } else {
+          if (kMode == kReplay) {
+            // d log(sigma_s) / d density and d log(albedo) / d albedo at the event
+            const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+            const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
+            scatter_density(J, lk, (J.scale * sd) / st_n);
+            ++cnt.grad_events;
+            if (J.grad_albedo != nullptr) {
+              ++cnt.albedo_events;
+              const V3 ga{(dL.x * Lr.x) / fmaxf(an.x, 1e-8f), (dL.y * Lr.y) / fmaxf(an.y, 1e-8f),
+                          (dL.z * Lr.z) / fmaxf(an.z, 1e-8f)};
+              scatter_albedo(J, lk, ga);
+            }
+          }
+          // a checkpoint already holds the throughput after the event
+          if (!(kMode == kReplay && task == kTaskCheckpoint))
+            bn = V3{bn.x * (ss_n.x / st_n), bn.y * (ss_n.y / st_n), bn.z * (ss_n.z / st_n)};
+        }
+        if (kMode == kAdjoint) ck_state = rng.state;
+        // isotropic phase sample (1D unused + 2D), plugins/twostatevolpath.py:275
+        pcg_skip1(rng);
+        const float pu0 = next1d(rng), pu1 = next1d(rng);
+        wo_next = uniform_sphere(pu0, pu1);
+        // NEE towards the environment, then ratio tracking
+        const float nu0 = next1d(rng), nu1 = next1d(rng);
+        w = uniform_sphere(nu0, nu1);
+        q = p;
+        {
+          float a;
+          slab(q, recip(w), a, tr_rem);
+        }
+        tro = 1.0f;
+        trn = 1.0f;
+        phase = kNee;
+        if (kMode == kReplay) {
+          if (task == kTaskCheckpoint) {
+            // NEE contribution known from the radiance pass: one shadow walk
+            // on the main stream scatters its gradient
+            s_nee = (dL.x * cn_task.x + dL.y * cn_task.y) + dL.z * cn_task.z;
+            Ln = V3{Ln.x + cn_task.x, Ln.y + cn_task.y, Ln.z + cn_task.z};
+            own_event = false;
+            phase = kNeeAdj;
+          } else {
+            rng_nee = rng;  // whole-path replay: walk for the transmittance, then again
           }
         }
-      }
-      // isotropic phase sample (1D unused + 2D), plugins/twostatevolpath.py:275
-      pcg_skip1(rng);
-      const float pu0 = next1d(rng), pu1 = next1d(rng);
-      wo_next = uniform_sphere(pu0, pu1);
-      // NEE towards the environment, then ratio tracking
-      const float nu0 = next1d(rng), nu1 = next1d(rng);
-      w = uniform_sphere(nu0, nu1);
-      q = p;
-      {
-        float a;
-        slab(q, recip(w), a, tr_rem);
-      }
-      tro = 1.0f;
-      trn = 1.0f;
-      phase = kNee;
-      if (kMode == kAdjoint && pass == 1) {
-        if (i_event < n_store) {
-          // transmittance known from the radiance pass: add the NEE
-          // contribution now and walk the shadow ray once to scatter its
-          // gradient, drawing from the main stream as the full walk would
-          const float en = emit_weight * tr_store[i_event];
-          const V3 cn{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
-                      ((bn.z * kInvFourPi) * mis) * en};
-          s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
-          Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
-          nee_saved_rng = false;
-          phase = kNeeAdj;
-        } else {
-          rng_nee = rng;
-          nee_saved_rng = true;
-        }
-        ++i_event;
       }
     }
 
@@ -259,7 +326,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         org = q;
         dir = w;
         tmax = tr_rem;
-        if (kMode == kAdjoint && phase == kNeeAdj && nee_saved_rng) r = &rng_nee;
+        if (kMode == kReplay && phase == kNeeAdj && task == kTaskWhole) r = &rng_nee;
       }
       if (!alive) {
         finished = true;
@@ -303,9 +370,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 const float wn = (2.0f * sn_n) / den, wo = 2.0f - wn;
                 bn = V3{bn.x * wn, bn.y * wn, bn.z * wn};
                 bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
-              } else if (kMode == kAdjoint && pass == 1) {
+              } else if (kMode == kReplay) {
                 const float sn = mu - st_n;
-                const float sd = (dL.x * Lrem.x + dL.y * Lrem.y) + dL.z * Lrem.z;
+                const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+                const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
                 scatter_density(J, lk, -(J.scale * sd) / sn);
                 ++cnt.grad_events;
               }
@@ -329,10 +397,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             pcg_skip3(rng);
             if (roulette<kMode>(J, rng, depth, bn, bo) && !(J.hide_emitters && depth == 0)) {
               const float k = depth == 0 ? 1.0f : mis;
-              const V3 cn{bn.x * k, bn.y * k, bn.z * k};
-              Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
+              Ln = V3{Ln.x + bn.x * k, Ln.y + bn.y * k, Ln.z + bn.z * k};
               if (kMode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
-              if (kMode == kAdjoint) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
             }
             finished = true;
           }
@@ -350,30 +416,36 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             const float en = emit_weight * trn;
             const V3 cn{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
                         ((bn.z * kInvFourPi) * mis) * en};
+            if (kMode == kAdjoint && !ck_lost) {
+              const unsigned long long slot = atomicAdd(Q.ckpt_count, 1ull);
+              if ((int64_t)slot < Q.ckpt_cap)
+                write_checkpoint(Q.ckpt + slot * 4, (uint32_t)path, depth, ck_state, p, bn, Ln, cn);
+              else
+                ck_lost = true;
+            }
             Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
             if (kMode == kTwoState) {
               const float eo = emit_weight * tro;
               Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
                       Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
             }
-            if (kMode == kAdjoint && pass == 1) {
-              // replay the shadow walk to back-propagate through its transmittance
+            if (kMode == kReplay) {
+              // whole-path replay: walk the shadow ray again (saved stream) to
+              // back-propagate through its transmittance
               s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
-              Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
               q = p;
               float a;
               slab(q, recip(w), a, tr_rem);
               trn = 1.0f;
               phase = kNeeAdj;
             } else {
-              if (kMode == kAdjoint && n_store < kTrStore) tr_store[n_store++] = trn;
               d = wo_next;
               float a;
               slab(p, recip(d), a, t_rem);
               phase = kMain;
             }
           }
-        } else {  // kNeeAdj: second walk with the saved stream
+        } else {  // kNeeAdj: the shadow walk with gradients
           bool done = !valid;
           if (valid) {
             const float sn = mu - st_n;
@@ -398,20 +470,15 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
 
     // -------------------------------------------------------------- path end
     if (finished) {
-      if (kMode == kAdjoint && pass == 0) {
-        // radiance pass finished: replay the same path with gradients
-        Ltot = Ln;
-        pass = 1;
-        phase = kStart;
-      } else {
-        if (kMode != kAdjoint) {
-          float4* o = Q.path_out + (Jp->path_begin + sid) * (kMode == kTwoState ? 2 : 1);
-          o[0] = make_float4(Ln.x, Ln.y, Ln.z, 0.0f);
-          if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
-        }
-        ++cnt.paths;
-        phase = kIdle;
+      if (kMode == kTwoState || kMode == kSingle) {
+        float4* o = Q.path_out + (Jp->path_begin + sid) * (kMode == kTwoState ? 2 : 1);
+        o[0] = make_float4(Ln.x, Ln.y, Ln.z, 0.0f);
+        if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
       }
+      if (kMode == kAdjoint) Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f);
+      if (kMode != kReplay) ++cnt.paths;
+      if (Jp->pixel_cost != nullptr) atomicAdd(Jp->pixel_cost + pix, n_iter - iter0);
+      phase = kIdle;
     }
   }
 }

@@ -62,29 +62,24 @@ __global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_cons
 }
 
 // ------------------------------------------------------ hand-out ordering
-// Pixels are handed to the persistent tracer longest-expected-path first: the
-// key is the length of the pixel-centre ray's chord through the medium cube,
-// in 256 buckets (bucket 0 = longest).  Misses (chord 0) come last, so the
-// queue ends on cheap paths instead of on a few long ones.
+// Pixels are handed to the persistent tracer most-expensive first, so that
+// the queue ends on cheap paths instead of on a few long ones: by the
+// measured path lengths of the previous call (cost_bucket), or by the length
+// of the pixel-centre ray's chord through the medium cube, in 256 buckets
+// (bucket 0 = longest; misses last).
 constexpr int kOrderBuckets = 256;
 
-__device__ __forceinline__ int order_key(const VolJob& J, int pix) {
-  V3 o, d;
-  camera_ray(J, pix % J.width, pix / J.width, 0.5f, 0.5f, o, d);
-  float tn, tf;
-  slab(o, recip(d), tn, tf);
-  const float chord = (tn <= tf && tf > 0.0f) ? tf - fmaxf(tn, 0.0f) : 0.0f;
-  int b = (int)(chord * (255.0f / 1.7320508f));
-  b = b < 0 ? 0 : (b > 255 ? 255 : b);
-  return 255 - b;
+__device__ __forceinline__ int order_key(const VolJob& J, int pix, const uint32_t* cost) {
+  return cost != nullptr ? cost_bucket(cost[pix]) : chord_key(J, pix);
 }
 
-__global__ void order_count_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* counts) {
+__global__ void order_count_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* counts,
+                                   const uint32_t* cost) {
   __shared__ uint32_t hist[kOrderBuckets];
   for (int k = threadIdx.x; k < kOrderBuckets; k += blockDim.x) hist[k] = 0;
   __syncthreads();
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix < npix) atomicAdd(&hist[order_key(J, pix)], 1u);
+  if (pix < npix) atomicAdd(&hist[order_key(J, pix, cost)], 1u);
   __syncthreads();
   for (int k = threadIdx.x; k < kOrderBuckets; k += blockDim.x)
     if (hist[k]) atomicAdd(counts + k, hist[k]);
@@ -106,9 +101,11 @@ __global__ void order_scan_kernel(uint32_t* counts) {
 }
 
 __global__ void order_place_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* starts,
-                                   uint32_t* order) {
+                                   uint32_t* order, uint32_t* cost) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix < npix) order[atomicAdd(starts + order_key(J, pix), 1u)] = (uint32_t)pix;
+  if (pix >= npix) return;
+  order[atomicAdd(starts + order_key(J, pix, cost), 1u)] = (uint32_t)pix;
+  if (cost != nullptr) cost[pix] = 0u;  // the next tracer call accumulates afresh
 }
 
 // Sum of a pixel's samples in sample order, divided by spp (the box-filter
@@ -213,11 +210,12 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
 // Resident blocks per SM of each tracer variant (queried once per process).
 static int resident_blocks(int mode) {
   static std::once_flag once;
-  static int blocks[3] = {1, 1, 1};
+  static int blocks[4] = {1, 1, 1, 1};
   std::call_once(once, [] {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_kernel<kTwoState>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_kernel<kSingle>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_kernel<kAdjoint>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], trace_kernel<kReplay>, kTraceBlock, 0);
     for (int& b : blocks) b = b < 1 ? 1 : b;
   });
   return blocks[mode];
@@ -243,17 +241,17 @@ void warm_launch_config() {
 static_assert(kOrderBuckets == kRenderOrderBuckets, "order bucket count mismatch");
 
 // Fills `order` with the job's pixels, longest expected path first.
-int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, cudaStream_t st) {
+int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, uint32_t* cost, cudaStream_t st) {
   const int npix = J.width * J.height;
   RCV_TRY_CUDA(cudaMemsetAsync(buckets, 0, kOrderBuckets * sizeof(uint32_t), st), "order reset");
   const int block = 256;
-  order_count_kernel<<<grid_for(npix, block), block, 0, st>>>(J, npix, buckets);
+  order_count_kernel<<<grid_for(npix, block), block, 0, st>>>(J, npix, buckets, cost);
   int rc = launched("order_count launch");
   if (rc) return rc;
   order_scan_kernel<<<1, kOrderBuckets, 0, st>>>(buckets);
   rc = launched("order_scan launch");
   if (rc) return rc;
-  order_place_kernel<<<grid_for(npix, block), block, 0, st>>>(J, npix, buckets, order);
+  order_place_kernel<<<grid_for(npix, block), block, 0, st>>>(J, npix, buckets, order, cost);
   return launched("order_place launch");
 }
 
@@ -261,10 +259,19 @@ int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, cudaStream
 // device job table.
 int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
                       const rcv_volpath_options* o, unsigned long long* queue_counter,
-                      float4* path_out, uint64_t* counters, cudaStream_t st) {
+                      float4* path_out, const AdjBuffers* adj, uint64_t* counters, cudaStream_t st) {
   Queue Q;
+  std::memset(&Q, 0, sizeof(Q));
   Q.counter = queue_counter;
-  Q.path_out = mode == kAdjoint ? nullptr : path_out;
+  Q.path_out = (mode == kTwoState || mode == kSingle) ? path_out : nullptr;
+  if (mode == kAdjoint || mode == kReplay) {
+    RCV_REQUIRE(adj != nullptr && adj->ckpt && adj->ckpt_count && adj->path_ltot, "adjoint buffers missing");
+    RCV_REQUIRE(total < (int64_t(1) << 32), "an adjoint launch must have fewer than 2^32 paths");
+    Q.ckpt = adj->ckpt;
+    Q.ckpt_count = adj->ckpt_count;
+    Q.ckpt_cap = adj->ckpt_cap;
+    Q.path_ltot = adj->path_ltot;
+  }
   Q.counters = reinterpret_cast<unsigned long long*>(counters);
   Q.jobs = jobs;
   Q.njobs = njobs;
@@ -273,11 +280,12 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   RCV_REQUIRE(Q.batch <= (1 << 20), "batch must be <= 2^20");
   Q.defer = (o != nullptr && o->defer > 0) ? o->defer : 8;
   RCV_REQUIRE(Q.defer <= 32, "defer must be in [1, 32]");
-  Q.pad = 0;
   RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
   int per_sm = resident_blocks(mode);
   if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
-  const int64_t warps_needed = (total + Q.batch - 1) / Q.batch;
+  // replay: the checkpoint tasks come on top of one camera task per path
+  const int64_t tasks = mode == kReplay ? 2 * total : total;
+  const int64_t warps_needed = (tasks + Q.batch - 1) / Q.batch;
   int64_t blocks = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
   const int64_t cap = int64_t(sm_count()) * per_sm;
   if (blocks > cap) blocks = cap;
@@ -285,7 +293,8 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   switch (mode) {
     case kTwoState: trace_kernel<kTwoState><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
     case kSingle: trace_kernel<kSingle><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
-    default: trace_kernel<kAdjoint><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
+    case kAdjoint: trace_kernel<kAdjoint><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
+    default: trace_kernel<kReplay><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
   }
   return launched("trace kernel launch");
 }
@@ -374,18 +383,33 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
   char* ws = static_cast<char*>(workspace);
   int rc = RCV_OK;
   J.pixel_order = nullptr;
-  if (o == nullptr || o->order == RCV_ORDER_LONGEST_FIRST) {
+  J.pixel_cost = nullptr;
+  const int order = o == nullptr ? RCV_ORDER_COST : o->order;
+  RCV_REQUIRE(order == RCV_ORDER_COST || order == RCV_ORDER_ROW_MAJOR || order == RCV_ORDER_LONGEST_FIRST,
+              "unknown pixel order %d", order);
+  if (order != RCV_ORDER_ROW_MAJOR) {
+    uint32_t* cost = order == RCV_ORDER_COST ? reinterpret_cast<uint32_t*>(ws + L.cost) : nullptr;
     rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
-                      st);
+                      cost, st);
     if (rc) return rc;
     J.pixel_order = reinterpret_cast<const uint32_t*>(ws + L.order);
-  } else {
-    RCV_REQUIRE(o->order == RCV_ORDER_ROW_MAJOR, "unknown pixel order %d", o->order);
+    J.pixel_cost = cost;
   }
   float4* po = reinterpret_cast<float4*>(ws + L.path_out);
-  rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o,
-                         reinterpret_cast<unsigned long long*>(ws + L.counter), po, counters, st);
-  if (rc || mode == kAdjoint) return rc;
+  unsigned long long* qc = reinterpret_cast<unsigned long long*>(ws + L.counter);
+  if (mode == kAdjoint) {
+    AdjBuffers A;
+    A.ckpt = reinterpret_cast<float4*>(ws + L.ckpt);
+    A.ckpt_count = qc + 1;
+    A.ckpt_cap = ckpt_capacity(J.path_count);
+    A.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
+    RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, sizeof(unsigned long long), st), "checkpoint reset");
+    rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st);
+    if (rc) return rc;
+    return launch_persistent(kReplay, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st);
+  }
+  rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o, qc, po, nullptr, counters, st);
+  if (rc) return rc;
   return launch_reduce(mode == kTwoState, po, 0, npix, J.spp, img_new, img_old, st);
 }
 

@@ -58,6 +58,7 @@ struct VolJob {
   int64_t path_begin;   // first global path index of this job (batched launches)
   int64_t path_count;   // width*height*spp
   const uint32_t* pixel_order;  // pixel handed out k-th (null = row-major)
+  uint32_t* pixel_cost;         // per-pixel sum of path lengths (loop iterations), or null
 };
 
 // Work queue of a (possibly multi-job) persistent launch.
@@ -66,14 +67,28 @@ struct Queue {
   float4* path_out;              // primal: per-path radiance [path][new, old]
   unsigned long long* counters;  // RCV_COUNTER_* totals of the launch or null
   const VolJob* jobs;            // device job table (batched launches) or null
-  int64_t total;                 // paths in the launch
+  int64_t total;                 // paths in the launch (replay: camera tasks)
   int32_t batch;                 // paths claimed per warp fetch
   int32_t njobs;
   int32_t defer;                 // lanes that must wait before a deferred branch runs
   int32_t pad;
+  // adjoint: scatter checkpoints (4 float4 each), how many were claimed (may
+  // exceed the capacity) and per-path (total radiance, checkpoint-lost flag)
+  float4* ckpt;
+  unsigned long long* ckpt_count;
+  int64_t ckpt_cap;
+  float4* path_ltot;
 };
 
-enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2 };
+enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2, kReplay = 3 };
+
+// Buffers of the two adjoint launches.
+struct AdjBuffers {
+  float4* ckpt;
+  unsigned long long* ckpt_count;
+  int64_t ckpt_cap;
+  float4* path_ltot;
+};
 
 struct Counts {
   uint32_t paths, lookups, nee_lookups, scatters;
@@ -216,14 +231,35 @@ __device__ __forceinline__ bool roulette(const VolJob& J, Pcg32& rng, int depth,
 // Validates a medium + sensor + options and fills a job for one launch.
 int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o, uint32_t seed,
                     int spp, VolJob* J);
-// Writes the job's pixels, longest expected path first, into `order`
+// Writes the job's pixels into `order`, most expensive first: by `cost` (the
+// per-pixel path lengths of the previous call, cleared here) or, when cost is
+// null, by the chord length of the pixel's centre ray through the medium
 // (buckets: 256 uint32 of scratch).
-int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, cudaStream_t st);
+int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, uint32_t* cost, cudaStream_t st);
+// Bucket (0 = first handed out) of a pixel by the chord of its centre ray
+// through the medium cube (misses last).
+__device__ __forceinline__ int chord_key(const VolJob& J, int pix) {
+  V3 o, d;
+  camera_ray(J, pix % J.width, pix / J.width, 0.5f, 0.5f, o, d);
+  float tn, tf;
+  slab(o, recip(d), tn, tf);
+  const float chord = (tn <= tf && tf > 0.0f) ? tf - fmaxf(tn, 0.0f) : 0.0f;
+  int b = (int)(chord * (255.0f / 1.7320508f));
+  b = b < 0 ? 0 : (b > 255 ? 255 : b);
+  return 255 - b;
+}
+
+// Bucket (0 = first handed out) of a pixel of cost c.
+__device__ __forceinline__ int cost_bucket(uint32_t c) {
+  if (c == 0u) return 255;
+  const int b = (int)(log2f((float)c) * 16.0f);
+  return 254 - (b < 254 ? b : 254);
+}
 // Persistent tracer launch (TraceMode `mode`) over `total` paths of one job
 // (jobs == NULL) or of a device job table of njobs entries.
 int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
                       const rcv_volpath_options* o, unsigned long long* queue_counter, float4* path_out,
-                      uint64_t* counters, cudaStream_t st);
+                      const AdjBuffers* adj, uint64_t* counters, cudaStream_t st);
 // Queries the occupancy and SM count the launchers cache, so that later
 // launches (e.g. under stream capture) make no device queries.
 void warm_launch_config();

@@ -37,10 +37,10 @@ class _VolumeIntegratorBase:
         self.batch = int(props.get("batch", 0))
         self.blocks_per_sm = int(props.get("blocks_per_sm", 0))
         self.defer = int(props.get("defer", 0))
-        order = props.get("order", "longest_first")
-        if order not in ("longest_first", "row_major"):
+        order = props.get("order", "cost")
+        if order not in _lib.ORDERS:
             raise ValueError(f"unknown pixel order {order!r}")
-        self.order = _lib.ORDER_LONGEST_FIRST if order == "longest_first" else _lib.ORDER_ROW_MAJOR
+        self.order = _lib.ORDERS[order]
         if self.max_depth < -1:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         self.is_checked = False
@@ -73,7 +73,8 @@ class _VolumeIntegratorBase:
         need = int(_lib.load().rcv_render_workspace_bytes(f.width, f.height, spp, mode)) + 256
         buf = self._scratch.get(device)
         if buf is None or buf.numel() < need:
-            buf = torch.empty(need, dtype=torch.uint8, device=device)
+            # zeroed once: the per-pixel cost it carries starts at zero
+            buf = torch.zeros(need, dtype=torch.uint8, device=device)
             self._scratch[device] = buf
         return (buf.data_ptr() + 255) & ~255
 

@@ -92,9 +92,11 @@ class StepServer:
     # ------------------------------------------------------------ memory
     @staticmethod
     def job_bytes(job: B.CVJob) -> int:
-        """Resident bytes of a job plus the per-path scratch it adds to a tick
-        (32 bytes per primal path)."""
-        return job.nbytes() + 32 * job.width * job.height * job.spp
+        """Resident bytes of a job plus the per-path scratch it adds to a tick:
+        32 bytes per primal path (radiance slots), 16 + 2 x 64 bytes per
+        gradient path (total radiance, scatter checkpoints)."""
+        npix = job.width * job.height
+        return job.nbytes() + 32 * npix * job.spp + 144 * npix * job.spp_grad
 
     def resident_bytes(self) -> int:
         return sum(self.job_bytes(j) for j in self.jobs.values())

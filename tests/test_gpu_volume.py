@@ -48,7 +48,7 @@ def frac_equal(a, b):
 
 
 @pytest.mark.parametrize("batch,blocks_per_sm,defer,order", [(1, 1, 1, "row_major"), (7, 2, 8, "longest_first"),
-                                                             (64, 0, 32, "longest_first")])
+                                                             (64, 0, 32, "cost")])
 @pytest.mark.parametrize("albedo_grid", [False, True])
 def test_two_state_matches_oracle(cuda, oracle, batch, blocks_per_sm, defer, order, albedo_grid):
     """The persistent schedule (queue batch, resident blocks, deferral
@@ -288,3 +288,25 @@ def test_cv_optimisation_reduces_loss(cuda):
         losses.append(loss.item())
     assert np.mean(losses[-5:]) < 0.7 * np.mean(losses[:3]), losses
     assert float(integ.w_s.max()) <= 1.0 and float(integ.w_s.min()) >= 0.0
+
+
+def test_cost_order_changes_schedule_not_results(cuda):
+    """RCV_ORDER_COST sorts each call's pixels by the path lengths the previous
+    call measured (kept in the workspace); repeated calls therefore run in
+    different orders and must give bit-identical images and gradients."""
+    scene, med, grids = make_scene(cuda, albedo_grid=True)
+    by_cost = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "order": "cost"})
+    rows = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "order": "row_major"})
+    ref_H, ref_F = rows.render_twostates(scene, 0, seed=21, spp=4)
+    for _ in range(3):
+        H, F = by_cost.render_twostates(scene, 0, seed=21, spp=4)
+        assert torch.equal(H, ref_H) and torch.equal(F, ref_F)
+    f = scene.sensors()[0].film()
+    ws = by_cost._scratch[cuda]
+    lib = _lib.load()
+    L_order = 256 + 1024  # counter + buckets; the cost array follows the order array
+    npix = f.width * f.height
+    cost_off = ((L_order + npix * 4 + 255) // 256) * 256
+    aligned = (ws.data_ptr() + 255) & ~255
+    cost = ws[aligned - ws.data_ptr() + cost_off:][: npix * 4].view(torch.int32)
+    assert int(cost.sum()) > 0  # the last call recorded its path lengths

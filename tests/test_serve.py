@@ -85,7 +85,7 @@ def fire_all():
 
 def test_admission_by_budget(fake_cuda):
     s = serve.StepServer(1000, device="cpu", clock=lambda: fake_cuda.t)
-    a, b, c = FakeJob(400 - 32), FakeJob(400 - 32), FakeJob(400 - 32)  # 400 B each with scratch
+    a, b, c = FakeJob(400 - 176), FakeJob(400 - 176), FakeJob(400 - 176)  # 400 B each with scratch
     ja, jb, jc = s.add_job(a), s.add_job(b), s.add_job(c)
     assert s.is_resident(ja) and s.is_resident(jb) and not s.is_resident(jc)
     with pytest.raises(ValueError):
