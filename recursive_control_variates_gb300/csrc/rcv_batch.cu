@@ -225,9 +225,9 @@ __global__ void batch_order_place_kernel(const BatchEntry* __restrict__ E, const
   const int j = job_of_block(bp, n, blockIdx.x);
   const BatchEntry& B = E[j];
   const int64_t pix = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
-  if (pix >= B.npix) return;
-  B.order[atomicAdd(B.buckets + cost_bucket(B.cost[pix]), 1u)] = (uint32_t)pix;
-  B.cost[pix] = 0u;
+  const bool valid = pix < B.npix;
+  place_block(valid ? cost_bucket(B.cost[pix]) : 0, valid, (uint32_t)pix, B.buckets, B.order);
+  if (valid) B.cost[pix] = 0u;
 }
 
 // Initial per-pixel cost of a job: its chord order (longest chord first).

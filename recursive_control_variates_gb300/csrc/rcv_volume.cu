@@ -103,9 +103,9 @@ __global__ void order_scan_kernel(uint32_t* counts) {
 __global__ void order_place_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* starts,
                                    uint32_t* order, uint32_t* cost) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= npix) return;
-  order[atomicAdd(starts + order_key(J, pix, cost), 1u)] = (uint32_t)pix;
-  if (cost != nullptr) cost[pix] = 0u;  // the next tracer call accumulates afresh
+  const bool valid = pix < npix;
+  place_block(valid ? order_key(J, pix, cost) : 0, valid, (uint32_t)pix, starts, order);
+  if (valid && cost != nullptr) cost[pix] = 0u;  // the next tracer call accumulates afresh
 }
 
 // Sum of a pixel's samples in sample order, divided by spp (the box-filter

@@ -249,6 +249,22 @@ __device__ __forceinline__ int chord_key(const VolJob& J, int pix) {
   return 255 - b;
 }
 
+// Places the pixels of one block in their buckets: block-local ranks from a
+// shared histogram, one global reservation per (block, bucket), so a popular
+// bucket costs one global atomic per block instead of one per pixel.  Order
+// within a bucket is arbitrary (it never changes results).
+__device__ __forceinline__ void place_block(int key, bool valid, uint32_t pix, uint32_t* starts,
+                                            uint32_t* order) {
+  __shared__ uint32_t cnt[256], base[256];
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) cnt[k] = 0u;
+  __syncthreads();
+  const uint32_t rank = valid ? atomicAdd(&cnt[key], 1u) : 0u;
+  __syncthreads();
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) base[k] = cnt[k] ? atomicAdd(starts + k, cnt[k]) : 0u;
+  __syncthreads();
+  if (valid) order[base[key] + rank] = pix;
+}
+
 // Bucket (0 = first handed out) of a pixel of cost c.
 __device__ __forceinline__ int cost_bucket(uint32_t c) {
   if (c == 0u) return 255;
