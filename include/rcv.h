@@ -65,6 +65,12 @@ typedef struct rcv_medium {
   const float* albedo_old;  /* device or NULL (then albedo_value is used)   */
   const float* albedo_new;  /* device or NULL                               */
   float albedo_value[3];
+  /* 0: one global majorant (scale * max density).  f > 0: a majorant
+   * supergrid of ceil(D/f) cells per axis traversed by DDA (the
+   * `majorant_resolution_factor` of the reference's media,
+   * plugins/twostatemedium.py:25-70); each cell holds scale * the largest
+   * density trilinear interpolation can return inside it. */
+  int32_t majorant_factor;
   void* workspace; /* device, rcv_medium_workspace_bytes(), 256-B aligned  */
 } rcv_medium;
 
@@ -112,7 +118,7 @@ void rcv_sample_tea_32(uint32_t v0, uint32_t v1, uint32_t out[2]);
 /* --------------------------------------------------------------- medium  */
 /* Bytes of device workspace a medium needs (packed lookup cells, majorants,
  * gradient accumulators). */
-uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid);
+uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid, int32_t majorant_factor);
 
 /* Packs the old/new grids into the lookup workspace and computes both
  * majorants (scale * max density).  Call after every state rotation.
@@ -361,7 +367,7 @@ typedef struct rcv_batch_job {
   float density_lo, density_hi, albedo_lo, albedo_hi; /* clamp ranges             */
   const double* adam_table; /* rcv_adam_table_fill(adam_beta1, adam_beta2)        */
   int32_t adam_table_len;
-  int32_t pad0;
+  int32_t majorant_factor;  /* as rcv_medium.majorant_factor                      */
   /* Parameters, double-buffered: before step `it`, density[it & 1] holds
    * theta_it (the `new` state) and density[(it & 1) ^ 1] holds theta_{it-1}
    * (`old`); the step writes theta_{it+1} into the latter.  Both buffers hold

@@ -46,6 +46,7 @@ class OracleScene(C.Structure):
         ("alb_old", C.c_void_p),
         ("alb_new", C.c_void_p),
         ("albedo_const", C.c_float * 3),
+        ("majorant_factor", C.c_int32),
     ]
 
 
@@ -191,7 +192,7 @@ class Scene:
     """Keeps the numpy grids alive while the C structure points at them."""
 
     def __init__(self, cam: Camera, dens_old, dens_new, albedo_old=None, albedo_new=None, albedo_const=0.8,
-                 max_depth=16, rr_depth=None, hide_emitters=False, scale=1.0):
+                 max_depth=16, rr_depth=None, hide_emitters=False, scale=1.0, majorant_factor=0):
         self.dens_old = np.ascontiguousarray(dens_old, np.float32)
         self.dens_new = np.ascontiguousarray(dens_new, np.float32)
         dz, dy, dx = self.dens_new.shape[:3]
@@ -211,6 +212,7 @@ class Scene:
         s.alb_new = None if self.alb_new is None else self.alb_new.ctypes.data
         ac = np.broadcast_to(np.asarray(albedo_const, np.float32), (3,))
         s.albedo_const[:] = [float(v) for v in ac]
+        s.majorant_factor = int(majorant_factor)
         self.c = s
         self.width, self.height = cam.width, cam.height
 

@@ -176,6 +176,7 @@ struct oracle_scene {
   const float* alb_old;  // [dz][dy][dx][3] or null
   const float* alb_new;
   float albedo_const[3];
+  int32_t majorant_factor;  // 0: global majorant; f: supergrid of ceil(D/f) cells per axis
 };
 }
 
@@ -233,6 +234,101 @@ float grid_max(const oracle_scene& S, const float* g) {
   return m;
 }
 
+// Majorant supergrid (plugins/twostatemedium.py:25-70): ceil(D/f) cells per
+// axis covering the unit cube; a cell bounds sigma_t over every point inside
+// it, i.e. scale * the largest density among the voxels trilinear
+// interpolation reads there.  `two` bounds both states, `nw` the new one.
+struct Supergrid {
+  int s[3] = {0, 0, 0};
+  std::vector<float> two, nw;
+
+  static int64_t floordiv(int64_t a, int64_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+  // voxels read by trilinear interpolation for x in [c/S, (c+1)/S)
+  static void span(int c, int S, int D, int& lo, int& hi) {
+    const int64_t den = 2 * int64_t(S);
+    lo = (int)floordiv(2 * int64_t(c) * D - S, den);
+    hi = (int)floordiv(2 * int64_t(c + 1) * D - S, den) + 1;
+    lo = std::min(std::max(lo, 0), D - 1);
+    hi = std::min(std::max(hi, 0), D - 1);
+  }
+
+  void build(const oracle_scene& S) {
+    const int f = S.majorant_factor;
+    if (f <= 0) return;
+    const int D[3] = {S.dx, S.dy, S.dz};
+    for (int a = 0; a < 3; ++a) s[a] = (D[a] + f - 1) / f;
+    two.assign((size_t)s[0] * s[1] * s[2], 0.0f);
+    nw.assign(two.size(), 0.0f);
+    for (int cz = 0; cz < s[2]; ++cz)
+      for (int cy = 0; cy < s[1]; ++cy)
+        for (int cx = 0; cx < s[0]; ++cx) {
+          int x0, x1, y0, y1, z0, z1;
+          span(cx, s[0], S.dx, x0, x1);
+          span(cy, s[1], S.dy, y0, y1);
+          span(cz, s[2], S.dz, z0, z1);
+          float mo = 0.0f, mn = 0.0f;
+          for (int z = z0; z <= z1; ++z)
+            for (int y = y0; y <= y1; ++y)
+              for (int x = x0; x <= x1; ++x) {
+                const int64_t v = ((int64_t)z * S.dy + y) * S.dx + x;
+                mo = std::fmax(mo, S.dens_old[v]);
+                mn = std::fmax(mn, S.dens_new[v]);
+              }
+          const size_t i = ((size_t)cz * s[1] + cy) * s[0] + cx;
+          two[i] = S.scale * std::fmax(mo, mn);
+          nw[i] = S.scale * mn;
+        }
+  }
+
+  bool active() const { return s[0] > 0; }
+
+  float at(const std::vector<float>& g, const V3& x) const {
+    auto cell = [](float p, int n) { return std::min(std::max((int)std::floor(p * (float)n), 0), n - 1); };
+    const int i = cell(x.x, s[0]), j = cell(x.y, s[1]), k = cell(x.z, s[2]);
+    return g[((size_t)k * s[1] + j) * s[0] + i];
+  }
+
+  // Distance at which the optical depth along o + t d reaches tau, walking the
+  // cells with a DDA and taking each segment's majorant at its midpoint;
+  // infinity when t would exceed tmax.  mu_at: majorant at the sampled point.
+  float flight(const std::vector<float>& g, const V3& o, const V3& d, float tmax, float tau, float& mu_at) const {
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    float tn[3], td[3];
+    for (int a = 0; a < 3; ++a) {
+      const float n = (float)s[a];
+      const int c = std::min(std::max((int)std::floor(oo[a] * n), 0), s[a] - 1);
+      if (dd[a] > 0.0f) {
+        tn[a] = ((float)(c + 1) / n - oo[a]) / dd[a];
+        td[a] = (1.0f / n) / dd[a];
+      } else if (dd[a] < 0.0f) {
+        tn[a] = ((float)c / n - oo[a]) / dd[a];
+        td[a] = -(1.0f / n) / dd[a];
+      } else {
+        tn[a] = kInf;
+        td[a] = kInf;
+      }
+    }
+    float t = 0.0f, acc = 0.0f;
+    for (int step = 0; step < s[0] + s[1] + s[2] + 4; ++step) {
+      const float t_next = std::fmin(std::fmin(tn[0], tn[1]), tn[2]);
+      const int k = tn[0] == t_next ? 0 : (tn[1] == t_next ? 1 : 2);
+      const float m = at(g, ray_at(o, 0.5f * (t + t_next), d));
+      const float acc_next = acc + m * (t_next - t);
+      const float t_hit = t + (tau - acc) / m;
+      if (m > 0.0f && t_hit < tmax && acc_next >= tau) {
+        mu_at = at(g, ray_at(o, t_hit, d));
+        return t_hit;
+      }
+      if (!(t_next < tmax)) break;
+      tn[k] += td[k];
+      t = t_next;
+      acc = acc_next;
+    }
+    return kInf;
+  }
+};
+
 // Gradient sink of the adjoint (double accumulators, one per worker).
 struct GradSink {
   std::vector<double> dens, alb;
@@ -274,10 +370,11 @@ struct PathOut {
 struct Tracer {
   const oracle_scene& S;
   int mode;         // kTwoState or kSingle
-  float mu;         // majorant used for free-flight sampling
+  float mu;         // global majorant used for free-flight sampling
   GradSink* sink;   // non-null: adjoint replay
   V3 dL{0, 0, 0};   // adjoint: dLoss/dL for this path
   V3 Ltot{0, 0, 0}; // adjoint: the path's total radiance (radiance pass)
+  const Supergrid* sg = nullptr;  // majorant supergrid, if the medium has one
 
   // Radiance the path still gathers after the contributions in `got`:
   // L_rem = L - got, one rounding per channel.
@@ -303,12 +400,15 @@ struct Tracer {
     return true;
   }
 
-  float inv_mu() const { return 1.0f / mu; }
-
-  float free_flight(Rng& rng) const {
+  // Free-flight distance from o along d within [0, tmax]; m = the majorant
+  // of the sampled collision (global, or its supergrid cell's).
+  float free_flight(Rng& rng, const V3& o, const V3& d, float tmax, float& m) const {
     const float u = rng.next1d();
     const float tau = -log_unit(1.0f - u);
-    return mu > 0.0f ? tau * inv_mu() : kInf;
+    m = mu;
+    if (sg != nullptr && sg->active())
+      return sg->flight(mode == kTwoState ? sg->two : sg->nw, o, d, tmax, tau, m);
+    return mu > 0.0f ? tau * (1.0f / mu) : kInf;
   }
 
   // Ratio-tracking transmittance from p along w to the cube boundary
@@ -323,20 +423,22 @@ struct Tracer {
     tro = 1.0f;
     trn = 1.0f;
     for (;;) {
-      const float t = free_flight(rng);
+      float m;
+      const float t = free_flight(rng, q, w, tr_rem, m);
       if (!(t <= tr_rem)) break;
+      const float inv_m = 1.0f / m;
       const V3 x = ray_at(q, t, w);
       const Corners c = corners(S, x);
       ++out.nee_lookups;
       const float st_n = sigma_t(S.dens_new, c);
       if (grad_scale) {
-        const float sn = mu - st_n;
+        const float sn = m - st_n;
         if (sn > 0.0f) sink->density(S, c, -(S.scale * *grad_scale) / sn);
       }
-      trn = trn * ((mu - st_n) * inv_mu());
+      trn = trn * ((m - st_n) * inv_m);
       if (mode == kTwoState) {
         const float st_o = sigma_t(S.dens_old, c);
-        tro = tro * ((mu - st_o) * inv_mu());
+        tro = tro * ((m - st_o) * inv_m);
       }
       q = x;
       tr_rem = tr_rem - t;
@@ -394,7 +496,9 @@ struct Tracer {
 
     for (;;) {
       if (!roulette(rng, depth, bn, bo)) return out;
-      const float t = free_flight(rng);
+      float m;
+      const float t = free_flight(rng, p, d, t_rem, m);
+      const float inv_m = 1.0f / m;
       if (!(t <= t_rem)) {
         // leaves the medium through the null boundary, then escapes
         rng.next1d();
@@ -416,17 +520,17 @@ struct Tracer {
       const float st_o = mode == kTwoState ? sigma_t(S.dens_old, c) : 0.0f;
       const float ur = rng.next1d();
       // mean of both states' sigma_t / mu (plugins/twostatevolpath.py:222-225)
-      const float prob = mode == kTwoState ? (st_n + st_o) * (0.5f * inv_mu()) : st_n * inv_mu();
+      const float prob = mode == kTwoState ? (st_n + st_o) * (0.5f * inv_m) : st_n * inv_m;
       if (ur >= prob) {
         // null collision
         if (mode == kTwoState) {
-          const float sn_o = mu - st_o, sn_n = mu - st_n;
+          const float sn_o = m - st_o, sn_n = m - st_n;
           const float den = sn_n + sn_o;
           const float wn = (2.0f * sn_n) / den, wo = 2.0f - wn;  // weights sum to 2
           bn = V3{bn.x * wn, bn.y * wn, bn.z * wn};
           bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
         } else if (sink) {
-          const float sn = mu - st_n;
+          const float sn = m - st_n;
           const V3 Lr = remaining(Ln);
           const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
           sink->density(S, c, -(S.scale * sd) / sn);
@@ -544,10 +648,13 @@ int oracle_render(const oracle_scene* S, int mode, uint32_t seed, int spp, int c
   const float mu_o = S->scale * grid_max(*S, S->dens_old);
   const float mu_n = S->scale * grid_max(*S, S->dens_new);
   const float mu = mode == kTwoState ? std::fmax(mu_o, mu_n) : mu_n;
+  Supergrid sg;
+  sg.build(*S);
   const int T = spp / chunk;
   std::vector<uint64_t> cnt((size_t)std::max(threads, 1) * 4, 0);
   parallel_rows(row0, row1, row_stride, threads, [&](int k, int y0, int y1) {
     Tracer tr{*S, mode, mu, nullptr};
+    tr.sg = &sg;
     for (int py = y0; py < y1; ++py)
       for (int px = 0; px < S->width; ++px) {
         const int pix = py * S->width + px;
@@ -596,6 +703,8 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
   if (!S || row0 < 0 || row1 > S->height || row0 > row1) return -1;
   if (!S || spp <= 0 || !grad_img || !grad_density) return -1;
   const float mu = S->scale * grid_max(*S, S->dens_new);
+  Supergrid sg;
+  sg.build(*S);
   const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
   const int nt = std::max(threads, 1);
   std::vector<GradSink> sinks(nt);
@@ -613,8 +722,10 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
         for (int s = 0; s < spp; ++s) {
           const uint32_t lane = (uint32_t)((int64_t)pix * spp + s);
           Tracer primal{*S, kSingle, mu, nullptr};
+          primal.sg = &sg;
           const PathOut o = primal.trace(seed, lane, px, py);
           Tracer adj{*S, kSingle, mu, &sinks[k], dL, o.L_new};
+          adj.sg = &sg;
           adj.trace(seed, lane, px, py);
         }
       }

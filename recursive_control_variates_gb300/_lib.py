@@ -51,6 +51,7 @@ class Medium(C.Structure):
         ("albedo_old", C.c_void_p),
         ("albedo_new", C.c_void_p),
         ("albedo_value", f3),
+        ("majorant_factor", C.c_int32),
         ("workspace", C.c_void_p),
     ]
 
@@ -136,7 +137,7 @@ class BatchJob(C.Structure):
         ("albedo_hi", C.c_float),
         ("adam_table", C.c_void_p),
         ("adam_table_len", C.c_int32),
-        ("pad0", C.c_int32),
+        ("majorant_factor", C.c_int32),
         ("density", C.c_void_p * 2),
         ("albedo", C.c_void_p * 2),
         ("density_m", C.c_void_p),
@@ -172,7 +173,7 @@ SIGNATURES = {
     "rcv_kernel_launches": (C.c_uint64, []),
     "rcv_device_info": (C.c_int, [P(C.c_int32), P(C.c_int32), P(C.c_int32)]),
     "rcv_sample_tea_32": (None, [C.c_uint32, C.c_uint32, P(C.c_uint32)]),
-    "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32]),
+    "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32, C.c_int32]),
     "rcv_medium_prepare": (C.c_int, [P(Medium), vp]),
     "rcv_render_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "rcv_render_twostates_volume": (

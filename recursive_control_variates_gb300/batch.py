@@ -83,14 +83,15 @@ class CVJob:
     ``warmup`` / ``beta1`` / ``beta2`` (and ``meta``'s ``pre_update``), the
     optimiser's ``lr`` / betas / epsilon and clamp ranges, and the loss.
     ``optimize_albedo`` (default: when the albedo is a grid) adds the albedo
-    grid to the optimised variables."""
+    grid to the optimised variables; ``majorant_factor`` > 0 gives the medium
+    a majorant supergrid (the reference's ``majorant_resolution_factor``)."""
 
     def __init__(self, density, albedo, target, sensor, *, spp: int, spp_grad: int = 0, max_depth: int = 6,
                  rr_depth: int = 5, hide_emitters: bool = False, scale: float = 1.0, seed: int = 0,
                  lr: float = 0.02, adam_betas=(0.9, 0.999), adam_eps: float = 1e-8,
                  density_bounds=(-_INF, _INF), albedo_bounds=(-_INF, _INF), warmup: int = 1, beta1: float = 0.9,
                  beta2: float = 0.999, pre_update: bool = False, loss: str = "l2", optimize_albedo=None,
-                 keep_images: bool = False, device="cuda"):
+                 keep_images: bool = False, majorant_factor: int = 0, device="cuda"):
         lib = _lib.load()
         self.device = torch.device(device)
         dev = self.device
@@ -159,6 +160,9 @@ class CVJob:
         j.density_lo, j.density_hi = float(density_bounds[0]), float(density_bounds[1])
         j.albedo_lo, j.albedo_hi = float(albedo_bounds[0]), float(albedo_bounds[1])
         j.adam_table, j.adam_table_len = self._tables[2].data_ptr(), self._tables[2].shape[0]
+        if int(majorant_factor) < 0:
+            raise ValueError("majorant_factor must be >= 0")
+        j.majorant_factor = int(majorant_factor)
         j.density[0], j.density[1] = self.density[0].data_ptr(), self.density[1].data_ptr()
         if self.albedo is not None:
             j.albedo[0], j.albedo[1] = self.albedo[0].data_ptr(), self.albedo[1].data_ptr()
@@ -221,7 +225,7 @@ class CVJob:
             albedo_bounds=opt.bounds.get(akey, (-_INF, _INF)) if akey else (-_INF, _INF),
             warmup=integrator.warmup, beta1=integrator.beta1, beta2=integrator.beta2,
             pre_update=getattr(integrator, "pre_update", False), loss=loss, optimize_albedo=akey is not None,
-            keep_images=keep_images, device=medium.device,
+            keep_images=keep_images, majorant_factor=medium.majorant_resolution_factor(), device=medium.device,
         )
 
     # ---------------------------------------------------------------- state

@@ -215,11 +215,30 @@ class _PackedMedium:
     def _states(self):
         raise NotImplementedError
 
+    def majorant_resolution_factor(self) -> int:
+        return self._factor()
+
+    def set_majorant_resolution_factor(self, factor: int) -> None:
+        """Supergrid resolution factor (plugins/twostatemedium.py:171-178,
+        utils.py:27-43); 0 = one global majorant."""
+        if int(factor) < 0:
+            raise ValueError("majorant_resolution_factor must be >= 0")
+        for m in self._media():
+            m.majorant_factor = int(factor)
+        self._workspace = None
+        self._dirty = True
+
+    def _media(self):
+        return (self,)
+
+    def _factor(self) -> int:
+        return self._states()[1].majorant_factor
+
     def workspace(self) -> torch.Tensor:
         if self._workspace is None:
             lib = _lib.load()
             dims = (C.c_int32 * 3)(*self.dims)
-            nbytes = int(lib.rcv_medium_workspace_bytes(dims, int(self.has_albedo_grid)))
+            nbytes = int(lib.rcv_medium_workspace_bytes(dims, int(self.has_albedo_grid), self._factor()))
             self._workspace = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
         return self._workspace
 
@@ -236,6 +255,7 @@ class _PackedMedium:
             m.albedo_old = old.albedo_grid.data_ptr()
             m.albedo_new = new.albedo_grid.data_ptr()
         m.albedo_value[:] = list(new.albedo_value)
+        m.majorant_factor = self._factor()
         m.workspace = aligned
         return m
 
@@ -281,8 +301,10 @@ class HeterogeneousMedium(_PackedMedium):
             raise ValueError("only the isotropic phase function is supported")
         if props.get("has_spectral_extinction", False):
             raise ValueError("spectrally varying extinction is not supported")
-        if int(props.get("majorant_resolution_factor", 0)) != 0:
-            raise ValueError("majorant supergrids are not supported")
+        # majorant supergrid of ceil(D/f) cells per axis (0: one global majorant)
+        self.majorant_factor = int(props.get("majorant_resolution_factor", 0))
+        if self.majorant_factor < 0:
+            raise ValueError("majorant_resolution_factor must be >= 0")
         self._workspace = None
         self._dirty = True
 
@@ -337,6 +359,9 @@ class TwoStateMedium(_PackedMedium):
 
     def _states(self):
         return self.old, self.new
+
+    def _media(self):
+        return (self.old, self.new, self.incoming)
 
     @property
     def dims(self):

@@ -67,7 +67,7 @@ static JobLayout job_layout(const rcv_batch_job& j) {
   L.header = off;
   off = align256(off + sizeof(JobHeader));
   L.medium = off;
-  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr).total);
+  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr, j.majorant_factor).total);
   L.buckets = off;
   off = align256(off + kRenderOrderBuckets * sizeof(uint32_t));
   L.order = off;
@@ -230,6 +230,20 @@ __global__ void batch_order_place_kernel(const BatchEntry* __restrict__ E, const
   if (valid) B.cost[pix] = 0u;
 }
 
+// Majorant supergrids of the jobs that have one (old = the other half of the
+// parameter double buffer, new = the current half).
+__global__ void batch_supergrid_kernel(const BatchEntry* __restrict__ E, const VolJob* __restrict__ two,
+                                       const int32_t* __restrict__ bp, int n) {
+  const int j = job_of_block(bp, n, blockIdx.x);
+  const BatchEntry& B = E[j];
+  const VolJob& J = two[j];
+  const int64_t i = int64_t(blockIdx.x - __ldg(bp + j)) * blockDim.x + threadIdx.x;
+  if (J.sg[0] == 0 || i >= int64_t(J.sg[0]) * J.sg[1] * J.sg[2]) return;
+  const int cur = B.hdr->step.cur;
+  supergrid_cell(i, J.sg, B.d.dims[0], B.d.dims[1], B.d.dims[2], B.d.scale, B.d.density[cur ^ 1],
+                 B.d.density[cur], const_cast<float*>(J.sg_two), const_cast<float*>(J.sg_new));
+}
+
 // Initial per-pixel cost of a job: its chord order (longest chord first).
 __global__ void cost_from_chord_kernel(const __grid_constant__ VolJob J, int npix, uint32_t* cost) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,6 +362,7 @@ static int validate_job(const rcv_batch_job* j, int idx) {
               "job %d: CV bias-correction tables are missing", idx);
   RCV_REQUIRE(j->adam_table && j->adam_table_len > 0, "job %d: Adam bias-correction table is missing", idx);
   RCV_REQUIRE(j->loss == RCV_LOSS_L2 || j->loss == RCV_LOSS_L1, "job %d: unknown loss kind %d", idx, j->loss);
+  RCV_REQUIRE(j->majorant_factor >= 0, "job %d: majorant_factor must be >= 0", idx);
   RCV_REQUIRE(j->workspace != nullptr && (reinterpret_cast<uintptr_t>(j->workspace) & 255u) == 0,
               "job %d: workspace must be non-NULL and 256-byte aligned", idx);
   return RCV_OK;
@@ -371,7 +386,7 @@ static PlanLayout plan_layout(int n, int64_t total_two_paths, int64_t total_adj_
   L.adj = off;
   off = align256(off + uint64_t(n) * sizeof(VolJob));
   L.prefix = off;
-  off = align256(off + 3u * uint64_t(n + 1) * sizeof(int32_t));
+  off = align256(off + 4u * uint64_t(n + 1) * sizeof(int32_t));
   L.queue = off;
   off = align256(off + 4u * sizeof(unsigned long long));
   L.counters = off;
@@ -398,6 +413,7 @@ static rcv_medium job_medium(const rcv_batch_job& j, const JobLayout& L) {
   m.albedo_old = j.albedo[0];
   m.albedo_new = j.albedo[1];
   std::memcpy(m.albedo_value, j.albedo_value, sizeof(m.albedo_value));
+  m.majorant_factor = j.majorant_factor;
   m.workspace = static_cast<char*>(j.workspace) + L.medium;
   return m;
 }
@@ -423,13 +439,13 @@ struct rcv_batch {
   BatchEntry* entries = nullptr;
   VolJob* two = nullptr;
   VolJob* adj = nullptr;
-  int32_t* prefix = nullptr;  // pack | image | update block prefixes, n + 1 each
+  int32_t* prefix = nullptr;  // pack | image | update | supergrid block prefixes, n + 1 each
   unsigned long long* queue = nullptr;
   uint64_t* counters = nullptr;
   float4* path_out = nullptr;
   AdjBuffers adjbuf{};
   int64_t total_two = 0, total_adj = 0;
-  int32_t pack_blocks = 0, pix_blocks = 0, vox_blocks = 0;
+  int32_t pack_blocks = 0, pix_blocks = 0, vox_blocks = 0, sg_blocks = 0;
   // host copies of the tables (kept until destroy: the upload reads them)
   std::vector<BatchEntry> h_entries;
   std::vector<VolJob> h_two, h_adj;
@@ -515,11 +531,12 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->h_entries.resize(n);
   b->h_two.resize(n);
   b->h_adj.resize(n);
-  b->h_prefix.assign(3 * size_t(n + 1), 0);
+  b->h_prefix.assign(4 * size_t(n + 1), 0);
   int32_t* pp = b->h_prefix.data();
   int32_t* pi = pp + (n + 1);
   int32_t* pv = pi + (n + 1);
-  int64_t two_total = 0, adj_total = 0, pack_blocks = 0, pix_blocks = 0, vox_blocks = 0;
+  int32_t* ps = pv + (n + 1);
+  int64_t two_total = 0, adj_total = 0, pack_blocks = 0, pix_blocks = 0, vox_blocks = 0, sg_blocks = 0;
   for (int j = 0; j < n; ++j) {
     const rcv_batch_job& d = jobs[j];
     const JobLayout L = job_layout(d);
@@ -551,7 +568,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     std::memset(&e, 0, sizeof(e));
     e.d = d;
     e.hdr = reinterpret_cast<JobHeader*>(ws + L.header);
-    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr);
+    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr, d.majorant_factor);
     char* mw = ws + L.medium;
     e.cells = reinterpret_cast<float4*>(mw + M.cells);
     e.has_albedo = d.albedo[0] != nullptr;
@@ -575,9 +592,11 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     pp[j] = (int32_t)pack_blocks;
     pi[j] = (int32_t)pix_blocks;
     pv[j] = (int32_t)vox_blocks;
+    ps[j] = (int32_t)sg_blocks;
     pack_blocks += grid_for(e.nc, kBatchBlock);
     pix_blocks += grid_for(e.npix, kBatchBlock);
     vox_blocks += grid_for(e.nv, kBatchBlock);
+    if (T.sg[0] > 0) sg_blocks += grid_for(int64_t(T.sg[0]) * T.sg[1] * T.sg[2], kBatchBlock);
     two_total += T.path_count;
     adj_total += A.path_count;
     if (pack_blocks >= INT32_MAX || pix_blocks >= INT32_MAX || vox_blocks >= INT32_MAX) {
@@ -589,6 +608,8 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   pp[n] = (int32_t)pack_blocks;
   pi[n] = (int32_t)pix_blocks;
   pv[n] = (int32_t)vox_blocks;
+  ps[n] = (int32_t)sg_blocks;
+  b->sg_blocks = (int32_t)sg_blocks;
   b->total_two = two_total;
   b->total_adj = adj_total;
   b->pack_blocks = (int32_t)pack_blocks;
@@ -640,12 +661,19 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   const int32_t* pp = b->prefix;
   const int32_t* pi = pp + (n + 1);
   const int32_t* pv = pi + (n + 1);
+  const int32_t* ps = pv + (n + 1);
+  const bool sg = b->sg_blocks > 0;
   batch_prologue_kernel<<<1, kBatchBlock, 0, st>>>(b->entries, b->two, b->adj, n);
   int rc = launched("batch prologue launch");
   if (rc) return rc;
   batch_pack_kernel<<<(unsigned)b->pack_blocks, kBatchBlock, 0, st>>>(b->entries, pp, n);
   rc = launched("batch pack launch");
   if (rc) return rc;
+  if (sg) {
+    batch_supergrid_kernel<<<(unsigned)b->sg_blocks, kBatchBlock, 0, st>>>(b->entries, b->two, ps, n);
+    rc = launched("batch supergrid launch");
+    if (rc) return rc;
+  }
   if (b->opt.order == RCV_ORDER_COST) {
     batch_order_count_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n);
     rc = launched("batch order count launch");
@@ -665,18 +693,18 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   RCV_TRY_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "fork wait");
   RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, sizeof(unsigned long long), b->side), "checkpoint reset");
   rc = launch_persistent(kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr, &b->adjbuf,
-                         b->counters + RCV_COUNTER_COUNT, b->side);
+                         b->counters + RCV_COUNTER_COUNT, b->side, sg);
   if (rc) return rc;
   RCV_TRY_CUDA(cudaEventRecord(b->join, b->side), "join record");
   rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr,
-                         b->counters, st);
+                         b->counters, st, sg);
   if (rc) return rc;
   batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
   rc = launched("batch image launch");
   if (rc) return rc;
   RCV_TRY_CUDA(cudaStreamWaitEvent(st, b->join, 0), "join wait");
   rc = launch_persistent(kReplay, none, b->adj, n, b->total_adj, &b->opt, b->queue + 2, nullptr, &b->adjbuf,
-                         b->counters + RCV_COUNTER_COUNT, st);
+                         b->counters + RCV_COUNTER_COUNT, st, sg);
   if (rc) return rc;
   batch_update_kernel<<<(unsigned)b->vox_blocks, kBatchBlock, 0, st>>>(b->entries, pv, n);
   return launched("batch update launch");
@@ -718,7 +746,7 @@ extern "C" uint64_t* rcv_batch_counters(rcv_batch* b) { return b != nullptr ? b-
 
 extern "C" int32_t rcv_batch_kernels_per_step(const rcv_batch* b) {
   if (b == nullptr) return RCV_ERR_INVALID;
-  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0);
+  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0) + (b->sg_blocks > 0 ? 1 : 0);
 }
 
 extern "C" int rcv_batch_destroy(rcv_batch* b) {

@@ -47,14 +47,22 @@ inline int launched(const char* what) {
 
 inline uint64_t align256(uint64_t v) { return (v + 255u) & ~uint64_t(255u); }
 
-// Layout of the medium workspace (all sections 256-byte aligned).
+// Majorant supergrid cells along an axis of D voxels for factor f (0 = none).
+inline int supergrid_cells(int D, int f) { return f > 0 ? (D + f - 1) / f : 0; }
+
+// Layout of the medium workspace (all sections 256-byte aligned).  With a
+// majorant supergrid: its cells for the two-state tracer (max of both
+// states) and for the single-state tracers (new state).
 struct MediumLayout {
-  uint64_t cells, albedo, maxbits, grad_cells, grad_albedo, total;
+  uint64_t cells, albedo, maxbits, grad_cells, grad_albedo, sg_two, sg_new, total;
 };
 
-inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo) {
+inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo, int majorant_factor) {
   const uint64_t nc = uint64_t(dims[0] + 1) * uint64_t(dims[1] + 1) * uint64_t(dims[2] + 1);
   const uint64_t nv = uint64_t(dims[0]) * uint64_t(dims[1]) * uint64_t(dims[2]);
+  const uint64_t ns = uint64_t(supergrid_cells(dims[0], majorant_factor)) *
+                      uint64_t(supergrid_cells(dims[1], majorant_factor)) *
+                      uint64_t(supergrid_cells(dims[2], majorant_factor));
   MediumLayout l;
   uint64_t off = 0;
   l.cells = off;
@@ -67,6 +75,10 @@ inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo) {
   off = align256(off + nc * 32u);
   l.grad_albedo = off;
   off = align256(off + (has_albedo ? nv * 16u : 0u));
+  l.sg_two = off;
+  off = align256(off + ns * 4u);
+  l.sg_new = off;
+  off = align256(off + ns * 4u);
   l.total = off;
   return l;
 }

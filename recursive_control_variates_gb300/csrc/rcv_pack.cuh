@@ -27,6 +27,39 @@ __device__ __forceinline__ void pack_cell(int64_t i, int dx, int dy, int dz, con
   c[3] = make_float4(new_d[i001], new_d[i101], new_d[i011], new_d[i111]);
 }
 
+// Voxels whose trilinear weight can be non-zero inside supergrid cell c of
+// S cells along an axis of D voxels: x in [c/S, (c+1)/S) reads voxels
+// floor(xD - 1/2) and floor(xD - 1/2) + 1, clamped to [0, D-1].
+__device__ __forceinline__ void supergrid_span(int c, int S, int D, int& lo, int& hi) {
+  const int64_t a = 2 * int64_t(c) * D - S, b = 2 * int64_t(c + 1) * D - S, den = 2 * int64_t(S);
+  const int64_t fa = a >= 0 ? a / den : -((-a + den - 1) / den);  // floor division
+  const int64_t fb = b >= 0 ? b / den : -((-b + den - 1) / den);
+  lo = clampi((int)fa, D - 1);
+  hi = clampi((int)fb + 1, D - 1);
+}
+
+// Majorants of supergrid cell i (x fastest): scale * the largest old / new
+// density (non-negative part) over its voxel span; two = max of both states.
+__device__ __forceinline__ void supergrid_cell(int64_t i, const int sg[3], int dx, int dy, int dz, float scale,
+                                               const float* __restrict__ old_d, const float* __restrict__ new_d,
+                                               float* __restrict__ sg_two, float* __restrict__ sg_new) {
+  const int cx = int(i % sg[0]), cy = int((i / sg[0]) % sg[1]), cz = int(i / (int64_t(sg[0]) * sg[1]));
+  int x0, x1, y0, y1, z0, z1;
+  supergrid_span(cx, sg[0], dx, x0, x1);
+  supergrid_span(cy, sg[1], dy, y0, y1);
+  supergrid_span(cz, sg[2], dz, z0, z1);
+  float mo = 0.0f, mn = 0.0f;
+  for (int z = z0; z <= z1; ++z)
+    for (int y = y0; y <= y1; ++y)
+      for (int x = x0; x <= x1; ++x) {
+        const int64_t v = (int64_t(z) * dy + y) * dx + x;
+        mo = fmaxf(mo, old_d[v]);
+        mn = fmaxf(mn, new_d[v]);
+      }
+  sg_two[i] = scale * fmaxf(mo, mn);
+  sg_new[i] = scale * mn;
+}
+
 // Voxel i of the old and the new RGB albedo as one 32-byte pair.
 __device__ __forceinline__ void pack_albedo(int64_t i, const float* __restrict__ old_a,
                                             const float* __restrict__ new_a, float4* __restrict__ albedo) {

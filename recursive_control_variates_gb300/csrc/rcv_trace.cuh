@@ -71,9 +71,9 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
   return Q.jobs[lo];
 }
 
-template <int kMode>
+// kSG: the launch may contain media with a majorant supergrid.
+template <int kMode, bool kSG>
 __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& cnt) {
-  constexpr bool kAdj = kMode == kAdjoint || kMode == kReplay;  // single-state `new`, gradients
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const float mis = 0.5f;  // power heuristic between two equal 1/(4 pi) pdfs
@@ -331,7 +331,17 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       if (!alive) {
         finished = true;
       } else {
-        const float t = free_flight(next1d(*r), mu, inv_mu);
+        // majorant of this collision: global, or the supergrid cell it lies in
+        float mu_c = mu, inv_c = inv_mu, hinv_c = half_inv_mu;
+        float t;
+        if (kSG && J.sg[0] > 0) {
+          const float tau = -log_unit(1.0f - next1d(*r));
+          t = supergrid_flight(J, kMode == kTwoState ? J.sg_two : J.sg_new, org, dir, tmax, tau, mu_c);
+          inv_c = 1.0f / mu_c;
+          hinv_c = 0.5f * inv_c;
+        } else {
+          t = free_flight(next1d(*r), mu, inv_mu);
+        }
         const bool valid = t <= tmax;
         Lookup lk;
         float rho_o = 0.0f, rho_n = 0.0f;
@@ -358,20 +368,20 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             // the single-state sigma_t / mu
             float prob;
             if (kMode == kTwoState)
-              prob = (st_n + st_o) * half_inv_mu;
+              prob = (st_n + st_o) * hinv_c;
             else
-              prob = st_n * inv_mu;
+              prob = st_n * inv_c;
             if (ur >= prob) {
               // null collision (plugins/twostatevolpath.py:227-231, 256-257);
               // the two weights sum to 2, equal states give exactly 1
               if (kMode == kTwoState) {
-                const float sn_o = mu - st_o, sn_n = mu - st_n;
+                const float sn_o = mu_c - st_o, sn_n = mu_c - st_n;
                 const float den = sn_n + sn_o;
                 const float wn = (2.0f * sn_n) / den, wo = 2.0f - wn;
                 bn = V3{bn.x * wn, bn.y * wn, bn.z * wn};
                 bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
               } else if (kMode == kReplay) {
-                const float sn = mu - st_n;
+                const float sn = mu_c - st_n;
                 const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
                 const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
                 scatter_density(J, lk, -(J.scale * sd) / sn);
@@ -406,8 +416,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           bool done = !valid;
           if (valid) {
             // ratio tracking (plugins/twostatevolpath.py:443-452)
-            trn = trn * ((mu - st_n) * inv_mu);
-            if (kMode == kTwoState) tro = tro * ((mu - st_o) * inv_mu);
+            trn = trn * ((mu_c - st_n) * inv_c);
+            if (kMode == kTwoState) tro = tro * ((mu_c - st_o) * inv_c);
             q = x;
             tr_rem = tr_rem - t;
             done = (kMode == kTwoState) ? (trn == 0.0f && tro == 0.0f) : (trn == 0.0f);
@@ -448,12 +458,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         } else {  // kNeeAdj: the shadow walk with gradients
           bool done = !valid;
           if (valid) {
-            const float sn = mu - st_n;
+            const float sn = mu_c - st_n;
             if (sn > 0.0f) {
               scatter_density(J, lk, -(J.scale * s_nee) / sn);
               ++cnt.grad_events;
             }
-            trn = trn * (sn * inv_mu);
+            trn = trn * (sn * inv_c);
             q = x;
             tr_rem = tr_rem - t;
             done = trn == 0.0f;

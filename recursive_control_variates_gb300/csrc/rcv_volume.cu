@@ -53,12 +53,22 @@ __device__ __forceinline__ void add_counts(unsigned long long* counters, const C
   }
 }
 
-template <int kMode>
+template <int kMode, bool kSG>
 __global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_constant__ VolJob J,
                                                             const __grid_constant__ Queue Q) {
   Counts cnt{0, 0, 0, 0, 0, 0};
-  trace_persistent<kMode>(J, Q, cnt);
+  trace_persistent<kMode, kSG>(J, Q, cnt);
   add_counts(Q.counters, cnt);
+}
+
+// Majorant supergrid of a medium (both states' cells and the new state's).
+__global__ void supergrid_kernel(int sx, int sy, int sz, int dx, int dy, int dz, float scale,
+                                 const float* __restrict__ old_d, const float* __restrict__ new_d,
+                                 float* __restrict__ sg_two, float* __restrict__ sg_new) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= int64_t(sx) * sy * sz) return;
+  const int sg[3] = {sx, sy, sz};
+  supergrid_cell(i, sg, dx, dy, dz, scale, old_d, new_d, sg_two, sg_new);
 }
 
 // ------------------------------------------------------ hand-out ordering
@@ -161,6 +171,7 @@ static int validate_medium(const rcv_medium* m) {
   RCV_REQUIRE((reinterpret_cast<uintptr_t>(m->workspace) & 255u) == 0,
               "medium workspace must be 256-byte aligned");
   RCV_REQUIRE(m->scale >= 0.0f, "medium scale must be non-negative");
+  RCV_REQUIRE(m->majorant_factor >= 0, "majorant_factor must be >= 0");
   return RCV_OK;
 }
 
@@ -192,7 +203,7 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   J->dy = m->dims[1];
   J->dz = m->dims[2];
   J->scale = m->scale;
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
+  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
   char* ws = static_cast<char*>(m->workspace);
   J->cells = reinterpret_cast<const float4*>(ws + L.cells);
   J->albedo = m->albedo_old ? reinterpret_cast<const float4*>(ws + L.albedo) : nullptr;
@@ -200,6 +211,11 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   J->albedo_const[1] = m->albedo_value[1];
   J->albedo_const[2] = m->albedo_value[2];
   J->maxbits = reinterpret_cast<const uint32_t*>(ws + L.maxbits);
+  J->sg[0] = supergrid_cells(m->dims[0], m->majorant_factor);
+  J->sg[1] = supergrid_cells(m->dims[1], m->majorant_factor);
+  J->sg[2] = supergrid_cells(m->dims[2], m->majorant_factor);
+  J->sg_two = J->sg[0] > 0 ? reinterpret_cast<const float*>(ws + L.sg_two) : nullptr;
+  J->sg_new = J->sg[0] > 0 ? reinterpret_cast<const float*>(ws + L.sg_new) : nullptr;
   J->grad_cells = reinterpret_cast<float4*>(ws + L.grad_cells);
   J->grad_albedo = m->albedo_old ? reinterpret_cast<float4*>(ws + L.grad_albedo) : nullptr;
   J->path_begin = 0;
@@ -208,17 +224,21 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
 }
 
 // Resident blocks per SM of each tracer variant (queried once per process).
-static int resident_blocks(int mode) {
+static int resident_blocks(int mode, bool sg) {
   static std::once_flag once;
-  static int blocks[4] = {1, 1, 1, 1};
+  static int blocks[8] = {1, 1, 1, 1, 1, 1, 1, 1};
   std::call_once(once, [] {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_kernel<kTwoState>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_kernel<kSingle>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_kernel<kAdjoint>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], trace_kernel<kReplay>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_kernel<kTwoState, false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_kernel<kSingle, false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_kernel<kAdjoint, false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], trace_kernel<kReplay, false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[4], trace_kernel<kTwoState, true>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[5], trace_kernel<kSingle, true>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[6], trace_kernel<kAdjoint, true>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[7], trace_kernel<kReplay, true>, kTraceBlock, 0);
     for (int& b : blocks) b = b < 1 ? 1 : b;
   });
-  return blocks[mode];
+  return blocks[mode + (sg ? 4 : 0)];
 }
 
 static int sm_count() {
@@ -234,7 +254,7 @@ static int sm_count() {
 }
 
 void warm_launch_config() {
-  (void)resident_blocks(kTwoState);
+  (void)resident_blocks(kTwoState, false);
   (void)sm_count();
 }
 
@@ -259,7 +279,8 @@ int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, uint32_t* 
 // device job table.
 int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
                       const rcv_volpath_options* o, unsigned long long* queue_counter,
-                      float4* path_out, const AdjBuffers* adj, uint64_t* counters, cudaStream_t st) {
+                      float4* path_out, const AdjBuffers* adj, uint64_t* counters, cudaStream_t st,
+                      bool supergrid) {
   Queue Q;
   std::memset(&Q, 0, sizeof(Q));
   Q.counter = queue_counter;
@@ -281,7 +302,8 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   Q.defer = (o != nullptr && o->defer > 0) ? o->defer : 8;
   RCV_REQUIRE(Q.defer <= 32, "defer must be in [1, 32]");
   RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
-  int per_sm = resident_blocks(mode);
+  const bool sg = supergrid || (jobs == nullptr && J.sg[0] > 0);
+  int per_sm = resident_blocks(mode, sg);
   if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
   // replay: the checkpoint tasks come on top of one camera task per path
   const int64_t tasks = mode == kReplay ? 2 * total : total;
@@ -290,11 +312,21 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   const int64_t cap = int64_t(sm_count()) * per_sm;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  switch (mode) {
-    case kTwoState: trace_kernel<kTwoState><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
-    case kSingle: trace_kernel<kSingle><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
-    case kAdjoint: trace_kernel<kAdjoint><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
-    default: trace_kernel<kReplay><<<(unsigned)blocks, kTraceBlock, 0, st>>>(J, Q); break;
+  const unsigned g = (unsigned)blocks;
+  if (sg) {
+    switch (mode) {
+      case kTwoState: trace_kernel<kTwoState, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+      case kSingle: trace_kernel<kSingle, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+      case kAdjoint: trace_kernel<kAdjoint, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+      default: trace_kernel<kReplay, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+    }
+  } else {
+    switch (mode) {
+      case kTwoState: trace_kernel<kTwoState, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+      case kSingle: trace_kernel<kSingle, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+      case kAdjoint: trace_kernel<kAdjoint, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+      default: trace_kernel<kReplay, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
+    }
   }
   return launched("trace kernel launch");
 }
@@ -312,7 +344,7 @@ int launch_reduce(bool two, const float4* po, int64_t path_begin, int64_t npix, 
 }
 
 int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cudaStream_t st) {
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
+  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
   const char* ws = static_cast<const char*>(m->workspace);
   const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
   const int block = 256;
@@ -330,7 +362,7 @@ int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cu
 }
 
 int reset_gradients(const rcv_medium* m, bool albedo, cudaStream_t st) {
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
+  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
   char* ws = static_cast<char*>(m->workspace);
   const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
   const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
@@ -343,9 +375,10 @@ int reset_gradients(const rcv_medium* m, bool albedo, cudaStream_t st) {
 
 using namespace rcv;
 
-extern "C" uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid) {
-  if (dims == nullptr || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return 0;
-  return medium_layout(dims, has_albedo_grid != 0).total;
+extern "C" uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid,
+                                               int32_t majorant_factor) {
+  if (dims == nullptr || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || majorant_factor < 0) return 0;
+  return medium_layout(dims, has_albedo_grid != 0, majorant_factor).total;
 }
 
 extern "C" uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp,
@@ -359,7 +392,7 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
   int rc = validate_medium(m);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr);
+  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
   char* ws = static_cast<char*>(m->workspace);
   RCV_TRY_CUDA(cudaMemsetAsync(ws + L.maxbits, 0, 16, st), "majorant reset");
   const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
@@ -369,7 +402,15 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
       reinterpret_cast<float4*>(ws + L.cells), m->albedo_old, m->albedo_new,
       m->albedo_old ? reinterpret_cast<float4*>(ws + L.albedo) : nullptr,
       reinterpret_cast<uint32_t*>(ws + L.maxbits));
-  return launched("pack_medium launch");
+  rc = launched("pack_medium launch");
+  if (rc || m->majorant_factor == 0) return rc;
+  const int sx = supergrid_cells(m->dims[0], m->majorant_factor);
+  const int sy = supergrid_cells(m->dims[1], m->majorant_factor);
+  const int sz = supergrid_cells(m->dims[2], m->majorant_factor);
+  supergrid_kernel<<<grid_for(int64_t(sx) * sy * sz, 128), 128, 0, st>>>(
+      sx, sy, sz, m->dims[0], m->dims[1], m->dims[2], m->scale, m->density_old, m->density_new,
+      reinterpret_cast<float*>(ws + L.sg_two), reinterpret_cast<float*>(ws + L.sg_new));
+  return launched("supergrid launch");
 }
 
 // Orders the pixels, runs the persistent tracer of one job and, for the
@@ -404,11 +445,11 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
     A.ckpt_cap = ckpt_capacity(J.path_count);
     A.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
     RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, sizeof(unsigned long long), st), "checkpoint reset");
-    rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st);
+    rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
     if (rc) return rc;
-    return launch_persistent(kReplay, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st);
+    return launch_persistent(kReplay, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
   }
-  rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o, qc, po, nullptr, counters, st);
+  rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o, qc, po, nullptr, counters, st, false);
   if (rc) return rc;
   return launch_reduce(mode == kTwoState, po, 0, npix, J.spp, img_new, img_old, st);
 }

@@ -59,6 +59,11 @@ struct VolJob {
   int64_t path_count;   // width*height*spp
   const uint32_t* pixel_order;  // pixel handed out k-th (null = row-major)
   uint32_t* pixel_cost;         // per-pixel sum of path lengths (loop iterations), or null
+  // majorant supergrid: cells per axis (0 = one global majorant) and the
+  // cells' majorants for the two-state tracer / the single-state tracers
+  int32_t sg[3];
+  const float* sg_two;
+  const float* sg_new;
 };
 
 // Work queue of a (possibly multi-job) persistent launch.
@@ -144,6 +149,60 @@ __device__ __forceinline__ float density_new(const VolJob& J, const Lookup& l) {
 }
 
 __device__ __forceinline__ int clampi(int v, int hi) { return v < 0 ? 0 : (v > hi ? hi : v); }
+
+// ------------------------------------------------------- majorant supergrid
+// Supergrid cell of a point (nearest lookup), clamped to the grid.
+__device__ __forceinline__ float supergrid_at(const VolJob& J, const float* __restrict__ maj, const V3& x) {
+  const int i = clampi((int)floorf(x.x * (float)J.sg[0]), J.sg[0] - 1);
+  const int j = clampi((int)floorf(x.y * (float)J.sg[1]), J.sg[1] - 1);
+  const int k = clampi((int)floorf(x.z * (float)J.sg[2]), J.sg[2] - 1);
+  return __ldg(maj + ((int64_t)k * J.sg[1] + j) * J.sg[0] + i);
+}
+
+// Free-flight distance of optical depth `tau` along o + t d, t in [0, tmax],
+// through the majorant supergrid (plugins/twostatemedium.py:25-70): a DDA
+// walk (Amanatides & Woo) accumulates majorant x segment length per cell,
+// the majorant of a segment being the cell at its midpoint, and stops inside
+// the cell where tau is reached.  Returns kInf when the walk leaves the
+// segment; otherwise mu_at = the majorant at the sampled point.
+__device__ __forceinline__ float supergrid_flight(const VolJob& J, const float* __restrict__ maj, const V3& o,
+                                                  const V3& d, float tmax, float tau, float& mu_at) {
+  const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+  float tn[3], td[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float S = (float)J.sg[a];
+    const int c = clampi((int)floorf(oo[a] * S), J.sg[a] - 1);
+    if (dd[a] > 0.0f) {
+      tn[a] = ((float)(c + 1) / S - oo[a]) / dd[a];
+      td[a] = (1.0f / S) / dd[a];
+    } else if (dd[a] < 0.0f) {
+      tn[a] = ((float)c / S - oo[a]) / dd[a];
+      td[a] = -(1.0f / S) / dd[a];
+    } else {
+      tn[a] = kInf;
+      td[a] = kInf;
+    }
+  }
+  float t = 0.0f, tau_acc = 0.0f;
+  const int max_steps = J.sg[0] + J.sg[1] + J.sg[2] + 4;
+  for (int s = 0; s < max_steps; ++s) {
+    const float t_next = fminf(fminf(tn[0], tn[1]), tn[2]);
+    const int k = tn[0] == t_next ? 0 : (tn[1] == t_next ? 1 : 2);
+    const float m = supergrid_at(J, maj, advance(o, 0.5f * (t + t_next), d));
+    const float tau_next = tau_acc + m * (t_next - t);
+    const float t_precise = t + (tau - tau_acc) / m;
+    if (m > 0.0f && t_precise < tmax && tau_next >= tau) {
+      mu_at = supergrid_at(J, maj, advance(o, t_precise, d));
+      return t_precise;
+    }
+    if (!(t_next < tmax)) break;
+    tn[k] += td[k];
+    t = t_next;
+    tau_acc = tau_next;
+  }
+  return kInf;
+}
 
 // Trilinear RGB albedo of one state (state 0 = old, 1 = new).
 __device__ __forceinline__ V3 albedo_at(const VolJob& J, const Lookup& l, int state) {
@@ -273,9 +332,11 @@ __device__ __forceinline__ int cost_bucket(uint32_t c) {
 }
 // Persistent tracer launch (TraceMode `mode`) over `total` paths of one job
 // (jobs == NULL) or of a device job table of njobs entries.
+// supergrid: some job of the table has a majorant supergrid (the kernel
+// variant that can traverse one is launched; single jobs decide from J.sg).
 int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
                       const rcv_volpath_options* o, unsigned long long* queue_counter, float4* path_out,
-                      const AdjBuffers* adj, uint64_t* counters, cudaStream_t st);
+                      const AdjBuffers* adj, uint64_t* counters, cudaStream_t st, bool supergrid);
 // Queries the occupancy and SM count the launchers cache, so that later
 // launches (e.g. under stream capture) make no device queries.
 void warm_launch_config();

@@ -228,14 +228,17 @@ def test_single_path_jobs_bitwise_over_many_steps(cuda, use_graph):
     comes from one thread in program order, so the whole optimisation is
     deterministic: parameters, moments, weights, statistics and images of the
     batched and the plain form stay bit-identical over many steps (this
-    exercises the device-side CV and Adam bias-correction tables)."""
+    exercises the device-side CV and Adam bias-correction tables, and the
+    batched supergrid of the third job)."""
     pairs = []
-    for k, (D, agrid) in enumerate([(6, True), (5, False)]):
+    for k, (D, agrid, factor) in enumerate([(6, True, 0), (5, False, 0), (12, False, 4)]):
         true = scenes.blob_density(D, 60 + k)
         alb = scenes.albedo_grid(D, 60 + k) if agrid else 0.8
         target = torch.full((1, 1, 3), 0.3 + 0.1 * k, device=cuda)
         alb0 = np.full_like(alb, 0.5) if agrid else alb
         plain = plain_setup(cuda, (0.5 * true).astype(np.float32), alb0, 1, 16, 0.05, 1)
+        if factor:  # a majorant supergrid on the third job
+            plain[0].named_shapes()["object"].interior_medium().set_majorant_resolution_factor(factor)
         job = batch.CVJob.from_scene(*plain, target, spp=1, seed=3 + k, keep_images=True)
         pairs.append((plain, job, target, 3 + k))
     b = batch.BatchedCV([p[1] for p in pairs], use_graph=use_graph)

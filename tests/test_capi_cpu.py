@@ -59,12 +59,15 @@ def test_invalid_arguments_rejected_on_host(rcvlib):
 
 def test_workspace_sizes(rcvlib):
     dims = (C.c_int32 * 3)(32, 32, 32)
-    n0 = rcvlib.rcv_medium_workspace_bytes(dims, 0)
-    n1 = rcvlib.rcv_medium_workspace_bytes(dims, 1)
+    n0 = rcvlib.rcv_medium_workspace_bytes(dims, 0, 0)
+    n1 = rcvlib.rcv_medium_workspace_bytes(dims, 1, 0)
+    n8 = rcvlib.rcv_medium_workspace_bytes(dims, 0, 8)  # 4^3 supergrid cells, two arrays
     cells = 33**3
     assert n0 >= cells * (64 + 32)
     assert n1 >= n0 + 32**3 * (32 + 16)
-    assert n0 % 256 == 0 and n1 % 256 == 0
+    assert n8 >= n0 + 2 * 4**3 * 4 and n8 <= n0 + 2 * 256
+    assert n0 % 256 == 0 and n1 % 256 == 0 and n8 % 256 == 0
     bad = (C.c_int32 * 3)(0, 4, 4)
-    assert rcvlib.rcv_medium_workspace_bytes(bad, 0) == 0
+    assert rcvlib.rcv_medium_workspace_bytes(bad, 0, 0) == 0
+    assert rcvlib.rcv_medium_workspace_bytes(dims, 0, -1) == 0
     assert rcvlib.rcv_loss_workspace_bytes(1000) >= 8 * 1024

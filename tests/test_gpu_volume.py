@@ -35,12 +35,12 @@ def make_scene(device, D=16, res=40, seeds=(1, 2), albedo_grid=False, max_depth=
     return scene, med, (old, new, alb_old, alb_new)
 
 
-def oracle_scene(O, scene, grids, max_depth, albedo_grid):
+def oracle_scene(O, scene, grids, max_depth, albedo_grid, majorant_factor=0):
     s = scene.sensors()[0].c_struct()
     cam = O.Camera(s.width, s.height, tuple(s.origin), tuple(s.forward), tuple(s.right), tuple(s.up))
     old, new, ao, an = grids
     return O.Scene(cam, old[..., 0], new[..., 0], albedo_old=ao, albedo_new=an, albedo_const=0.8,
-                   max_depth=max_depth, rr_depth=max_depth)
+                   max_depth=max_depth, rr_depth=max_depth, majorant_factor=majorant_factor)
 
 
 def frac_equal(a, b):
@@ -310,3 +310,35 @@ def test_cost_order_changes_schedule_not_results(cuda):
     aligned = (ws.data_ptr() + 255) & ~255
     cost = ws[aligned - ws.data_ptr() + cost_off:][: npix * 4].view(torch.int32)
     assert int(cost.sum()) > 0  # the last call recorded its path lengths
+
+
+@pytest.mark.parametrize("factor", [3, 8])
+def test_supergrid_tracers_match_oracle(cuda, oracle, factor):
+    """Majorant supergrid (plugins/twostatemedium.py:25-70): the DDA
+    free-flight sampling of the two-state, single-state and adjoint kernels
+    follows the oracle's float operations (images bit-identical on >= 99.9 %
+    of pixels, gradients 2e-5), and it samples fewer collisions."""
+    scene, med, grids = make_scene(cuda, albedo_grid=True, D=24, res=32)
+    osc = oracle_scene(oracle, scene, grids, 8, True, factor)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
+    cnt_global = integ.counters(cuda).clone()
+    integ.render_twostates(scene, 0, seed=3, spp=4)
+    cnt_global = (integ.counters(cuda) - cnt_global).cpu().numpy()
+    med.set_majorant_resolution_factor(factor)
+    c0 = integ.counters(cuda).clone()
+    H, F = integ.render_twostates(scene, 0, seed=3, spp=4)
+    cnt_sg = (integ.counters(cuda) - c0).cpu().numpy()
+    Ho, Fo = oracle.render_twostates(osc, seed=3, spp=4)
+    H, F = H.cpu().numpy(), F.cpu().numpy()
+    assert frac_equal(F, Fo) >= 0.999 and frac_equal(H, Ho) >= 0.999
+    assert cnt_sg[1] + cnt_sg[2] < cnt_global[1] + cnt_global[2]
+    img = integ.render(scene, 0, seed=9, spp=4).cpu().numpy()
+    assert frac_equal(img, oracle.render(osc, seed=9, spp=4)) >= 0.999
+    params = rcv.traverse(scene)
+    gimg = np.random.default_rng(6).normal(0, 1, (32, 32, 3)).astype(np.float32)
+    grads = integ.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=31, spp=4)
+    od, oa = oracle.backward(osc, seed=31, spp=4, grad_img=gimg)
+    gd = grads[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
+    ga = grads[scenes.ALBEDO_KEY].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(gd - od) <= 2e-5 * np.linalg.norm(od)
+    assert np.linalg.norm(ga - oa) <= 2e-5 * np.linalg.norm(oa)

@@ -54,9 +54,28 @@ def test_unknown_plugin_and_unsupported_options():
         rcv.load_dict({"type": "constant", "radiance": 2.0})
     dens = scenes.blob_density(4, 0)
     bad = scenes.medium_dict(dens, 0.8)
-    bad["majorant_resolution_factor"] = 8
+    bad["majorant_resolution_factor"] = -1
     with pytest.raises(ValueError):
         rcv.load_dict(bad, device="cpu")
+
+
+def test_majorant_resolution_factor():
+    """`majorant_resolution_factor` (experiments.py:70,187,306) is accepted on the
+    heterogeneous media; the two-state medium reports and sets the factor of
+    its states (plugins/twostatemedium.py:171-178)."""
+    dens = scenes.blob_density(16, 0)
+    m = scenes.medium_dict(dens, 0.8)
+    m["majorant_resolution_factor"] = 8
+    med = rcv.load_dict(m, device="cpu")
+    assert med.majorant_resolution_factor() == 8 and med.c_struct().majorant_factor == 8
+    scene = cpu_scene()
+    tm = scene.named_shapes()["object"].interior_medium()
+    assert tm.majorant_resolution_factor() == 0
+    tm.set_majorant_resolution_factor(4)
+    assert tm.majorant_resolution_factor() == 4 and tm.c_struct().majorant_factor == 4
+    assert tm.old.majorant_factor == tm.incoming.majorant_factor == 4
+    with pytest.raises(ValueError):
+        tm.set_majorant_resolution_factor(-2)
 
 
 def test_seed_rules():
