@@ -175,7 +175,7 @@ def initial_density(cfg, true_density, phase: str):
 class Job:
     """One optimisation job of the configuration, resident on the device."""
 
-    def __init__(self, cfg, device, seed: int, phase: str = "late", target=None):
+    def __init__(self, cfg, device, seed: int, phase: str = "late", target=None, majorant_factor: int = 0):
         import torch
 
         import recursive_control_variates_gb300 as rcv
@@ -194,6 +194,8 @@ class Job:
         self.has_albedo = not np.isscalar(alb)
         self.init_albedo = np.full_like(alb, 0.5) if self.has_albedo else alb
         self.scene = rcv.load_dict(scenes.scene_dict(self.init_density, self.init_albedo, res=cfg.res), device=device)
+        if majorant_factor:
+            self.scene.named_shapes()["object"].interior_medium().set_majorant_resolution_factor(majorant_factor)
         self.params = rcv.traverse(self.scene)
         self.integrator = rcv.load_dict({
             "type": "cv",
@@ -328,6 +330,10 @@ def run_ours(args, cfg):
     early = None
     if not args.no_early:
         early = time_phase(args, cfg, device, dist, job.target, "early", world, flush)
+    supergrid = None
+    if args.majorant_factor > 0:
+        supergrid = time_phase(args, cfg, device, dist, job.target, "late", world, flush,
+                               majorant_factor=args.majorant_factor)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -359,6 +365,7 @@ def run_ours(args, cfg):
         "clocks": clocks.summary(),
         "phase": "late (density starts at 0.8 x the true grid)",
         "early_phase": early,
+        "supergrid": supergrid,
         "batched": batched,
         "served": served,
     }
@@ -368,11 +375,13 @@ def run_ours(args, cfg):
         dist.destroy_process_group()
 
 
-def time_phase(args, cfg, device, dist, target, phase, world, flush):
-    """Device-timed steps of a second job started in another phase."""
+def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_factor=0):
+    """Device-timed steps of a second job started in another phase (or with
+    a majorant supergrid)."""
     import torch
 
-    job = Job(cfg, device, seed=replica_seed(dist_info()[0]) + 77, phase=phase, target=target)
+    job = Job(cfg, device, seed=replica_seed(dist_info()[0]) + 77, phase=phase, target=target,
+              majorant_factor=majorant_factor)
     for _ in range(args.warmup):
         job.step()
     stream = torch.cuda.current_stream(device)
@@ -390,6 +399,7 @@ def time_phase(args, cfg, device, dist, target, phase, world, flush):
     paths = job.paths_per_step()
     return {"value": paths * world * args.steps / total, "unit": UNIT, "ms_per_step": total * 1e3 / args.steps,
             "start": f"density {'constant ' + str(cfg.init) if phase == 'early' else '0.8 x true grid'}",
+            "majorant": f"supergrid, factor {majorant_factor}" if majorant_factor else "global",
             "lookups_per_path": float((d[1] + d[2]) / max(d[0], 1.0))}
 
 
@@ -698,6 +708,8 @@ def main(argv=None):
                     help="all: the headline line (plain cfg2) with the batched and served forms; batched / served: "
                          "only that form, printed as its own JSON object (profiling runs)")
     ap.add_argument("--batched-jobs", type=int, default=32)
+    ap.add_argument("--majorant-factor", type=int, default=8,
+                    help="also time the headline step with a majorant supergrid of this factor (0 = skip)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--plain-rounds", type=int, default=2)

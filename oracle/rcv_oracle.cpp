@@ -283,45 +283,44 @@ struct Supergrid {
 
   bool active() const { return s[0] > 0; }
 
-  float at(const std::vector<float>& g, const V3& x) const {
-    auto cell = [](float p, int n) { return std::min(std::max((int)std::floor(p * (float)n), 0), n - 1); };
-    const int i = cell(x.x, s[0]), j = cell(x.y, s[1]), k = cell(x.z, s[2]);
-    return g[((size_t)k * s[1] + j) * s[0] + i];
-  }
-
   // Distance at which the optical depth along o + t d reaches tau, walking the
-  // cells with a DDA and taking each segment's majorant at its midpoint;
-  // infinity when t would exceed tmax.  mu_at: majorant at the sampled point.
+  // cells along the ray and accumulating majorant x length; infinity when t
+  // would exceed tmax.  mu_at: the majorant of the cell the collision lies in.
   float flight(const std::vector<float>& g, const V3& o, const V3& d, float tmax, float tau, float& mu_at) const {
     const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
     float tn[3], td[3];
+    int c[3], st[3];
     for (int a = 0; a < 3; ++a) {
       const float n = (float)s[a];
-      const int c = std::min(std::max((int)std::floor(oo[a] * n), 0), s[a] - 1);
-      if (dd[a] > 0.0f) {
-        tn[a] = ((float)(c + 1) / n - oo[a]) / dd[a];
+      c[a] = std::min(std::max((int)std::floor(oo[a] * n), 0), s[a] - 1);
+      st[a] = dd[a] > 0.0f ? 1 : (dd[a] < 0.0f ? -1 : 0);
+      if (st[a] > 0) {
+        tn[a] = ((float)(c[a] + 1) / n - oo[a]) / dd[a];
         td[a] = (1.0f / n) / dd[a];
-      } else if (dd[a] < 0.0f) {
-        tn[a] = ((float)c / n - oo[a]) / dd[a];
+      } else if (st[a] < 0) {
+        tn[a] = ((float)c[a] / n - oo[a]) / dd[a];
         td[a] = -(1.0f / n) / dd[a];
       } else {
         tn[a] = kInf;
         td[a] = kInf;
       }
     }
+    auto clampc = [&](int v, int a) { return std::min(std::max(v, 0), s[a] - 1); };
     float t = 0.0f, acc = 0.0f;
     for (int step = 0; step < s[0] + s[1] + s[2] + 4; ++step) {
       const float t_next = std::fmin(std::fmin(tn[0], tn[1]), tn[2]);
       const int k = tn[0] == t_next ? 0 : (tn[1] == t_next ? 1 : 2);
-      const float m = at(g, ray_at(o, 0.5f * (t + t_next), d));
+      const float m = g[((size_t)clampc(c[2], 2) * s[1] + clampc(c[1], 1)) * s[0] + clampc(c[0], 0)];
       const float acc_next = acc + m * (t_next - t);
-      const float t_hit = t + (tau - acc) / m;
-      if (m > 0.0f && t_hit < tmax && acc_next >= tau) {
-        mu_at = at(g, ray_at(o, t_hit, d));
+      if (m > 0.0f && acc_next >= tau) {
+        const float t_hit = t + (tau - acc) / m;
+        if (!(t_hit < tmax)) return kInf;
+        mu_at = m;
         return t_hit;
       }
       if (!(t_next < tmax)) break;
       tn[k] += td[k];
+      c[k] += st[k];
       t = t_next;
       acc = acc_next;
     }

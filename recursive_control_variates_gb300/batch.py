@@ -471,11 +471,12 @@ def cfg4_mix(n_jobs: int = 32, seed: int = 4, max_depth: int = 32):
 
 
 def make_mix_jobs(mix, device="cuda", target_spp: int = 64, phase: str = "late", lr: float = 0.02,
-                  keep_images: bool = False, seed_offset: int = 1000):
+                  keep_images: bool = False, seed_offset: int = 1000, supergrid: bool = False):
     """CVJob per entry of a size mix: Gaussian-blob medium of job seed
     seed_offset + j (constant albedo 0.8), target = the true grid rendered at
     target_spp, initial grid 0.8 x the true grid ('late') or constant 1.0
-    ('early'), rr_depth = max_depth."""
+    ('early'), rr_depth = max_depth.  supergrid: each job's medium gets the
+    majorant supergrid factor of scenes.majorant_factor_for."""
     from . import load_dict, scenes
 
     jobs = []
@@ -485,9 +486,10 @@ def make_mix_jobs(mix, device="cuda", target_spp: int = 64, phase: str = "late",
         base = load_dict({"type": "prbvolpath", "max_depth": m["max_depth"], "rr_depth": m["max_depth"]})
         target = base.render(scene, 0, seed=17843 + k, spp=target_spp)
         init = (0.8 * dens) if phase == "late" else np.full_like(dens, 1.0)
+        factor = scenes.majorant_factor_for(dens.shape[:3]) if supergrid else 0
         jobs.append(CVJob(init, 0.8, target, scene.sensors()[0], spp=m["spp"], max_depth=m["max_depth"],
                           rr_depth=m["max_depth"], seed=seed_offset * 7 + k * 1000, lr=lr, density_bounds=(0.0, 250.0),
-                          keep_images=keep_images, device=device))
+                          keep_images=keep_images, majorant_factor=factor, device=device))
         del scene
     return jobs
 

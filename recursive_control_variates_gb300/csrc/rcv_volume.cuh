@@ -151,53 +151,55 @@ __device__ __forceinline__ float density_new(const VolJob& J, const Lookup& l) {
 __device__ __forceinline__ int clampi(int v, int hi) { return v < 0 ? 0 : (v > hi ? hi : v); }
 
 // ------------------------------------------------------- majorant supergrid
-// Supergrid cell of a point (nearest lookup), clamped to the grid.
-__device__ __forceinline__ float supergrid_at(const VolJob& J, const float* __restrict__ maj, const V3& x) {
-  const int i = clampi((int)floorf(x.x * (float)J.sg[0]), J.sg[0] - 1);
-  const int j = clampi((int)floorf(x.y * (float)J.sg[1]), J.sg[1] - 1);
-  const int k = clampi((int)floorf(x.z * (float)J.sg[2]), J.sg[2] - 1);
-  return __ldg(maj + ((int64_t)k * J.sg[1] + j) * J.sg[0] + i);
-}
-
 // Free-flight distance of optical depth `tau` along o + t d, t in [0, tmax],
 // through the majorant supergrid (plugins/twostatemedium.py:25-70): a DDA
-// walk (Amanatides & Woo) accumulates majorant x segment length per cell,
-// the majorant of a segment being the cell at its midpoint, and stops inside
-// the cell where tau is reached.  Returns kInf when the walk leaves the
-// segment; otherwise mu_at = the majorant at the sampled point.
+// walk (Amanatides & Woo) accumulates majorant x segment length per cell and
+// stops inside the cell where tau is reached.  The segment's majorant is the
+// DDA's current cell (the reference looks the grid up at the segment's
+// midpoint: the same cell up to floating-point ties on cell faces), and the
+// sampled collision takes that cell's majorant, so sigma_n >= 0.  Returns
+// kInf when the walk leaves the segment.
 __device__ __forceinline__ float supergrid_flight(const VolJob& J, const float* __restrict__ maj, const V3& o,
                                                   const V3& d, float tmax, float tau, float& mu_at) {
   const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
   float tn[3], td[3];
+  int c[3], step[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float S = (float)J.sg[a];
-    const int c = clampi((int)floorf(oo[a] * S), J.sg[a] - 1);
+    c[a] = clampi((int)floorf(oo[a] * S), J.sg[a] - 1);
     if (dd[a] > 0.0f) {
-      tn[a] = ((float)(c + 1) / S - oo[a]) / dd[a];
+      tn[a] = ((float)(c[a] + 1) / S - oo[a]) / dd[a];
       td[a] = (1.0f / S) / dd[a];
+      step[a] = 1;
     } else if (dd[a] < 0.0f) {
-      tn[a] = ((float)c / S - oo[a]) / dd[a];
+      tn[a] = ((float)c[a] / S - oo[a]) / dd[a];
       td[a] = -(1.0f / S) / dd[a];
+      step[a] = -1;
     } else {
       tn[a] = kInf;
       td[a] = kInf;
+      step[a] = 0;
     }
   }
+  const int sx = J.sg[0], sxy = J.sg[0] * J.sg[1];
   float t = 0.0f, tau_acc = 0.0f;
   const int max_steps = J.sg[0] + J.sg[1] + J.sg[2] + 4;
   for (int s = 0; s < max_steps; ++s) {
     const float t_next = fminf(fminf(tn[0], tn[1]), tn[2]);
     const int k = tn[0] == t_next ? 0 : (tn[1] == t_next ? 1 : 2);
-    const float m = supergrid_at(J, maj, advance(o, 0.5f * (t + t_next), d));
+    const float m = __ldg(maj + clampi(c[2], J.sg[2] - 1) * sxy + clampi(c[1], J.sg[1] - 1) * sx +
+                          clampi(c[0], J.sg[0] - 1));
     const float tau_next = tau_acc + m * (t_next - t);
-    const float t_precise = t + (tau - tau_acc) / m;
-    if (m > 0.0f && t_precise < tmax && tau_next >= tau) {
-      mu_at = supergrid_at(J, maj, advance(o, t_precise, d));
-      return t_precise;
+    if (m > 0.0f && tau_next >= tau) {
+      const float t_hit = t + (tau - tau_acc) / m;
+      if (!(t_hit < tmax)) return kInf;
+      mu_at = m;
+      return t_hit;
     }
     if (!(t_next < tmax)) break;
     tn[k] += td[k];
+    c[k] += step[k];
     t = t_next;
     tau_acc = tau_next;
   }

@@ -126,6 +126,17 @@ def config_grids(cfg: VolumeConfig, seed: int | None = None):
     return dens, alb
 
 
+def majorant_factor_for(density_res) -> int:
+    """Supergrid factor of utils.adjust_majorant_res_factor (utils.py:27-43):
+    8, reduced until the smallest side has at least 4 supergrid cells; 0 (no
+    supergrid) when even factor 2 does not."""
+    f = 8
+    min_side = int(min(density_res[:3]))
+    while f > 1 and min_side // f < 4:
+        f -= 1
+    return f if f > 1 else 0
+
+
 DENSITY_KEY = "object.interior_medium.sigma_t.data"
 ALBEDO_KEY = "object.interior_medium.albedo.data"
 
