@@ -188,6 +188,36 @@ int rcv_render_backward_volume(const rcv_medium* medium, const rcv_sensor* senso
                                const float* grad_img, float* grad_density, float* grad_albedo,
                                void* workspace, uint64_t* counters, void* stream);
 
+/* ------------------------------------------------ volpathsimple integrator */
+/* Switches of VolpathSimpleIntegrator (plugins/volpathsimple.py:20-51):
+ * use_nee, use_drt, use_drt_subsampling, use_drt_mis (each 0 or 1; the
+ * reference's defaults are all 1).  NULL selects the defaults. */
+typedef struct rcv_volpathsimple_flags {
+  int32_t use_nee, use_drt, use_drt_subsampling, use_drt_mis;
+} rcv_volpathsimple_flags;
+
+/* Scratch of rcv_render_volpathsimple: 16 bytes per path. */
+uint64_t rcv_volpathsimple_workspace_bytes(int32_t width, int32_t height, int32_t spp);
+
+/* Primal of the simplified volumetric path tracer on the current (new)
+ * parameters: delta tracking to real interactions, NEE towards the
+ * environment, MIS at the environment.  Replaces
+ * VolpathSimpleIntegrator.sample (plugins/volpathsimple.py:53-327). */
+int rcv_render_volpathsimple(const rcv_medium* medium, const rcv_sensor* sensor,
+                             const rcv_volpath_options* opts, const rcv_volpathsimple_flags* flags,
+                             uint32_t seed, int32_t spp, float* img, void* workspace, void* stream);
+
+/* Adjoint of the simplified tracer: path replay with the scattering,
+ * transmittance and NEE terms and differential ratio tracking.  Gradients
+ * as rcv_render_backward_volume.  Replaces the render_backward of the
+ * `adjoint_integrator` built from {"type": "volpathsimple"}
+ * (plugins/volpathsimple.py:53-327, 508-778; experiments.py:131,245,364). */
+int rcv_render_backward_volpathsimple(const rcv_medium* medium, const rcv_sensor* sensor,
+                                      const rcv_volpath_options* opts,
+                                      const rcv_volpathsimple_flags* flags, uint32_t seed,
+                                      int32_t spp, const float* grad_img, float* grad_density,
+                                      float* grad_albedo, void* stream);
+
 /* ------------------------------------------------------- surface scenes */
 #define RCV_MAX_SPHERES 8
 

@@ -153,6 +153,15 @@ def lib():
         L.oracle_log_unit.restype = None
         L.oracle_uniform_sphere.argtypes = [vp, C.c_int, vp]
         L.oracle_uniform_sphere.restype = None
+        L.oracle_vps_alt_seed.argtypes = [C.c_uint32]
+        L.oracle_vps_alt_seed.restype = C.c_uint32
+        L.oracle_exp_nonpos.argtypes = [C.c_float]
+        L.oracle_exp_nonpos.restype = C.c_float
+        L.oracle_vps_render.argtypes = [C.POINTER(OracleScene), vp, C.c_uint32, C.c_int, vp, C.c_int, C.c_int, C.c_int,
+                                        C.c_int]
+        L.oracle_vps_render.restype = C.c_int
+        L.oracle_vps_backward.argtypes = [C.POINTER(OracleScene), vp, C.c_uint32, C.c_int, vp, vp, vp, C.c_int]
+        L.oracle_vps_backward.restype = C.c_int
         _lib = L
     return _lib
 
@@ -408,3 +417,47 @@ def adam_step(p, g, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8, lo=-np.inf, hi=np.i
     p = (p - (lr_t * m) / (np.sqrt(v) + f32(eps))).astype(f32)
     p = np.clip(p, f32(lo), f32(hi)).astype(f32)
     return p, m, v
+
+
+# ------------------------------------------------------------ volpathsimple
+VPS_DEFAULT = dict(use_nee=True, use_drt=True, use_drt_subsampling=True, use_drt_mis=True)
+
+
+def _vps_flags(flags):
+    f = dict(VPS_DEFAULT)
+    f.update(flags or {})
+    return np.array([int(bool(f[k])) for k in ("use_nee", "use_drt", "use_drt_subsampling", "use_drt_mis")],
+                    np.int32)
+
+
+def vps_render(scene: Scene, seed: int, spp: int, flags=None, threads: int | None = None, rows: tuple = (0, 0, 1)):
+    """volpathsimple primal image (plugins/volpathsimple.py)."""
+    fl = _vps_flags(flags)
+    img = np.zeros((scene.height, scene.width, 3), np.float32)
+    rc = lib().oracle_vps_render(C.byref(scene.c), fl.ctypes.data, seed & 0xFFFFFFFF, spp, img.ctypes.data,
+                                 threads or default_threads(), *_rows(rows))
+    if rc:
+        raise ValueError("oracle_vps_render: invalid arguments")
+    return img
+
+
+def vps_backward(scene: Scene, seed: int, spp: int, grad_img, flags=None, threads: int | None = None):
+    """volpathsimple adjoint: (grad_density float64, grad_albedo or None)."""
+    fl = _vps_flags(flags)
+    g = np.ascontiguousarray(grad_img, np.float32)
+    gd = np.zeros(scene.dens_new.shape[:3], np.float64)
+    ga = None if scene.alb_new is None else np.zeros(scene.dens_new.shape[:3] + (3,), np.float64)
+    rc = lib().oracle_vps_backward(C.byref(scene.c), fl.ctypes.data, seed & 0xFFFFFFFF, spp, g.ctypes.data,
+                                   gd.ctypes.data, None if ga is None else ga.ctypes.data,
+                                   threads or default_threads())
+    if rc:
+        raise ValueError("oracle_vps_backward: invalid arguments")
+    return gd, ga
+
+
+def vps_alt_seed(seed: int) -> int:
+    return int(lib().oracle_vps_alt_seed(seed & 0xFFFFFFFF))
+
+
+def exp_nonpos(x: float) -> float:
+    return float(lib().oracle_exp_nonpos(float(x)))

@@ -771,3 +771,463 @@ void oracle_uniform_sphere(const float* u, int n, float* out) {
 }
 
 }  // extern "C"
+
+// ===================================================================
+// volpathsimple (plugins/volpathsimple.py): the reference's simplified
+// volumetric path tracer and its adjoint, used as `adjoint_integrator` in
+// every grid experiment (experiments.py:131,245,364).
+//
+// Primal (VolpathSimpleIntegrator.sample, :53-327): per loop iteration
+//   Russian roulette (1D), a *real* interaction by delta tracking
+//   (sample_real_interaction :349-395: per collision a free-flight 1D and, if
+//   inside the segment, a real/null 1D), NEE towards the environment (2D +
+//   one 1D per ratio-tracking step, :398-491), then the phase sample (1D + 2D).
+//   A path that leaves the cube sees the environment with the MIS weight of
+//   its last scattering event (:296-321).  After reaching the medium one 1D is
+//   drawn to seed the adjoint's second stream (:103-113).
+// Adjoint (render_backward of the path-replay base integrator): the primal
+//   pass gives L; a second pass replays the same draws with L_rem = L minus
+//   the NEE contributions so far and back-propagates:
+//   - at each real interaction, the scattering term with MIS weight
+//     s^2/(1+s^2), s = sigma_t (:160-186);
+//   - at each real interaction or escape, the transmittance of the last
+//     segment through 4 uniform samples (:597-620);
+//   - each NEE shadow ray by replaying its ratio tracking (:412-422, :481-505);
+//   - one differential-ratio-tracking term per path: a reservoir picks one
+//     scattering event (:743-778, weight = throughput), and after the path a
+//     distance is resampled on that event's segment in proportion to the
+//     transmittance, with a recursive path estimating the in-scattered
+//     radiance there, MIS weight 1/(1+s^2) (:508-594, :623-668).
+//   The adjoint's extra random numbers come from a second stream whose seed
+//   is sample_tea_32(bits of lane 0's seeding draw, 1) (:108-113).
+// sample_interaction_drt lives in the Mitsuba fork the reference depends on
+// (not in the reference tree); it is restated as: distance t' on [0, tmax]
+// from the majorant's exponential truncated to the segment, pdf
+// mu e^{-mu t'} / (1 - e^{-mu tmax}), weight T^(t') / pdf with T^ a ratio-
+// tracking estimate on [0, t'], so weight x f(t') estimates the integral of
+// T(t) f(t) over the segment.
+// ===================================================================
+namespace {
+
+// e^x for x <= 0: n = round(x log2 e), r = x - n ln2 (ln 2 split as in
+// log_unit), Taylor polynomial of degree 8 on |r| <= ln2/2, times 2^n.
+float exp_nonpos(float x) {
+  if (!(x > -87.0f)) return 0.0f;
+  const float n = std::rint(x * 1.44269504088896341f);
+  float r = std::fmaf(n, -0.693145751953125f, x);
+  r = std::fmaf(n, -1.4286068203094172e-06f, r);
+  float p = 1.0f / 40320.0f;
+  p = std::fmaf(r, p, 1.0f / 5040.0f);
+  p = std::fmaf(r, p, 1.0f / 720.0f);
+  p = std::fmaf(r, p, 1.0f / 120.0f);
+  p = std::fmaf(r, p, 1.0f / 24.0f);
+  p = std::fmaf(r, p, 1.0f / 6.0f);
+  p = std::fmaf(r, p, 0.5f);
+  p = std::fmaf(r, p, 1.0f);
+  p = std::fmaf(r, p, 1.0f);
+  union { float f; uint32_t u; } s;
+  s.u = (uint32_t)((int)n + 127) << 23;
+  return p * s.f;
+}
+
+struct VpsFlags {
+  int32_t use_nee, use_drt, use_drt_subsampling, use_drt_mis;
+};
+
+struct VpsSegment {
+  V3 o, d;
+  float tmax;  // distance to the cube boundary
+};
+
+struct Vps {
+  const oracle_scene& S;
+  VpsFlags F;
+  float mu;  // majorant of `new`
+  const Supergrid* sg;
+  GradSink* sink = nullptr;
+
+  float flight(Rng& r, const V3& o, const V3& d, float tmax, float& m) const {
+    const float tau = -log_unit(1.0f - r.next1d());
+    m = mu;
+    if (sg != nullptr && sg->active()) return sg->flight(sg->nw, o, d, tmax, tau, m);
+    return mu > 0.0f ? tau * (1.0f / mu) : kInf;
+  }
+
+  float sigma_t(const Corners& c) const { return S.scale * trilinear(S, S.dens_new, 1, 0, c); }
+
+  // Delta tracking to the next real interaction; returns its distance from
+  // seg.o (the sum of the free-flight distances) or kInf on escape.
+  float real_interaction(Rng& r, const VpsSegment& seg) const {
+    V3 p = seg.o;
+    float rem = seg.tmax, t_acc = 0.0f;
+    for (;;) {
+      float m;
+      const float t = flight(r, p, seg.d, rem, m);
+      if (!(t <= rem)) return kInf;
+      const V3 x = ray_at(p, t, seg.d);
+      const float st = sigma_t(corners(S, x));
+      const float ratio = m != 0.0f ? st / m : 0.0f;
+      const float u = r.next1d();
+      t_acc = t_acc + t;
+      if (u < ratio) return t_acc;
+      p = x;
+      rem = rem - t;
+    }
+  }
+
+  // Ratio-tracking transmittance from o along w to distance tmax.  With
+  // `adj`, back-propagates adj . d log(T).
+  float transmittance(Rng& r, const V3& o, const V3& w, float tmax, const V3* adj) const {
+    V3 q = o;
+    float rem = tmax, tr = 1.0f;
+    for (;;) {
+      float m;
+      const float t = flight(r, q, w, rem, m);
+      if (!(t <= rem)) break;
+      const V3 x = ray_at(q, t, w);
+      const Corners c = corners(S, x);
+      const float sn = m - sigma_t(c);
+      const float contrib = m != 0.0f ? sn / m : sn;
+      if (adj != nullptr && contrib > 0.0f) {
+        const float wn = (adj->x + adj->y) + adj->z;  // adj already carries dL
+        sink->density(S, c, -(S.scale * wn) / sn);
+      }
+      tr = tr * contrib;
+      q = x;
+      rem = rem - t;
+      if (tr == 0.0f) break;
+    }
+    return tr;
+  }
+
+  // NEE towards the environment from x with throughput thr (:398-446).
+  V3 nee(Rng& r, const V3& x, const V3& thr, const V3* dL) const {
+    Rng replay = r;
+    const float u0 = r.next1d(), u1 = r.next1d();
+    const V3 w = square_to_uniform_sphere(u0, u1);
+    float tn, tf;
+    cube_hit(x, w, tn, tf);
+    const float tr = transmittance(r, x, w, tf, nullptr);
+    const float mis = 0.5f;
+    const float en = (1.0f / kInvFourPi) * tr;
+    const V3 c{((thr.x * kInvFourPi) * mis) * en, ((thr.y * kInvFourPi) * mis) * en,
+               ((thr.z * kInvFourPi) * mis) * en};
+    if (dL != nullptr) {
+      // replay the shadow walk with the same numbers (:412-422)
+      const V3 adj{dL->x * c.x, dL->y * c.y, dL->z * c.z};
+      replay.next1d();
+      replay.next1d();
+      transmittance(replay, x, w, tf, &adj);
+    }
+    return c;
+  }
+
+  // Primal path from a segment (the loop of sample(), :126-290 and the
+  // environment term :296-321).  depth / has_scattered / last pdf as the
+  // path state of a recursive call (:73-99).
+  V3 primal_from(Rng& r, VpsSegment seg, int depth, bool has_scattered, bool active) const {
+    V3 L{0, 0, 0}, thr{1, 1, 1};
+    bool escaped = false;
+    while (active) {
+      const float q = std::fmin(std::fmax(std::fmax(thr.x, thr.y), thr.z), 0.99f);
+      const bool rr = depth > S.rr_depth;
+      const bool alive = thr.x != 0.0f || thr.y != 0.0f || thr.z != 0.0f;
+      const float u = r.next1d();
+      if (!alive || (rr && !(u < q))) break;
+      if (rr) {
+        const float iq = 1.0f / q;
+        thr = V3{thr.x * iq, thr.y * iq, thr.z * iq};
+      }
+      const float t = real_interaction(r, seg);
+      if (!(t < kInf)) {
+        escaped = true;
+        break;
+      }
+      const V3 x = ray_at(seg.o, t, seg.d);
+      const V3 a = albedo(S, S.alb_new, corners(S, x));
+      has_scattered = true;
+      thr = V3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
+      depth += 1;
+      if (depth >= S.max_depth) break;
+      if (F.use_nee) {
+        const V3 c = nee(r, x, thr, nullptr);
+        L = V3{L.x + c.x, L.y + c.y, L.z + c.z};
+      }
+      r.next1d();
+      const float pu0 = r.next1d(), pu1 = r.next1d();
+      seg.o = x;
+      seg.d = square_to_uniform_sphere(pu0, pu1);
+      float tn, tf;
+      cube_hit(seg.o, seg.d, tn, tf);
+      if (!(tf > 0.0f)) break;  // accidental escape (:279-283)
+      seg.tmax = tf;
+    }
+    if (escaped && !(depth <= 0 && S.hide_emitters)) {
+      const float k = (F.use_nee && has_scattered) ? 0.5f : 1.0f;
+      L = V3{L.x + thr.x * k, L.y + thr.y * k, L.z + thr.z * k};
+    }
+    return L;
+  }
+
+  // Camera ray of sample `lane`, then the medium entry (reach_medium,
+  // :329-346).  Returns false when the ray misses the cube.
+  bool camera(Rng& r, int px, int py, V3& o, V3& d, VpsSegment& seg) const {
+    const float u0 = r.next1d(), u1 = r.next1d();
+    const float fx = (float)px + u0, fy = (float)py + u1;
+    const float inv_w = 1.0f / (float)S.width, inv_h = 1.0f / (float)S.height;
+    const float nx = fx * inv_w, ny = fy * inv_h;
+    const float a = std::fmaf(2.0f, nx, -1.0f), b = std::fmaf(-2.0f, ny, 1.0f);
+    V3 rr;
+    rr.x = std::fmaf(b, S.cam_u[0], std::fmaf(a, S.cam_r[0], S.cam_f[0]));
+    rr.y = std::fmaf(b, S.cam_u[1], std::fmaf(a, S.cam_r[1], S.cam_f[1]));
+    rr.z = std::fmaf(b, S.cam_u[2], std::fmaf(a, S.cam_r[2], S.cam_f[2]));
+    const float inv_len = 1.0f / std::sqrt(std::fmaf(rr.z, rr.z, std::fmaf(rr.y, rr.y, rr.x * rr.x)));
+    d = V3{rr.x * inv_len, rr.y * inv_len, rr.z * inv_len};
+    o = V3{S.cam_o[0], S.cam_o[1], S.cam_o[2]};
+    r.next1d();  // colour channel
+    float tn, tf;
+    cube_hit(o, d, tn, tf);
+    if (!(tn <= tf && tf > 0.0f)) return false;
+    seg.o = ray_at(o, std::fmax(tn, 0.0f), d);
+    seg.d = d;
+    cube_hit(seg.o, d, tn, tf);
+    seg.tmax = tf;
+    return true;
+  }
+
+  V3 render_path(uint32_t seed, uint32_t lane, int px, int py) const {
+    Rng r = lane_rng(seed, lane);
+    V3 o, d;
+    VpsSegment seg;
+    if (!camera(r, px, py, o, d, seg)) {
+      const float k = S.hide_emitters ? 0.0f : 1.0f;
+      return V3{k, k, k};
+    }
+    r.next1d();  // seeds the adjoint's second stream
+    return primal_from(r, seg, 0, false, true);
+  }
+
+  // Differential ratio tracking on `seg` (restated sample_interaction_drt,
+  // :540-594) with adjoint `adj` (dL x sampling weight).
+  void drt(Rng& alt, const VpsSegment& seg, int depth, const V3& adj) const {
+    if (!(mu > 0.0f)) return;
+    const float e = exp_nonpos(-(mu * seg.tmax));
+    const float u = alt.next1d();
+    const float tp = -log_unit(1.0f - u * (1.0f - e)) / mu;
+    const float pdf = (mu * exp_nonpos(-(mu * tp))) / (1.0f - e);
+    const float tr = transmittance(alt, seg.o, seg.d, tp, nullptr);
+    const float wdrt = tr / pdf;
+    const V3 x = ray_at(seg.o, tp, seg.d);
+    const Corners c = corners(S, x);
+    const float st = sigma_t(c);
+    const V3 a = albedo(S, S.alb_new, c);
+    // in-scattered radiance at x: NEE + a recursive path (sample_recursive, :623-668)
+    V3 Li{0, 0, 0};
+    if (F.use_nee) Li = nee(alt, x, V3{1, 1, 1}, nullptr);
+    alt.next1d();
+    const float pu0 = alt.next1d(), pu1 = alt.next1d();
+    VpsSegment next{x, square_to_uniform_sphere(pu0, pu1), 0.0f};
+    float tn, tf;
+    cube_hit(next.o, next.d, tn, tf);
+    const bool ok = tf > 0.0f;
+    next.tmax = tf;
+    const int next_depth = depth + 1;
+    const bool active = ok && next_depth < S.max_depth;
+    if (active) alt.next1d();  // the recursive call's seeding draw (:103)
+    const V3 Lr = primal_from(alt, next, next_depth, true, active);
+    Li = V3{Li.x + Lr.x, Li.y + Lr.y, Li.z + Lr.z};
+    const float mis = F.use_drt_mis ? 1.0f / (1.0f + st * st) : 1.0f;
+    const float k0 = mis * wdrt;
+    const V3 k{(k0 * adj.x) * Li.x, (k0 * adj.y) * Li.y, (k0 * adj.z) * Li.z};
+    sink->density(S, c, S.scale * ((k.x * a.x + k.y * a.y) + k.z * a.z));
+    sink->albedo(S, c, V3{k.x * st, k.y * st, k.z * st});
+  }
+
+  // Adjoint pass of one sample: replays the primal's draws with L_rem.
+  void backward_path(uint32_t seed, uint32_t alt_seed, uint32_t lane, int px, int py, const V3& dL) const {
+    const V3 Ltot = render_path(seed, lane, px, py);
+    Rng r = lane_rng(seed, lane);
+    Rng alt = lane_rng(alt_seed, lane);
+    V3 o, d;
+    VpsSegment seg;
+    if (!camera(r, px, py, o, d, seg)) return;
+    r.next1d();
+    V3 res = Ltot, thr{1, 1, 1};
+    int depth = 0;
+    // reservoir of one scattering event for DRT (:743-778)
+    V3 wsum{0, 0, 0}, cur{0, 0, 0};
+    bool have = false;
+    VpsSegment keep{};
+    int keep_depth = 0;
+    for (;;) {
+      const float q = std::fmin(std::fmax(std::fmax(thr.x, thr.y), thr.z), 0.99f);
+      const bool rr = depth > S.rr_depth;
+      const bool alive = thr.x != 0.0f || thr.y != 0.0f || thr.z != 0.0f;
+      const float u = r.next1d();
+      if (!alive || (rr && !(u < q))) break;
+      if (rr) {
+        const float iq = 1.0f / q;
+        thr = V3{thr.x * iq, thr.y * iq, thr.z * iq};
+      }
+      const float t = real_interaction(r, seg);
+      const bool escape = !(t < kInf);
+      // DRT estimates the in-scattering integral over the whole segment, so
+      // it runs for every segment the path traverses, escaping or not (the
+      // loop's `active` mask, :158-163)
+      if (F.use_drt) {
+        if (F.use_drt_subsampling) {
+          wsum = V3{wsum.x + thr.x, wsum.y + thr.y, wsum.z + thr.z};
+          const float pick = alt.next1d();
+          const float ratio = ((thr.x / wsum.x + thr.y / wsum.y) + thr.z / wsum.z) / 3.0f;
+          if (pick <= ratio) {
+            cur = thr;
+            keep = seg;
+            keep_depth = depth;
+            have = true;
+          }
+        } else {
+          drt(alt, seg, depth, V3{dL.x * thr.x, dL.y * thr.y, dL.z * thr.z});
+        }
+      }
+      if (!escape) {
+        const V3 x = ray_at(seg.o, t, seg.d);
+        const Corners c = corners(S, x);
+        const float st = sigma_t(c);
+        const V3 a = albedo(S, S.alb_new, c);
+        if (!F.use_drt || F.use_drt_mis) {
+          const float mis = F.use_drt ? (st * st) / (1.0f + st * st) : 1.0f;
+          const float inv_pdf = 1.0f / st;
+          const V3 k{((mis * dL.x) * (res.x / std::fmax(1e-8f, a.x))) * inv_pdf,
+                     ((mis * dL.y) * (res.y / std::fmax(1e-8f, a.y))) * inv_pdf,
+                     ((mis * dL.z) * (res.z / std::fmax(1e-8f, a.z))) * inv_pdf};
+          sink->density(S, c, S.scale * ((k.x * a.x + k.y * a.y) + k.z * a.z));
+          sink->albedo(S, c, V3{k.x * st, k.y * st, k.z * st});
+        }
+      }
+      {
+        // transmittance of the last segment: 4 uniform samples (:597-620)
+        const float interval = escape ? seg.tmax : t;
+        const float w = (dL.x * res.x + dL.y * res.y) + dL.z * res.z;
+        const float coef = -(w * (interval * 0.25f));
+        for (int j = 0; j < 4; ++j) {
+          const float tj = alt.next1d() * interval;
+          sink->density(S, corners(S, ray_at(seg.o, tj, seg.d)), S.scale * coef);
+        }
+      }
+      if (escape) break;
+      const V3 x = ray_at(seg.o, t, seg.d);
+      const V3 a = albedo(S, S.alb_new, corners(S, x));
+      thr = V3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
+      depth += 1;
+      if (depth >= S.max_depth) break;
+      if (F.use_nee) {
+        const V3 c = nee(r, x, thr, &dL);
+        res = V3{res.x - c.x, res.y - c.y, res.z - c.z};
+      }
+      r.next1d();
+      const float pu0 = r.next1d(), pu1 = r.next1d();
+      seg.o = x;
+      seg.d = square_to_uniform_sphere(pu0, pu1);
+      float tn, tf;
+      cube_hit(seg.o, seg.d, tn, tf);
+      if (!(tf > 0.0f)) break;
+      seg.tmax = tf;
+    }
+    if (F.use_drt && F.use_drt_subsampling && have) {
+      const float dmean = ((cur.x + cur.y) + cur.z) / 3.0f;
+      if (dmean != 0.0f) {
+        const float wmean = ((wsum.x + wsum.y) + wsum.z) / 3.0f;
+        const V3 sw{(wmean * cur.x) / dmean, (wmean * cur.y) / dmean, (wmean * cur.z) / dmean};
+        drt(alt, keep, keep_depth, V3{sw.x * dL.x, sw.y * dL.y, sw.z * dL.z});
+      }
+    }
+  }
+};
+
+// Seed of the adjoint's second stream: sample_tea_32(bits of the seeding
+// draw of lane 0, 1)[0] (:108-113); lane 0's fourth draw (film 2D, channel).
+uint32_t vps_alt_seed(uint32_t seed) {
+  Rng r = lane_rng(seed, 0);
+  r.next1d();
+  r.next1d();
+  r.next1d();
+  const float u = r.next1d();
+  uint32_t bits;
+  std::memcpy(&bits, &u, 4);
+  uint32_t a, b;
+  tea(bits, 1u, 4, a, b);
+  return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t oracle_vps_alt_seed(uint32_t seed) { return vps_alt_seed(seed); }
+
+float oracle_exp_nonpos(float x) { return exp_nonpos(x); }
+
+// volpathsimple primal image [height][width][3] (box film, sample order).
+int oracle_vps_render(const oracle_scene* S, const int32_t flags[4], uint32_t seed, int spp, float* out, int threads,
+                      int row0, int row1, int row_stride) {
+  if (S && row1 <= 0) row1 = S->height;
+  if (!S || !flags || !out || spp <= 0 || row0 < 0 || row1 > S->height || row0 > row1) return -1;
+  Supergrid sg;
+  sg.build(*S);
+  const Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, S->scale * grid_max(*S, S->dens_new), &sg};
+  parallel_rows(row0, row1, row_stride, threads, [&](int, int y0, int y1) {
+    for (int py = y0; py < y1; ++py)
+      for (int px = 0; px < S->width; ++px) {
+        const int pix = py * S->width + px;
+        V3 acc{0, 0, 0};
+        for (int s = 0; s < spp; ++s) {
+          const V3 L = vps.render_path(seed, (uint32_t)((int64_t)pix * spp + s), px, py);
+          acc = V3{acc.x + L.x, acc.y + L.y, acc.z + L.z};
+        }
+        const float fs = (float)spp;
+        out[pix * 3 + 0] = acc.x / fs;
+        out[pix * 3 + 1] = acc.y / fs;
+        out[pix * 3 + 2] = acc.z / fs;
+      }
+  });
+  return 0;
+}
+
+// volpathsimple adjoint: gradients (double) ADDED to grad_density and, when
+// the scene has an albedo grid and grad_albedo is set, to grad_albedo.
+int oracle_vps_backward(const oracle_scene* S, const int32_t flags[4], uint32_t seed, int spp, const float* grad_img,
+                        double* grad_density, double* grad_albedo, int threads) {
+  if (!S || !flags || spp <= 0 || !grad_img || !grad_density) return -1;
+  Supergrid sg;
+  sg.build(*S);
+  const float mu = S->scale * grid_max(*S, S->dens_new);
+  const uint32_t alt_seed = vps_alt_seed(seed);
+  const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
+  const int nt = std::max(threads, 1);
+  std::vector<GradSink> sinks(nt);
+  const bool alb = grad_albedo != nullptr && S->alb_new != nullptr;
+  for (auto& s : sinks) {
+    s.dens.assign(nv, 0.0);
+    if (alb) s.alb.assign(nv * 3, 0.0);
+  }
+  parallel_rows(0, S->height, 1, threads, [&](int k, int y0, int y1) {
+    Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, mu, &sg};
+    vps.sink = &sinks[k];
+    for (int py = y0; py < y1; ++py)
+      for (int px = 0; px < S->width; ++px) {
+        const int pix = py * S->width + px;
+        const float fs = (float)spp;
+        const V3 dL{grad_img[pix * 3 + 0] / fs, grad_img[pix * 3 + 1] / fs, grad_img[pix * 3 + 2] / fs};
+        for (int s = 0; s < spp; ++s)
+          vps.backward_path(seed, alt_seed, (uint32_t)((int64_t)pix * spp + s), px, py, dL);
+      }
+  });
+  for (auto& s : sinks) {
+    for (int64_t i = 0; i < nv; ++i) grad_density[i] += s.dens[i];
+    if (alb)
+      for (int64_t i = 0; i < nv * 3; ++i) grad_albedo[i] += s.alb[i];
+  }
+  return 0;
+}
+
+}  // extern "C"

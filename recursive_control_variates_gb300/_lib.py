@@ -68,6 +68,15 @@ class VolpathOptions(C.Structure):
     ]
 
 
+class VpsFlags(C.Structure):
+    _fields_ = [
+        ("use_nee", C.c_int32),
+        ("use_drt", C.c_int32),
+        ("use_drt_subsampling", C.c_int32),
+        ("use_drt_mis", C.c_int32),
+    ]
+
+
 ORDER_COST = 0
 ORDER_ROW_MAJOR = 1
 ORDER_LONGEST_FIRST = 2
@@ -189,6 +198,14 @@ SIGNATURES = {
     "rcv_render_backward_volume": (
         C.c_int,
         [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
+    ),
+    "rcv_volpathsimple_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32]),
+    "rcv_render_volpathsimple": (
+        C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), P(VpsFlags), C.c_uint32, C.c_int32, vp, vp, vp]
+    ),
+    "rcv_render_backward_volpathsimple": (
+        C.c_int,
+        [P(Medium), P(Sensor), P(VolpathOptions), P(VpsFlags), C.c_uint32, C.c_int32, vp, vp, vp, vp],
     ),
     "rcv_surface_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32]),
     "rcv_surface_prepare": (C.c_int, [P(SurfaceScene), vp]),

@@ -132,6 +132,28 @@ RCV_HD float log_unit(float x) {
   return fmaf(fe, 0.693145751953125f, fmaf(fe, 1.4286068203094172e-06f, lm));
 }
 
+// e^x for x <= 0: n = round(x log2 e), r = x - n ln2 (ln 2 split as in
+// log_unit, so n * the first part is exact), Taylor polynomial of degree 8 on
+// |r| <= ln2/2 (truncation < 2^-28 relative), times 2^n.  0 below -87.
+RCV_HD float exp_nonpos(float x) {
+  if (!(x > -87.0f)) return 0.0f;
+  const float n = rintf(x * 1.44269504088896341f);
+  float r = fmaf(n, -0.693145751953125f, x);
+  r = fmaf(n, -1.4286068203094172e-06f, r);
+  float p = 1.0f / 40320.0f;
+  p = fmaf(r, p, 1.0f / 5040.0f);
+  p = fmaf(r, p, 1.0f / 720.0f);
+  p = fmaf(r, p, 1.0f / 120.0f);
+  p = fmaf(r, p, 1.0f / 24.0f);
+  p = fmaf(r, p, 1.0f / 6.0f);
+  p = fmaf(r, p, 0.5f);
+  p = fmaf(r, p, 1.0f);
+  p = fmaf(r, p, 1.0f);
+  union { float f; uint32_t u; } s;
+  s.u = (uint32_t)((int)n + 127) << 23;
+  return p * s.f;
+}
+
 // sin and cos of 2*pi*u for u in [0, 1).  Exact quadrant reduction on u, then
 // Taylor series of sin / cos on [0, pi/4].
 RCV_HD void sincos_2pi(float u, float& s, float& c) {

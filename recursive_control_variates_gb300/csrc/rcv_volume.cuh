@@ -297,6 +297,11 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
 // null, by the chord length of the pixel's centre ray through the medium
 // (buckets: 256 uint32 of scratch).
 int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, uint32_t* cost, cudaStream_t st);
+// Clears the medium workspace's cell (and albedo) gradient accumulators.
+int reset_gradients(const rcv_medium* m, bool albedo, cudaStream_t st);
+// Adds the folded voxel gradients of the medium workspace to grad_density
+// (and grad_albedo when set and the medium has an albedo grid).
+int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cudaStream_t st);
 // Bucket (0 = first handed out) of a pixel by the chord of its centre ray
 // through the medium cube (misses last).
 __device__ __forceinline__ int chord_key(const VolJob& J, int pix) {

@@ -6,6 +6,7 @@ from ..core import register_integrator
 from .cv_integrator import CVIntegrator, MetaIntegrator
 from .twostatepath import TwoStatePRBIntegrator
 from .twostatevolpath import PRBVolpathIntegrator, TwoStatePRBVolpathIntegrator
+from .volpathsimple import VolpathSimpleIntegrator
 from .welford import StatisticsEstimator, WelfordVarianceEstimator
 
 register_integrator("twostateprb", TwoStatePRBIntegrator)
@@ -13,6 +14,7 @@ register_integrator("meta", MetaIntegrator)
 register_integrator("cv", CVIntegrator)
 register_integrator("twostateprbvolpath", TwoStatePRBVolpathIntegrator)
 register_integrator("prbvolpath", PRBVolpathIntegrator)
+register_integrator("volpathsimple", VolpathSimpleIntegrator)
 
 __all__ = [
     "CVIntegrator",
@@ -20,6 +22,7 @@ __all__ = [
     "TwoStatePRBIntegrator",
     "TwoStatePRBVolpathIntegrator",
     "PRBVolpathIntegrator",
+    "VolpathSimpleIntegrator",
     "StatisticsEstimator",
     "WelfordVarianceEstimator",
 ]

@@ -17,9 +17,25 @@ def cpu_scene(two_state=True, albedo=0.8, D=4):
 def test_plugin_names_registered():
     from recursive_control_variates_gb300.core import _KINDS
 
-    for name in ("cv", "meta", "twostateprbvolpath", "twostateprb", "prbvolpath"):
+    for name in ("cv", "meta", "twostateprbvolpath", "twostateprb", "prbvolpath", "volpathsimple"):
         assert _KINDS[name] == "integrator"
     assert _KINDS["twostatemedium"] == "medium"
+
+
+def test_volpathsimple_options():
+    """Switches of plugins/volpathsimple.py:33-48 (all on by default) and its
+    use as the `adjoint_integrator` of `cv` (experiments.py:131,245,364)."""
+    v = rcv.load_dict({"type": "volpathsimple"})
+    f = v.flags()
+    assert (f.use_nee, f.use_drt, f.use_drt_subsampling, f.use_drt_mis) == (1, 1, 1, 1)
+    v = rcv.load_dict({"type": "volpathsimple", "use_drt_mis": False, "use_nee": False, "max_depth": 12})
+    f = v.flags()
+    assert (f.use_nee, f.use_drt, f.use_drt_subsampling, f.use_drt_mis) == (0, 1, 1, 0)
+    assert v.max_depth == 12 and "use_drt_mis = False" in v.to_string()
+    integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath"},
+                           "adjoint_integrator": {"type": "volpathsimple"}})
+    assert type(integ.adjoint_integrator).__name__ == "VolpathSimpleIntegrator"
+    assert v._checked_medium(cpu_scene(two_state=False)) is not None  # a plain medium is accepted
 
 
 def test_cv_requires_two_state_integrator():

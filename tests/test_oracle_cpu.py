@@ -231,3 +231,95 @@ def test_supergrid_single_state_and_adjoint_unbiased(oracle):
     # not vacuous: denser media darken the image in most seeds (the estimates
     # are heavy-tailed through 1/sigma_n, so the sign, not the spread, is used)
     assert np.mean(ta < 0) >= 0.75 and np.mean(tb < 0) >= 0.75
+
+
+# ------------------------------------------------------------ volpathsimple
+def test_exp_nonpos_accuracy(oracle):
+    xs = np.float32(-np.linspace(0.0, 86.9, 4001))
+    got = np.array([oracle.exp_nonpos(float(x)) for x in xs], np.float64)
+    ref = np.exp(xs.astype(np.float64))
+    assert np.max(np.abs(got - ref) / ref) < 2.0 ** -23
+    assert oracle.exp_nonpos(0.0) == 1.0 and oracle.exp_nonpos(-100.0) == 0.0
+
+
+def test_vps_alt_seed_definition(oracle):
+    """Second stream of the adjoint: sample_tea_32(bits of lane 0's seeding
+    draw, 1)[0] (plugins/volpathsimple.py:108-113); the seeding draw is the
+    fourth number of lane 0's stream (film 2D, channel 1D)."""
+    for seed in (0, 7, 12345):
+        u = oracle.rng_stream(seed, 0, 4)[3]
+        bits = int(np.float32(u).view(np.uint32))
+        assert oracle.vps_alt_seed(seed) == oracle.sample_tea_32(bits, 1)
+
+
+def _vps_scene(O, albedo=0.8, D=8, res=20, depth=6, factor=0):
+    cam = O.camera_basis(res, res)
+    theta = blob_density(D, 4)[..., 0] * 0.5
+    alb = albedo if np.isscalar(albedo) else albedo
+    return O.Scene(cam, theta, theta, albedo_old=None if np.isscalar(alb) else alb,
+                   albedo_new=None if np.isscalar(alb) else alb, albedo_const=0.8, max_depth=depth,
+                   majorant_factor=factor), theta, cam
+
+
+@pytest.mark.parametrize("factor", [0, 4])
+def test_vps_primal_unbiased(oracle, factor):
+    """volpathsimple renders the image of the single-state estimator (both
+    estimate the same radiance): means within 2 %."""
+    sc, theta, cam = _vps_scene(oracle, factor=factor)
+    a = np.mean([oracle.render(sc, seed=s, spp=64).astype(np.float64).mean() for s in range(8)])
+    b = np.mean([oracle.vps_render(sc, seed=s, spp=64).astype(np.float64).mean() for s in range(8)])
+    assert abs(a - b) < 0.02 * a, (a, b)
+    nn = oracle.vps_render(sc, seed=3, spp=64, flags={"use_nee": False})
+    assert abs(float(nn.mean()) - a) < 0.05 * a
+
+
+@pytest.mark.parametrize("flags", [{}, {"use_drt": False}, {"use_drt_subsampling": False},
+                                   {"use_drt_mis": False}, {"use_nee": False}])
+def test_vps_adjoint_matches_finite_differences(oracle, flags):
+    """The volpathsimple adjoint (DRT scattering term, 4-sample transmittance
+    term, NEE replay; plugins/volpathsimple.py:160-620) against central
+    differences estimated with the two-state tracer (old = theta - h delta,
+    new = theta + h delta share random numbers)."""
+    sc, theta, cam = _vps_scene(oracle)
+    res = sc.width
+    rng = np.random.default_rng(0)
+    dLdimg = rng.normal(0, 1, (res, res, 3)).astype(np.float32) + 0.5
+    runs = np.array([oracle.vps_backward(sc, seed=100 + s, spp=32, grad_img=dLdimg, flags=flags)[0]
+                     for s in range(24)])
+    delta = theta / theta.max()
+    h = 0.02
+    s2 = oracle.Scene(cam, theta - h * delta, theta + h * delta, albedo_const=0.8, max_depth=6)
+    est = []
+    for seed in range(12):
+        H, F = oracle.render_twostates(s2, seed=7 + seed, spp=64)
+        est.append(float(((F.astype(np.float64) - H) * dLdimg).sum() / (2 * h)))
+    fd, fd_sem = np.mean(est), np.std(est) / np.sqrt(len(est))
+    proj = (runs * delta).sum(axis=(1, 2, 3))
+    adj, adj_sem = proj.mean(), proj.std() / np.sqrt(len(proj))
+    assert abs(fd - adj) < 4 * np.hypot(adj_sem, fd_sem) + 1e-4, (adj, adj_sem, fd, fd_sem)
+    assert abs(fd) > 4 * fd_sem  # the check is not vacuous
+
+
+def test_vps_albedo_gradient_matches_finite_differences(oracle):
+    """Albedo-grid gradient of volpathsimple against central differences of
+    the two-state tracer with old/new albedo = a -+ h."""
+    D, res = 8, 20
+    cam = oracle.camera_basis(res, res)
+    theta = blob_density(D, 4)[..., 0] * 0.5
+    alb = np.full((D, D, D, 3), 0.6, np.float32)
+    sc = oracle.Scene(cam, theta, theta, albedo_old=alb, albedo_new=alb, max_depth=6)
+    dLdimg = np.ones((res, res, 3), np.float32)
+    runs = np.array([oracle.vps_backward(sc, seed=200 + s, spp=32, grad_img=dLdimg)[1] for s in range(16)])
+    h = 0.05
+    delta = np.zeros_like(alb)
+    delta[..., 1] = 1.0  # green channel everywhere
+    s2 = oracle.Scene(cam, theta, theta, albedo_old=alb - h * delta, albedo_new=alb + h * delta, max_depth=6)
+    est = []
+    for seed in range(12):
+        H, F = oracle.render_twostates(s2, seed=9 + seed, spp=64)
+        est.append(float(((F.astype(np.float64) - H) * dLdimg).sum() / (2 * h)))
+    fd, fd_sem = np.mean(est), np.std(est) / np.sqrt(len(est))
+    proj = (runs * delta).sum(axis=(1, 2, 3, 4))
+    adj, adj_sem = proj.mean(), proj.std() / np.sqrt(len(proj))
+    assert abs(fd - adj) < 4 * np.hypot(adj_sem, fd_sem) + 1e-4, (adj, adj_sem, fd, fd_sem)
+    assert fd > 4 * fd_sem
