@@ -40,23 +40,48 @@ extern "C" {
 #define RCV_COUNTER_ALBEDO_EVENTS 5 /* adjoint: albedo gradient scatters        */
 #define RCV_COUNTER_COUNT 8
 
-/* Perspective pinhole sensor.  `right` / `up` are the camera basis vectors
- * already scaled by tan(fov_x/2) and tan(fov_x/2)*height/width; pixel (x, y)
- * with film offset (u, v) maps to the direction
- * forward + (2(x+u)/width - 1) right + (1 - 2(y+v)/height) up. */
+/* Sub-sensors of a `batch` sensor (Mitsuba's batch sensor, used by every
+ * grid scene of the reference, experiments.py:28-50). */
+#define RCV_MAX_SENSORS 16
+
+/* World-space pinhole frame: origin, forward direction, and the right / up
+ * basis vectors already scaled by tan(fov_x/2) and tan(fov_x/2)*h/w of the
+ * sensor's own film. */
+typedef struct rcv_camera_frame {
+  float origin[3];
+  float forward[3];
+  float right[3];
+  float up[3];
+} rcv_camera_frame;
+
+/* Perspective pinhole sensor, or a batch of `count` of them rendering side
+ * by side into one film.  Single sensor (count 0 or 1): pixel (x, y) with
+ * film offset (u, v) maps to the direction
+ * forward + (2(x+u)/width - 1) right + (1 - 2(y+v)/height) up.
+ * Batch (count = n > 1, width a multiple of n): the film position
+ * s = (x+u)/width selects sub-sensor k = min(floor(s n), n-1) and the
+ * sub-sensor sees the position s n - floor(s n) of its own film; sub-sensor 0
+ * is the frame of the fields below, sub-sensor k >= 1 is more[k-1]. */
 typedef struct rcv_sensor {
-  int32_t width;
+  int32_t width;   /* film width (all sub-sensors)  */
   int32_t height;
   float origin[3];
   float forward[3];
   float right[3];
   float up[3];
+  int32_t count;   /* sub-sensors: 0 or 1 = a single sensor, at most RCV_MAX_SENSORS */
+  int32_t pad;
+  rcv_camera_frame more[RCV_MAX_SENSORS - 1];
 } rcv_sensor;
 
-/* Two-state heterogeneous medium filling the unit cube [0,1]^3 behind a null
- * boundary.  Grids are x-fastest float32 arrays of shape [Dz][Dy][Dx] (density)
- * and [Dz][Dy][Dx][3] (albedo), sampled trilinearly at voxel centres with
- * clamp-to-edge.  sigma_t = scale * density, sigma_s = albedo * sigma_t. */
+/* Two-state heterogeneous medium filling an axis-aligned box behind a null
+ * boundary: the unit cube [0,1]^3 mapped by to_world = translate(box_min) *
+ * scale(box_size) (the `to_world` of the reference's cube shape and grids,
+ * experiments.py:57,64,79,285).  A box_size component of 0 means 1, so a
+ * zero-initialised box is the unit cube.  Grids are x-fastest float32 arrays
+ * of shape [Dz][Dy][Dx] (density) and [Dz][Dy][Dx][3] (albedo), sampled
+ * trilinearly at voxel centres with clamp-to-edge.  sigma_t = scale *
+ * density per unit world distance, sigma_s = albedo * sigma_t. */
 typedef struct rcv_medium {
   int32_t dims[3]; /* Dx, Dy, Dz */
   float scale;
@@ -72,6 +97,8 @@ typedef struct rcv_medium {
    * density trilinear interpolation can return inside it. */
   int32_t majorant_factor;
   void* workspace; /* device, rcv_medium_workspace_bytes(), 256-B aligned  */
+  float box_min[3];  /* world position of the grid's (0,0,0) corner         */
+  float box_size[3]; /* world extent along x, y, z (0 = 1)                  */
 } rcv_medium;
 
 typedef struct rcv_volpath_options {
@@ -108,6 +135,9 @@ const char* rcv_last_error(void);
 uint64_t rcv_kernel_launches(void);
 /* Compute capability and SM count of the current device (no allocation). */
 int rcv_device_info(int32_t* major, int32_t* minor, int32_t* sm_count);
+/* sizeof() of a public struct by its type name ("rcv_sensor", ...), 0 for an
+ * unknown name: lets foreign-function bindings check their layouts. */
+uint64_t rcv_struct_size(const char* name);
 
 /* -------------------------------------------------------------- sampling */
 /* TEA hash (4 rounds); out[0] is what the reference uses as the default
@@ -398,6 +428,8 @@ typedef struct rcv_batch_job {
   const double* adam_table; /* rcv_adam_table_fill(adam_beta1, adam_beta2)        */
   int32_t adam_table_len;
   int32_t majorant_factor;  /* as rcv_medium.majorant_factor                      */
+  float box_min[3];         /* as rcv_medium.box_min / box_size                   */
+  float box_size[3];
   /* Parameters, double-buffered: before step `it`, density[it & 1] holds
    * theta_it (the `new` state) and density[(it & 1) ^ 1] holds theta_{it-1}
    * (`old`); the step writes theta_{it+1} into the latter.  Both buffers hold

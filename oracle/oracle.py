@@ -47,6 +47,10 @@ class OracleScene(C.Structure):
         ("alb_new", C.c_void_p),
         ("albedo_const", C.c_float * 3),
         ("majorant_factor", C.c_int32),
+        ("box_min", C.c_float * 3),
+        ("box_size", C.c_float * 3),
+        ("n_cams", C.c_int32),
+        ("cams", (C.c_float * 12) * 15),
     ]
 
 
@@ -198,10 +202,20 @@ def camera_basis(width, height, origin=(0.5, 0.5, 3.5), target=(0.5, 0.5, 0.5), 
 
 
 class Scene:
-    """Keeps the numpy grids alive while the C structure points at them."""
+    """Keeps the numpy grids alive while the C structure points at them.
 
-    def __init__(self, cam: Camera, dens_old, dens_new, albedo_old=None, albedo_new=None, albedo_const=0.8,
-                 max_depth=16, rr_depth=None, hide_emitters=False, scale=1.0, majorant_factor=0):
+    ``cam``: one Camera, or a list of Cameras of equal film size rendering
+    side by side into one film (a batch sensor).  ``box_min`` / ``box_size``:
+    the medium box, to_world = translate(box_min) * scale(box_size)."""
+
+    def __init__(self, cam, dens_old, dens_new, albedo_old=None, albedo_new=None, albedo_const=0.8,
+                 max_depth=16, rr_depth=None, hide_emitters=False, scale=1.0, majorant_factor=0,
+                 box_min=(0.0, 0.0, 0.0), box_size=(1.0, 1.0, 1.0)):
+        cams = list(cam) if isinstance(cam, (list, tuple)) else [cam]
+        if not 1 <= len(cams) <= 16 or any((c.width, c.height) != (cams[0].width, cams[0].height) for c in cams):
+            raise ValueError("a batch film takes 1..16 sub-sensors of one film size")
+        cam = Camera(cams[0].width * len(cams), cams[0].height, cams[0].origin, cams[0].forward, cams[0].right,
+                     cams[0].up)
         self.dens_old = np.ascontiguousarray(dens_old, np.float32)
         self.dens_new = np.ascontiguousarray(dens_new, np.float32)
         dz, dy, dx = self.dens_new.shape[:3]
@@ -222,6 +236,11 @@ class Scene:
         ac = np.broadcast_to(np.asarray(albedo_const, np.float32), (3,))
         s.albedo_const[:] = [float(v) for v in ac]
         s.majorant_factor = int(majorant_factor)
+        s.box_min[:] = [float(np.float32(v)) for v in box_min]
+        s.box_size[:] = [float(np.float32(v)) for v in box_size]
+        s.n_cams = len(cams)
+        for k, c in enumerate(cams[1:]):
+            s.cams[k][:] = [*c.origin, *c.forward, *c.right, *c.up]
         self.c = s
         self.width, self.height = cam.width, cam.height
 

@@ -177,6 +177,12 @@ struct oracle_scene {
   const float* alb_new;
   float albedo_const[3];
   int32_t majorant_factor;  // 0: global majorant; f: supergrid of ceil(D/f) cells per axis
+  // medium box: to_world = translate(box_min) * scale(box_size), size 0 = 1
+  float box_min[3], box_size[3];
+  // batch film: n_cams sub-sensors side by side (<= 1: the camera above);
+  // sub-sensor k >= 1 is cams[k-1] = origin, forward, right, up (world space)
+  int32_t n_cams;
+  float cams[15][12];
 };
 }
 
@@ -232,6 +238,52 @@ float grid_max(const oracle_scene& S, const float* g) {
   const int64_t n = (int64_t)S.dx * S.dy * S.dz;
   for (int64_t i = 0; i < n; ++i) m = std::fmax(m, g[i]);
   return m;
+}
+
+// Inverse box size (1 for a zero or unit size).
+V3 inv_box(const oracle_scene& S) {
+  V3 r;
+  r.x = S.box_size[0] > 0.0f ? 1.0f / S.box_size[0] : 1.0f;
+  r.y = S.box_size[1] > 0.0f ? 1.0f / S.box_size[1] : 1.0f;
+  r.z = S.box_size[2] > 0.0f ? 1.0f / S.box_size[2] : 1.0f;
+  return r;
+}
+
+// A world direction in box coordinates: distances along the ray stay world
+// distances.
+V3 to_box(const oracle_scene& S, const V3& w) {
+  const V3 ib = inv_box(S);
+  return V3{w.x * ib.x, w.y * ib.y, w.z * ib.z};
+}
+
+// Camera ray of film position (px + u0, py + u1) in box coordinates.  A batch
+// film (Mitsuba's batch sensor) gives the position s = (px + u0) / width to
+// sub-sensor k = min(floor(s n), n - 1) as s n - floor(s n).
+void camera_ray(const oracle_scene& S, int px, int py, float u0, float u1, V3& o, V3& d) {
+  const float fx = (float)px + u0, fy = (float)py + u1;
+  const float inv_w = 1.0f / (float)S.width, inv_h = 1.0f / (float)S.height;
+  float nx = fx * inv_w;
+  const float ny = fy * inv_h;
+  int k = 0;
+  if (S.n_cams > 1) {
+    const float idx_f = nx * (float)S.n_cams;
+    const int idx = (int)idx_f;
+    k = std::min(idx, S.n_cams - 1);
+    nx = idx_f - (float)idx;
+  }
+  const float* co = k == 0 ? S.cam_o : S.cams[k - 1];
+  const float* cf = k == 0 ? S.cam_f : S.cams[k - 1] + 3;
+  const float* cr = k == 0 ? S.cam_r : S.cams[k - 1] + 6;
+  const float* cu = k == 0 ? S.cam_u : S.cams[k - 1] + 9;
+  const float a = std::fmaf(2.0f, nx, -1.0f), b = std::fmaf(-2.0f, ny, 1.0f);
+  V3 r;
+  r.x = std::fmaf(b, cu[0], std::fmaf(a, cr[0], cf[0]));
+  r.y = std::fmaf(b, cu[1], std::fmaf(a, cr[1], cf[1]));
+  r.z = std::fmaf(b, cu[2], std::fmaf(a, cr[2], cf[2]));
+  const float inv_len = 1.0f / std::sqrt(std::fmaf(r.z, r.z, std::fmaf(r.y, r.y, r.x * r.x)));
+  d = to_box(S, V3{r.x * inv_len, r.y * inv_len, r.z * inv_len});
+  const V3 ib = inv_box(S);
+  o = V3{(co[0] - S.box_min[0]) * ib.x, (co[1] - S.box_min[1]) * ib.y, (co[2] - S.box_min[2]) * ib.z};
 }
 
 // Majorant supergrid (plugins/twostatemedium.py:25-70): ceil(D/f) cells per
@@ -451,17 +503,8 @@ struct Tracer {
     Rng rng = lane_rng(seed, lane);
     // camera ray from the film sample (box filter: the sample stays in its pixel)
     const float u0 = rng.next1d(), u1 = rng.next1d();
-    const float fx = (float)px + u0, fy = (float)py + u1;
-    const float inv_w = 1.0f / (float)S.width, inv_h = 1.0f / (float)S.height;
-    const float nx = fx * inv_w, ny = fy * inv_h;
-    const float a = std::fmaf(2.0f, nx, -1.0f), b = std::fmaf(-2.0f, ny, 1.0f);
-    V3 r;
-    r.x = std::fmaf(b, S.cam_u[0], std::fmaf(a, S.cam_r[0], S.cam_f[0]));
-    r.y = std::fmaf(b, S.cam_u[1], std::fmaf(a, S.cam_r[1], S.cam_f[1]));
-    r.z = std::fmaf(b, S.cam_u[2], std::fmaf(a, S.cam_r[2], S.cam_f[2]));
-    const float inv_len = 1.0f / std::sqrt(std::fmaf(r.z, r.z, std::fmaf(r.y, r.y, r.x * r.x)));
-    V3 d{r.x * inv_len, r.y * inv_len, r.z * inv_len};
-    const V3 o{S.cam_o[0], S.cam_o[1], S.cam_o[2]};
+    V3 o, d;
+    camera_ray(S, px, py, u0, u1, o, d);
     (void)rng.next1d();  // colour channel (grey extinction: unused)
 
     V3 bo{1, 1, 1}, bn{1, 1, 1};
@@ -563,10 +606,10 @@ struct Tracer {
       // phase function sample: isotropic, 1D (unused) + 2D
       rng.next1d();
       const float pu0 = rng.next1d(), pu1 = rng.next1d();
-      const V3 wo = square_to_uniform_sphere(pu0, pu1);
+      const V3 wo = to_box(S, square_to_uniform_sphere(pu0, pu1));
       // next event estimation towards the constant environment
       const float nu0 = rng.next1d(), nu1 = rng.next1d();
-      const V3 w = square_to_uniform_sphere(nu0, nu1);
+      const V3 w = to_box(S, square_to_uniform_sphere(nu0, nu1));
       const Rng rng_before = rng;
       float tro, trn;
       transmittance(rng, x, w, tro, trn, out, nullptr);
@@ -904,7 +947,7 @@ struct Vps {
   V3 nee(Rng& r, const V3& x, const V3& thr, const V3* dL) const {
     Rng replay = r;
     const float u0 = r.next1d(), u1 = r.next1d();
-    const V3 w = square_to_uniform_sphere(u0, u1);
+    const V3 w = to_box(S, square_to_uniform_sphere(u0, u1));
     float tn, tf;
     cube_hit(x, w, tn, tf);
     const float tr = transmittance(r, x, w, tf, nullptr);
@@ -956,7 +999,7 @@ struct Vps {
       r.next1d();
       const float pu0 = r.next1d(), pu1 = r.next1d();
       seg.o = x;
-      seg.d = square_to_uniform_sphere(pu0, pu1);
+      seg.d = to_box(S, square_to_uniform_sphere(pu0, pu1));
       float tn, tf;
       cube_hit(seg.o, seg.d, tn, tf);
       if (!(tf > 0.0f)) break;  // accidental escape (:279-283)
@@ -973,17 +1016,7 @@ struct Vps {
   // :329-346).  Returns false when the ray misses the cube.
   bool camera(Rng& r, int px, int py, V3& o, V3& d, VpsSegment& seg) const {
     const float u0 = r.next1d(), u1 = r.next1d();
-    const float fx = (float)px + u0, fy = (float)py + u1;
-    const float inv_w = 1.0f / (float)S.width, inv_h = 1.0f / (float)S.height;
-    const float nx = fx * inv_w, ny = fy * inv_h;
-    const float a = std::fmaf(2.0f, nx, -1.0f), b = std::fmaf(-2.0f, ny, 1.0f);
-    V3 rr;
-    rr.x = std::fmaf(b, S.cam_u[0], std::fmaf(a, S.cam_r[0], S.cam_f[0]));
-    rr.y = std::fmaf(b, S.cam_u[1], std::fmaf(a, S.cam_r[1], S.cam_f[1]));
-    rr.z = std::fmaf(b, S.cam_u[2], std::fmaf(a, S.cam_r[2], S.cam_f[2]));
-    const float inv_len = 1.0f / std::sqrt(std::fmaf(rr.z, rr.z, std::fmaf(rr.y, rr.y, rr.x * rr.x)));
-    d = V3{rr.x * inv_len, rr.y * inv_len, rr.z * inv_len};
-    o = V3{S.cam_o[0], S.cam_o[1], S.cam_o[2]};
+    camera_ray(S, px, py, u0, u1, o, d);
     r.next1d();  // colour channel
     float tn, tf;
     cube_hit(o, d, tn, tf);
@@ -1026,7 +1059,7 @@ struct Vps {
     if (F.use_nee) Li = nee(alt, x, V3{1, 1, 1}, nullptr);
     alt.next1d();
     const float pu0 = alt.next1d(), pu1 = alt.next1d();
-    VpsSegment next{x, square_to_uniform_sphere(pu0, pu1), 0.0f};
+    VpsSegment next{x, to_box(S, square_to_uniform_sphere(pu0, pu1)), 0.0f};
     float tn, tf;
     cube_hit(next.o, next.d, tn, tf);
     const bool ok = tf > 0.0f;
@@ -1127,7 +1160,7 @@ struct Vps {
       r.next1d();
       const float pu0 = r.next1d(), pu1 = r.next1d();
       seg.o = x;
-      seg.d = square_to_uniform_sphere(pu0, pu1);
+      seg.d = to_box(S, square_to_uniform_sphere(pu0, pu1));
       float tn, tf;
       cube_hit(seg.o, seg.d, tn, tf);
       if (!(tf > 0.0f)) break;

@@ -31,6 +31,13 @@ f3 = C.c_float * 3
 i3 = C.c_int32 * 3
 
 
+MAX_SENSORS = 16
+
+
+class CameraFrame(C.Structure):
+    _fields_ = [("origin", f3), ("forward", f3), ("right", f3), ("up", f3)]
+
+
 class Sensor(C.Structure):
     _fields_ = [
         ("width", C.c_int32),
@@ -39,6 +46,9 @@ class Sensor(C.Structure):
         ("forward", f3),
         ("right", f3),
         ("up", f3),
+        ("count", C.c_int32),
+        ("pad", C.c_int32),
+        ("more", CameraFrame * (MAX_SENSORS - 1)),
     ]
 
 
@@ -53,6 +63,8 @@ class Medium(C.Structure):
         ("albedo_value", f3),
         ("majorant_factor", C.c_int32),
         ("workspace", C.c_void_p),
+        ("box_min", f3),
+        ("box_size", f3),
     ]
 
 
@@ -147,6 +159,8 @@ class BatchJob(C.Structure):
         ("adam_table", C.c_void_p),
         ("adam_table_len", C.c_int32),
         ("majorant_factor", C.c_int32),
+        ("box_min", f3),
+        ("box_size", f3),
         ("density", C.c_void_p * 2),
         ("albedo", C.c_void_p * 2),
         ("density_m", C.c_void_p),
@@ -181,6 +195,7 @@ SIGNATURES = {
     "rcv_last_error": (C.c_char_p, []),
     "rcv_kernel_launches": (C.c_uint64, []),
     "rcv_device_info": (C.c_int, [P(C.c_int32), P(C.c_int32), P(C.c_int32)]),
+    "rcv_struct_size": (C.c_uint64, [C.c_char_p]),
     "rcv_sample_tea_32": (None, [C.c_uint32, C.c_uint32, P(C.c_uint32)]),
     "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32, C.c_int32]),
     "rcv_medium_prepare": (C.c_int, [P(Medium), vp]),
@@ -256,6 +271,21 @@ def library_path() -> Path:
     return _build.lib_path()
 
 
+# ctypes mirrors of the public structs, checked against the library at load
+STRUCTS = {
+    "rcv_camera_frame": CameraFrame,
+    "rcv_sensor": Sensor,
+    "rcv_medium": Medium,
+    "rcv_volpath_options": VolpathOptions,
+    "rcv_sphere": SphereDesc,
+    "rcv_surface_scene": SurfaceScene,
+    "rcv_cv_state": CvState,
+    "rcv_batch_job": BatchJob,
+    "rcv_batch_job_status": BatchJobStatus,
+    "rcv_volpathsimple_flags": VpsFlags,
+}
+
+
 def load() -> C.CDLL:
     """Loads librcv, building it first when the sources changed."""
     global _lib
@@ -268,6 +298,10 @@ def load() -> C.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        for cname, struct in STRUCTS.items():
+            got, want = int(lib.rcv_struct_size(cname.encode())), C.sizeof(struct)
+            if got != want:
+                raise RuntimeError(f"librcv {cname} is {got} bytes, the binding's {want}: stale build")
         _lib = lib
         return lib
 

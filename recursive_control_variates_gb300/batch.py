@@ -84,14 +84,16 @@ class CVJob:
     optimiser's ``lr`` / betas / epsilon and clamp ranges, and the loss.
     ``optimize_albedo`` (default: when the albedo is a grid) adds the albedo
     grid to the optimised variables; ``majorant_factor`` > 0 gives the medium
-    a majorant supergrid (the reference's ``majorant_resolution_factor``)."""
+    a majorant supergrid (the reference's ``majorant_resolution_factor``);
+    ``box`` (a ``core.BoxTransform``, default the unit cube) places the grid
+    in the world.  The sensor may be a ``batch`` sensor."""
 
     def __init__(self, density, albedo, target, sensor, *, spp: int, spp_grad: int = 0, max_depth: int = 6,
                  rr_depth: int = 5, hide_emitters: bool = False, scale: float = 1.0, seed: int = 0,
                  lr: float = 0.02, adam_betas=(0.9, 0.999), adam_eps: float = 1e-8,
                  density_bounds=(-_INF, _INF), albedo_bounds=(-_INF, _INF), warmup: int = 1, beta1: float = 0.9,
                  beta2: float = 0.999, pre_update: bool = False, loss: str = "l2", optimize_albedo=None,
-                 keep_images: bool = False, majorant_factor: int = 0, device="cuda"):
+                 keep_images: bool = False, majorant_factor: int = 0, box=None, device="cuda"):
         lib = _lib.load()
         self.device = torch.device(device)
         dev = self.device
@@ -163,6 +165,9 @@ class CVJob:
         if int(majorant_factor) < 0:
             raise ValueError("majorant_factor must be >= 0")
         j.majorant_factor = int(majorant_factor)
+        if box is not None:  # a core.BoxTransform: the medium's to_world
+            j.box_min[:] = [float(np.float32(v)) for v in box.box_min]
+            j.box_size[:] = [float(np.float32(v)) for v in box.box_size]
         j.density[0], j.density[1] = self.density[0].data_ptr(), self.density[1].data_ptr()
         if self.albedo is not None:
             j.albedo[0], j.albedo[1] = self.albedo[0].data_ptr(), self.albedo[1].data_ptr()
@@ -225,7 +230,8 @@ class CVJob:
             albedo_bounds=opt.bounds.get(akey, (-_INF, _INF)) if akey else (-_INF, _INF),
             warmup=integrator.warmup, beta1=integrator.beta1, beta2=integrator.beta2,
             pre_update=getattr(integrator, "pre_update", False), loss=loss, optimize_albedo=akey is not None,
-            keep_images=keep_images, majorant_factor=medium.majorant_resolution_factor(), device=medium.device,
+            keep_images=keep_images, majorant_factor=medium.majorant_resolution_factor(), box=new.box,
+            device=medium.device,
         )
 
     # ---------------------------------------------------------------- state

@@ -101,6 +101,67 @@ def look_at(origin, target, up) -> LookAt:
     return LookAt(tuple(map(float, origin)), tuple(map(float, target)), tuple(map(float, up)))
 
 
+@dataclass(frozen=True)
+class BoxTransform:
+    """Axis-aligned affine map x -> scale * x + translate (positive scale):
+    the ``to_world`` of the reference's medium boxes, ``T.scale(s)`` and
+    ``T.translate(t).scale(s)`` (experiments.py:57,64,79,285).  Composes like
+    Mitsuba's transforms: ``a.scale(s)`` is the product a * scale(s), so
+    ``T.translate(t).scale(s)`` maps x to t + s x."""
+
+    scale_: tuple = (1.0, 1.0, 1.0)
+    translate_: tuple = (0.0, 0.0, 0.0)
+
+    def __post_init__(self):
+        if any(not (v > 0 and math.isfinite(v)) for v in self.scale_):
+            raise ValueError("box transforms need a positive, finite scale")
+
+    def __matmul__(self, other: "BoxTransform") -> "BoxTransform":
+        s = tuple(a * b for a, b in zip(self.scale_, other.scale_))
+        t = tuple(a * b + c for a, b, c in zip(self.scale_, other.translate_, self.translate_))
+        return BoxTransform(s, t)
+
+    def scale(self, v) -> "BoxTransform":
+        return self @ T.scale(v)
+
+    def translate(self, v) -> "BoxTransform":
+        return self @ T.translate(v)
+
+    @property
+    def box_min(self) -> tuple:
+        return self.translate_
+
+    @property
+    def box_size(self) -> tuple:
+        return self.scale_
+
+
+def _vec3(v) -> tuple:
+    a = np.broadcast_to(np.asarray(v, np.float64), (3,))
+    return tuple(float(x) for x in a)
+
+
+class T:
+    """``mitsuba.scalar_rgb.Transform4f`` as the reference's scene
+    dictionaries use it: ``T.look_at(origin=, target=, up=)`` for sensors,
+    ``T.scale(s)`` / ``T.translate(t)`` (chained) for the medium box."""
+
+    @staticmethod
+    def look_at(origin, target, up) -> LookAt:
+        return look_at(origin, target, up)
+
+    @staticmethod
+    def scale(v) -> BoxTransform:
+        return BoxTransform(_vec3(v), (0.0, 0.0, 0.0))
+
+    @staticmethod
+    def translate(v) -> BoxTransform:
+        return BoxTransform((1.0, 1.0, 1.0), _vec3(v))
+
+
+UNIT_BOX = BoxTransform()
+
+
 # ------------------------------------------------------------------ sensors
 class Film:
     def __init__(self, props: Properties):
@@ -146,7 +207,9 @@ class PerspectiveSensor:
     def sampler(self):
         return self.sampler_
 
-    def c_struct(self) -> _lib.Sensor:
+    def frame(self, width: int, height: int) -> tuple:
+        """(origin, forward, right * tan(fov/2), up * tan(fov/2) * h / w) as
+        float32 values, for a film of width x height."""
         o = np.array(self.to_world.origin, np.float64)
         t = np.array(self.to_world.target, np.float64)
         up = np.array(self.to_world.up, np.float64)
@@ -156,14 +219,53 @@ class PerspectiveSensor:
         right /= np.linalg.norm(right)
         cam_up = np.cross(right, fwd)
         tx = math.tan(math.radians(self.fov) * 0.5)
+        ty = tx * height / width
+        f32 = lambda v: [float(np.float32(x)) for x in v]  # noqa: E731
+        return f32(o), f32(fwd), f32(right * tx), f32(cam_up * ty)
+
+    def c_struct(self) -> _lib.Sensor:
         w, h = self.film_.width, self.film_.height
-        ty = tx * h / w
         s = _lib.Sensor()
         s.width, s.height = w, h
-        s.origin[:] = [float(np.float32(v)) for v in o]
-        s.forward[:] = [float(np.float32(v)) for v in fwd]
-        s.right[:] = [float(np.float32(v)) for v in right * tx]
-        s.up[:] = [float(np.float32(v)) for v in cam_up * ty]
+        s.origin[:], s.forward[:], s.right[:], s.up[:] = self.frame(w, h)
+        s.count = 1
+        return s
+
+
+class BatchSensor:
+    """``batch`` (Mitsuba's batch sensor; every grid scene of the reference,
+    experiments.py:28-50,141-164,257-281): the perspective sub-sensors of the
+    dictionary render side by side into one film of width n * w; sub-sensor k
+    sees pixels [k w, (k+1) w) with a film of w x height.  Sub-sensors are
+    taken in dictionary order."""
+
+    def __init__(self, props: Properties):
+        self.film_ = props.get("film", None) or Film(Properties("hdrfilm", {}))
+        self.sampler_ = props.get("sampler", None) or IndependentSampler(Properties("independent", {}))
+        self.sensors = [v for v in props.values() if isinstance(v, PerspectiveSensor)]
+        n = len(self.sensors)
+        if not 1 <= n <= _lib.MAX_SENSORS:
+            raise ValueError(f"a batch sensor takes 1..{_lib.MAX_SENSORS} perspective sensors, got {n}")
+        if self.film_.width % n:
+            raise ValueError(f"batch film width {self.film_.width} is not a multiple of its {n} sensors")
+
+    def film(self) -> Film:
+        return self.film_
+
+    def sampler(self):
+        return self.sampler_
+
+    def c_struct(self) -> _lib.Sensor:
+        n = len(self.sensors)
+        w, h = self.film_.width, self.film_.height
+        sub_w = w // n
+        s = _lib.Sensor()
+        s.width, s.height = w, h
+        s.origin[:], s.forward[:], s.right[:], s.up[:] = self.sensors[0].frame(sub_w, h)
+        s.count = n
+        for k, sub in enumerate(self.sensors[1:]):
+            f = s.more[k]
+            f.origin[:], f.forward[:], f.right[:], f.up[:] = sub.frame(sub_w, h)
         return s
 
 
@@ -196,13 +298,27 @@ def _as_tensor(x, device, channels: int) -> torch.Tensor:
 
 
 class GridVolume:
-    """``gridvolume`` with in-memory ``data`` of shape (Dz, Dy, Dx, C)."""
+    """``gridvolume``: in-memory ``data`` of shape (Dz, Dy, Dx, C) or a
+    ``.vol`` ``filename``.  The grid spans ``to_world`` applied to the unit
+    cube (``use_grid_bbox``: the bounding box stored in the file instead).
+    ``accel`` only selects Mitsuba's texture path and changes nothing here."""
 
     def __init__(self, props: Properties):
-        if "filename" in props:
-            raise ValueError("gridvolume from .vol files is not supported; pass 'data'")
-        self.raw = props["data"]
         self.device = _device(props)
+        to_world = props.get("to_world", UNIT_BOX)
+        if not isinstance(to_world, BoxTransform):
+            raise ValueError("gridvolume to_world must be an axis-aligned scale/translate (T.scale, T.translate)")
+        if "filename" in props:
+            from .io import read_vol
+
+            g = read_vol(props["filename"])
+            self.raw = g.data
+            if props.get("use_grid_bbox", False):
+                size = tuple(b - a for a, b in zip(g.bbox_min, g.bbox_max))
+                to_world = to_world @ BoxTransform(size, tuple(g.bbox_min))
+        else:
+            self.raw = props["data"]
+        self.to_world = to_world
 
 
 class _PackedMedium:
@@ -257,6 +373,8 @@ class _PackedMedium:
         m.albedo_value[:] = list(new.albedo_value)
         m.majorant_factor = self._factor()
         m.workspace = aligned
+        m.box_min[:] = [float(np.float32(v)) for v in new.box.box_min]
+        m.box_size[:] = [float(np.float32(v)) for v in new.box.box_size]
         return m
 
     def prepare(self, stream) -> _lib.Medium:
@@ -281,6 +399,7 @@ class HeterogeneousMedium(_PackedMedium):
         if not isinstance(st, GridVolume):
             raise ValueError("sigma_t must be a gridvolume")
         self.density = _as_tensor(st.raw, self.device, 1)
+        self.box = st.to_world
         alb = props.get("albedo", 0.75)
         self.albedo_grid = None
         self.albedo_value = (0.75, 0.75, 0.75)
@@ -288,6 +407,8 @@ class HeterogeneousMedium(_PackedMedium):
             self.albedo_grid = _as_tensor(alb.raw, self.device, 3)
             if self.albedo_grid.shape[:3] != self.density.shape[:3]:
                 raise ValueError("albedo and sigma_t grids must have the same resolution")
+            if alb.to_world != self.box:
+                raise ValueError("albedo and sigma_t grids must have the same to_world")
         else:
             if isinstance(alb, dict):
                 alb = alb.get("value", 0.75)
@@ -329,6 +450,21 @@ class HeterogeneousMedium(_PackedMedium):
     def traverse(self) -> dict[str, torch.Tensor]:
         return self.param_tensors()
 
+    def set_grid(self, sub: str, value: torch.Tensor) -> None:
+        """Replaces a grid by one of another resolution (utils.upsample,
+        utils.py:177-192, hands the optimiser a finer grid)."""
+        t = _as_tensor(value, self.device, 1 if sub == "sigma_t.data" else 3)
+        if sub == "sigma_t.data":
+            self.density = t
+        elif sub == "albedo.data" and self.albedo_grid is not None:
+            self.albedo_grid = t
+        else:
+            raise KeyError(sub)
+        if self.albedo_grid is not None and self.albedo_grid.shape[:3] != self.density.shape[:3]:
+            raise ValueError("albedo and sigma_t grids must have the same resolution")
+        self._workspace = None
+        self._dirty = True
+
     def parameters_changed(self, keys=None) -> None:
         self._dirty = True
 
@@ -349,6 +485,8 @@ class TwoStateMedium(_PackedMedium):
                 raise ValueError("twostatemedium expects heterogeneous media for old/new/incoming")
         if not (self.old.dims == self.new.dims == self.incoming.dims):
             raise ValueError("old/new/incoming grids must have the same resolution")
+        if not (self.old.box == self.new.box == self.incoming.box):
+            raise ValueError("old/new/incoming grids must have the same to_world")
         if (self.old.albedo_grid is None) != (self.new.albedo_grid is None) or (
             self.new.albedo_grid is None
         ) != (self.incoming.albedo_grid is None):
@@ -374,6 +512,16 @@ class TwoStateMedium(_PackedMedium):
     def traverse(self) -> dict[str, torch.Tensor]:
         return self.incoming.param_tensors()
 
+    def set_grid(self, sub: str, value: torch.Tensor) -> None:
+        """A new resolution for all three states (utils.upsample).  The
+        rotation that follows makes old = new = the new grid; the integrators
+        are reset with the upsampling (utils.py:190), so their first step
+        does not use the old state's image."""
+        for m in (self.old, self.new, self.incoming):
+            m.set_grid(sub, value)
+        self._workspace = None
+        self._dirty = True
+
     def parameters_changed(self, keys=None) -> None:
         o, n, i = self.old, self.new, self.incoming
         o.density, n.density = n.density, o.density
@@ -390,16 +538,41 @@ class NullBSDF:
         pass
 
 
+def _check_unit_cube_mesh(path) -> None:
+    """The reference bounds its media with common/meshes/cube_unit.obj; any
+    OBJ whose vertices are the corners of [0,1]^3 is accepted."""
+    verts = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("v "):
+                verts.append([float(x) for x in line.split()[1:4]])
+    v = np.array(verts, np.float64)
+    if v.size == 0 or not np.all(np.isclose(v, 0.0) | np.isclose(v, 1.0)) or \
+            not np.allclose(v.min(axis=0), 0.0) or not np.allclose(v.max(axis=0), 1.0):
+        raise ValueError(f"{path}: the medium boundary must be the unit-cube mesh (corners of [0,1]^3)")
+
+
 class CubeShape:
-    """Unit cube [0,1]^3 (the 'cube_unit' mesh of the reference scenes)."""
+    """Medium boundary: the unit cube [0,1]^3 (the 'cube_unit' mesh of the
+    reference scenes) mapped by ``to_world`` (an axis-aligned scale and
+    translation, experiments.py:79,285).  Registered as ``cube`` and as
+    ``obj`` (whose ``filename`` must hold the unit-cube mesh)."""
 
     def __init__(self, props: Properties):
         bsdf = props.get("bsdf", None)
         if bsdf is not None and not isinstance(bsdf, NullBSDF):
             raise ValueError("the medium boundary must use a 'null' BSDF")
-        if "to_world" in props:
-            raise ValueError("the medium boundary is the unit cube; to_world is not supported")
+        self.to_world = props.get("to_world", UNIT_BOX)
+        if not isinstance(self.to_world, BoxTransform):
+            raise ValueError("the medium boundary's to_world must be an axis-aligned scale/translate")
+        if "filename" in props:
+            _check_unit_cube_mesh(props["filename"])
         self.interior = props.get("interior", None)
+        med = self.interior
+        if med is not None and hasattr(med, "dims"):
+            box = med.new.box if hasattr(med, "new") else med.box
+            if box != self.to_world:
+                raise ValueError("the medium's grids and its boundary shape must have the same to_world")
 
     def interior_medium(self):
         return self.interior
@@ -416,7 +589,7 @@ class Scene:
         for k, v in props.items():
             if k == "device":
                 continue
-            if isinstance(v, PerspectiveSensor):
+            if isinstance(v, (PerspectiveSensor, BatchSensor)):
                 self.sensors_.append(v)
             elif isinstance(v, ConstantEmitter):
                 self.emitters_.append(v)
@@ -486,7 +659,7 @@ class SceneParameters:
         if cur is not None and tuple(v.shape) != tuple(cur.shape):
             if v.numel() == 1:
                 v = v.reshape(()).expand(cur.shape)
-            else:
+            elif not (hasattr(owner, "set_grid") and v.dim() == cur.dim() == 4 and v.shape[-1] == cur.shape[-1]):
                 raise ValueError(f"parameter '{key}' has shape {tuple(cur.shape)}, got {tuple(v.shape)}")
         self._values[key] = v
         self._pending.add(key)
@@ -500,8 +673,12 @@ class SceneParameters:
         for key in self._pending:
             owner, sub = self._owners[key]
             dst = owner.traverse()[sub]
+            val = self._values[key].detach()
             with torch.no_grad():
-                dst.copy_(self._values[key].detach().to(dst.device, torch.float32).reshape(dst.shape))
+                if tuple(val.shape) != tuple(dst.shape) and val.numel() != dst.numel():
+                    owner.set_grid(sub, val)  # a new resolution
+                else:
+                    dst.copy_(val.to(dst.device, torch.float32).reshape(dst.shape))
             owners[id(owner)] = owner
         self._pending.clear()
         for owner in owners.values():
@@ -522,6 +699,7 @@ def traverse(scene: Scene) -> SceneParameters:
 for _name, _ctor, _kind in [
     ("scene", Scene, "scene"),
     ("perspective", PerspectiveSensor, "sensor"),
+    ("batch", BatchSensor, "sensor"),
     ("hdrfilm", Film, "film"),
     ("box", BoxFilter, "rfilter"),
     ("independent", IndependentSampler, "sampler"),
@@ -531,6 +709,7 @@ for _name, _ctor, _kind in [
     ("heterogeneous", HeterogeneousMedium, "medium"),
     ("null", NullBSDF, "bsdf"),
     ("cube", CubeShape, "shape"),
+    ("obj", CubeShape, "shape"),
 ]:
     register_object(_kind, _name, _ctor)
 register_medium("twostatemedium", TwoStateMedium)

@@ -414,6 +414,8 @@ static rcv_medium job_medium(const rcv_batch_job& j, const JobLayout& L) {
   m.albedo_new = j.albedo[1];
   std::memcpy(m.albedo_value, j.albedo_value, sizeof(m.albedo_value));
   m.majorant_factor = j.majorant_factor;
+  std::memcpy(m.box_min, j.box_min, sizeof(m.box_min));
+  std::memcpy(m.box_size, j.box_size, sizeof(m.box_size));
   m.workspace = static_cast<char*>(j.workspace) + L.medium;
   return m;
 }

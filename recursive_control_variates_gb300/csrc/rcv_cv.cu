@@ -167,6 +167,25 @@ extern "C" int rcv_device_info(int32_t* major, int32_t* minor, int32_t* sm_count
   return RCV_OK;
 }
 
+extern "C" uint64_t rcv_struct_size(const char* name) {
+  if (name == nullptr) return 0;
+  struct Entry {
+    const char* name;
+    uint64_t size;
+  };
+  static const Entry table[] = {
+      {"rcv_camera_frame", sizeof(rcv_camera_frame)}, {"rcv_sensor", sizeof(rcv_sensor)},
+      {"rcv_medium", sizeof(rcv_medium)},             {"rcv_volpath_options", sizeof(rcv_volpath_options)},
+      {"rcv_sphere", sizeof(rcv_sphere)},             {"rcv_surface_scene", sizeof(rcv_surface_scene)},
+      {"rcv_cv_state", sizeof(rcv_cv_state)},         {"rcv_batch_job", sizeof(rcv_batch_job)},
+      {"rcv_batch_job_status", sizeof(rcv_batch_job_status)},
+      {"rcv_volpathsimple_flags", sizeof(rcv_volpathsimple_flags)},
+  };
+  for (const Entry& e : table)
+    if (std::strcmp(e.name, name) == 0) return e.size;
+  return 0;
+}
+
 extern "C" void rcv_sample_tea_32(uint32_t v0, uint32_t v1, uint32_t out[2]) {
   uint32_t a, b;
   tea(v0, v1, 4, a, b);

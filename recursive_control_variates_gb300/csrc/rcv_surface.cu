@@ -86,6 +86,7 @@ static int make_surf_job(const rcv_surface_scene* sc, const rcv_sensor* s, const
   if (rc) return rc;
   RCV_REQUIRE(s != nullptr && o != nullptr, "sensor / options are NULL");
   RCV_REQUIRE(s->width > 0 && s->height > 0, "film size must be positive");
+  RCV_REQUIRE(s->count <= 1, "the surface tracer renders a single sensor (batch sensors: media only)");
   RCV_REQUIRE(spp > 0, "spp must be positive");
   RCV_REQUIRE(o->max_depth >= -1, "max_depth must be >= -1");
   RCV_REQUIRE(int64_t(s->width) * s->height * spp < (int64_t(1) << 32),

@@ -283,10 +283,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         // isotropic phase sample (1D unused + 2D), plugins/twostatevolpath.py:275
         pcg_skip1(rng);
         const float pu0 = next1d(rng), pu1 = next1d(rng);
-        wo_next = uniform_sphere(pu0, pu1);
+        wo_next = to_box(J, uniform_sphere(pu0, pu1));
         // NEE towards the environment, then ratio tracking
         const float nu0 = next1d(rng), nu1 = next1d(rng);
-        w = uniform_sphere(nu0, nu1);
+        w = to_box(J, uniform_sphere(nu0, nu1));
         q = p;
         {
           float a;

@@ -4,6 +4,7 @@
 // gradient fold back to voxel layout.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -185,14 +186,34 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   RCV_REQUIRE(o->max_depth >= -1, "max_depth must be >= -1");
   RCV_REQUIRE(int64_t(s->width) * s->height * spp < (int64_t(1) << 32),
               "width * height * spp must be below 2^32 (one random stream per path)");
+  const int n_cams = s->count > 1 ? s->count : 1;
+  RCV_REQUIRE(n_cams <= RCV_MAX_SENSORS, "a batch sensor has at most %d sub-sensors", RCV_MAX_SENSORS);
+  RCV_REQUIRE(s->width % n_cams == 0, "batch film width %d is not a multiple of its %d sensors", s->width,
+              n_cams);
+  float inv_box[3];
+  for (int a = 0; a < 3; ++a) {
+    RCV_REQUIRE(m->box_size[a] >= 0.0f && std::isfinite(m->box_size[a]) && std::isfinite(m->box_min[a]),
+                "medium box must have a finite, non-negative size");
+    inv_box[a] = m->box_size[a] > 0.0f ? 1.0f / m->box_size[a] : 1.0f;
+  }
   std::memset(J, 0, sizeof(VolJob));
   J->width = s->width;
   J->height = s->height;
   J->spp = spp;
-  J->cam_o = V3{s->origin[0], s->origin[1], s->origin[2]};
-  J->cam_f = V3{s->forward[0], s->forward[1], s->forward[2]};
-  J->cam_r = V3{s->right[0], s->right[1], s->right[2]};
-  J->cam_u = V3{s->up[0], s->up[1], s->up[2]};
+  J->n_cams = n_cams;
+  J->inv_box = V3{inv_box[0], inv_box[1], inv_box[2]};
+  for (int k = 0; k < n_cams; ++k) {
+    const float* o = k == 0 ? s->origin : s->more[k - 1].origin;
+    const float* f = k == 0 ? s->forward : s->more[k - 1].forward;
+    const float* r = k == 0 ? s->right : s->more[k - 1].right;
+    const float* u = k == 0 ? s->up : s->more[k - 1].up;
+    // camera origin in box coordinates; the directions stay in world space
+    J->cam[k].o = V3{(o[0] - m->box_min[0]) * inv_box[0], (o[1] - m->box_min[1]) * inv_box[1],
+                     (o[2] - m->box_min[2]) * inv_box[2]};
+    J->cam[k].f = V3{f[0], f[1], f[2]};
+    J->cam[k].r = V3{r[0], r[1], r[2]};
+    J->cam[k].u = V3{u[0], u[1], u[2]};
+  }
   J->inv_w = 1.0f / (float)s->width;
   J->inv_h = 1.0f / (float)s->height;
   J->max_depth = o->max_depth < 0 ? 0x7fffffff : o->max_depth;

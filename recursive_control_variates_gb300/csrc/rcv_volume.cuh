@@ -1,6 +1,9 @@
 // Two-state volumetric path tracer, single-state tracer and seed-replay
-// adjoint for a heterogeneous medium in the unit cube behind a null boundary,
-// lit by a constant white environment (radiance 1).
+// adjoint for a heterogeneous medium in an axis-aligned box behind a null
+// boundary, lit by a constant white environment (radiance 1).  The tracers
+// work in box coordinates (the unit cube of the grid): a world direction d
+// becomes d / box_size, so every distance along a ray stays a world distance
+// and sigma_t keeps its world units.
 //
 // Restates the per-path algorithm of the reference:
 //   plugins/twostatevolpath.py:141-385  sample_twostates (main loop)
@@ -33,14 +36,24 @@
 
 namespace rcv {
 
+// Pinhole frame of one (sub-)sensor: origin in box coordinates, world-space
+// forward / right / up (right and up scaled by the field of view).
+struct CamFrame {
+  V3 o, f, r, u;
+};
+
 // Packed lookup cell: 8 corners of the old and the new density, 64 bytes.
 //   [0] old v000 v100 v010 v110   [1] old v001 v101 v011 v111
 //   [2] new v000 ...              [3] new v001 ...
 struct VolJob {
   // film / camera
-  int32_t width, height, spp, pad0;
-  V3 cam_o, cam_f, cam_r, cam_u;
+  int32_t width, height, spp;
+  int32_t n_cams;      // sub-sensors of a batch film (1 = a single sensor)
   float inv_w, inv_h;  // 1/width, 1/height
+  // box transform: a world direction d moves by d * inv_box in box
+  // coordinates, so distances along a ray stay world distances
+  V3 inv_box;
+  CamFrame cam[RCV_MAX_SENSORS];
   // integrator
   int32_t max_depth, rr_depth, hide_emitters;
   uint32_t seed;
@@ -102,21 +115,38 @@ struct Counts {
 
 __device__ __forceinline__ float bits_to_float(uint32_t b) { return __uint_as_float(b); }
 
+// A world direction in box coordinates (exact identity for the unit cube).
+__device__ __forceinline__ V3 to_box(const VolJob& J, const V3& w) {
+  return V3{w.x * J.inv_box.x, w.y * J.inv_box.y, w.z * J.inv_box.z};
+}
+
+// Camera ray of film position (px + u0, py + u1), origin and direction in box
+// coordinates.  A batch film hands the position s = (px + u0) / width to
+// sub-sensor k = min(floor(s n), n - 1) as s n - floor(s n) (Mitsuba's batch
+// sensor, sensors/batch.cpp sample_ray).
 __device__ __forceinline__ void camera_ray(const VolJob& J, int px, int py, float u0, float u1,
                                            V3& o, V3& d) {
   const float fx = (float)px + u0;
   const float fy = (float)py + u1;
-  const float nx = fx * J.inv_w;
+  float nx = fx * J.inv_w;
   const float ny = fy * J.inv_h;
+  int k = 0;
+  if (J.n_cams > 1) {
+    const float idx_f = nx * (float)J.n_cams;
+    const int idx = (int)idx_f;
+    k = idx < J.n_cams - 1 ? idx : J.n_cams - 1;
+    nx = idx_f - (float)idx;
+  }
+  const CamFrame& C = J.cam[k];
   const float a = fmaf(2.0f, nx, -1.0f);
   const float b = fmaf(-2.0f, ny, 1.0f);
   V3 r;
-  r.x = fmaf(b, J.cam_u.x, fmaf(a, J.cam_r.x, J.cam_f.x));
-  r.y = fmaf(b, J.cam_u.y, fmaf(a, J.cam_r.y, J.cam_f.y));
-  r.z = fmaf(b, J.cam_u.z, fmaf(a, J.cam_r.z, J.cam_f.z));
+  r.x = fmaf(b, C.u.x, fmaf(a, C.r.x, C.f.x));
+  r.y = fmaf(b, C.u.y, fmaf(a, C.r.y, C.f.y));
+  r.z = fmaf(b, C.u.z, fmaf(a, C.r.z, C.f.z));
   const float inv_len = 1.0f / sqrtf(fmaf(r.z, r.z, fmaf(r.y, r.y, r.x * r.x)));
-  d = V3{r.x * inv_len, r.y * inv_len, r.z * inv_len};
-  o = J.cam_o;
+  d = to_box(J, V3{r.x * inv_len, r.y * inv_len, r.z * inv_len});
+  o = C.o;
 }
 
 struct Lookup {

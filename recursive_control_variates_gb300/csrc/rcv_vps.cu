@@ -121,7 +121,7 @@ struct Vps {
   __device__ V3 nee(Pcg32& r, const V3& x, const V3& thr, const V3* dL) const {
     Pcg32 replay = r;
     const float u0 = next1d(r), u1 = next1d(r);
-    const V3 w = uniform_sphere(u0, u1);
+    const V3 w = to_box(J, uniform_sphere(u0, u1));
     const float tf = exit_distance(x, w);
     const float tr = transmittance(r, x, w, tf, nullptr);
     const float mis = 0.5f;
@@ -168,7 +168,7 @@ struct Vps {
       pcg_skip1(r);
       const float pu0 = next1d(r), pu1 = next1d(r);
       seg.o = x;
-      seg.d = uniform_sphere(pu0, pu1);
+      seg.d = to_box(J, uniform_sphere(pu0, pu1));
       const float tf = exit_distance(seg.o, seg.d);
       if (!(tf > 0.0f)) break;  // accidental escape (:279-283)
       seg.tmax = tf;
@@ -225,7 +225,7 @@ struct Vps {
     if (P.use_nee) Li = nee(alt, x, V3{1, 1, 1}, nullptr);
     pcg_skip1(alt);
     const float pu0 = next1d(alt), pu1 = next1d(alt);
-    VpsSeg next{x, uniform_sphere(pu0, pu1), 0.0f};
+    VpsSeg next{x, to_box(J, uniform_sphere(pu0, pu1)), 0.0f};
     const float tf = exit_distance(next.o, next.d);
     const bool ok = tf > 0.0f;
     next.tmax = tf;
@@ -319,7 +319,7 @@ struct Vps {
       pcg_skip1(r);
       const float pu0 = next1d(r), pu1 = next1d(r);
       seg.o = x;
-      seg.d = uniform_sphere(pu0, pu1);
+      seg.d = to_box(J, uniform_sphere(pu0, pu1));
       const float tf = exit_distance(seg.o, seg.d);
       if (!(tf > 0.0f)) break;
       seg.tmax = tf;

@@ -85,10 +85,15 @@ CONFIGS = {
 }
 
 
-def medium_dict(density, albedo) -> dict:
+def medium_dict(density, albedo, box=None) -> dict:
+    """``heterogeneous`` medium dictionary; ``box`` (a ``core.BoxTransform``)
+    is the grids' ``to_world``."""
+    grid = {"type": "gridvolume", "data": density}
+    if box is not None:
+        grid["to_world"] = box
     m = {
         "type": "heterogeneous",
-        "sigma_t": {"type": "gridvolume", "data": density},
+        "sigma_t": grid,
         "scale": 1.0,
         "phase": {"type": "isotropic"},
     }
@@ -96,26 +101,63 @@ def medium_dict(density, albedo) -> dict:
         m["albedo"] = albedo if albedo is not None else 0.8
     else:
         m["albedo"] = {"type": "gridvolume", "data": albedo}
+        if box is not None:
+            m["albedo"]["to_world"] = box
     return m
 
 
-def scene_dict(density, albedo, res: int, two_state: bool = True, spp: int = 4) -> dict:
+def scene_dict(density, albedo, res: int, two_state: bool = True, spp: int = 4, box=None, views=None,
+               height: int | None = None) -> dict:
     """Scene dictionary for ``load_dict`` (reference layout: a cube 'object'
-    whose interior is a (two-state) medium, experiments.py:72-95)."""
-    med = medium_dict(density, albedo)
+    whose interior is a (two-state) medium, experiments.py:72-95).
+
+    ``box``: the medium's ``to_world`` (``core.T.translate(t).scale(s)``).
+    ``views``: (origin, target, up) triples of a ``batch`` sensor of
+    len(views) sub-sensors, each with a res x height film
+    (experiments.py:28-50); default one perspective sensor."""
+    med = medium_dict(density, albedo, box)
     interior = {"type": "twostatemedium", "old": med, "new": med, "incoming": med} if two_state else med
-    return {
-        "type": "scene",
-        "sensor": {
+    h = res if height is None else int(height)
+    sampler = {"type": "independent", "sample_count": spp}
+    if views is None:
+        sensor = {
             "type": "perspective",
             "fov": 45.0,
             "to_world": look_at(CAMERA_ORIGIN, CAMERA_TARGET, CAMERA_UP),
-            "film": {"type": "hdrfilm", "width": res, "height": res, "rfilter": {"type": "box"}},
-            "sampler": {"type": "independent", "sample_count": spp},
-        },
+            "film": {"type": "hdrfilm", "width": res, "height": h, "rfilter": {"type": "box"}},
+            "sampler": sampler,
+        }
+    else:
+        sensor = {
+            "type": "batch",
+            "film": {"type": "hdrfilm", "width": res * len(views), "height": h, "rfilter": {"type": "box"}},
+            "sampler": sampler,
+        }
+        for i, (o, t, u) in enumerate(views):
+            sensor[f"sensor_{i:02d}"] = {"type": "perspective", "fov": 45.0, "to_world": look_at(o, t, u)}
+    obj = {"type": "cube", "bsdf": {"type": "null"}, "interior": interior}
+    if box is not None:
+        obj["to_world"] = box
+    return {
+        "type": "scene",
+        "sensor": sensor,
         "emitter": {"type": "constant", "radiance": 1.0},
-        "object": {"type": "cube", "bsdf": {"type": "null"}, "interior": interior},
+        "object": obj,
     }
+
+
+def orbit_views(box, n: int, distance: float = 2.0, height: float = 0.0, phase: float = 0.1):
+    """n look-at views on a circle around the box centre (the batch sensors
+    of experiments.py:44-50,157-164)."""
+    lo = np.array(box.box_min if box is not None else (0.0, 0.0, 0.0), np.float64)
+    size = np.array(box.box_size if box is not None else (1.0, 1.0, 1.0), np.float64)
+    c = lo + 0.5 * size
+    views = []
+    for i in range(n):
+        th = 2 * np.pi / n * i + phase
+        o = (c[0] + distance * np.cos(th), c[1] + height, c[2] + distance * np.sin(th))
+        views.append((o, tuple(c), (0.0, 1.0, 0.0)))
+    return views
 
 
 def config_grids(cfg: VolumeConfig, seed: int | None = None):

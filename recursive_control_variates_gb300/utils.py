@@ -86,6 +86,55 @@ def clamp(params: dict, opt) -> None:
                 clamp_(opt[key].data, param["clamp"][0], param["clamp"][1])
 
 
+def upsample_grid(t: torch.Tensor, shape=None) -> torch.Tensor:
+    """``dr.upsample`` of a tensor: nearest-neighbour up-sampling, every
+    element repeated along each axis by the ratio of the target shape to the
+    source shape (a whole multiple; Dr.Jit's documented behaviour for
+    tensors).  Default target: twice the resolution of every axis but the
+    last (the channels), as utils.upsample asks for (utils.py:181-183)."""
+    if shape is None:
+        shape = (*[2 * x for x in t.shape[:-1]], t.shape[-1])
+    if len(shape) != t.dim():
+        raise ValueError(f"upsample: target shape {tuple(shape)} does not match a {t.dim()}-D tensor")
+    out = t
+    for axis, (a, b) in enumerate(zip(t.shape, shape)):
+        if b % a:
+            raise ValueError(f"upsample: target extent {b} is not a multiple of {a} (axis {axis})")
+        if b != a:
+            out = out.repeat_interleave(b // a, dim=axis)
+    return out
+
+
+def upsample(scene, params: dict, opt, integrator) -> None:
+    """utils.upsample (utils.py:177-192): doubles the resolution of every
+    optimised grid (4-D) or texture (3-D) tensor in the optimiser, re-sizes
+    the majorant supergrid of the density when ``use_majorant_supergrid`` is
+    set (utils.adjust_majorant_res_factor, utils.py:27-43) and resets the
+    integrator's control-variate state.  The next ``params.update(opt)``
+    hands the new grids to the scene."""
+    from . import scenes
+
+    for key in params["variables"]:
+        t = opt[key]
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"Upsampling is only supported for tensors, got type {type(t)}.")
+        if t.dim() not in (3, 4):
+            raise ValueError(f"Upsampling expects a 3 or 4D tensor. Got {t.dim()}.")
+        opt[key] = upsample_grid(t.detach())
+        if ".sigma_t." in key and params.get("use_majorant_supergrid", False):
+            new_res = tuple(opt[key].shape)
+            for shape in scene.shapes():
+                med = shape.interior_medium() if hasattr(shape, "interior_medium") else None
+                if med is not None and hasattr(med, "set_majorant_resolution_factor"):
+                    med.set_majorant_resolution_factor(scenes.majorant_factor_for(new_res[:3]))
+    integrator.reset()
+
+
+def upsample_steps(n_steps: int, fractions) -> list[int]:
+    """Iterations at which run_opt upsamples (optimize.py:69-72)."""
+    return [int(n_steps * w) for w in fractions]
+
+
 def sample_tea_32(v0: int, v1: int) -> tuple[int, int]:
     return _lib.sample_tea_32(v0, v1)
 

@@ -118,41 +118,134 @@ def test_traverse_keys_and_rotation():
     assert torch.equal(med.old.density, a) and torch.equal(med.new.density, b)
     assert torch.equal(med.incoming.density, b)
     with pytest.raises(ValueError):
-        params[scenes.DENSITY_KEY] = torch.zeros(2, 2, 2, 1)
+        params[scenes.DENSITY_KEY] = torch.zeros(2, 2, 2, 3)  # wrong channel count
 
 
-def test_params_update_from_optimizer_keys():
-    scene = cpu_scene()
+def test_upsample_resizes_all_states():
+    """utils.upsample (utils.py:177-192): nearest-neighbour doubling of the
+    optimised grid (Dr.Jit's tensor upsample), supergrid factor re-chosen,
+    integrator reset; the next params.update gives old = new = incoming the
+    new resolution."""
+    scene = cpu_scene(D=4)
     params = rcv.traverse(scene)
-
-    class FakeOpt(dict):
-        pass
-
-    opt = FakeOpt({scenes.DENSITY_KEY: torch.full((4, 4, 4, 1), 1.0, requires_grad=True), "other": torch.zeros(1)})
+    opt = rcv.ad.Adam(lr=0.1, device="cpu")
+    g = torch.arange(64, dtype=torch.float32).reshape(4, 4, 4, 1)
+    opt[scenes.DENSITY_KEY] = g
     params.update(opt)
-    assert params[scenes.DENSITY_KEY] is opt[scenes.DENSITY_KEY]
-    assert scenes.DENSITY_KEY in params.differentiable()
+    integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath"}})
+    integ.init_buffers()
+    assert integ.init
+    rcv.utils.upsample(scene, {"variables": {scenes.DENSITY_KEY: {}}, "use_majorant_supergrid": True}, opt, integ)
+    up = opt[scenes.DENSITY_KEY]
+    assert tuple(up.shape) == (8, 8, 8, 1) and not integ.init
+    assert torch.equal(up[::2, ::2, ::2], g) and torch.equal(up[1::2, 1::2, 1::2], g)
+    params.update(opt)
+    med = scene.named_shapes()["object"].interior_medium()
+    for st in (med.old, med.new, med.incoming):
+        assert tuple(st.density.shape) == (8, 8, 8, 1) and torch.equal(st.density, up.detach())
+    assert med.majorant_resolution_factor() == 2  # largest f with 8 // f >= 4
+    assert rcv.utils.upsample_steps(2000, [0.04, 0.16, 0.36, 0.64]) == [80, 320, 720, 1280]
+    with pytest.raises(ValueError):
+        rcv.utils.upsample_grid(torch.zeros(3, 3, 1), shape=(4, 4, 1))
 
 
-def test_sensor_basis():
-    scene = cpu_scene()
+def test_box_transforms_and_batch_sensor(tmp_path):
+    """T.scale / T.translate compose like Mitsuba's transforms; the medium
+    box reaches the C struct; a `batch` sensor fills one frame per
+    sub-sensor with the sub-film aspect (experiments.py:28-50,285)."""
+    from recursive_control_variates_gb300.core import T
+
+    tw = T.translate([0.5, -1.0, 2.0]).scale([6.5, 7.5, 10])
+    assert tw.box_min == (0.5, -1.0, 2.0) and tw.box_size == (6.5, 7.5, 10.0)
+    tw2 = T.scale([2, 2, 2]).translate([1, 0, 0])  # x -> 2 (x + t)
+    assert tw2.box_min == (2.0, 0.0, 0.0)
+    with pytest.raises(ValueError):
+        T.scale([1, -1, 1])
+    dens = scenes.blob_density(4, 0)
+    med = {"type": "heterogeneous", "sigma_t": {"type": "gridvolume", "data": dens, "to_world": tw},
+           "albedo": 0.8, "scale": 2.0}
+    obj = tmp_path / "cube_unit.obj"
+    obj.write_text("".join(f"v {x} {y} {z}\n" for x in (0, 1) for y in (0, 1) for z in (0, 1)) + "f 1 2 3\n")
+    sensors = {f"sensor_{i:02d}": {"type": "perspective", "fov": 45,
+                                   "to_world": T.look_at(origin=[3 * i, 1, 5], target=[3, 4, 7], up=[0, 1, 0])}
+               for i in range(4)}
+    batch = {"type": "batch", "film": {"type": "hdrfilm", "width": 4 * 16, "height": 12}, **sensors}
+    scene = rcv.load_dict({"type": "scene", "sensor": batch, "emitter": {"type": "constant"},
+                           "object": {"type": "obj", "filename": str(obj), "bsdf": {"type": "null"},
+                                      "to_world": tw, "interior": med}}, device="cpu")
+    m = scene.named_shapes()["object"].interior_medium().c_struct()
+    assert tuple(m.box_min) == (0.5, -1.0, 2.0) and tuple(m.box_size) == (6.5, 7.5, 10.0)
     s = scene.sensors()[0].c_struct()
-    f = np.array(s.forward)
-    r = np.array(s.right)
-    u = np.array(s.up)
-    assert np.allclose(f, [0, 0, -1], atol=1e-6)
-    assert np.isclose(np.linalg.norm(r), np.tan(np.radians(22.5)), atol=1e-6)
-    assert abs(float(f @ r)) < 1e-6 and abs(float(f @ u)) < 1e-6
+    assert (s.width, s.height, s.count) == (64, 12, 4)
+    assert tuple(s.origin) == (0.0, 1.0, 5.0) and tuple(s.more[2].origin) == (9.0, 1.0, 5.0)
+    # right / up scaled with the sub-film aspect 16:12
+    r, u = np.array(s.right), np.array(s.up)
+    assert np.isclose(np.linalg.norm(u) / np.linalg.norm(r), 12 / 16, rtol=1e-6)
+    with pytest.raises(ValueError):  # shape and grid disagree on to_world
+        rcv.load_dict({"type": "obj", "filename": str(obj), "to_world": T.scale([1, 2, 1]),
+                       "interior": med}, device="cpu")
+    bad = tmp_path / "not_a_cube.obj"
+    bad.write_text("v 0 0 0\nv 2 1 1\n")
+    with pytest.raises(ValueError):
+        rcv.load_dict({"type": "obj", "filename": str(bad)}, device="cpu")
+    with pytest.raises(ValueError):  # 64 px do not split into 3 sensors
+        rcv.load_dict({"type": "batch", "film": {"type": "hdrfilm", "width": 64, "height": 12},
+                       **{k: sensors[k] for k in list(sensors)[:3]}})
 
 
-def test_blob_generator_matches_specification():
-    D = 16
-    rho = scenes.blob_density(D, 0)[..., 0].astype(np.float64)
-    rng = np.random.default_rng(0)
-    c = rng.uniform(0.2, 0.8, (8, 3))
-    s = rng.uniform(0.05, 0.15, 8)
-    a = rng.uniform(5, 20, 8)
-    i, j, k = 3, 7, 11  # z, y, x
-    x = np.array([k + 0.5, j + 0.5, i + 0.5]) / D
-    expect = sum(a[n] * np.exp(-np.sum((x - c[n]) ** 2) / (2 * s[n] ** 2)) for n in range(8))
-    assert np.isclose(rho[i, j, k], expect, rtol=1e-6)
+def _zips_half_exr(img):
+    """A ZIPS-compressed OpenEXR file with half channels B, G, R, made with
+    the published steps: byte interleave, predictor, zlib."""
+    import struct
+    import zlib
+
+    from recursive_control_variates_gb300 import io
+
+    h, w, _ = img.shape
+    chlist = b"".join(n + b"\0" + struct.pack("<i4xii", 1, 1, 1) for n in (b"B", b"G", b"R")) + b"\0"
+    box = struct.pack("<4i", 0, 0, w - 1, h - 1)
+    header = struct.pack("<ii", 20000630, 2)
+    header += io._attr("channels", "chlist", chlist)
+    header += io._attr("compression", "compression", bytes([2]))
+    header += io._attr("dataWindow", "box2i", box)
+    header += io._attr("displayWindow", "box2i", box)
+    header += io._attr("lineOrder", "lineOrder", bytes([0]))
+    header += b"\0"
+    planes = img[:, :, [2, 1, 0]].transpose(0, 2, 1).astype("<f2")  # per line: B, G, R
+    chunks, offsets = b"", []
+    base = len(header) + 8 * h
+    for y in range(h):
+        t = np.frombuffer(planes[y].tobytes(), np.uint8)
+        inter = np.concatenate([t[0::2], t[1::2]]).astype(np.int64)
+        pred = inter.copy()
+        pred[1:] = (inter[1:] - inter[:-1] + 128) & 0xFF
+        comp = zlib.compress(pred.astype(np.uint8).tobytes())
+        if len(comp) >= t.size:  # the format stores such chunks uncompressed
+            comp = t.tobytes()
+        offsets.append(base + len(chunks))
+        chunks += struct.pack("<ii", y, len(comp)) + comp
+    return header + struct.pack(f"<{h}Q", *offsets) + chunks
+
+
+def test_vol_and_exr_files(tmp_path):
+    """Mitsuba .vol grids and OpenEXR images: round trips, a ZIPS EXR with
+    half channels, and a gridvolume loaded from a file with its bbox."""
+    from recursive_control_variates_gb300 import io
+
+    g = np.random.default_rng(0).random((3, 4, 5, 3)).astype(np.float32)
+    io.write_vol(tmp_path / "a.vol", g, (0, 0, 0), (1.0, 1.2, 1.5))
+    v = io.read_vol(tmp_path / "a.vol")
+    assert np.array_equal(v.data, g) and np.allclose(v.bbox_max, (1.0, 1.2, 1.5))
+    img = np.random.default_rng(1).random((7, 9, 3)).astype(np.float32)
+    io.write_exr(tmp_path / "a.exr", img)
+    assert np.array_equal(io.read_exr(tmp_path / "a.exr"), img)
+    # smooth rows compress, random rows are stored raw
+    smooth = np.broadcast_to(np.linspace(0, 1, 40, dtype=np.float32)[None, :, None], (6, 40, 3)).copy()
+    for im in (img, smooth):
+        (tmp_path / "z.exr").write_bytes(_zips_half_exr(im))
+        np.testing.assert_array_equal(io.read_exr(tmp_path / "z.exr"), im.astype(np.float16).astype(np.float32))
+    io.write_vol(tmp_path / "d.vol", scenes.blob_density(4, 0), (1, 2, 3), (2, 4, 6))
+    gv = rcv.load_dict({"type": "gridvolume", "filename": str(tmp_path / "d.vol"), "use_grid_bbox": True},
+                       device="cpu")
+    assert gv.to_world.box_min == (1.0, 2.0, 3.0) and gv.to_world.box_size == (1.0, 2.0, 3.0)
+    assert np.array_equal(np.asarray(gv.raw), scenes.blob_density(4, 0))

@@ -115,6 +115,65 @@ def test_closed_form_transmittance(oracle):
     assert abs(img.mean() - expect.mean()) < 4 * np.sqrt((sd**2).sum()) / img.size + 2e-3
 
 
+def _footprint_transmittance(cam, px0, res_w, res_h, sigma, box_min, box_size, sub=8):
+    """Footprint averages of exp(-sigma * chord) over the pixels of one
+    sub-sensor, chords through the world box [box_min, box_min + box_size]."""
+    o, f, r, u = (np.array(v, np.float64) for v in (cam.origin, cam.forward, cam.right, cam.up))
+    lo = np.array(box_min, np.float64)
+    hi = lo + np.array(box_size, np.float64)
+    s = (np.arange(sub) + 0.5) / sub
+    out = np.zeros((res_h, res_w))
+    for py in range(res_h):
+        for px in range(res_w):
+            a = 2 * (px + s[None, :]) / res_w - 1
+            b = 1 - 2 * (py + s[:, None]) / res_h
+            d = f + a[..., None] * r + b[..., None] * u
+            d = d / np.linalg.norm(d, axis=-1, keepdims=True)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                t0 = (lo - o) / d
+                t1 = (hi - o) / d
+            tn = np.max(np.minimum(t0, t1), -1)
+            tf = np.min(np.maximum(t0, t1), -1)
+            chord = np.where(tn <= tf, np.maximum(tf - np.maximum(tn, 0), 0), 0)
+            out[py, px] = np.exp(-sigma * chord).mean()
+    return out
+
+
+def test_box_transform_and_batch_film_closed_form(oracle):
+    """Medium box to_world = translate * scale (experiments.py:57,64,79,285)
+    and a batch film of 3 sub-sensors around it (experiments.py:28-50): with
+    albedo 0 and constant density every sub-image is the footprint average of
+    exp(-sigma * world chord) seen by its own sub-sensor."""
+    w, h, sigma = 10, 8, 1.5
+    box_min, box_size = (-0.3, 0.1, 0.2), (1.0, 1.2, 1.5)
+    centre = np.array(box_min) + 0.5 * np.array(box_size)
+    cams = []
+    for k in range(3):
+        th = 2 * np.pi * k / 3 + 0.1
+        origin = centre + np.array([2.6 * np.cos(th), 0.4, 2.6 * np.sin(th)])
+        cams.append(oracle.camera_basis(w, h, origin=tuple(origin), target=tuple(centre), up=(0, 1, 0), fov=45))
+    dens = np.full((6, 5, 4), sigma, np.float32)  # non-cubic grid, constant
+    sc = oracle.Scene(cams, dens, dens, albedo_const=0.0, max_depth=16, box_min=box_min, box_size=box_size)
+    assert (sc.width, sc.height) == (3 * w, h)
+    spp = 512
+    img = oracle.render(sc, seed=5, spp=spp)[..., 0].astype(np.float64)
+    for k in range(3):
+        expect = _footprint_transmittance(cams[k], 0, w, h, sigma, box_min, box_size, sub=24)
+        got = img[:, k * w:(k + 1) * w]
+        # Bernoulli noise of the estimate plus the footprint quadrature error
+        # at silhouette pixels
+        sd = np.sqrt(np.maximum(expect * (1 - expect), 1e-4) / spp) + 0.004
+        z = np.abs(got - expect) / sd
+        assert np.mean(z < 3.5) > 0.95, (k, z.max())
+        assert abs(got.mean() - expect.mean()) < 4 * np.sqrt((sd**2).sum()) / got.size + 2e-3
+        assert expect.min() < 0.6  # the box is in view of every sub-sensor
+    # the single-state and two-state tracers and volpathsimple agree
+    H, F = oracle.render_twostates(sc, seed=5, spp=spp)
+    assert np.array_equal(H, F) and np.array_equal(F[..., 0].astype(np.float64), img)
+    v = oracle.vps_render(sc, seed=6, spp=spp)[..., 0].astype(np.float64)
+    assert abs(v.mean() - img.mean()) < 0.01
+
+
 def test_cv_welford_golden(oracle, golden_cv):
     """The numpy restatement reproduces the reference's own CVIntegrator /
     MetaIntegrator / StatisticsEstimator code bit for bit."""
