@@ -99,6 +99,11 @@ typedef struct rcv_medium {
   void* workspace; /* device, rcv_medium_workspace_bytes(), 256-B aligned  */
   float box_min[3];  /* world position of the grid's (0,0,0) corner         */
   float box_size[3]; /* world extent along x, y, z (0 = 1)                  */
+  /* Resolution of the albedo grids when it differs from the density's
+   * (e.g. 264x136x136 density with 256x128x128 albedo, experiments.py:56,63);
+   * all 0 = the density's.  Both grids span the same box. */
+  int32_t albedo_dims[3];
+  int32_t pad;
 } rcv_medium;
 
 typedef struct rcv_volpath_options {
@@ -149,6 +154,9 @@ void rcv_sample_tea_32(uint32_t v0, uint32_t v1, uint32_t out[2]);
 /* Bytes of device workspace a medium needs (packed lookup cells, majorants,
  * gradient accumulators). */
 uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid, int32_t majorant_factor);
+/* The same from a medium description (dims, albedo_dims, albedo_old != NULL,
+ * majorant_factor); needed when the albedo grid has its own resolution. */
+uint64_t rcv_medium_workspace_bytes_for(const rcv_medium* medium);
 
 /* Packs the old/new grids into the lookup workspace and computes both
  * majorants (scale * max density).  Call after every state rotation.

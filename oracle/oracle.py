@@ -51,6 +51,9 @@ class OracleScene(C.Structure):
         ("box_size", C.c_float * 3),
         ("n_cams", C.c_int32),
         ("cams", (C.c_float * 12) * 15),
+        ("adx", C.c_int32),
+        ("ady", C.c_int32),
+        ("adz", C.c_int32),
     ]
 
 
@@ -238,6 +241,8 @@ class Scene:
         s.majorant_factor = int(majorant_factor)
         s.box_min[:] = [float(np.float32(v)) for v in box_min]
         s.box_size[:] = [float(np.float32(v)) for v in box_size]
+        if self.alb_new is not None and self.alb_new.shape[:3] != (dz, dy, dx):
+            s.adz, s.ady, s.adx = self.alb_new.shape[:3]  # the albedo grid's own resolution
         s.n_cams = len(cams)
         for k, c in enumerate(cams[1:]):
             s.cams[k][:] = [*c.origin, *c.forward, *c.right, *c.up]
@@ -283,7 +288,7 @@ def backward(scene: Scene, seed: int, spp: int, grad_img, threads: int | None = 
     """(grad_density [dz,dy,dx] float64, grad_albedo [dz,dy,dx,3] or None)."""
     g = np.ascontiguousarray(grad_img, np.float32)
     gd = np.zeros(scene.dens_new.shape[:3], np.float64)
-    ga = None if scene.alb_new is None else np.zeros(scene.dens_new.shape[:3] + (3,), np.float64)
+    ga = None if scene.alb_new is None else np.zeros(scene.alb_new.shape[:3] + (3,), np.float64)
     rc = lib().oracle_backward(C.byref(scene.c), seed & 0xFFFFFFFF, spp, g.ctypes.data, gd.ctypes.data,
                                None if ga is None else ga.ctypes.data, threads or default_threads(), *_rows(rows))
     if rc:
@@ -465,7 +470,7 @@ def vps_backward(scene: Scene, seed: int, spp: int, grad_img, flags=None, thread
     fl = _vps_flags(flags)
     g = np.ascontiguousarray(grad_img, np.float32)
     gd = np.zeros(scene.dens_new.shape[:3], np.float64)
-    ga = None if scene.alb_new is None else np.zeros(scene.dens_new.shape[:3] + (3,), np.float64)
+    ga = None if scene.alb_new is None else np.zeros(scene.alb_new.shape[:3] + (3,), np.float64)
     rc = lib().oracle_vps_backward(C.byref(scene.c), fl.ctypes.data, seed & 0xFFFFFFFF, spp, g.ctypes.data,
                                    gd.ctypes.data, None if ga is None else ga.ctypes.data,
                                    threads or default_threads())

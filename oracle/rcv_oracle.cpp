@@ -183,6 +183,8 @@ struct oracle_scene {
   // sub-sensor k >= 1 is cams[k-1] = origin, forward, right, up (world space)
   int32_t n_cams;
   float cams[15][12];
+  // albedo grid resolution when it differs from the density's (0 = same)
+  int32_t adx, ady, adz;
 };
 }
 
@@ -228,9 +230,49 @@ float trilinear(const oracle_scene& S, const float* g, int stride, int ch, const
   return lerp(c0, c1, c.fz);
 }
 
-V3 albedo(const oracle_scene& S, const float* grid, const Corners& c) {
+// Albedo grid resolution (the density's unless set).
+void albedo_dims(const oracle_scene& S, int& ax, int& ay, int& az) {
+  const bool own = S.adx > 0;
+  ax = own ? S.adx : S.dx;
+  ay = own ? S.ady : S.dy;
+  az = own ? S.adz : S.dz;
+}
+
+// Corners of the albedo grid at x: the density's when both have one
+// resolution (both grids span the unit cube).
+Corners albedo_corners(const oracle_scene& S, const V3& x, const Corners& c) {
+  int ax, ay, az;
+  albedo_dims(S, ax, ay, az);
+  if (ax == S.dx && ay == S.dy && az == S.dz) return c;
+  Corners a;
+  axis(x.x, ax, a.x0, a.x1, a.fx);
+  axis(x.y, ay, a.y0, a.y1, a.fy);
+  axis(x.z, az, a.z0, a.z1, a.fz);
+  return a;
+}
+
+inline int64_t avidx(const oracle_scene& S, int x, int y, int z) {
+  int ax, ay, az;
+  albedo_dims(S, ax, ay, az);
+  return ((int64_t)z * ay + y) * ax + x;
+}
+
+float albedo_channel(const oracle_scene& S, const float* g, int ch, const Corners& c) {
+  auto v = [&](int x, int y, int z) { return g[avidx(S, x, y, z) * 3 + ch]; };
+  const float c00 = lerp(v(c.x0, c.y0, c.z0), v(c.x1, c.y0, c.z0), c.fx);
+  const float c10 = lerp(v(c.x0, c.y1, c.z0), v(c.x1, c.y1, c.z0), c.fx);
+  const float c01 = lerp(v(c.x0, c.y0, c.z1), v(c.x1, c.y0, c.z1), c.fx);
+  const float c11 = lerp(v(c.x0, c.y1, c.z1), v(c.x1, c.y1, c.z1), c.fx);
+  const float c0 = lerp(c00, c10, c.fy);
+  const float c1 = lerp(c01, c11, c.fy);
+  return lerp(c0, c1, c.fz);
+}
+
+// Trilinear RGB albedo at x (c: the density corners at x).
+V3 albedo(const oracle_scene& S, const float* grid, const V3& x, const Corners& c) {
   if (grid == nullptr) return V3{S.albedo_const[0], S.albedo_const[1], S.albedo_const[2]};
-  return V3{trilinear(S, grid, 3, 0, c), trilinear(S, grid, 3, 1, c), trilinear(S, grid, 3, 2, c)};
+  const Corners a = albedo_corners(S, x, c);
+  return V3{albedo_channel(S, grid, 0, a), albedo_channel(S, grid, 1, a), albedo_channel(S, grid, 2, a)};
 }
 
 float grid_max(const oracle_scene& S, const float* g) {
@@ -396,14 +438,15 @@ struct GradSink {
     dens[vidx(S, c.x0, c.y1, c.z1)] += b1 * gx0;
     dens[vidx(S, c.x1, c.y1, c.z1)] += b1 * c.fx;
   }
-  void albedo(const oracle_scene& S, const Corners& c, const V3& g) {
+  void albedo(const oracle_scene& S, const V3& x, const Corners& dc, const V3& g) {
     if (alb.empty()) return;
+    const Corners c = albedo_corners(S, x, dc);
     const float wx[2] = {1.0f - c.fx, c.fx}, wy[2] = {1.0f - c.fy, c.fy}, wz[2] = {1.0f - c.fz, c.fz};
     const int xs[2] = {c.x0, c.x1}, ys[2] = {c.y0, c.y1}, zs[2] = {c.z0, c.z1};
     for (int k = 0; k < 8; ++k) {
       const int i = k & 1, j = (k >> 1) & 1, m = k >> 2;
       const float w = (wz[m] * wy[j]) * wx[i];
-      const int64_t v = vidx(S, xs[i], ys[j], zs[m]);
+      const int64_t v = avidx(S, xs[i], ys[j], zs[m]);
       alb[v * 3 + 0] += g.x * w;
       alb[v * 3 + 1] += g.y * w;
       alb[v * 3 + 2] += g.z * w;
@@ -585,10 +628,10 @@ struct Tracer {
       depth += 1;
       if (depth >= S.max_depth) return out;
       ++out.scatters;
-      const V3 an = albedo(S, S.alb_new, c);
+      const V3 an = albedo(S, S.alb_new, x, c);
       const V3 ssn{st_n * an.x, st_n * an.y, st_n * an.z};
       if (mode == kTwoState) {
-        const V3 ao = albedo(S, S.alb_old, c);
+        const V3 ao = albedo(S, S.alb_old, x, c);
         const V3 sso{st_o * ao.x, st_o * ao.y, st_o * ao.z};
         const float den = st_n + st_o;
         bn = V3{bn.x * ((2.0f * ssn.x) / den), bn.y * ((2.0f * ssn.y) / den), bn.z * ((2.0f * ssn.z) / den)};
@@ -599,7 +642,7 @@ struct Tracer {
           const V3 Lr = remaining(Ln);
           const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
           sink->density(S, c, (S.scale * sd) / st_n);
-          sink->albedo(S, c, V3{(dL.x * Lr.x) / std::fmax(an.x, 1e-8f), (dL.y * Lr.y) / std::fmax(an.y, 1e-8f),
+          sink->albedo(S, x, c, V3{(dL.x * Lr.x) / std::fmax(an.x, 1e-8f), (dL.y * Lr.y) / std::fmax(an.y, 1e-8f),
                                 (dL.z * Lr.z) / std::fmax(an.z, 1e-8f)});
         }
       }
@@ -748,12 +791,15 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
   Supergrid sg;
   sg.build(*S);
   const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
+  int adx, ady, adz;
+  albedo_dims(*S, adx, ady, adz);
+  const int64_t na = (int64_t)adx * ady * adz;
   const int nt = std::max(threads, 1);
   std::vector<GradSink> sinks(nt);
   const bool alb = grad_albedo != nullptr && S->alb_new != nullptr;
   for (auto& s : sinks) {
     s.dens.assign(nv, 0.0);
-    if (alb) s.alb.assign(nv * 3, 0.0);
+    if (alb) s.alb.assign(na * 3, 0.0);
   }
   parallel_rows(row0, row1, row_stride, threads, [&](int k, int y0, int y1) {
     for (int py = y0; py < y1; ++py)
@@ -775,7 +821,7 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
   for (auto& s : sinks) {
     for (int64_t i = 0; i < nv; ++i) grad_density[i] += s.dens[i];
     if (alb)
-      for (int64_t i = 0; i < nv * 3; ++i) grad_albedo[i] += s.alb[i];
+      for (int64_t i = 0; i < na * 3; ++i) grad_albedo[i] += s.alb[i];
   }
   return 0;
 }
@@ -987,7 +1033,7 @@ struct Vps {
         break;
       }
       const V3 x = ray_at(seg.o, t, seg.d);
-      const V3 a = albedo(S, S.alb_new, corners(S, x));
+      const V3 a = albedo(S, S.alb_new, x, corners(S, x));
       has_scattered = true;
       thr = V3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
       depth += 1;
@@ -1053,7 +1099,7 @@ struct Vps {
     const V3 x = ray_at(seg.o, tp, seg.d);
     const Corners c = corners(S, x);
     const float st = sigma_t(c);
-    const V3 a = albedo(S, S.alb_new, c);
+    const V3 a = albedo(S, S.alb_new, x, c);
     // in-scattered radiance at x: NEE + a recursive path (sample_recursive, :623-668)
     V3 Li{0, 0, 0};
     if (F.use_nee) Li = nee(alt, x, V3{1, 1, 1}, nullptr);
@@ -1073,7 +1119,7 @@ struct Vps {
     const float k0 = mis * wdrt;
     const V3 k{(k0 * adj.x) * Li.x, (k0 * adj.y) * Li.y, (k0 * adj.z) * Li.z};
     sink->density(S, c, S.scale * ((k.x * a.x + k.y * a.y) + k.z * a.z));
-    sink->albedo(S, c, V3{k.x * st, k.y * st, k.z * st});
+    sink->albedo(S, x, c, V3{k.x * st, k.y * st, k.z * st});
   }
 
   // Adjoint pass of one sample: replays the primal's draws with L_rem.
@@ -1126,7 +1172,7 @@ struct Vps {
         const V3 x = ray_at(seg.o, t, seg.d);
         const Corners c = corners(S, x);
         const float st = sigma_t(c);
-        const V3 a = albedo(S, S.alb_new, c);
+        const V3 a = albedo(S, S.alb_new, x, c);
         if (!F.use_drt || F.use_drt_mis) {
           const float mis = F.use_drt ? (st * st) / (1.0f + st * st) : 1.0f;
           const float inv_pdf = 1.0f / st;
@@ -1134,7 +1180,7 @@ struct Vps {
                      ((mis * dL.y) * (res.y / std::fmax(1e-8f, a.y))) * inv_pdf,
                      ((mis * dL.z) * (res.z / std::fmax(1e-8f, a.z))) * inv_pdf};
           sink->density(S, c, S.scale * ((k.x * a.x + k.y * a.y) + k.z * a.z));
-          sink->albedo(S, c, V3{k.x * st, k.y * st, k.z * st});
+          sink->albedo(S, x, c, V3{k.x * st, k.y * st, k.z * st});
         }
       }
       {
@@ -1149,7 +1195,7 @@ struct Vps {
       }
       if (escape) break;
       const V3 x = ray_at(seg.o, t, seg.d);
-      const V3 a = albedo(S, S.alb_new, corners(S, x));
+      const V3 a = albedo(S, S.alb_new, x, corners(S, x));
       thr = V3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
       depth += 1;
       if (depth >= S.max_depth) break;
@@ -1236,12 +1282,15 @@ int oracle_vps_backward(const oracle_scene* S, const int32_t flags[4], uint32_t 
   const float mu = S->scale * grid_max(*S, S->dens_new);
   const uint32_t alt_seed = vps_alt_seed(seed);
   const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
+  int adx, ady, adz;
+  albedo_dims(*S, adx, ady, adz);
+  const int64_t na = (int64_t)adx * ady * adz;
   const int nt = std::max(threads, 1);
   std::vector<GradSink> sinks(nt);
   const bool alb = grad_albedo != nullptr && S->alb_new != nullptr;
   for (auto& s : sinks) {
     s.dens.assign(nv, 0.0);
-    if (alb) s.alb.assign(nv * 3, 0.0);
+    if (alb) s.alb.assign(na * 3, 0.0);
   }
   parallel_rows(0, S->height, 1, threads, [&](int k, int y0, int y1) {
     Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, mu, &sg};
@@ -1258,7 +1307,7 @@ int oracle_vps_backward(const oracle_scene* S, const int32_t flags[4], uint32_t 
   for (auto& s : sinks) {
     for (int64_t i = 0; i < nv; ++i) grad_density[i] += s.dens[i];
     if (alb)
-      for (int64_t i = 0; i < nv * 3; ++i) grad_albedo[i] += s.alb[i];
+      for (int64_t i = 0; i < na * 3; ++i) grad_albedo[i] += s.alb[i];
   }
   return 0;
 }

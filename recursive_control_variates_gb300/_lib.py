@@ -65,6 +65,8 @@ class Medium(C.Structure):
         ("workspace", C.c_void_p),
         ("box_min", f3),
         ("box_size", f3),
+        ("albedo_dims", i3),
+        ("pad", C.c_int32),
     ]
 
 
@@ -198,6 +200,7 @@ SIGNATURES = {
     "rcv_struct_size": (C.c_uint64, [C.c_char_p]),
     "rcv_sample_tea_32": (None, [C.c_uint32, C.c_uint32, P(C.c_uint32)]),
     "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32, C.c_int32]),
+    "rcv_medium_workspace_bytes_for": (C.c_uint64, [P(Medium)]),
     "rcv_medium_prepare": (C.c_int, [P(Medium), vp]),
     "rcv_render_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "rcv_render_twostates_volume": (

@@ -352,16 +352,34 @@ class _PackedMedium:
 
     def workspace(self) -> torch.Tensor:
         if self._workspace is None:
-            lib = _lib.load()
-            dims = (C.c_int32 * 3)(*self.dims)
-            nbytes = int(lib.rcv_medium_workspace_bytes(dims, int(self.has_albedo_grid), self._factor()))
+            m = self._describe(0)
+            nbytes = int(_lib.load().rcv_medium_workspace_bytes_for(C.byref(m)))
+            if nbytes <= 0:
+                raise ValueError("invalid medium description")
             self._workspace = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
         return self._workspace
 
+    @property
+    def albedo_dims(self):
+        g = self._states()[1].albedo_grid
+        if g is None:
+            return self.dims
+        dz, dy, dx, _ = g.shape
+        return (dx, dy, dz)
+
+    def albedo_grad_buffer(self):
+        """Zeroed (Dz, Dy, Dx, 3) gradient of the albedo grid, or None."""
+        if not self.has_albedo_grid:
+            return None
+        ax, ay, az = self.albedo_dims
+        return torch.zeros((az, ay, ax, 3), dtype=torch.float32, device=self.device)
+
     def c_struct(self) -> _lib.Medium:
-        old, new = self._states()
         ws = self.workspace()
-        aligned = (ws.data_ptr() + 255) & ~255
+        return self._describe((ws.data_ptr() + 255) & ~255)
+
+    def _describe(self, aligned: int) -> _lib.Medium:
+        old, new = self._states()
         m = _lib.Medium()
         m.dims[:] = list(self.dims)
         m.scale = new.scale
@@ -375,6 +393,8 @@ class _PackedMedium:
         m.workspace = aligned
         m.box_min[:] = [float(np.float32(v)) for v in new.box.box_min]
         m.box_size[:] = [float(np.float32(v)) for v in new.box.box_size]
+        if self.has_albedo_grid and tuple(self.albedo_dims) != tuple(self.dims):
+            m.albedo_dims[:] = list(self.albedo_dims)
         return m
 
     def prepare(self, stream) -> _lib.Medium:
@@ -404,9 +424,8 @@ class HeterogeneousMedium(_PackedMedium):
         self.albedo_grid = None
         self.albedo_value = (0.75, 0.75, 0.75)
         if isinstance(alb, GridVolume):
+            # the albedo grid may have its own resolution (experiments.py:56,63)
             self.albedo_grid = _as_tensor(alb.raw, self.device, 3)
-            if self.albedo_grid.shape[:3] != self.density.shape[:3]:
-                raise ValueError("albedo and sigma_t grids must have the same resolution")
             if alb.to_world != self.box:
                 raise ValueError("albedo and sigma_t grids must have the same to_world")
         else:
@@ -460,8 +479,6 @@ class HeterogeneousMedium(_PackedMedium):
             self.albedo_grid = t
         else:
             raise KeyError(sub)
-        if self.albedo_grid is not None and self.albedo_grid.shape[:3] != self.density.shape[:3]:
-            raise ValueError("albedo and sigma_t grids must have the same resolution")
         self._workspace = None
         self._dirty = True
 
@@ -487,6 +504,9 @@ class TwoStateMedium(_PackedMedium):
             raise ValueError("old/new/incoming grids must have the same resolution")
         if not (self.old.box == self.new.box == self.incoming.box):
             raise ValueError("old/new/incoming grids must have the same to_world")
+        if self.new.albedo_grid is not None and not (
+                self.old.albedo_grid.shape == self.new.albedo_grid.shape == self.incoming.albedo_grid.shape):
+            raise ValueError("old/new/incoming albedo grids must have the same resolution")
         if (self.old.albedo_grid is None) != (self.new.albedo_grid is None) or (
             self.new.albedo_grid is None
         ) != (self.incoming.albedo_grid is None):

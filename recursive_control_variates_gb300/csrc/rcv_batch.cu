@@ -67,7 +67,7 @@ static JobLayout job_layout(const rcv_batch_job& j) {
   L.header = off;
   off = align256(off + sizeof(JobHeader));
   L.medium = off;
-  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr, j.majorant_factor).total);
+  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr ? uint64_t(j.dims[0]) * j.dims[1] * j.dims[2] : 0u, j.majorant_factor).total);
   L.buckets = off;
   off = align256(off + kRenderOrderBuckets * sizeof(uint32_t));
   L.order = off;
@@ -570,7 +570,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     std::memset(&e, 0, sizeof(e));
     e.d = d;
     e.hdr = reinterpret_cast<JobHeader*>(ws + L.header);
-    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr, d.majorant_factor);
+    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr ? uint64_t(d.dims[0]) * d.dims[1] * d.dims[2] : 0u, d.majorant_factor);
     char* mw = ws + L.medium;
     e.cells = reinterpret_cast<float4*>(mw + M.cells);
     e.has_albedo = d.albedo[0] != nullptr;

@@ -57,9 +57,11 @@ struct MediumLayout {
   uint64_t cells, albedo, maxbits, grad_cells, grad_albedo, sg_two, sg_new, total;
 };
 
-inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo, int majorant_factor) {
+// albedo_voxels: voxels of the albedo grid (0 = no albedo grid).
+inline MediumLayout medium_layout(const int32_t dims[3], uint64_t albedo_voxels, int majorant_factor) {
   const uint64_t nc = uint64_t(dims[0] + 1) * uint64_t(dims[1] + 1) * uint64_t(dims[2] + 1);
-  const uint64_t nv = uint64_t(dims[0]) * uint64_t(dims[1]) * uint64_t(dims[2]);
+  const uint64_t nv = albedo_voxels;
+  const bool has_albedo = nv > 0;
   const uint64_t ns = uint64_t(supergrid_cells(dims[0], majorant_factor)) *
                       uint64_t(supergrid_cells(dims[1], majorant_factor)) *
                       uint64_t(supergrid_cells(dims[2], majorant_factor));
@@ -81,6 +83,23 @@ inline MediumLayout medium_layout(const int32_t dims[3], bool has_albedo, int ma
   off = align256(off + ns * 4u);
   l.total = off;
   return l;
+}
+
+// Albedo grid resolution of a medium: its own when set, else the density's.
+inline void albedo_dims_of(const rcv_medium* m, int32_t out[3]) {
+  const bool own = m->albedo_dims[0] > 0 || m->albedo_dims[1] > 0 || m->albedo_dims[2] > 0;
+  for (int a = 0; a < 3; ++a) out[a] = own ? m->albedo_dims[a] : m->dims[a];
+}
+
+inline uint64_t albedo_voxels_of(const rcv_medium* m) {
+  if (m->albedo_old == nullptr) return 0;
+  int32_t ad[3];
+  albedo_dims_of(m, ad);
+  return uint64_t(ad[0]) * uint64_t(ad[1]) * uint64_t(ad[2]);
+}
+
+inline MediumLayout medium_layout(const rcv_medium* m) {
+  return medium_layout(m->dims, albedo_voxels_of(m), m->majorant_factor);
 }
 
 // Scratch layout of one tracer call (all offsets 256-byte aligned):

@@ -249,12 +249,13 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         finished = true;
       } else {
         const Lookup lk = locate(J, p);
+        const AlbedoLookup alk = albedo_lookup(J, lk, p);
         const float st_n = sc_n, st_o = sc_o;
-        const V3 an = albedo_at(J, lk, 1);
+        const V3 an = albedo_at(J, alk, 1);
         const V3 ss_n{st_n * an.x, st_n * an.y, st_n * an.z};
         if (kMode == kTwoState) {
           // plugins/twostatevolpath.py:259-260
-          const V3 ao = albedo_at(J, lk, 0);
+          const V3 ao = albedo_at(J, alk, 0);
           const V3 ss_o{st_o * ao.x, st_o * ao.y, st_o * ao.z};
           const float den = st_n + st_o;
           bn = V3{bn.x * ((2.0f * ss_n.x) / den), bn.y * ((2.0f * ss_n.y) / den),
@@ -272,7 +273,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               ++cnt.albedo_events;
               const V3 ga{(dL.x * Lr.x) / fmaxf(an.x, 1e-8f), (dL.y * Lr.y) / fmaxf(an.y, 1e-8f),
                           (dL.z * Lr.z) / fmaxf(an.z, 1e-8f)};
-              scatter_albedo(J, lk, ga);
+              scatter_albedo(J, alk, ga);
             }
           }
           // a checkpoint already holds the throughput after the event

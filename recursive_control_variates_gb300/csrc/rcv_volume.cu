@@ -17,10 +17,11 @@ namespace rcv {
 constexpr int kTraceBlock = 128;
 
 // ------------------------------------------------------------------ packing
+// One thread per cell / voxel / albedo voxel (na: albedo grid voxels).
 __global__ void pack_medium_kernel(int dx, int dy, int dz, const float* __restrict__ old_d,
                                    const float* __restrict__ new_d, float4* __restrict__ cells,
                                    const float* __restrict__ old_a, const float* __restrict__ new_a,
-                                   float4* __restrict__ albedo, uint32_t* __restrict__ maxbits) {
+                                   float4* __restrict__ albedo, int64_t na, uint32_t* __restrict__ maxbits) {
   const int64_t nc = int64_t(dx + 1) * (dy + 1) * (dz + 1);
   const int64_t nv = int64_t(dx) * dy * dz;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -29,8 +30,8 @@ __global__ void pack_medium_kernel(int dx, int dy, int dz, const float* __restri
   if (i < nv) {
     mo = old_d[i];
     mn = new_d[i];
-    if (albedo != nullptr) pack_albedo(i, old_a, new_a, albedo);
   }
+  if (albedo != nullptr && i < na) pack_albedo(i, old_a, new_a, albedo);
   // majorant: maximum density of each state (non-negative part)
   reduce_majorants(mo, mn, maxbits);
 }
@@ -173,6 +174,9 @@ static int validate_medium(const rcv_medium* m) {
               "medium workspace must be 256-byte aligned");
   RCV_REQUIRE(m->scale >= 0.0f, "medium scale must be non-negative");
   RCV_REQUIRE(m->majorant_factor >= 0, "majorant_factor must be >= 0");
+  const bool own = m->albedo_dims[0] != 0 || m->albedo_dims[1] != 0 || m->albedo_dims[2] != 0;
+  RCV_REQUIRE(!own || (m->albedo_dims[0] > 0 && m->albedo_dims[1] > 0 && m->albedo_dims[2] > 0),
+              "albedo_dims must be all positive or all 0");
   return RCV_OK;
 }
 
@@ -224,10 +228,16 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   J->dy = m->dims[1];
   J->dz = m->dims[2];
   J->scale = m->scale;
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
+  const MediumLayout L = medium_layout(m);
   char* ws = static_cast<char*>(m->workspace);
   J->cells = reinterpret_cast<const float4*>(ws + L.cells);
   J->albedo = m->albedo_old ? reinterpret_cast<const float4*>(ws + L.albedo) : nullptr;
+  int32_t ad[3];
+  albedo_dims_of(m, ad);
+  J->adx = ad[0];
+  J->ady = ad[1];
+  J->adz = ad[2];
+  J->albedo_own_res = (ad[0] != m->dims[0] || ad[1] != m->dims[1] || ad[2] != m->dims[2]) ? 1 : 0;
   J->albedo_const[0] = m->albedo_value[0];
   J->albedo_const[1] = m->albedo_value[1];
   J->albedo_const[2] = m->albedo_value[2];
@@ -365,7 +375,7 @@ int launch_reduce(bool two, const float4* po, int64_t path_begin, int64_t npix, 
 }
 
 int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cudaStream_t st) {
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
+  const MediumLayout L = medium_layout(m);
   const char* ws = static_cast<const char*>(m->workspace);
   const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
   const int block = 256;
@@ -375,20 +385,21 @@ int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cu
   int rc = launched("fold_density launch");
   if (rc) return rc;
   if (grad_albedo != nullptr && m->albedo_old != nullptr) {
-    fold_albedo_kernel<<<grid_for(nv, block), block, 0, st>>>(
-        nv, reinterpret_cast<const float4*>(ws + L.grad_albedo), grad_albedo);
+    const int64_t na = (int64_t)albedo_voxels_of(m);
+    fold_albedo_kernel<<<grid_for(na, block), block, 0, st>>>(
+        na, reinterpret_cast<const float4*>(ws + L.grad_albedo), grad_albedo);
     rc = launched("fold_albedo launch");
   }
   return rc;
 }
 
 int reset_gradients(const rcv_medium* m, bool albedo, cudaStream_t st) {
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
+  const MediumLayout L = medium_layout(m);
   char* ws = static_cast<char*>(m->workspace);
   const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
-  const int64_t nv = int64_t(m->dims[0]) * m->dims[1] * m->dims[2];
+  const int64_t na = (int64_t)albedo_voxels_of(m);
   RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_cells, 0, nc * 32, st), "gradient reset");
-  if (albedo) RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_albedo, 0, nv * 16, st), "gradient reset");
+  if (albedo) RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_albedo, 0, na * 16, st), "gradient reset");
   return RCV_OK;
 }
 
@@ -399,7 +410,15 @@ using namespace rcv;
 extern "C" uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid,
                                                int32_t majorant_factor) {
   if (dims == nullptr || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || majorant_factor < 0) return 0;
-  return medium_layout(dims, has_albedo_grid != 0, majorant_factor).total;
+  const uint64_t nv = has_albedo_grid ? uint64_t(dims[0]) * uint64_t(dims[1]) * uint64_t(dims[2]) : 0u;
+  return medium_layout(dims, nv, majorant_factor).total;
+}
+
+extern "C" uint64_t rcv_medium_workspace_bytes_for(const rcv_medium* m) {
+  if (m == nullptr || m->dims[0] <= 0 || m->dims[1] <= 0 || m->dims[2] <= 0 || m->majorant_factor < 0) return 0;
+  for (int a = 0; a < 3; ++a)
+    if (m->albedo_dims[a] < 0) return 0;
+  return medium_layout(m).total;
 }
 
 extern "C" uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp,
@@ -413,15 +432,16 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
   int rc = validate_medium(m);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const MediumLayout L = medium_layout(m->dims, m->albedo_old != nullptr, m->majorant_factor);
+  const MediumLayout L = medium_layout(m);
   char* ws = static_cast<char*>(m->workspace);
   RCV_TRY_CUDA(cudaMemsetAsync(ws + L.maxbits, 0, 16, st), "majorant reset");
   const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
+  const int64_t na = (int64_t)albedo_voxels_of(m);
   const int block = 256;
-  pack_medium_kernel<<<grid_for(nc, block), block, 0, st>>>(
+  pack_medium_kernel<<<grid_for(nc > na ? nc : na, block), block, 0, st>>>(
       m->dims[0], m->dims[1], m->dims[2], m->density_old, m->density_new,
       reinterpret_cast<float4*>(ws + L.cells), m->albedo_old, m->albedo_new,
-      m->albedo_old ? reinterpret_cast<float4*>(ws + L.albedo) : nullptr,
+      m->albedo_old ? reinterpret_cast<float4*>(ws + L.albedo) : nullptr, na,
       reinterpret_cast<uint32_t*>(ws + L.maxbits));
   rc = launched("pack_medium launch");
   if (rc || m->majorant_factor == 0) return rc;

@@ -61,13 +61,15 @@ struct VolJob {
   int32_t dx, dy, dz;
   float scale;
   const float4* __restrict__ cells;   // (dz+1)(dy+1)(dx+1) * 4
-  const float4* __restrict__ albedo;  // dz*dy*dx * 2 (old, new) or null
+  const float4* __restrict__ albedo;  // adz*ady*adx * 2 (old, new) or null
+  int32_t adx, ady, adz;              // albedo grid resolution
+  int32_t albedo_own_res;             // 1: differs from the density's
   float albedo_const[3];
   const uint32_t* maxbits;  // [0] max old density, [1] max new density (bits)
   // adjoint
   const float* grad_img;
   float4* grad_cells;   // (dz+1)(dy+1)(dx+1) * 2
-  float4* grad_albedo;  // dz*dy*dx (rgb + pad) or null
+  float4* grad_albedo;  // adz*ady*adx (rgb + pad) or null
   int64_t path_begin;   // first global path index of this job (batched launches)
   int64_t path_count;   // width*height*spp
   const uint32_t* pixel_order;  // pixel handed out k-th (null = row-major)
@@ -236,14 +238,25 @@ __device__ __forceinline__ float supergrid_flight(const VolJob& J, const float* 
   return kInf;
 }
 
+// Albedo grid coordinates of a point: the density lookup's when both grids
+// have one resolution, else its own (both grids span the unit cube).
+struct AlbedoLookup {
+  Axis ax, ay, az;
+};
+
+__device__ __forceinline__ AlbedoLookup albedo_lookup(const VolJob& J, const Lookup& l, const V3& x) {
+  if (!J.albedo_own_res) return AlbedoLookup{l.ax, l.ay, l.az};
+  return AlbedoLookup{axis_coord(x.x, J.adx), axis_coord(x.y, J.ady), axis_coord(x.z, J.adz)};
+}
+
 // Trilinear RGB albedo of one state (state 0 = old, 1 = new).
-__device__ __forceinline__ V3 albedo_at(const VolJob& J, const Lookup& l, int state) {
+__device__ __forceinline__ V3 albedo_at(const VolJob& J, const AlbedoLookup& l, int state) {
   if (J.albedo == nullptr) return V3{J.albedo_const[0], J.albedo_const[1], J.albedo_const[2]};
-  const int x0 = clampi(l.ax.cell - 1, J.dx - 1), x1 = clampi(l.ax.cell, J.dx - 1);
-  const int y0 = clampi(l.ay.cell - 1, J.dy - 1), y1 = clampi(l.ay.cell, J.dy - 1);
-  const int z0 = clampi(l.az.cell - 1, J.dz - 1), z1 = clampi(l.az.cell, J.dz - 1);
+  const int x0 = clampi(l.ax.cell - 1, J.adx - 1), x1 = clampi(l.ax.cell, J.adx - 1);
+  const int y0 = clampi(l.ay.cell - 1, J.ady - 1), y1 = clampi(l.ay.cell, J.ady - 1);
+  const int z0 = clampi(l.az.cell - 1, J.adz - 1), z1 = clampi(l.az.cell, J.adz - 1);
   auto at = [&](int x, int y, int z) {
-    return __ldg(J.albedo + (((int64_t)z * J.dy + y) * J.dx + x) * 2 + state);
+    return __ldg(J.albedo + (((int64_t)z * J.ady + y) * J.adx + x) * 2 + state);
   };
   const float4 a000 = at(x0, y0, z0), a100 = at(x1, y0, z0), a010 = at(x0, y1, z0),
                a110 = at(x1, y1, z0), a001 = at(x0, y0, z1), a101 = at(x1, y0, z1),
@@ -280,10 +293,10 @@ __device__ __forceinline__ void scatter_density(const VolJob& J, const Lookup& l
   atomicAdd(dst + 1, make_float4(b0 * gx0, b0 * fx, b1 * gx0, b1 * fx));
 }
 
-__device__ __forceinline__ void scatter_albedo(const VolJob& J, const Lookup& l, const V3& g) {
-  const int x0 = clampi(l.ax.cell - 1, J.dx - 1), x1 = clampi(l.ax.cell, J.dx - 1);
-  const int y0 = clampi(l.ay.cell - 1, J.dy - 1), y1 = clampi(l.ay.cell, J.dy - 1);
-  const int z0 = clampi(l.az.cell - 1, J.dz - 1), z1 = clampi(l.az.cell, J.dz - 1);
+__device__ __forceinline__ void scatter_albedo(const VolJob& J, const AlbedoLookup& l, const V3& g) {
+  const int x0 = clampi(l.ax.cell - 1, J.adx - 1), x1 = clampi(l.ax.cell, J.adx - 1);
+  const int y0 = clampi(l.ay.cell - 1, J.ady - 1), y1 = clampi(l.ay.cell, J.ady - 1);
+  const int z0 = clampi(l.az.cell - 1, J.adz - 1), z1 = clampi(l.az.cell, J.adz - 1);
   const float fx = l.ax.f, fy = l.ay.f, fz = l.az.f;
   const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
   const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
@@ -291,7 +304,7 @@ __device__ __forceinline__ void scatter_albedo(const VolJob& J, const Lookup& l,
   for (int k = 0; k < 8; ++k) {
     const int i = k & 1, j = (k >> 1) & 1, m = k >> 2;
     const float w = (wz[m] * wy[j]) * wx[i];
-    float4* dst = J.grad_albedo + ((int64_t)zs[m] * J.dy + ys[j]) * J.dx + xs[i];
+    float4* dst = J.grad_albedo + ((int64_t)zs[m] * J.ady + ys[j]) * J.adx + xs[i];
     atomicAdd(dst, make_float4(g.x * w, g.y * w, g.z * w, 0.0f));
   }
 }

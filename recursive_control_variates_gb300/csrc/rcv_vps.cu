@@ -156,7 +156,8 @@ struct Vps {
         break;
       }
       const V3 x = advance(seg.o, t, seg.d);
-      const V3 a = albedo_at(J, locate(J, x), 1);
+      const Lookup lx = locate(J, x);
+      const V3 a = albedo_at(J, albedo_lookup(J, lx, x), 1);
       has_scattered = true;
       thr = V3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
       depth += 1;
@@ -219,8 +220,9 @@ struct Vps {
     const float wdrt = tr / pdf;
     const V3 x = advance(seg.o, tp, seg.d);
     const Lookup l = locate(J, x);
+    const AlbedoLookup al = albedo_lookup(J, l, x);
     const float st = sigma_t(l);
-    const V3 a = albedo_at(J, l, 1);
+    const V3 a = albedo_at(J, al, 1);
     V3 Li{0, 0, 0};
     if (P.use_nee) Li = nee(alt, x, V3{1, 1, 1}, nullptr);
     pcg_skip1(alt);
@@ -238,7 +240,7 @@ struct Vps {
     const float k0 = mis * wdrt;
     const V3 k{(k0 * adj.x) * Li.x, (k0 * adj.y) * Li.y, (k0 * adj.z) * Li.z};
     scatter_density(J, l, J.scale * ((k.x * a.x + k.y * a.y) + k.z * a.z));
-    if (J.grad_albedo != nullptr) scatter_albedo(J, l, V3{k.x * st, k.y * st, k.z * st});
+    if (J.grad_albedo != nullptr) scatter_albedo(J, al, V3{k.x * st, k.y * st, k.z * st});
   }
 
   __device__ void backward_path(uint32_t sid, int pix, const V3& dL) const {
@@ -285,8 +287,9 @@ struct Vps {
       if (!escape) {
         const V3 x = advance(seg.o, t, seg.d);
         const Lookup l = locate(J, x);
+        const AlbedoLookup al = albedo_lookup(J, l, x);
         const float st = sigma_t(l);
-        const V3 a = albedo_at(J, l, 1);
+        const V3 a = albedo_at(J, al, 1);
         if (!P.use_drt || P.use_drt_mis) {
           const float mis = P.use_drt ? (st * st) / (1.0f + st * st) : 1.0f;
           const float inv_pdf = 1.0f / st;
@@ -294,7 +297,7 @@ struct Vps {
                      ((mis * dL.y) * (res.y / fmaxf(1e-8f, a.y))) * inv_pdf,
                      ((mis * dL.z) * (res.z / fmaxf(1e-8f, a.z))) * inv_pdf};
           scatter_density(J, l, J.scale * ((k.x * a.x + k.y * a.y) + k.z * a.z));
-          if (J.grad_albedo != nullptr) scatter_albedo(J, l, V3{k.x * st, k.y * st, k.z * st});
+          if (J.grad_albedo != nullptr) scatter_albedo(J, al, V3{k.x * st, k.y * st, k.z * st});
         }
       }
       {
@@ -308,7 +311,8 @@ struct Vps {
       }
       if (escape) break;
       const V3 x = advance(seg.o, t, seg.d);
-      const V3 a = albedo_at(J, locate(J, x), 1);
+      const Lookup lx = locate(J, x);
+      const V3 a = albedo_at(J, albedo_lookup(J, lx, x), 1);
       thr = V3{thr.x * a.x, thr.y * a.y, thr.z * a.z};
       depth += 1;
       if (depth >= J.max_depth) break;

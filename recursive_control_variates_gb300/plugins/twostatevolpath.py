@@ -152,7 +152,7 @@ class _VolumeIntegratorBase:
         o = self.options()
         dx, dy, dz = medium.dims
         gd = torch.zeros((dz, dy, dx, 1), dtype=torch.float32, device=medium.device)
-        ga = torch.zeros((dz, dy, dx, 3), dtype=torch.float32, device=medium.device) if medium.has_albedo_grid else None
+        ga = medium.albedo_grad_buffer()
         with profiling.region("trace_adjoint", medium.device):
             _lib.check(
                 _lib.load().rcv_render_backward_volume(

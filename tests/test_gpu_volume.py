@@ -345,16 +345,19 @@ def test_supergrid_tracers_match_oracle(cuda, oracle, factor):
 
 
 # ------------------------------------------- medium box and batch sensor
-def box_batch_scene(device, seeds=(1, 2), albedo_grid=True, n_views=3, res=16, height=12, spp=4):
+def box_batch_scene(device, seeds=(1, 2), albedo_grid=True, n_views=3, res=16, height=12, spp=4,
+                    albedo_res=(12, 10, 8)):
     """The grid scenes' shape (experiments.py:28-80, 285): a non-cubic grid
-    in a translated, scaled box seen by a batch of sub-sensors around it."""
+    in a translated, scaled box seen by a batch of sub-sensors around it;
+    ``albedo_res`` (Dz, Dy, Dx) may differ from the density's 12 x 10 x 8."""
     from recursive_control_variates_gb300.core import T
 
     box = T.translate([-0.3, 0.1, 0.2]).scale([1.0, 1.2, 1.5])
     old = np.ascontiguousarray(scenes.blob_density(12, seeds[0])[:, :10, :8])  # Dz, Dy, Dx = 12, 10, 8
     new = np.ascontiguousarray(scenes.blob_density(12, seeds[1])[:, :10, :8])
-    ao = np.ascontiguousarray(scenes.albedo_grid(12, seeds[0])[:, :10, :8]) if albedo_grid else None
-    an = np.ascontiguousarray(scenes.albedo_grid(12, seeds[1])[:, :10, :8]) if albedo_grid else None
+    az, ay, ax = albedo_res
+    ao = np.ascontiguousarray(scenes.albedo_grid(16, seeds[0])[:az, :ay, :ax]) if albedo_grid else None
+    an = np.ascontiguousarray(scenes.albedo_grid(16, seeds[1])[:az, :ay, :ax]) if albedo_grid else None
     views = scenes.orbit_views(box, n_views, distance=2.6, height=0.4)
     d = scenes.scene_dict(new, an if albedo_grid else 0.8, res=res, height=height, spp=spp, box=box, views=views)
     scene = rcv.load_dict(d, device=device)
@@ -412,6 +415,34 @@ def test_box_and_batch_film_match_oracle(cuda, oracle, factor):
     vd = vg[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
     ovd, _ = oracle.vps_backward(osc, seed=22, spp=4, grad_img=gimg)
     assert np.linalg.norm(vd - ovd) <= 2e-5 * np.linalg.norm(ovd)
+
+
+def test_albedo_grid_with_own_resolution_matches_oracle(cuda, oracle):
+    """Albedo grid at its own resolution (experiments.py:56,63): tracers,
+    adjoint (albedo gradient on the albedo grid) and volpathsimple against
+    the oracle."""
+    scene, med, grids = box_batch_scene(cuda, albedo_res=(7, 9, 5))
+    assert med.albedo_dims == (5, 9, 7) and med.dims == (8, 10, 12)
+    osc = oracle_box_scene(oracle, scene, med, grids, 8)
+    assert (osc.c.adx, osc.c.ady, osc.c.adz) == (5, 9, 7)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
+    H, F = integ.render_twostates(scene, 0, seed=31, spp=4)
+    Ho, Fo = oracle.render_twostates(osc, seed=31, spp=4)
+    assert frac_equal(F.cpu().numpy(), Fo) >= 0.999 and frac_equal(H.cpu().numpy(), Ho) >= 0.999
+    params = rcv.traverse(scene)
+    gimg = np.random.default_rng(9).normal(0, 1, (12, 48, 3)).astype(np.float32)
+    grads = integ.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=32, spp=4)
+    od, oa = oracle.backward(osc, seed=32, spp=4, grad_img=gimg)
+    ga = grads[scenes.ALBEDO_KEY].cpu().numpy().astype(np.float64)
+    assert ga.shape == (7, 9, 5, 3) == oa.shape
+    gd = grads[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
+    assert np.linalg.norm(gd - od) <= 2e-5 * np.linalg.norm(od)
+    assert np.linalg.norm(ga - oa) <= 2e-5 * np.linalg.norm(oa)
+    vps = rcv.load_dict({"type": "volpathsimple", "max_depth": 8, "rr_depth": 8})
+    vg = vps.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=33, spp=4)
+    _, ova = oracle.vps_backward(osc, seed=33, spp=4, grad_img=gimg)
+    va = vg[scenes.ALBEDO_KEY].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(va - ova) <= 2e-5 * np.linalg.norm(ova)
 
 
 def test_batched_engine_with_box_and_batch_film(cuda):

@@ -174,6 +174,39 @@ def test_box_transform_and_batch_film_closed_form(oracle):
     assert abs(v.mean() - img.mean()) < 0.01
 
 
+def test_albedo_grid_with_own_resolution(oracle):
+    """An albedo grid may have its own resolution (experiments.py:56,63:
+    264x136x136 density, 256x128x128 albedo).  A constant grid at any
+    resolution interpolates to exactly its value, so images and density
+    gradients equal those of the constant albedo bit for bit, and the albedo
+    gradients of two resolutions have the same total (up to the float
+    rounding of the corner weights)."""
+    cam = oracle.camera_basis(16, 16)
+    old = blob_density(8, 1)
+    new = blob_density(8, 2)
+    plain = oracle.Scene(cam, old, new, albedo_const=0.8, max_depth=8)
+    totals = []
+    for res in [(5, 7, 9), (8, 8, 8), (16, 12, 3)]:
+        a = np.full(res + (3,), 0.8, np.float32)
+        sc = oracle.Scene(cam, old, new, albedo_old=a, albedo_new=a, max_depth=8)
+        assert (sc.c.adz, sc.c.ady, sc.c.adx) == (res if res != (8, 8, 8) else (0, 0, 0))
+        H, F = oracle.render_twostates(sc, seed=4, spp=4)
+        Hp, Fp = oracle.render_twostates(plain, seed=4, spp=4)
+        assert np.array_equal(H, Hp) and np.array_equal(F, Fp)
+        g = np.random.default_rng(3).normal(0, 1, (16, 16, 3)).astype(np.float32)
+        gd, ga = oracle.backward(sc, seed=9, spp=4, grad_img=g, threads=1)
+        gdp, _ = oracle.backward(plain, seed=9, spp=4, grad_img=g, threads=1)
+        assert np.array_equal(gd, gdp) and ga.shape == res + (3,)
+        totals.append(ga.sum(axis=(0, 1, 2)))
+        v = oracle.vps_render(sc, seed=2, spp=4)
+        assert np.array_equal(v, oracle.vps_render(plain, seed=2, spp=4))
+        _, va = oracle.vps_backward(sc, seed=5, spp=4, grad_img=g)
+        assert va.shape == res + (3,)
+    # the float corner weights of one event sum to 1 within a few ulp
+    np.testing.assert_allclose(totals[0], totals[1], rtol=1e-6)
+    np.testing.assert_allclose(totals[2], totals[1], rtol=1e-6)
+
+
 def test_cv_welford_golden(oracle, golden_cv):
     """The numpy restatement reproduces the reference's own CVIntegrator /
     MetaIntegrator / StatisticsEstimator code bit for bit."""
