@@ -226,6 +226,22 @@ int rcv_render_backward_volume(const rcv_medium* medium, const rcv_sensor* senso
                                const float* grad_img, float* grad_density, float* grad_albedo,
                                void* workspace, uint64_t* counters, void* stream);
 
+/* rcv_render_backward_volume in two calls.  The first pass of the adjoint
+ * (each path's radiance and its scatter checkpoints) does not depend on
+ * grad_img, so it can run as soon as the parameters are known — e.g. on a
+ * second stream beside the primal render — and the second call, given
+ * grad_img, only replays.  The replay call must get the same medium state,
+ * sensor, options, seed, spp and workspace as the radiance call, and be
+ * ordered after it; the pair gives the same gradients as
+ * rcv_render_backward_volume. */
+int rcv_render_adjoint_radiance(const rcv_medium* medium, const rcv_sensor* sensor,
+                                const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                                void* workspace, uint64_t* counters, void* stream);
+int rcv_render_backward_replay(const rcv_medium* medium, const rcv_sensor* sensor,
+                               const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                               const float* grad_img, float* grad_density, float* grad_albedo,
+                               void* workspace, uint64_t* counters, void* stream);
+
 /* ------------------------------------------------ volpathsimple integrator */
 /* Switches of VolpathSimpleIntegrator (plugins/volpathsimple.py:20-51):
  * use_nee, use_drt, use_drt_subsampling, use_drt_mis (each 0 or 1; the

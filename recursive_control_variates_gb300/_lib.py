@@ -217,6 +217,13 @@ SIGNATURES = {
         C.c_int,
         [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
     ),
+    "rcv_render_adjoint_radiance": (
+        C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp]
+    ),
+    "rcv_render_backward_replay": (
+        C.c_int,
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
+    ),
     "rcv_volpathsimple_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32]),
     "rcv_render_volpathsimple": (
         C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), P(VpsFlags), C.c_uint32, C.c_int32, vp, vp, vp]

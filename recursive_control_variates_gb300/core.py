@@ -326,7 +326,35 @@ class _PackedMedium:
     accumulators) shared by single- and two-state media."""
 
     _workspace: torch.Tensor | None = None
-    _dirty: bool = True
+
+    # `_dirty`: the grids changed since the last pack.  Setting it also bumps
+    # `version`, which tells an adjoint pass started ahead of time whether
+    # the parameters it traced are still current.
+    @property
+    def _dirty(self) -> bool:
+        return self.__dict__.get("_dirty_flag", True)
+
+    @_dirty.setter
+    def _dirty(self, value: bool) -> None:
+        if value:
+            self.__dict__["_version"] = self.version + 1
+        self.__dict__["_dirty_flag"] = bool(value)
+
+    @property
+    def version(self) -> int:
+        return self.__dict__.get("_version", 0)
+
+    def add_reader(self, event) -> None:
+        """A CUDA event after which work on another stream stops reading the
+        workspace; repacking or replacing the workspace waits for it."""
+        self.__dict__.setdefault("_readers", []).append(event)
+
+    def _wait_readers(self) -> None:
+        readers = self.__dict__.pop("_readers", [])
+        if readers:
+            s = torch.cuda.current_stream(self.device)
+            for ev in readers:
+                s.wait_event(ev)
 
     def _states(self):
         raise NotImplementedError
@@ -341,6 +369,7 @@ class _PackedMedium:
             raise ValueError("majorant_resolution_factor must be >= 0")
         for m in self._media():
             m.majorant_factor = int(factor)
+        self._wait_readers()
         self._workspace = None
         self._dirty = True
 
@@ -403,6 +432,7 @@ class _PackedMedium:
             raise RuntimeError("rendering requires the medium on a CUDA device")
         m = self.c_struct()
         if self._dirty:
+            self._wait_readers()
             _lib.check(_lib.load().rcv_medium_prepare(C.byref(m), stream), "rcv_medium_prepare")
             self._dirty = False
         return m
@@ -479,6 +509,7 @@ class HeterogeneousMedium(_PackedMedium):
             self.albedo_grid = t
         else:
             raise KeyError(sub)
+        self._wait_readers()
         self._workspace = None
         self._dirty = True
 
@@ -539,6 +570,7 @@ class TwoStateMedium(_PackedMedium):
         does not use the old state's image."""
         for m in (self.old, self.new, self.incoming):
             m.set_grid(sub, value)
+        self._wait_readers()
         self._workspace = None
         self._dirty = True
 

@@ -456,8 +456,14 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
 
 // Orders the pixels, runs the persistent tracer of one job and, for the
 // primal tracers, reduces the per-path radiance into the output image(s).
+// Adjoint stages: both launches, the radiance pass alone, or the replay alone
+// (which reuses the pixel order, checkpoints and total radiance the radiance
+// pass left in the same workspace).
+enum AdjStage { kAdjBoth = 0, kAdjRadiance = 1, kAdjReplay = 2 };
+
 static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, void* workspace,
-                          uint64_t* counters, float* img_new, float* img_old, cudaStream_t st) {
+                          uint64_t* counters, float* img_new, float* img_old, cudaStream_t st,
+                          int stage = kAdjBoth) {
   RCV_REQUIRE(workspace != nullptr && (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
               "render workspace must be non-NULL and 256-byte aligned");
   const int64_t npix = int64_t(J.width) * J.height;
@@ -471,9 +477,11 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
               "unknown pixel order %d", order);
   if (order != RCV_ORDER_ROW_MAJOR) {
     uint32_t* cost = order == RCV_ORDER_COST ? reinterpret_cast<uint32_t*>(ws + L.cost) : nullptr;
-    rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
-                      cost, st);
-    if (rc) return rc;
+    if (stage != kAdjReplay) {
+      rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
+                        cost, st);
+      if (rc) return rc;
+    }
     J.pixel_order = reinterpret_cast<const uint32_t*>(ws + L.order);
     J.pixel_cost = cost;
   }
@@ -485,9 +493,11 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
     A.ckpt_count = qc + 1;
     A.ckpt_cap = ckpt_capacity(J.path_count);
     A.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
-    RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, sizeof(unsigned long long), st), "checkpoint reset");
-    rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
-    if (rc) return rc;
+    if (stage != kAdjReplay) {
+      RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, sizeof(unsigned long long), st), "checkpoint reset");
+      rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
+      if (rc || stage == kAdjRadiance) return rc;
+    }
     return launch_persistent(kReplay, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
   }
   rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o, qc, po, nullptr, counters, st, false);
@@ -517,11 +527,9 @@ extern "C" int rcv_render_volume(const rcv_medium* m, const rcv_sensor* s,
   return run_single_job(kSingle, J, o, workspace, counters, img, nullptr, static_cast<cudaStream_t>(stream));
 }
 
-extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor* s,
-                                          const rcv_volpath_options* o, uint32_t seed,
-                                          int32_t spp, const float* grad_img,
-                                          float* grad_density, float* grad_albedo,
-                                          void* workspace, uint64_t* counters, void* stream) {
+static int backward_volume(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o, uint32_t seed,
+                           int32_t spp, const float* grad_img, float* grad_density, float* grad_albedo,
+                           void* workspace, uint64_t* counters, void* stream, int stage) {
   VolJob J;
   int rc = make_volume_job(m, s, o, seed, spp, &J);
   if (rc) return rc;
@@ -532,9 +540,36 @@ extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor*
   if (rc) return rc;
   if (!want_albedo) J.grad_albedo = nullptr;
   J.grad_img = grad_img;
-  rc = run_single_job(kAdjoint, J, o, workspace, counters, nullptr, nullptr, st);
+  rc = run_single_job(kAdjoint, J, o, workspace, counters, nullptr, nullptr, st, stage);
   if (rc) return rc;
   return launch_fold(m, grad_density, want_albedo ? grad_albedo : nullptr, st);
+}
+
+extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor* s,
+                                          const rcv_volpath_options* o, uint32_t seed,
+                                          int32_t spp, const float* grad_img,
+                                          float* grad_density, float* grad_albedo,
+                                          void* workspace, uint64_t* counters, void* stream) {
+  return backward_volume(m, s, o, seed, spp, grad_img, grad_density, grad_albedo, workspace, counters, stream,
+                         kAdjBoth);
+}
+
+extern "C" int rcv_render_adjoint_radiance(const rcv_medium* m, const rcv_sensor* s,
+                                           const rcv_volpath_options* o, uint32_t seed, int32_t spp,
+                                           void* workspace, uint64_t* counters, void* stream) {
+  VolJob J;
+  int rc = make_volume_job(m, s, o, seed, spp, &J);
+  if (rc) return rc;
+  return run_single_job(kAdjoint, J, o, workspace, counters, nullptr, nullptr, static_cast<cudaStream_t>(stream),
+                        kAdjRadiance);
+}
+
+extern "C" int rcv_render_backward_replay(const rcv_medium* m, const rcv_sensor* s,
+                                          const rcv_volpath_options* o, uint32_t seed, int32_t spp,
+                                          const float* grad_img, float* grad_density, float* grad_albedo,
+                                          void* workspace, uint64_t* counters, void* stream) {
+  return backward_volume(m, s, o, seed, spp, grad_img, grad_density, grad_albedo, workspace, counters, stream,
+                         kAdjReplay);
 }
 
 // ------------------------------------------------- allocation-free render

@@ -122,6 +122,10 @@ class CVIntegrator:
     def render_backward(self, scene, params, grad_in, sensor=0, seed: int = 0, spp: int = 0):
         return self.adjoint_integrator.render_backward(scene, params, grad_in, sensor, seed, spp)
 
+    def prefetch_adjoint(self, scene, sensor=0, seed: int = 0, spp: int = 0):
+        pre = getattr(self.adjoint_integrator, "prefetch_adjoint", None)
+        return pre(scene, sensor, seed, spp) if pre is not None else None
+
 
 class MetaIntegrator:
     """``meta`` (plugins/metaintegrator.py:7-147): methods ``baseline``,
@@ -197,3 +201,7 @@ class MetaIntegrator:
 
     def render_backward(self, scene, params, grad_in, sensor=0, seed: int = 0, spp: int = 0):
         return self.adjoint_integrator.render_backward(scene, params, grad_in, sensor, seed, spp)
+
+    def prefetch_adjoint(self, scene, sensor=0, seed: int = 0, spp: int = 0):
+        pre = getattr(self.adjoint_integrator, "prefetch_adjoint", None)
+        return pre(scene, sensor, seed, spp) if pre is not None else None

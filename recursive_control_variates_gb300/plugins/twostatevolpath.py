@@ -43,9 +43,14 @@ class _VolumeIntegratorBase:
         self.order = _lib.ORDERS[order]
         if self.max_depth < -1:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
+        # run the adjoint's radiance pass beside the primal render (rcv.render)
+        self.overlap_adjoint = bool(props.get("overlap_adjoint", True))
         self.is_checked = False
         self._counters: dict[torch.device, torch.Tensor] = {}
         self._scratch: dict[torch.device, torch.Tensor] = {}
+        self._adj_scratch: dict[torch.device, torch.Tensor] = {}
+        self._side: dict[torch.device, torch.cuda.Stream] = {}
+        self._ticket = None  # (key, done event) of an adjoint radiance pass started ahead
 
     # ------------------------------------------------------------- helpers
     def options(self) -> _lib.VolpathOptions:
@@ -77,6 +82,74 @@ class _VolumeIntegratorBase:
             buf = torch.zeros(need, dtype=torch.uint8, device=device)
             self._scratch[device] = buf
         return (buf.data_ptr() + 255) & ~255
+
+    def adjoint_scratch(self, device, sensor, spp: int) -> int:
+        """256-B aligned scratch of the adjoint launches (its own buffer, so
+        an adjoint radiance pass on the side stream never shares scratch with
+        a primal render)."""
+        device = torch.device(device)
+        f = sensor.film()
+        need = int(_lib.load().rcv_render_workspace_bytes(f.width, f.height, spp, _lib.MODE_ADJOINT)) + 256
+        buf = self._adj_scratch.get(device)
+        if buf is None or buf.numel() < need:
+            self._drain_ticket(device)  # the old buffer may still be in use
+            buf = torch.zeros(need, dtype=torch.uint8, device=device)
+            self._adj_scratch[device] = buf
+        return (buf.data_ptr() + 255) & ~255
+
+    def _drain_ticket(self, device):
+        t, self._ticket = self._ticket, None
+        if t is not None:
+            torch.cuda.current_stream(device).wait_event(t[1])
+
+    def _adjoint_key(self, medium, sensor, seed: int, spp: int):
+        o = self.options()
+        return (id(medium), medium.version, id(sensor), seed & 0xFFFFFFFF, int(spp),
+                tuple(getattr(o, f) for f, _ in o._fields_))
+
+    def prefetch_adjoint(self, scene, sensor=0, seed: int = 0, spp: int = 0):
+        """Prepares the adjoint's first launch (each path's radiance and its
+        scatter checkpoints), which does not depend on the image gradient.
+        Returns a function that enqueues it on a side stream, ordered after
+        the medium's packing but not after the work enqueued in between (the
+        primal render), or None when there is nothing to overlap.
+        ``render_backward`` with the same arguments then only replays."""
+        if not self.overlap_adjoint:
+            return None
+        medium = self._checked_medium(scene)
+        sensor = self.sensor_of(scene, sensor)
+        spp = self.resolve_spp(sensor, spp)
+        dev = medium.device
+        main = torch.cuda.current_stream(dev)
+        m = medium.prepare(main.cuda_stream)
+        s = sensor.c_struct()
+        o = self.options()
+        ws = self.adjoint_scratch(dev, sensor, spp)
+        packed = torch.cuda.Event()
+        packed.record(main)
+        key = self._adjoint_key(medium, sensor, seed, spp)
+        side = self._side.get(dev)
+        if side is None:
+            side = self._side[dev] = torch.cuda.Stream(dev)
+        counters = self.counters(dev)
+
+        def launch():
+            self._drain_ticket(dev)
+            side.wait_event(packed)
+            with torch.cuda.stream(side), profiling.region("trace_adjoint_radiance", dev):
+                _lib.check(
+                    _lib.load().rcv_render_adjoint_radiance(
+                        C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, ws, counters.data_ptr(),
+                        side.cuda_stream,
+                    ),
+                    "rcv_render_adjoint_radiance",
+                )
+            done = torch.cuda.Event()
+            done.record(side)
+            medium.add_reader(done)
+            self._ticket = (key, done)
+
+        return launch
 
     @staticmethod
     def medium_of(scene):
@@ -146,22 +219,30 @@ class _VolumeIntegratorBase:
         f = sensor.film()
         if tuple(g.shape) != (f.height, f.width, 3):
             raise ValueError(f"grad_in has shape {tuple(g.shape)}, expected {(f.height, f.width, 3)}")
-        st = stream_handle(medium.device)
+        dev = medium.device
+        ticket, key = self._ticket, None
+        if ticket is not None:
+            key = self._adjoint_key(medium, sensor, seed, spp)
+        self._drain_ticket(dev)  # orders this stream after a radiance pass started ahead
+        st = stream_handle(dev)
         m = medium.prepare(st)
         s = sensor.c_struct()
         o = self.options()
         dx, dy, dz = medium.dims
-        gd = torch.zeros((dz, dy, dx, 1), dtype=torch.float32, device=medium.device)
+        gd = torch.zeros((dz, dy, dx, 1), dtype=torch.float32, device=dev)
         ga = medium.albedo_grad_buffer()
-        with profiling.region("trace_adjoint", medium.device):
+        ws = self.adjoint_scratch(dev, sensor, spp)
+        # the radiance pass already ran for exactly these arguments: replay only
+        fn = ("rcv_render_backward_replay" if ticket is not None and ticket[0] == key and medium.version == key[1]
+              else "rcv_render_backward_volume")
+        self.last_adjoint_call = fn
+        with profiling.region("trace_adjoint", dev):
             _lib.check(
-                _lib.load().rcv_render_backward_volume(
+                getattr(_lib.load(), fn)(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, g.data_ptr(), gd.data_ptr(),
-                    ga.data_ptr() if ga is not None else None,
-                    self.scratch(medium.device, sensor, spp, _lib.MODE_ADJOINT),
-                    self.counters(medium.device).data_ptr(), st,
+                    ga.data_ptr() if ga is not None else None, ws, self.counters(dev).data_ptr(), st,
                 ),
-                "rcv_render_backward_volume",
+                fn,
             )
         out = {}
         keys = list(params.keys()) if params is not None else []

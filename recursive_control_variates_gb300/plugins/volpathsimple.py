@@ -32,6 +32,10 @@ class VolpathSimpleIntegrator(PRBVolpathIntegrator):
         self.use_drt_mis = bool(props.get("use_drt_mis", True))
         self._vps_scratch: dict[torch.device, torch.Tensor] = {}
 
+    def prefetch_adjoint(self, scene, sensor=0, seed: int = 0, spp: int = 0):
+        """The DRT adjoint is one launch per call: nothing to start ahead."""
+        return None
+
     def flags(self) -> _lib.VpsFlags:
         f = _lib.VpsFlags()
         f.use_nee = int(self.use_nee)

@@ -25,7 +25,14 @@ class _RenderOp(torch.autograd.Function):
         ctx.job = job
         ctx.shapes = [t.shape for t in tensors]
         with torch.no_grad():
+            # the adjoint's radiance pass needs only the parameters and the
+            # gradient seed: it runs on a side stream beside the primal
+            # render, and the backward pass then only replays
+            pre = getattr(job.integrator, "prefetch_adjoint", None)
+            launch = pre(job.scene, job.sensor, job.seed_grad, job.spp_grad) if pre is not None else None
             img = job.integrator.render(job.scene, job.sensor, job.seed, job.spp)
+            if launch is not None:
+                launch()
         return img
 
     @staticmethod

@@ -189,6 +189,38 @@ def test_autograd_render_matches_direct_backward(cuda):
     torch.testing.assert_close(opt[scenes.DENSITY_KEY].grad, direct[scenes.DENSITY_KEY], rtol=1e-4, atol=1e-6)
 
 
+def test_adjoint_started_ahead_matches_full_adjoint(cuda):
+    """The adjoint's radiance pass started on a side stream before the
+    gradient is known (rcv_render_adjoint_radiance) plus the replay equals
+    the one-call adjoint; a parameter change in between invalidates it."""
+    scene, med, grids = make_scene(cuda, res=32, albedo_grid=True)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
+    g = torch.randn((32, 32, 3), device=cuda)
+    full = integ.render_backward(scene, params, g, 0, seed=5, spp=4)
+    assert integ.last_adjoint_call == "rcv_render_backward_volume"
+    launch = integ.prefetch_adjoint(scene, 0, seed=5, spp=4)
+    H, F = integ.render_twostates(scene, 0, seed=9, spp=4)  # primal work in between
+    launch()
+    split = integ.render_backward(scene, params, g, 0, seed=5, spp=4)
+    assert integ.last_adjoint_call == "rcv_render_backward_replay"
+    for key in (scenes.DENSITY_KEY, scenes.ALBEDO_KEY):
+        a, b = full[key].double(), split[key].double()
+        assert float((a - b).norm()) <= 2e-5 * float(a.norm())
+    H2, F2 = integ.render_twostates(scene, 0, seed=9, spp=4)
+    assert torch.equal(H, H2) and torch.equal(F, F2)
+    # stale: another seed, or the parameters changed after the radiance pass
+    integ.prefetch_adjoint(scene, 0, seed=6, spp=4)()
+    integ.render_backward(scene, params, g, 0, seed=7, spp=4)
+    assert integ.last_adjoint_call == "rcv_render_backward_volume"
+    integ.prefetch_adjoint(scene, 0, seed=5, spp=4)()
+    med.new.density.mul_(1.01)
+    med._dirty = True
+    changed = integ.render_backward(scene, params, g, 0, seed=5, spp=4)
+    assert integ.last_adjoint_call == "rcv_render_backward_volume"
+    assert not torch.equal(changed[scenes.DENSITY_KEY], full[scenes.DENSITY_KEY])
+
+
 def test_finite_differences_32_voxels(cuda):
     """Adjoint vs central differences (h = 1e-3) on 32 random voxels of a
     64^3 density + albedo grid (config-2 medium at 96^2), with the
