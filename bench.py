@@ -19,6 +19,7 @@ collective in the data path); value = all ranks' paths / max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import math
 import os
@@ -268,7 +269,6 @@ def run_ours(args, cfg):
     # ------------------------------------------------- device-timed region
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    c0 = job.counters()
     launches0 = lib.rcv_kernel_launches()
     timer = profiling.KernelTimer()
     if dist is not None:
@@ -284,7 +284,6 @@ def run_ours(args, cfg):
     if dist is not None:
         dist.barrier()
     launches = lib.rcv_kernel_launches() - launches0
-    c1 = job.counters()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     local_total_s = sum(step_ms) / 1e3
     total_s = reduce_max(local_total_s, dist, device)
@@ -297,7 +296,6 @@ def run_ours(args, cfg):
     # launch durations overlap; the per-kernel durations come from a few more
     # steps with the two passes one after the other (same kernels, same
     # inputs), each launch alone on the GPU.
-    delta = (c1 - c0).cpu().numpy().astype(np.float64) / args.steps
     inner = job.integrator.integrator
     inner.overlap_adjoint = False
     serial = profiling.KernelTimer()
@@ -309,6 +307,7 @@ def run_ours(args, cfg):
     kern_serial = serial.summary()
     # the counters mix both tracers; split with a separate 1-step measurement
     c_two, c_adj = split_counters(job)
+    delta = (c_two + c_adj).astype(np.float64)  # event counts of one step (counted separately)
     algo = algorithmic_bytes(cfg, job.has_albedo, c_two, c_adj)
     dom = max(("trace_twostate", "trace_adjoint"), key=lambda k: kern_serial.get(k, {}).get("total_ms", 0.0))
     peaks = measured_peaks()
@@ -401,7 +400,6 @@ def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_fa
     for _ in range(args.warmup):
         job.step()
     stream = torch.cuda.current_stream(device)
-    c0 = job.counters()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
     for i, (a, b) in enumerate(ev):
@@ -411,7 +409,8 @@ def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_fa
         b.record(stream)
     torch.cuda.synchronize()
     total = reduce_max(sum(a.elapsed_time(b) for a, b in ev) / 1e3, dist, device)
-    d = (job.counters() - c0).cpu().numpy().astype(np.float64) / args.steps
+    c_two, c_adj = split_counters(job)
+    d = (c_two + c_adj).astype(np.float64)
     paths = job.paths_per_step()
     return {"value": paths * world * args.steps / total, "unit": UNIT, "ms_per_step": total * 1e3 / args.steps,
             "start": f"density {'constant ' + str(cfg.init) if phase == 'early' else '0.8 x true grid'}",
@@ -420,10 +419,12 @@ def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_fa
 
 
 def split_counters(job):
-    """Per-kernel counters of one extra (untimed) step."""
+    """Per-kernel counters of one extra (untimed) step, with the counting
+    tracer variants."""
     import torch
 
     integ = job.integrator.integrator
+    integ.count_events = True
     cnt = integ.counters(job.device)
     job.params.update(job.opt)
     before = cnt.clone()
@@ -433,6 +434,7 @@ def split_counters(job):
     integ.render_backward(job.scene, job.params, g, 0, seed=job.seed + 2 * 10**6, spp=job.cfg.spp_grad)
     after = cnt.clone()
     torch.cuda.synchronize()
+    integ.count_events = False
     return (mid - before).cpu().numpy(), (after - mid).cpu().numpy()
 
 
@@ -497,7 +499,6 @@ def batched_form(args, device, flush):
     b.step(args.warmup)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.batched_steps)]
-    c0 = b.counters().clone()
     with ClockSampler(device.index or 0) as clocks:
         for i, (a, e) in enumerate(ev):
             flush.fill_(float(i))
@@ -506,8 +507,13 @@ def batched_form(args, device, flush):
             e.record(stream)
         torch.cuda.synchronize()
     ms = [a.elapsed_time(e) for a, e in ev]
-    dc = (b.counters() - c0).cpu().numpy().astype(np.float64) / len(ms)
     b.close()
+    # event counts of one more step, by the counting tracer variants
+    bc = batch.BatchedCV(jobs, options=dataclasses.replace(best, count_events=True), use_graph=False)
+    bc.step()
+    torch.cuda.synchronize()
+    dc = bc.counters().cpu().numpy().astype(np.float64)
+    bc.close()
     total = sum(ms) / 1e3
     value = paths * len(ms) / total
     plain_value = plain_ms = plain_wall = None

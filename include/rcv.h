@@ -115,6 +115,9 @@ typedef struct rcv_volpath_options {
   int32_t defer;         /* lanes that must wait before a path-start or
                             scattering branch runs, 1..32, 0 = 8                 */
   int32_t order;         /* pixel hand-out order, RCV_ORDER_*                     */
+  int32_t count_events;  /* batched launches: accumulate the RCV_COUNTER_* totals
+                            behind rcv_batch_counters (single-job calls count when
+                            their `counters` argument is non-NULL)               */
 } rcv_volpath_options;
 
 /* Pixel hand-out orders of the persistent tracers.  Results do not depend on

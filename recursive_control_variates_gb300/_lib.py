@@ -79,6 +79,7 @@ class VolpathOptions(C.Structure):
         ("blocks_per_sm", C.c_int32),
         ("defer", C.c_int32),
         ("order", C.c_int32),
+        ("count_events", C.c_int32),
     ]
 
 

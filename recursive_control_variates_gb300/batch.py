@@ -310,10 +310,12 @@ class LaunchOptions:
     blocks_per_sm: int = 0   # resident tracer blocks per SM (0 = occupancy limit)
     defer: int = 8           # lanes that must wait before a deferred branch runs
     order: str = "cost"      # pixel hand-out order: cost | longest_first | row_major
+    count_events: bool = False  # accumulate the tracer event counts (counters())
 
     def c_struct(self) -> _lib.VolpathOptions:
         o = _lib.VolpathOptions()
         o.batch, o.blocks_per_sm, o.defer = self.batch, self.blocks_per_sm, self.defer
+        o.count_events = int(self.count_events)
         if self.order not in _lib.ORDERS:
             raise ValueError(f"unknown pixel order {self.order!r}")
         o.order = _lib.ORDERS[self.order]

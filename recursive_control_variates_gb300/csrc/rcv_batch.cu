@@ -694,19 +694,21 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   RCV_TRY_CUDA(cudaEventRecord(b->fork, st), "fork record");
   RCV_TRY_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "fork wait");
   RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, sizeof(unsigned long long), b->side), "checkpoint reset");
+  // event counts only when asked for: the counting tracers hold the counts in registers
+  uint64_t* cnt = b->opt.count_events ? b->counters : nullptr;
   rc = launch_persistent(kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr, &b->adjbuf,
-                         b->counters + RCV_COUNTER_COUNT, b->side, sg);
+                         cnt ? cnt + RCV_COUNTER_COUNT : nullptr, b->side, sg);
   if (rc) return rc;
   RCV_TRY_CUDA(cudaEventRecord(b->join, b->side), "join record");
   rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr,
-                         b->counters, st, sg);
+                         cnt, st, sg);
   if (rc) return rc;
   batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
   rc = launched("batch image launch");
   if (rc) return rc;
   RCV_TRY_CUDA(cudaStreamWaitEvent(st, b->join, 0), "join wait");
   rc = launch_persistent(kReplay, none, b->adj, n, b->total_adj, &b->opt, b->queue + 2, nullptr, &b->adjbuf,
-                         b->counters + RCV_COUNTER_COUNT, st, sg);
+                         cnt ? cnt + RCV_COUNTER_COUNT : nullptr, st, sg);
   if (rc) return rc;
   batch_update_kernel<<<(unsigned)b->vox_blocks, kBatchBlock, 0, st>>>(b->entries, pv, n);
   return launched("batch update launch");

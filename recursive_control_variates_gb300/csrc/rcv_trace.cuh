@@ -71,8 +71,10 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
   return Q.jobs[lo];
 }
 
-// kSG: the launch may contain media with a majorant supergrid.
-template <int kMode, bool kSG>
+// kSG: the launch may contain media with a majorant supergrid.  kCount: the
+// launch accumulates the RCV_COUNTER_* event counts (off, the counters cost
+// no registers).
+template <int kMode, bool kSG, bool kCount>
 __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& cnt) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -268,9 +270,9 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
             const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
             scatter_density(J, lk, (J.scale * sd) / st_n);
-            ++cnt.grad_events;
+            if (kCount) ++cnt.grad_events;
             if (J.grad_albedo != nullptr) {
-              ++cnt.albedo_events;
+              if (kCount) ++cnt.albedo_events;
               const V3 ga{(dL.x * Lr.x) / fmaxf(an.x, 1e-8f), (dL.y * Lr.y) / fmaxf(an.y, 1e-8f),
                           (dL.z * Lr.z) / fmaxf(an.z, 1e-8f)};
               scatter_albedo(J, alk, ga);
@@ -354,10 +356,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             density2(J, lk, rho_o, rho_n);
           else
             rho_n = density_new(J, lk);
-          if (phase == kMain)
-            ++cnt.lookups;
-          else
-            ++cnt.nee_lookups;
+          if (kCount) {
+            if (phase == kMain)
+              ++cnt.lookups;
+            else
+              ++cnt.nee_lookups;
+          }
         }
         const float st_o = J.scale * rho_o, st_n = J.scale * rho_n;
 
@@ -386,7 +390,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
                 const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
                 scatter_density(J, lk, -(J.scale * sd) / sn);
-                ++cnt.grad_events;
+                if (kCount) ++cnt.grad_events;
               }
               p = x;
               t_rem = t_rem - t;
@@ -396,7 +400,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               if (depth >= J.max_depth) {
                 finished = true;
               } else {
-                ++cnt.scatters;
+                if (kCount) ++cnt.scatters;
                 p = x;
                 sc_n = st_n;
                 sc_o = st_o;
@@ -462,7 +466,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             const float sn = mu_c - st_n;
             if (sn > 0.0f) {
               scatter_density(J, lk, -(J.scale * s_nee) / sn);
-              ++cnt.grad_events;
+              if (kCount) ++cnt.grad_events;
             }
             trn = trn * (sn * inv_c);
             q = x;
@@ -487,7 +491,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
       }
       if (kMode == kAdjoint) Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f);
-      if (kMode != kReplay) ++cnt.paths;
+      if (kCount && kMode != kReplay) ++cnt.paths;
       if (Jp->pixel_cost != nullptr) atomicAdd(Jp->pixel_cost + pix, n_iter - iter0);
       phase = kIdle;
     }

@@ -55,13 +55,28 @@ __device__ __forceinline__ void add_counts(unsigned long long* counters, const C
   }
 }
 
-template <int kMode, bool kSG>
+template <int kMode, bool kSG, bool kCount>
 __global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_constant__ VolJob J,
                                                             const __grid_constant__ Queue Q) {
   Counts cnt{0, 0, 0, 0, 0, 0};
-  trace_persistent<kMode, kSG>(J, Q, cnt);
-  add_counts(Q.counters, cnt);
+  trace_persistent<kMode, kSG, kCount>(J, Q, cnt);
+  if (kCount) add_counts(Q.counters, cnt);
 }
+
+// Tracer variants by index mode + 4 * supergrid + 8 * counting.
+using TraceKernel = void (*)(VolJob, Queue);
+static const TraceKernel kTraceKernels[16] = {
+    trace_kernel<kTwoState, false, false>, trace_kernel<kSingle, false, false>,
+    trace_kernel<kAdjoint, false, false>,  trace_kernel<kReplay, false, false>,
+    trace_kernel<kTwoState, true, false>,  trace_kernel<kSingle, true, false>,
+    trace_kernel<kAdjoint, true, false>,   trace_kernel<kReplay, true, false>,
+    trace_kernel<kTwoState, false, true>,  trace_kernel<kSingle, false, true>,
+    trace_kernel<kAdjoint, false, true>,   trace_kernel<kReplay, false, true>,
+    trace_kernel<kTwoState, true, true>,   trace_kernel<kSingle, true, true>,
+    trace_kernel<kAdjoint, true, true>,    trace_kernel<kReplay, true, true>,
+};
+
+static int trace_variant(int mode, bool sg, bool count) { return mode + (sg ? 4 : 0) + (count ? 8 : 0); }
 
 // Majorant supergrid of a medium (both states' cells and the new state's).
 __global__ void supergrid_kernel(int sx, int sy, int sz, int dx, int dy, int dz, float scale,
@@ -255,21 +270,17 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
 }
 
 // Resident blocks per SM of each tracer variant (queried once per process).
-static int resident_blocks(int mode, bool sg) {
+static int resident_blocks(int variant) {
   static std::once_flag once;
-  static int blocks[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+  static int blocks[16];
   std::call_once(once, [] {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_kernel<kTwoState, false>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_kernel<kSingle, false>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_kernel<kAdjoint, false>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], trace_kernel<kReplay, false>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[4], trace_kernel<kTwoState, true>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[5], trace_kernel<kSingle, true>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[6], trace_kernel<kAdjoint, true>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[7], trace_kernel<kReplay, true>, kTraceBlock, 0);
-    for (int& b : blocks) b = b < 1 ? 1 : b;
+    for (int v = 0; v < 16; ++v) {
+      blocks[v] = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[v], kTraceKernels[v], kTraceBlock, 0);
+      if (blocks[v] < 1) blocks[v] = 1;
+    }
   });
-  return blocks[mode + (sg ? 4 : 0)];
+  return blocks[variant];
 }
 
 static int sm_count() {
@@ -285,7 +296,7 @@ static int sm_count() {
 }
 
 void warm_launch_config() {
-  (void)resident_blocks(kTwoState, false);
+  (void)resident_blocks(0);
   (void)sm_count();
 }
 
@@ -334,7 +345,8 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   RCV_REQUIRE(Q.defer <= 32, "defer must be in [1, 32]");
   RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
   const bool sg = supergrid || (jobs == nullptr && J.sg[0] > 0);
-  int per_sm = resident_blocks(mode, sg);
+  const int variant = trace_variant(mode, sg, counters != nullptr);
+  int per_sm = resident_blocks(variant);
   if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
   // replay: the checkpoint tasks come on top of one camera task per path
   const int64_t tasks = mode == kReplay ? 2 * total : total;
@@ -344,21 +356,7 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   const unsigned g = (unsigned)blocks;
-  if (sg) {
-    switch (mode) {
-      case kTwoState: trace_kernel<kTwoState, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-      case kSingle: trace_kernel<kSingle, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-      case kAdjoint: trace_kernel<kAdjoint, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-      default: trace_kernel<kReplay, true><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-    }
-  } else {
-    switch (mode) {
-      case kTwoState: trace_kernel<kTwoState, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-      case kSingle: trace_kernel<kSingle, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-      case kAdjoint: trace_kernel<kAdjoint, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-      default: trace_kernel<kReplay, false><<<g, kTraceBlock, 0, st>>>(J, Q); break;
-    }
-  }
+  kTraceKernels[variant]<<<g, kTraceBlock, 0, st>>>(J, Q);
   return launched("trace kernel launch");
 }
 

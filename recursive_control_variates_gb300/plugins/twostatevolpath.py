@@ -45,6 +45,9 @@ class _VolumeIntegratorBase:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         # run the adjoint's radiance pass beside the primal render (rcv.render)
         self.overlap_adjoint = bool(props.get("overlap_adjoint", True))
+        # accumulate the RCV_COUNTER_* event counts into counters() (the
+        # counting tracer variants hold the counts in registers)
+        self.count_events = bool(props.get("count_events", False))
         self.is_checked = False
         self._counters: dict[torch.device, torch.Tensor] = {}
         self._scratch: dict[torch.device, torch.Tensor] = {}
@@ -63,6 +66,10 @@ class _VolumeIntegratorBase:
         o.defer = self.defer
         o.order = self.order
         return o
+
+    def counters_ptr(self, device):
+        """Device address of counters() when counting, else None."""
+        return self.counters(device).data_ptr() if self.count_events else None
 
     def counters(self, device) -> torch.Tensor:
         device = torch.device(device)
@@ -131,7 +138,7 @@ class _VolumeIntegratorBase:
         side = self._side.get(dev)
         if side is None:
             side = self._side[dev] = torch.cuda.Stream(dev)
-        counters = self.counters(dev)
+        counters = self.counters_ptr(dev)
 
         def launch():
             self._drain_ticket(dev)
@@ -139,7 +146,7 @@ class _VolumeIntegratorBase:
             with torch.cuda.stream(side), profiling.region("trace_adjoint_radiance", dev):
                 _lib.check(
                     _lib.load().rcv_render_adjoint_radiance(
-                        C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, ws, counters.data_ptr(),
+                        C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, ws, counters,
                         side.cuda_stream,
                     ),
                     "rcv_render_adjoint_radiance",
@@ -198,7 +205,7 @@ class _VolumeIntegratorBase:
                 _lib.load().rcv_render_volume(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, img.data_ptr(),
                     self.scratch(medium.device, sensor, spp, _lib.MODE_SINGLE),
-                    self.counters(medium.device).data_ptr(), st,
+                    self.counters_ptr(medium.device), st,
                 ),
                 "rcv_render_volume",
             )
@@ -240,7 +247,7 @@ class _VolumeIntegratorBase:
             _lib.check(
                 getattr(_lib.load(), fn)(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, g.data_ptr(), gd.data_ptr(),
-                    ga.data_ptr() if ga is not None else None, ws, self.counters(dev).data_ptr(), st,
+                    ga.data_ptr() if ga is not None else None, ws, self.counters_ptr(dev), st,
                 ),
                 fn,
             )
@@ -298,7 +305,7 @@ class TwoStatePRBVolpathIntegrator(_VolumeIntegratorBase):
                 _lib.load().rcv_render_twostates_volume(
                     C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, H.data_ptr(), F.data_ptr(),
                     self.scratch(medium.device, sensor, spp, _lib.MODE_TWOSTATE),
-                    self.counters(medium.device).data_ptr(), st,
+                    self.counters_ptr(medium.device), st,
                 ),
                 "rcv_render_twostates_volume",
             )

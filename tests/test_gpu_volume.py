@@ -209,6 +209,7 @@ def test_adjoint_started_ahead_matches_full_adjoint(cuda):
         assert float((a - b).norm()) <= 2e-5 * float(a.norm())
     H2, F2 = integ.render_twostates(scene, 0, seed=9, spp=4)
     assert torch.equal(H, H2) and torch.equal(F, F2)
+    assert int(integ.counters(cuda).abs().sum()) == 0  # event counting is off by default
     # stale: another seed, or the parameters changed after the radiance pass
     integ.prefetch_adjoint(scene, 0, seed=6, spp=4)()
     integ.render_backward(scene, params, g, 0, seed=7, spp=4)
@@ -352,7 +353,7 @@ def test_supergrid_tracers_match_oracle(cuda, oracle, factor):
     of pixels, gradients 2e-5), and it samples fewer collisions."""
     scene, med, grids = make_scene(cuda, albedo_grid=True, D=24, res=32)
     osc = oracle_scene(oracle, scene, grids, 8, True, factor)
-    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8, "count_events": True})
     cnt_global = integ.counters(cuda).clone()
     integ.render_twostates(scene, 0, seed=3, spp=4)
     cnt_global = (integ.counters(cuda) - cnt_global).cpu().numpy()
