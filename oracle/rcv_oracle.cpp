@@ -633,11 +633,14 @@ struct Tracer {
       if (mode == kTwoState) {
         const V3 ao = albedo(S, S.alb_old, x, c);
         const V3 sso{st_o * ao.x, st_o * ao.y, st_o * ao.z};
-        const float den = st_n + st_o;
-        bn = V3{bn.x * ((2.0f * ssn.x) / den), bn.y * ((2.0f * ssn.y) / den), bn.z * ((2.0f * ssn.z) / den)};
-        bo = V3{bo.x * ((2.0f * sso.x) / den), bo.y * ((2.0f * sso.y) / den), bo.z * ((2.0f * sso.z) / den)};
+        // sigma_s / mean sigma_t as ss * (2 / (st_n + st_o)): for equal
+        // states 2 / (2 st) == 1 / st exactly, the single-state weight below
+        const float k2 = 2.0f / (st_n + st_o);
+        bn = V3{bn.x * (ssn.x * k2), bn.y * (ssn.y * k2), bn.z * (ssn.z * k2)};
+        bo = V3{bo.x * (sso.x * k2), bo.y * (sso.y * k2), bo.z * (sso.z * k2)};
       } else {
-        bn = V3{bn.x * (ssn.x / st_n), bn.y * (ssn.y / st_n), bn.z * (ssn.z / st_n)};
+        const float k1 = 1.0f / st_n;
+        bn = V3{bn.x * (ssn.x * k1), bn.y * (ssn.y * k1), bn.z * (ssn.z * k1)};
         if (sink) {
           const V3 Lr = remaining(Ln);
           const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;

@@ -178,9 +178,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       inv_mu = 1.0f / mu;
       half_inv_mu = 0.5f * inv_mu;
       // k-th pixel of the job's hand-out order, sample s of that pixel
-      const int64_t local = path - J.path_begin;
-      const uint32_t k = (uint32_t)(local / J.spp);
-      const uint32_t smp = (uint32_t)(local - (int64_t)k * J.spp);
+      // 32-bit index arithmetic: a job has fewer than 2^32 paths
+      const uint32_t local = (uint32_t)(path - J.path_begin);
+      const uint32_t uspp = (uint32_t)J.spp;
+      const uint32_t k = local / uspp;
+      const uint32_t smp = local - k * uspp;
       pix = J.pixel_order != nullptr ? (int)__ldg(J.pixel_order + k) : (int)k;
       sid = (uint32_t)pix * (uint32_t)J.spp + smp;
       seed_lane(rng, J.seed, sid);
@@ -215,7 +217,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       } else {
         const float u0 = next1d(rng), u1 = next1d(rng);
         V3 o;
-        camera_ray(J, pix % J.width, pix / J.width, u0, u1, o, d);
+        const uint32_t py = (uint32_t)pix / (uint32_t)J.width;
+        camera_ray(J, (int)((uint32_t)pix - py * (uint32_t)J.width), (int)py, u0, u1, o, d);
         (void)next1d(rng);  // colour channel for free-flight sampling (grey extinction)
         if (!roulette<kMode>(J, rng, depth, bn, bo)) {
           finished = true;
@@ -259,11 +262,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           // plugins/twostatevolpath.py:259-260
           const V3 ao = albedo_at(J, alk, 0);
           const V3 ss_o{st_o * ao.x, st_o * ao.y, st_o * ao.z};
-          const float den = st_n + st_o;
-          bn = V3{bn.x * ((2.0f * ss_n.x) / den), bn.y * ((2.0f * ss_n.y) / den),
-                  bn.z * ((2.0f * ss_n.z) / den)};
-          bo = V3{bo.x * ((2.0f * ss_o.x) / den), bo.y * ((2.0f * ss_o.y) / den),
-                  bo.z * ((2.0f * ss_o.z) / den)};
+          // one division: 2 / (st_n + st_o) equals 1 / st_n exactly for equal
+          // states, so those keep the single-state weights bit for bit
+          const float k2 = 2.0f / (st_n + st_o);
+          bn = V3{bn.x * (ss_n.x * k2), bn.y * (ss_n.y * k2), bn.z * (ss_n.z * k2)};
+          bo = V3{bo.x * (ss_o.x * k2), bo.y * (ss_o.y * k2), bo.z * (ss_o.z * k2)};
         } else {
           if (kMode == kReplay) {
             // d log(sigma_s) / d density and d log(albedo) / d albedo at the event
@@ -279,14 +282,22 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             }
           }
           // a checkpoint already holds the throughput after the event
-          if (!(kMode == kReplay && task == kTaskCheckpoint))
-            bn = V3{bn.x * (ss_n.x / st_n), bn.y * (ss_n.y / st_n), bn.z * (ss_n.z / st_n)};
+          if (!(kMode == kReplay && task == kTaskCheckpoint)) {
+            const float k1 = 1.0f / st_n;
+            bn = V3{bn.x * (ss_n.x * k1), bn.y * (ss_n.y * k1), bn.z * (ss_n.z * k1)};
+          }
         }
         if (kMode == kAdjoint) ck_state = rng.state;
         // isotropic phase sample (1D unused + 2D), plugins/twostatevolpath.py:275
         pcg_skip1(rng);
         const float pu0 = next1d(rng), pu1 = next1d(rng);
         wo_next = to_box(J, uniform_sphere(pu0, pu1));
+        {
+          // exit distance of the next segment, needed when the NEE walk
+          // ends; computed here, where many lanes run together
+          float a;
+          slab(p, recip(wo_next), a, t_rem);
+        }
         // NEE towards the environment, then ratio tracking
         const float nu0 = next1d(rng), nu1 = next1d(rng);
         w = to_box(J, uniform_sphere(nu0, nu1));
@@ -454,9 +465,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               trn = 1.0f;
               phase = kNeeAdj;
             } else {
-              d = wo_next;
-              float a;
-              slab(p, recip(d), a, t_rem);
+              d = wo_next;  // t_rem was set at the scattering event
               phase = kMain;
             }
           }
@@ -474,9 +483,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             done = trn == 0.0f;
           }
           if (done) {
-            d = wo_next;
-            float a;
-            slab(p, recip(d), a, t_rem);
+            d = wo_next;  // t_rem was set at the scattering event
             phase = kMain;
           }
         }
