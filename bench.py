@@ -715,8 +715,9 @@ def run_reference(args, cfg):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    # p50/p99 over >= 200 steps after >= 16 warm-up steps (optimize.py:105)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=16)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="cfg2")
     ap.add_argument("--no-e2e", action="store_true")
@@ -733,7 +734,7 @@ def main(argv=None):
     ap.add_argument("--majorant-factor", type=int, default=8,
                     help="also time the headline step with a majorant supergrid of this factor (0 = skip)")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--batched-steps", type=int, default=200)
     ap.add_argument("--plain-rounds", type=int, default=2)
     ap.add_argument("--served-requests", type=int, default=400)
     ap.add_argument("--target-spp", type=int, default=64, help="spp of the batched/served jobs' target renders")
