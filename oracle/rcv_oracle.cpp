@@ -334,6 +334,7 @@ void camera_ray(const oracle_scene& S, int px, int py, float u0, float u1, V3& o
 // interpolation reads there.  `two` bounds both states, `nw` the new one.
 struct Supergrid {
   int s[3] = {0, 0, 0};
+  float inv[3] = {0.0f, 0.0f, 0.0f};  // 1 / s
   std::vector<float> two, nw;
 
   static int64_t floordiv(int64_t a, int64_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
@@ -351,7 +352,10 @@ struct Supergrid {
     const int f = S.majorant_factor;
     if (f <= 0) return;
     const int D[3] = {S.dx, S.dy, S.dz};
-    for (int a = 0; a < 3; ++a) s[a] = (D[a] + f - 1) / f;
+    for (int a = 0; a < 3; ++a) {
+      s[a] = (D[a] + f - 1) / f;
+      inv[a] = 1.0f / (float)s[a];
+    }
     two.assign((size_t)s[0] * s[1] * s[2], 0.0f);
     nw.assign(two.size(), 0.0f);
     for (int cz = 0; cz < s[2]; ++cz)
@@ -388,12 +392,15 @@ struct Supergrid {
       const float n = (float)s[a];
       c[a] = std::min(std::max((int)std::floor(oo[a] * n), 0), s[a] - 1);
       st[a] = dd[a] > 0.0f ? 1 : (dd[a] < 0.0f ? -1 : 0);
+      // cell faces at c / s = c * (1 / s); one division per axis
       if (st[a] > 0) {
-        tn[a] = ((float)(c[a] + 1) / n - oo[a]) / dd[a];
-        td[a] = (1.0f / n) / dd[a];
+        const float inv_d = 1.0f / dd[a];
+        tn[a] = ((float)(c[a] + 1) * inv[a] - oo[a]) * inv_d;
+        td[a] = inv[a] * inv_d;
       } else if (st[a] < 0) {
-        tn[a] = ((float)c[a] / n - oo[a]) / dd[a];
-        td[a] = -(1.0f / n) / dd[a];
+        const float inv_d = 1.0f / dd[a];
+        tn[a] = ((float)c[a] * inv[a] - oo[a]) * inv_d;
+        td[a] = -(inv[a] * inv_d);
       } else {
         tn[a] = kInf;
         td[a] = kInf;

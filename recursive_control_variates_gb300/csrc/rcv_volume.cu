@@ -260,6 +260,7 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   J->sg[0] = supergrid_cells(m->dims[0], m->majorant_factor);
   J->sg[1] = supergrid_cells(m->dims[1], m->majorant_factor);
   J->sg[2] = supergrid_cells(m->dims[2], m->majorant_factor);
+  for (int a = 0; a < 3; ++a) J->sg_inv[a] = J->sg[a] > 0 ? 1.0f / (float)J->sg[a] : 0.0f;
   J->sg_two = J->sg[0] > 0 ? reinterpret_cast<const float*>(ws + L.sg_two) : nullptr;
   J->sg_new = J->sg[0] > 0 ? reinterpret_cast<const float*>(ws + L.sg_new) : nullptr;
   J->grad_cells = reinterpret_cast<float4*>(ws + L.grad_cells);

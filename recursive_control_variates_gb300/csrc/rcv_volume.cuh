@@ -77,6 +77,7 @@ struct VolJob {
   // majorant supergrid: cells per axis (0 = one global majorant) and the
   // cells' majorants for the two-state tracer / the single-state tracers
   int32_t sg[3];
+  float sg_inv[3];  // 1 / sg (host-computed)
   const float* sg_two;
   const float* sg_new;
 };
@@ -183,6 +184,28 @@ __device__ __forceinline__ float density_new(const VolJob& J, const Lookup& l) {
 __device__ __forceinline__ int clampi(int v, int hi) { return v < 0 ? 0 : (v > hi ? hi : v); }
 
 // ------------------------------------------------------- majorant supergrid
+// DDA set-up along one axis: cell of o, distance to the next cell face and
+// between faces, step direction (inv_n = 1 / S; one division).
+__device__ __forceinline__ void dda_axis(float o, float d, int S, float inv_n, int& c, float& tn, float& td,
+                                         int& step) {
+  c = clampi((int)floorf(o * (float)S), S - 1);
+  if (d > 0.0f) {
+    const float inv_d = 1.0f / d;
+    tn = ((float)(c + 1) * inv_n - o) * inv_d;
+    td = inv_n * inv_d;
+    step = 1;
+  } else if (d < 0.0f) {
+    const float inv_d = 1.0f / d;
+    tn = ((float)c * inv_n - o) * inv_d;
+    td = -(inv_n * inv_d);
+    step = -1;
+  } else {
+    tn = kInf;
+    td = kInf;
+    step = 0;
+  }
+}
+
 // Free-flight distance of optical depth `tau` along o + t d, t in [0, tmax],
 // through the majorant supergrid (plugins/twostatemedium.py:25-70): a DDA
 // walk (Amanatides & Woo) accumulates majorant x segment length per cell and
@@ -191,37 +214,22 @@ __device__ __forceinline__ int clampi(int v, int hi) { return v < 0 ? 0 : (v > h
 // midpoint: the same cell up to floating-point ties on cell faces), and the
 // sampled collision takes that cell's majorant, so sigma_n >= 0.  Returns
 // kInf when the walk leaves the segment.
+// The walk keeps its state in scalars (a dynamically indexed array would
+// live in local memory).
 __device__ __forceinline__ float supergrid_flight(const VolJob& J, const float* __restrict__ maj, const V3& o,
                                                   const V3& d, float tmax, float tau, float& mu_at) {
-  const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
-  float tn[3], td[3];
-  int c[3], step[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float S = (float)J.sg[a];
-    c[a] = clampi((int)floorf(oo[a] * S), J.sg[a] - 1);
-    if (dd[a] > 0.0f) {
-      tn[a] = ((float)(c[a] + 1) / S - oo[a]) / dd[a];
-      td[a] = (1.0f / S) / dd[a];
-      step[a] = 1;
-    } else if (dd[a] < 0.0f) {
-      tn[a] = ((float)c[a] / S - oo[a]) / dd[a];
-      td[a] = -(1.0f / S) / dd[a];
-      step[a] = -1;
-    } else {
-      tn[a] = kInf;
-      td[a] = kInf;
-      step[a] = 0;
-    }
-  }
+  int c0, c1, c2, s0, s1, s2;
+  float tn0, tn1, tn2, td0, td1, td2;
+  dda_axis(o.x, d.x, J.sg[0], J.sg_inv[0], c0, tn0, td0, s0);
+  dda_axis(o.y, d.y, J.sg[1], J.sg_inv[1], c1, tn1, td1, s1);
+  dda_axis(o.z, d.z, J.sg[2], J.sg_inv[2], c2, tn2, td2, s2);
   const int sx = J.sg[0], sxy = J.sg[0] * J.sg[1];
   float t = 0.0f, tau_acc = 0.0f;
   const int max_steps = J.sg[0] + J.sg[1] + J.sg[2] + 4;
   for (int s = 0; s < max_steps; ++s) {
-    const float t_next = fminf(fminf(tn[0], tn[1]), tn[2]);
-    const int k = tn[0] == t_next ? 0 : (tn[1] == t_next ? 1 : 2);
-    const float m = __ldg(maj + clampi(c[2], J.sg[2] - 1) * sxy + clampi(c[1], J.sg[1] - 1) * sx +
-                          clampi(c[0], J.sg[0] - 1));
+    const float t_next = fminf(fminf(tn0, tn1), tn2);
+    const float m = __ldg(maj + clampi(c2, J.sg[2] - 1) * sxy + clampi(c1, J.sg[1] - 1) * sx +
+                          clampi(c0, J.sg[0] - 1));
     const float tau_next = tau_acc + m * (t_next - t);
     if (m > 0.0f && tau_next >= tau) {
       const float t_hit = t + (tau - tau_acc) / m;
@@ -230,8 +238,16 @@ __device__ __forceinline__ float supergrid_flight(const VolJob& J, const float* 
       return t_hit;
     }
     if (!(t_next < tmax)) break;
-    tn[k] += td[k];
-    c[k] += step[k];
+    if (tn0 == t_next) {
+      tn0 += td0;
+      c0 += s0;
+    } else if (tn1 == t_next) {
+      tn1 += td1;
+      c1 += s1;
+    } else {
+      tn2 += td2;
+      c2 += s2;
+    }
     t = t_next;
     tau_acc = tau_next;
   }
