@@ -9,11 +9,15 @@ namespace rcv {
 
 // Cell i of a (dx+1)(dy+1)(dz+1) lattice: the 8 clamped corner voxels of the
 // old and the new density.
+// 32-bit index arithmetic: 4 (dx+1)(dy+1)(dz+1) < 2^32 is enforced on the host.
 __device__ __forceinline__ void pack_cell(int64_t i, int dx, int dy, int dz, const float* __restrict__ old_d,
                                           const float* __restrict__ new_d, float4* __restrict__ cells) {
-  const int cx = int(i % (dx + 1));
-  const int cy = int((i / (dx + 1)) % (dy + 1));
-  const int cz = int(i / (int64_t(dx + 1) * (dy + 1)));
+  const uint32_t ex = (uint32_t)(dx + 1), ey = (uint32_t)(dy + 1);
+  const uint32_t row = (uint32_t)i / ex;
+  const int cx = int((uint32_t)i - row * ex);
+  const uint32_t cz_u = row / ey;
+  const int cy = int(row - cz_u * ey);
+  const int cz = int(cz_u);
   const int x0 = clampi(cx - 1, dx - 1), x1 = clampi(cx, dx - 1);
   const int y0 = clampi(cy - 1, dy - 1), y1 = clampi(cy, dy - 1);
   const int z0 = clampi(cz - 1, dz - 1), z1 = clampi(cz, dz - 1);
@@ -121,7 +125,11 @@ __device__ __forceinline__ int fold_candidates(int i, int D, int* cell, int* bit
 
 // Gradient of voxel i: the sum of its corner entries in every cell that uses it.
 __device__ __forceinline__ float fold_voxel(int64_t i, int dx, int dy, int dz, const float* __restrict__ gcells) {
-  const int x = int(i % dx), y = int((i / dx) % dy), z = int(i / (int64_t(dx) * dy));
+  // 32-bit index arithmetic (the voxel count is below the cell count, < 2^30)
+  const uint32_t row = (uint32_t)i / (uint32_t)dx;
+  const int x = int((uint32_t)i - row * (uint32_t)dx);
+  const uint32_t z_u = row / (uint32_t)dy;
+  const int y = int(row - z_u * (uint32_t)dy), z = int(z_u);
   int cxs[4], bxs[4], cys[4], bys[4], czs[4], bzs[4];
   const int nx = fold_candidates(x, dx, cxs, bxs);
   const int ny = fold_candidates(y, dy, cys, bys);

@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 
 #include "rcv_common.h"
 #include "rcv_pack.cuh"
@@ -389,9 +390,18 @@ static int vps_setup(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath
   return RCV_OK;
 }
 
+// Grid-stride launch: at most 16 blocks of 128 threads per SM.
 static unsigned vps_grid(int64_t paths) {
+  static std::once_flag once;
+  static int sms = 1;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  });
   int64_t blocks = (paths + 127) / 128;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > int64_t(sms) * 16) blocks = int64_t(sms) * 16;
   return (unsigned)(blocks < 1 ? 1 : blocks);
 }
 
