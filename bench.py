@@ -355,6 +355,7 @@ def run_ours(args, cfg):
     has_albedo = job.has_albedo
     del job
     torch.cuda.empty_cache()
+    surface = None if args.no_surface else surface_form(args, device, dist, world, flush)
     # the batched and served forms run on a single GPU only (rank 0 of one)
     batched = None if (args.no_batched or world > 1) else batched_form(args, device, flush)
     served = None if (args.no_served or world > 1) else served_form(args, device)
@@ -381,6 +382,7 @@ def run_ours(args, cfg):
         "phase": "late (density starts at 0.8 x the true grid)",
         "early_phase": early,
         "supergrid": supergrid,
+        "surface": surface,
         "batched": batched,
         "served": served,
     }
@@ -388,6 +390,61 @@ def run_ours(args, cfg):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def surface_form(args, device, dist, world, flush):
+    """cfg3: the two-state surface tracer (`twostateprb`) step on a 1024^2
+    film (ground plane with a 512^2 RGB texture, 3 spheres, an area light),
+    spp 8, depth 8, through the plain API; device-timed steps."""
+    import torch
+
+    import recursive_control_variates_gb300 as rcv
+    from recursive_control_variates_gb300 import scenes
+
+    cfg = scenes.SURFACE_CONFIGS["cfg3"]
+    true_tex = scenes.value_noise(cfg.tex_res, 7)
+    ref_scene = rcv.load_dict(scenes.surface_scene_dict(true_tex, cfg.res), device=device)
+    base = rcv.load_dict({"type": "twostateprb", "max_depth": cfg.max_depth, "rr_depth": cfg.rr_depth})
+    target = base.render(ref_scene, 0, seed=17843, spp=64).contiguous()
+    del ref_scene
+    init = np.full_like(true_tex, cfg.init)
+    scene = rcv.load_dict(scenes.surface_scene_dict(init, cfg.res), device=device)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprb", "max_depth": cfg.max_depth,
+                                                         "rr_depth": cfg.rr_depth}})
+    opt = rcv.ad.Adam(lr=cfg.lr)
+    opt[scenes.TEXTURE_KEY] = init
+    opt.set_bounds(scenes.TEXTURE_KEY, 0.0, 1.0)
+    params.update(opt)
+    params.update(opt)
+    it = [0]
+
+    def step():
+        params.update(opt)
+        img = rcv.render(scene, params, integrator=integ, seed=replica_seed(dist_info()[0]) + it[0], spp=cfg.spp)
+        rcv.l2_loss(img, target).backward()
+        opt.step()
+        it[0] += 1
+
+    for _ in range(args.warmup):
+        step()
+    stream = torch.cuda.current_stream(device)
+    steps = max(args.steps // 4, 10)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i, (a, b) in enumerate(ev):
+        flush.fill_(float(i))
+        a.record(stream)
+        step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sorted(a.elapsed_time(b) for a, b in ev)
+    total = reduce_max(sum(ms) / 1e3, dist, device)
+    paths = cfg.paths_per_step()
+    return {"workload": f"cfg3: {cfg.res}^2 two-state surface scene (plane + {cfg.tex_res}^2 RGB texture, 3 spheres, "
+                        f"area light), spp={cfg.spp}, spp_grad={cfg.spp_grad}, max_depth={cfg.max_depth}, cv_ps",
+            "value": paths * world * steps / total, "unit": UNIT, "ms_per_step": total * 1e3 / steps, "steps": steps,
+            "p50_ms": pctl(ms, 0.5), "p99_ms": pctl(ms, 0.99), "paths_per_step": paths}
 
 
 def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_factor=0):
@@ -726,6 +783,7 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (cfg4) form")
+    ap.add_argument("--no-surface", action="store_true", help="skip the surface-scene (cfg3) step")
     ap.add_argument("--no-served", action="store_true", help="skip the served (cfg5) form")
     ap.add_argument("--form", choices=["all", "batched", "served"], default="all",
                     help="all: the headline line (plain cfg2) with the batched and served forms; batched / served: "
