@@ -229,6 +229,22 @@ int rcv_render_backward_volume(const rcv_medium* medium, const rcv_sensor* senso
                                const float* grad_img, float* grad_density, float* grad_albedo,
                                void* workspace, uint64_t* counters, void* stream);
 
+/* Forward-mode derivative of the single-state render on the current
+ * parameters along a tangent of the density grid ([Dz][Dy][Dx], device, or
+ * NULL) and / or of the albedo grid ([aDz][aDy][aDx][3], device, or NULL):
+ * dimg ([height][width][3], overwritten) = d image / d epsilon at
+ * theta + epsilon * tangent, estimated by path replay with `spp` paths per
+ * pixel from `seed` (the same radiance pass as rcv_render_backward_volume,
+ * then the replay tasks gather the tangent where the adjoint scatters).
+ * The medium's gradient accumulators are overwritten.  Replaces
+ * CVIntegrator.render_forward / MetaIntegrator.render_forward
+ * (plugins/cv_integrator.py:79-85, plugins/metaintegrator.py:132-138), i.e.
+ * the forward mode of the path-replay integrator. */
+int rcv_render_forward_volume(const rcv_medium* medium, const rcv_sensor* sensor,
+                              const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                              const float* tangent_density, const float* tangent_albedo, float* dimg,
+                              void* workspace, uint64_t* counters, void* stream);
+
 /* rcv_render_backward_volume in two calls.  The first pass of the adjoint
  * (each path's radiance and its scatter checkpoints) does not depend on
  * grad_img, so it can run as soon as the parameters are known — e.g. on a

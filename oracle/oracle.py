@@ -146,6 +146,8 @@ def lib():
         L.oracle_backward.argtypes = [C.POINTER(OracleScene), C.c_uint32, C.c_int, vp, vp, vp, C.c_int, C.c_int,
                                       C.c_int, C.c_int]
         L.oracle_backward.restype = C.c_int
+        L.oracle_forward.argtypes = [C.POINTER(OracleScene), C.c_uint32, C.c_int, vp, vp, vp, C.c_int]
+        L.oracle_forward.restype = C.c_int
         L.oracle_surface_render.argtypes = [C.POINTER(OracleSurface), C.c_int, C.c_uint32, C.c_int, vp, vp, C.c_int]
         L.oracle_surface_render.restype = C.c_int
         L.oracle_surface_backward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int]
@@ -294,6 +296,20 @@ def backward(scene: Scene, seed: int, spp: int, grad_img, threads: int | None = 
     if rc:
         raise ValueError("oracle_backward: invalid arguments")
     return gd, ga
+
+
+def forward(scene: Scene, seed: int, spp: int, tangent_density=None, tangent_albedo=None,
+            threads: int | None = None):
+    """Forward-mode derivative image (float32 [H][W][3]) of the single-state
+    render along the given tangents."""
+    td = None if tangent_density is None else np.ascontiguousarray(tangent_density, np.float32)
+    ta = None if tangent_albedo is None else np.ascontiguousarray(tangent_albedo, np.float32)
+    out = np.zeros((scene.height, scene.width, 3), np.float32)
+    rc = lib().oracle_forward(C.byref(scene.c), seed & 0xFFFFFFFF, spp, None if td is None else td.ctypes.data,
+                              None if ta is None else ta.ctypes.data, out.ctypes.data, threads or default_threads())
+    if rc:
+        raise ValueError("oracle_forward: invalid arguments")
+    return out
 
 
 def sample_tea_32(v0: int, v1: int) -> int:

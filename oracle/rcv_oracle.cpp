@@ -430,9 +430,19 @@ struct Supergrid {
 };
 
 // Gradient sink of the adjoint (double accumulators, one per worker).
+// Where the adjoint's gradient terms go: scattered into voxel gradients, or
+// (forward mode, tan_d / tan_a set) gathered against a tangent field into
+// `acc`, the derivative of the path's contribution along the tangent.
 struct GradSink {
   std::vector<double> dens, alb;
+  const float* tan_d = nullptr;  // [dz][dy][dx] density tangent
+  const float* tan_a = nullptr;  // [adz][ady][adx][3] albedo tangent
+  double acc = 0.0;
   void density(const oracle_scene& S, const Corners& c, float g) {
+    if (tan_d != nullptr || tan_a != nullptr) {
+      if (tan_d != nullptr) acc += (double)g * (double)trilinear(S, tan_d, 1, 0, c);
+      return;
+    }
     const float gx0 = 1.0f - c.fx, gy0 = 1.0f - c.fy, gz0 = 1.0f - c.fz;
     const float a = g * gz0, b = g * c.fz;
     const float a0 = a * gy0, a1 = a * c.fy, b0 = b * gy0, b1 = b * c.fy;
@@ -446,6 +456,14 @@ struct GradSink {
     dens[vidx(S, c.x1, c.y1, c.z1)] += b1 * c.fx;
   }
   void albedo(const oracle_scene& S, const V3& x, const Corners& dc, const V3& g) {
+    if (tan_d != nullptr || tan_a != nullptr) {
+      if (tan_a != nullptr) {
+        const Corners a = albedo_corners(S, x, dc);
+        acc += (double)g.x * albedo_channel(S, tan_a, 0, a) + (double)g.y * albedo_channel(S, tan_a, 1, a) +
+               (double)g.z * albedo_channel(S, tan_a, 2, a);
+      }
+      return;
+    }
     if (alb.empty()) return;
     const Corners c = albedo_corners(S, x, dc);
     const float wx[2] = {1.0f - c.fx, c.fx}, wy[2] = {1.0f - c.fy, c.fy}, wz[2] = {1.0f - c.fz, c.fz};
@@ -833,6 +851,44 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
     if (alb)
       for (int64_t i = 0; i < na * 3; ++i) grad_albedo[i] += s.alb[i];
   }
+  return 0;
+}
+
+// Forward-mode derivative image [height][width][3] of the single-state
+// render along a density tangent [dz][dy][dx] and / or an albedo tangent
+// [adz][ady][adx][3] (either may be null): per sample and channel k, the
+// adjoint replay with dL = e_k gathers the tangent where it would scatter.
+int oracle_forward(const oracle_scene* S, uint32_t seed, int spp, const float* tan_d, const float* tan_a,
+                   float* out, int threads) {
+  if (!S || spp <= 0 || !out || (!tan_d && !tan_a)) return -1;
+  const float mu = S->scale * grid_max(*S, S->dens_new);
+  Supergrid sg;
+  sg.build(*S);
+  const float* ta = S->alb_new != nullptr ? tan_a : nullptr;
+  parallel_rows(0, S->height, 1, threads, [&](int, int y0, int y1) {
+    for (int py = y0; py < y1; ++py)
+      for (int px = 0; px < S->width; ++px) {
+        const int pix = py * S->width + px;
+        double d[3] = {0.0, 0.0, 0.0};
+        for (int s = 0; s < spp; ++s) {
+          const uint32_t lane = (uint32_t)((int64_t)pix * spp + s);
+          Tracer primal{*S, kSingle, mu, nullptr};
+          primal.sg = &sg;
+          const PathOut o = primal.trace(seed, lane, px, py);
+          for (int k = 0; k < 3; ++k) {
+            GradSink g;
+            g.tan_d = tan_d;
+            g.tan_a = ta;
+            const V3 e{k == 0 ? 1.0f : 0.0f, k == 1 ? 1.0f : 0.0f, k == 2 ? 1.0f : 0.0f};
+            Tracer adj{*S, kSingle, mu, &g, e, o.L_new};
+            adj.sg = &sg;
+            adj.trace(seed, lane, px, py);
+            d[k] += g.acc;
+          }
+        }
+        for (int k = 0; k < 3; ++k) out[pix * 3 + k] = (float)(d[k] / spp);
+      }
+  });
   return 0;
 }
 

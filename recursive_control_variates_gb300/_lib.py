@@ -218,6 +218,10 @@ SIGNATURES = {
         C.c_int,
         [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
     ),
+    "rcv_render_forward_volume": (
+        C.c_int,
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp, vp],
+    ),
     "rcv_render_adjoint_radiance": (
         C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp]
     ),

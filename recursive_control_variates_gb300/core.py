@@ -738,7 +738,14 @@ class SceneParameters:
         return self
 
     def differentiable(self) -> dict[str, torch.Tensor]:
-        return {k: v for k, v in self._values.items() if isinstance(v, torch.Tensor) and v.requires_grad}
+        """Values that take part in differentiation: tensors that require a
+        gradient (reverse mode) or carry a forward-mode tangent."""
+        from torch.autograd import forward_ad
+
+        def tracked(v):
+            return v.requires_grad or forward_ad.unpack_dual(v).tangent is not None
+
+        return {k: v for k, v in self._values.items() if isinstance(v, torch.Tensor) and tracked(v)}
 
     def owner_of(self, key):
         return self._owners[key]

@@ -33,6 +33,11 @@
 //             the same random numbers and scatters the gradients; a task
 //             stops at the next scattering event, which has its own task.
 // A path whose checkpoints did not fit is replayed whole by its camera task.
+//   kForward  the same replay tasks for forward-mode derivatives: at each
+//             event where kReplay scatters dL . L_rem times a factor into the
+//             grid gradient, it adds L_rem times the factor applied to the
+//             tangent field to the task's image derivative, which goes to its
+//             pixel at the end of the task.
 // Replaying segments instead of whole paths keeps every task short, so the
 // launch does not end on a few paths that scatter dozens of times.
 #pragma once
@@ -81,9 +86,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   const float mis = 0.5f;  // power heuristic between two equal 1/(4 pi) pdfs
   const float emit_weight = 1.0f / kInvFourPi;
   const unsigned defer = (unsigned)Q.defer;
+  // replay tasks, scattering the image gradient (kReplay) or gathering a
+  // tangent field (kForward)
+  constexpr bool kRep = kMode == kReplay || kMode == kForward;
   // replay: camera tasks [0, paths), then the checkpoints that were written
   const int64_t total =
-      kMode == kReplay ? Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap) : Q.total;
+      kRep ? Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap) : Q.total;
 
   int64_t batch_next = 0, batch_end = 0;
   bool queue_empty = false;
@@ -93,7 +101,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   float mu = 0.0f, inv_mu = 0.0f, half_inv_mu = 0.0f;
   int pix = 0;
   uint32_t sid = 0;  // sample index within the job: pixel * spp + sample
-  V3 dL{0.0f, 0.0f, 0.0f};
+  V3 dL{0.0f, 0.0f, 0.0f};  // kReplay: dLoss/dL of the pixel; kForward: the task's image derivative
 
   Pcg32 rng, rng_nee;  // rng_nee: whole-path replay, stream of the second shadow walk
   // main path state
@@ -160,7 +168,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     if (run_start && phase == kStart) {
       iter0 = n_iter;
       // replay: a checkpoint task resumes at its scattering event
-      const bool resume = kMode == kReplay && path >= Q.total;
+      const bool resume = kRep && path >= Q.total;
       float4 r0, r1, r2, r3;
       if (resume) {
         const float4* rec = Q.ckpt + (path - Q.total) * 4;
@@ -192,10 +200,14 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       Ln = V3{0, 0, 0};
       depth = 0;
       if (kMode == kAdjoint) ck_lost = false;
-      if (kMode == kReplay) {
-        const float* g = J.grad_img + (int64_t)pix * 3;
-        const float fs = (float)J.spp;
-        dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
+      if (kRep) {
+        if (kMode == kReplay) {
+          const float* g = J.grad_img + (int64_t)pix * 3;
+          const float fs = (float)J.spp;
+          dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
+        } else {
+          dL = V3{0.0f, 0.0f, 0.0f};
+        }
         const float4 lt = Q.path_ltot[path];
         Ltot = V3{lt.x, lt.y, lt.z};
         task = resume ? kTaskCheckpoint : (lt.w != 0.0f ? kTaskWhole : kTaskSegment);
@@ -248,9 +260,9 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     // ------------------------------------------------- real scattering event
     if (run_scat && phase == kScatter) {
       const VolJob& J = *Jp;
-      if (kMode == kReplay && task == kTaskSegment) {
+      if (kRep && task == kTaskSegment) {
         finished = true;  // the event has its own checkpoint task
-      } else if (kMode == kReplay && task == kTaskCheckpoint && !own_event) {
+      } else if (kRep && task == kTaskCheckpoint && !own_event) {
         finished = true;
       } else {
         const Lookup lk = locate(J, p);
@@ -280,9 +292,22 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                           (dL.z * Lr.z) / fmaxf(an.z, 1e-8f)};
               scatter_albedo(J, alk, ga);
             }
+          } else if (kMode == kForward) {
+            // the same terms applied to the tangent field: L_rem times
+            // d log(sigma_s) along the tangent, per channel
+            const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+            const float f = (J.scale * tangent_density(J, lk)) / st_n;
+            dL = V3{dL.x + Lr.x * f, dL.y + Lr.y * f, dL.z + Lr.z * f};
+            if (kCount) ++cnt.grad_events;
+            if (J.grad_albedo != nullptr) {
+              if (kCount) ++cnt.albedo_events;
+              const V3 ta = tangent_albedo(J, alk);
+              dL = V3{dL.x + Lr.x * (ta.x / fmaxf(an.x, 1e-8f)), dL.y + Lr.y * (ta.y / fmaxf(an.y, 1e-8f)),
+                      dL.z + Lr.z * (ta.z / fmaxf(an.z, 1e-8f))};
+            }
           }
           // a checkpoint already holds the throughput after the event
-          if (!(kMode == kReplay && task == kTaskCheckpoint)) {
+          if (!(kRep && task == kTaskCheckpoint)) {
             const float k1 = 1.0f / st_n;
             bn = V3{bn.x * (ss_n.x * k1), bn.y * (ss_n.y * k1), bn.z * (ss_n.z * k1)};
           }
@@ -309,11 +334,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         tro = 1.0f;
         trn = 1.0f;
         phase = kNee;
-        if (kMode == kReplay) {
+        if (kRep) {
           if (task == kTaskCheckpoint) {
             // NEE contribution known from the radiance pass: one shadow walk
-            // on the main stream scatters its gradient
-            s_nee = (dL.x * cn_task.x + dL.y * cn_task.y) + dL.z * cn_task.z;
+            // on the main stream scatters its gradient (gathers the tangent)
+            if (kMode == kReplay) s_nee = (dL.x * cn_task.x + dL.y * cn_task.y) + dL.z * cn_task.z;
             Ln = V3{Ln.x + cn_task.x, Ln.y + cn_task.y, Ln.z + cn_task.z};
             own_event = false;
             phase = kNeeAdj;
@@ -340,7 +365,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         org = q;
         dir = w;
         tmax = tr_rem;
-        if (kMode == kReplay && phase == kNeeAdj && task == kTaskWhole) r = &rng_nee;
+        if (kRep && phase == kNeeAdj && task == kTaskWhole) r = &rng_nee;
       }
       if (!alive) {
         finished = true;
@@ -402,6 +427,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
                 scatter_density(J, lk, -(J.scale * sd) / sn);
                 if (kCount) ++cnt.grad_events;
+              } else if (kMode == kForward) {
+                const float sn = mu_c - st_n;
+                const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+                const float f = -(J.scale * tangent_density(J, lk)) / sn;
+                dL = V3{dL.x + Lr.x * f, dL.y + Lr.y * f, dL.z + Lr.z * f};
+                if (kCount) ++cnt.grad_events;
               }
               p = x;
               t_rem = t_rem - t;
@@ -455,10 +486,13 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
                       Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
             }
-            if (kMode == kReplay) {
+            if (kRep) {
               // whole-path replay: walk the shadow ray again (saved stream) to
               // back-propagate through its transmittance
-              s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
+              if (kMode == kReplay)
+                s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
+              else
+                cn_task = cn;
               q = p;
               float a;
               slab(q, recip(w), a, tr_rem);
@@ -474,7 +508,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           if (valid) {
             const float sn = mu_c - st_n;
             if (sn > 0.0f) {
-              scatter_density(J, lk, -(J.scale * s_nee) / sn);
+              if (kMode == kForward) {
+                const float f = -(J.scale * tangent_density(J, lk)) / sn;
+                dL = V3{dL.x + cn_task.x * f, dL.y + cn_task.y * f, dL.z + cn_task.z * f};
+              } else {
+                scatter_density(J, lk, -(J.scale * s_nee) / sn);
+              }
               if (kCount) ++cnt.grad_events;
             }
             trn = trn * (sn * inv_c);
@@ -498,7 +537,16 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
       }
       if (kMode == kAdjoint) Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f);
-      if (kCount && kMode != kReplay) ++cnt.paths;
+      if (kMode == kForward && (dL.x != 0.0f || dL.y != 0.0f || dL.z != 0.0f)) {
+        // the task's share of its pixel's derivative (the pixel value is the
+        // mean of its samples)
+        const float fs = (float)Jp->spp;
+        float* o = Jp->out_img + (int64_t)pix * 3;
+        atomicAdd(o + 0, dL.x / fs);
+        atomicAdd(o + 1, dL.y / fs);
+        atomicAdd(o + 2, dL.z / fs);
+      }
+      if (kCount && !kRep) ++cnt.paths;
       if (Jp->pixel_cost != nullptr) atomicAdd(Jp->pixel_cost + pix, n_iter - iter0);
       phase = kIdle;
     }

@@ -63,20 +63,22 @@ __global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_cons
   if (kCount) add_counts(Q.counters, cnt);
 }
 
-// Tracer variants by index mode + 4 * supergrid + 8 * counting.
+// Tracer variants by index mode + kTraceModes * (supergrid + 2 * counting).
 using TraceKernel = void (*)(VolJob, Queue);
-static const TraceKernel kTraceKernels[16] = {
-    trace_kernel<kTwoState, false, false>, trace_kernel<kSingle, false, false>,
-    trace_kernel<kAdjoint, false, false>,  trace_kernel<kReplay, false, false>,
-    trace_kernel<kTwoState, true, false>,  trace_kernel<kSingle, true, false>,
-    trace_kernel<kAdjoint, true, false>,   trace_kernel<kReplay, true, false>,
-    trace_kernel<kTwoState, false, true>,  trace_kernel<kSingle, false, true>,
-    trace_kernel<kAdjoint, false, true>,   trace_kernel<kReplay, false, true>,
-    trace_kernel<kTwoState, true, true>,   trace_kernel<kSingle, true, true>,
-    trace_kernel<kAdjoint, true, true>,    trace_kernel<kReplay, true, true>,
+template <bool kSG, bool kCount>
+struct TraceVariants {
+  static constexpr TraceKernel k[kTraceModes] = {
+      trace_kernel<kTwoState, kSG, kCount>, trace_kernel<kSingle, kSG, kCount>,
+      trace_kernel<kAdjoint, kSG, kCount>, trace_kernel<kReplay, kSG, kCount>,
+      trace_kernel<kForward, kSG, kCount>};
 };
+static const TraceKernel* const kTraceTables[4] = {
+    TraceVariants<false, false>::k, TraceVariants<true, false>::k, TraceVariants<false, true>::k,
+    TraceVariants<true, true>::k};
+constexpr int kTraceVariants = 4 * kTraceModes;
 
-static int trace_variant(int mode, bool sg, bool count) { return mode + (sg ? 4 : 0) + (count ? 8 : 0); }
+static int trace_variant(int mode, bool sg, bool count) { return mode + kTraceModes * ((sg ? 1 : 0) + (count ? 2 : 0)); }
+static TraceKernel trace_kernel_of(int variant) { return kTraceTables[variant / kTraceModes][variant % kTraceModes]; }
 
 // Majorant supergrid of a medium (both states' cells and the new state's).
 __global__ void supergrid_kernel(int sx, int sy, int sz, int dx, int dy, int dz, float scale,
@@ -172,6 +174,32 @@ __global__ void fold_albedo_kernel(int64_t nv, const float4* __restrict__ ga,
   grad[i * 3 + 0] += g.x;
   grad[i * 3 + 1] += g.y;
   grad[i * 3 + 2] += g.z;
+}
+
+// Forward mode: the tangent of the density packed like a cell gradient
+// record (8 corners, the layout tangent_density reads), and the albedo
+// tangent as one float4 per albedo voxel.
+__global__ void pack_tangent_kernel(int dx, int dy, int dz, const float* __restrict__ t,
+                                    float4* __restrict__ cells) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= int64_t(dx + 1) * (dy + 1) * (dz + 1)) return;
+  const uint32_t ex = (uint32_t)(dx + 1), ey = (uint32_t)(dy + 1);
+  const uint32_t row = (uint32_t)i / ex;
+  const int cx = int((uint32_t)i - row * ex);
+  const uint32_t cz_u = row / ey;
+  const int cy = int(row - cz_u * ey), cz = int(cz_u);
+  const int x0 = clampi(cx - 1, dx - 1), x1 = clampi(cx, dx - 1);
+  const int y0 = clampi(cy - 1, dy - 1), y1 = clampi(cy, dy - 1);
+  const int z0 = clampi(cz - 1, dz - 1), z1 = clampi(cz, dz - 1);
+  auto v = [&](int x, int y, int z) { return t[(int64_t(z) * dy + y) * dx + x]; };
+  cells[i * 2 + 0] = make_float4(v(x0, y0, z0), v(x1, y0, z0), v(x0, y1, z0), v(x1, y1, z0));
+  cells[i * 2 + 1] = make_float4(v(x0, y0, z1), v(x1, y0, z1), v(x0, y1, z1), v(x1, y1, z1));
+}
+
+__global__ void pack_tangent_albedo_kernel(int64_t na, const float* __restrict__ t, float4* __restrict__ out) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= na) return;
+  out[i] = make_float4(t[i * 3 + 0], t[i * 3 + 1], t[i * 3 + 2], 0.0f);
 }
 
 // ------------------------------------------------------------- host helpers
@@ -273,11 +301,11 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
 // Resident blocks per SM of each tracer variant (queried once per process).
 static int resident_blocks(int variant) {
   static std::once_flag once;
-  static int blocks[16];
+  static int blocks[kTraceVariants];
   std::call_once(once, [] {
-    for (int v = 0; v < 16; ++v) {
+    for (int v = 0; v < kTraceVariants; ++v) {
       blocks[v] = 1;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[v], kTraceKernels[v], kTraceBlock, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[v], trace_kernel_of(v), kTraceBlock, 0);
       if (blocks[v] < 1) blocks[v] = 1;
     }
   });
@@ -328,7 +356,7 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   std::memset(&Q, 0, sizeof(Q));
   Q.counter = queue_counter;
   Q.path_out = (mode == kTwoState || mode == kSingle) ? path_out : nullptr;
-  if (mode == kAdjoint || mode == kReplay) {
+  if (mode == kAdjoint || mode == kReplay || mode == kForward) {
     RCV_REQUIRE(adj != nullptr && adj->ckpt && adj->ckpt_count && adj->path_ltot, "adjoint buffers missing");
     RCV_REQUIRE(total < (int64_t(1) << 32), "an adjoint launch must have fewer than 2^32 paths");
     Q.ckpt = adj->ckpt;
@@ -350,14 +378,14 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   int per_sm = resident_blocks(variant);
   if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
   // replay: the checkpoint tasks come on top of one camera task per path
-  const int64_t tasks = mode == kReplay ? 2 * total : total;
+  const int64_t tasks = (mode == kReplay || mode == kForward) ? 2 * total : total;
   const int64_t warps_needed = (tasks + Q.batch - 1) / Q.batch;
   int64_t blocks = (warps_needed + (kTraceBlock / 32) - 1) / (kTraceBlock / 32);
   const int64_t cap = int64_t(sm_count()) * per_sm;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   const unsigned g = (unsigned)blocks;
-  kTraceKernels[variant]<<<g, kTraceBlock, 0, st>>>(J, Q);
+  trace_kernel_of(variant)<<<g, kTraceBlock, 0, st>>>(J, Q);
   return launched("trace kernel launch");
 }
 
@@ -458,7 +486,7 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
 // Adjoint stages: both launches, the radiance pass alone, or the replay alone
 // (which reuses the pixel order, checkpoints and total radiance the radiance
 // pass left in the same workspace).
-enum AdjStage { kAdjBoth = 0, kAdjRadiance = 1, kAdjReplay = 2 };
+enum AdjStage { kAdjBoth = 0, kAdjRadiance = 1, kAdjReplay = 2, kAdjForward = 3 };
 
 static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, void* workspace,
                           uint64_t* counters, float* img_new, float* img_old, cudaStream_t st,
@@ -497,7 +525,8 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
       rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
       if (rc || stage == kAdjRadiance) return rc;
     }
-    return launch_persistent(kReplay, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
+    return launch_persistent(stage == kAdjForward ? kForward : kReplay, J, nullptr, 0, J.path_count, o, qc,
+                             nullptr, &A, counters, st, false);
   }
   rc = launch_persistent(mode, J, nullptr, 0, J.path_count, o, qc, po, nullptr, counters, st, false);
   if (rc) return rc;
@@ -551,6 +580,45 @@ extern "C" int rcv_render_backward_volume(const rcv_medium* m, const rcv_sensor*
                                           void* workspace, uint64_t* counters, void* stream) {
   return backward_volume(m, s, o, seed, spp, grad_img, grad_density, grad_albedo, workspace, counters, stream,
                          kAdjBoth);
+}
+
+extern "C" int rcv_render_forward_volume(const rcv_medium* m, const rcv_sensor* s,
+                                         const rcv_volpath_options* o, uint32_t seed, int32_t spp,
+                                         const float* tangent_density, const float* tangent_albedo,
+                                         float* dimg, void* workspace, uint64_t* counters, void* stream) {
+  VolJob J;
+  int rc = make_volume_job(m, s, o, seed, spp, &J);
+  if (rc) return rc;
+  RCV_REQUIRE(dimg != nullptr, "output derivative image is NULL");
+  RCV_REQUIRE(tangent_density != nullptr || tangent_albedo != nullptr, "no tangent given");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the medium's gradient records hold the packed tangent during the call
+  const MediumLayout L = medium_layout(m);
+  char* ws = static_cast<char*>(m->workspace);
+  const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
+  const int block = 256;
+  if (tangent_density != nullptr) {
+    pack_tangent_kernel<<<grid_for(nc, block), block, 0, st>>>(m->dims[0], m->dims[1], m->dims[2],
+                                                               tangent_density,
+                                                               reinterpret_cast<float4*>(ws + L.grad_cells));
+    rc = launched("pack_tangent launch");
+    if (rc) return rc;
+  } else {
+    RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_cells, 0, nc * 32, st), "tangent reset");
+  }
+  const bool albedo = tangent_albedo != nullptr && m->albedo_old != nullptr;
+  if (albedo) {
+    const int64_t na = (int64_t)albedo_voxels_of(m);
+    pack_tangent_albedo_kernel<<<grid_for(na, block), block, 0, st>>>(
+        na, tangent_albedo, reinterpret_cast<float4*>(ws + L.grad_albedo));
+    rc = launched("pack_tangent_albedo launch");
+    if (rc) return rc;
+  } else {
+    J.grad_albedo = nullptr;
+  }
+  RCV_TRY_CUDA(cudaMemsetAsync(dimg, 0, size_t(J.width) * J.height * 3 * sizeof(float), st), "derivative reset");
+  J.out_img = dimg;
+  return run_single_job(kAdjoint, J, o, workspace, counters, nullptr, nullptr, st, kAdjForward);
 }
 
 extern "C" int rcv_render_adjoint_radiance(const rcv_medium* m, const rcv_sensor* s,

@@ -66,10 +66,12 @@ struct VolJob {
   int32_t albedo_own_res;             // 1: differs from the density's
   float albedo_const[3];
   const uint32_t* maxbits;  // [0] max old density, [1] max new density (bits)
-  // adjoint
+  // adjoint (forward mode: grad_cells / grad_albedo hold the packed tangent
+  // field, out_img receives the image derivative)
   const float* grad_img;
   float4* grad_cells;   // (dz+1)(dy+1)(dx+1) * 2
   float4* grad_albedo;  // adz*ady*adx (rgb + pad) or null
+  float* out_img;
   int64_t path_begin;   // first global path index of this job (batched launches)
   int64_t path_count;   // width*height*spp
   const uint32_t* pixel_order;  // pixel handed out k-th (null = row-major)
@@ -101,7 +103,11 @@ struct Queue {
   float4* path_ltot;
 };
 
-enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2, kReplay = 3 };
+// kForward: the replay tasks of kReplay, gathering a tangent field at every
+// gradient event (forward-mode derivative of the image) instead of
+// scattering the image gradient into the grids.
+enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2, kReplay = 3, kForward = 4 };
+constexpr int kTraceModes = 5;
 
 // Buffers of the two adjoint launches.
 struct AdjBuffers {
@@ -323,6 +329,31 @@ __device__ __forceinline__ void scatter_albedo(const VolJob& J, const AlbedoLook
     float4* dst = J.grad_albedo + ((int64_t)zs[m] * J.ady + ys[j]) * J.adx + xs[i];
     atomicAdd(dst, make_float4(g.x * w, g.y * w, g.z * w, 0.0f));
   }
+}
+
+// Forward mode: the tangent of the density at a lookup (trilinear over the
+// cell record in grad_cells, the layout scatter_density writes) and of the
+// albedo (grad_albedo, one float4 per albedo voxel).
+__device__ __forceinline__ float tangent_density(const VolJob& J, const Lookup& l) {
+  const float4* c = J.grad_cells + l.cell * 2;
+  return trilerp(__ldg(c), __ldg(c + 1), l.ax.f, l.ay.f, l.az.f);
+}
+
+__device__ __forceinline__ V3 tangent_albedo(const VolJob& J, const AlbedoLookup& l) {
+  const int x0 = clampi(l.ax.cell - 1, J.adx - 1), x1 = clampi(l.ax.cell, J.adx - 1);
+  const int y0 = clampi(l.ay.cell - 1, J.ady - 1), y1 = clampi(l.ay.cell, J.ady - 1);
+  const int z0 = clampi(l.az.cell - 1, J.adz - 1), z1 = clampi(l.az.cell, J.adz - 1);
+  auto at = [&](int x, int y, int z) { return __ldg(J.grad_albedo + ((int64_t)z * J.ady + y) * J.adx + x); };
+  const float4 a000 = at(x0, y0, z0), a100 = at(x1, y0, z0), a010 = at(x0, y1, z0), a110 = at(x1, y1, z0),
+               a001 = at(x0, y0, z1), a101 = at(x1, y0, z1), a011 = at(x0, y1, z1), a111 = at(x1, y1, z1);
+  const float fx = l.ax.f, fy = l.ay.f, fz = l.az.f;
+  auto tri = [&](float v000, float v100, float v010, float v110, float v001, float v101, float v011, float v111) {
+    return lerpf(lerpf(lerpf(v000, v100, fx), lerpf(v010, v110, fx), fy),
+                 lerpf(lerpf(v001, v101, fx), lerpf(v011, v111, fx), fy), fz);
+  };
+  return V3{tri(a000.x, a100.x, a010.x, a110.x, a001.x, a101.x, a011.x, a111.x),
+            tri(a000.y, a100.y, a010.y, a110.y, a001.y, a101.y, a011.y, a111.y),
+            tri(a000.z, a100.z, a010.z, a110.z, a001.z, a101.z, a011.z, a111.z)};
 }
 
 // Russian roulette at the top of an iteration (plugins/twostatevolpath.py:182-188).

@@ -116,8 +116,8 @@ class CVIntegrator:
         self.it += 1
         return img.clone()
 
-    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0):
-        return self.adjoint_integrator.render_forward(scene, params, sensor, seed, spp)
+    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0, tangents=None):
+        return self.adjoint_integrator.render_forward(scene, params, sensor, seed, spp, tangents=tangents)
 
     def render_backward(self, scene, params, grad_in, sensor=0, seed: int = 0, spp: int = 0):
         return self.adjoint_integrator.render_backward(scene, params, grad_in, sensor, seed, spp)
@@ -196,8 +196,8 @@ class MetaIntegrator:
             return self.integrator.render(scene, sensor, seed, spp, develop, evaluate)
         return img
 
-    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0):
-        return self.adjoint_integrator.render_forward(scene, params, sensor, seed, spp)
+    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0, tangents=None):
+        return self.adjoint_integrator.render_forward(scene, params, sensor, seed, spp, tangents=tangents)
 
     def render_backward(self, scene, params, grad_in, sensor=0, seed: int = 0, spp: int = 0):
         return self.adjoint_integrator.render_backward(scene, params, grad_in, sensor, seed, spp)

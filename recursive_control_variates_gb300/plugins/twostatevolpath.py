@@ -263,8 +263,58 @@ class _VolumeIntegratorBase:
                 out[key] = ga
         return out
 
-    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0):
-        raise NotImplementedError("forward-mode derivatives are not provided; use render_backward")
+    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0, tangents=None):
+        """Forward-mode derivative of the render of the current parameters:
+        the (H, W, 3) image derivative along the tangent of each
+        differentiable medium parameter (density ``...sigma_t.data``,
+        albedo grid ``...albedo.data``).  ``tangents`` maps keys to tensors
+        shaped like the parameters; by default each parameter tensor's
+        ``.grad`` is its tangent (the role of ``dr.grad`` in the reference's
+        forward mode).  Estimated by path replay from ``seed`` with ``spp``
+        paths per pixel (rcv_render_forward_volume)."""
+        medium = self._checked_medium(scene)
+        sensor = self.sensor_of(scene, sensor)
+        spp = self.resolve_spp(sensor, spp)
+        dev = medium.device
+        td = ta = None
+        keys = list(params.keys()) if params is not None else []
+        for key in keys:
+            owner, sub = params.owner_of(key)
+            if owner is not medium:
+                continue
+            if tangents is not None:
+                t = tangents.get(key)
+            else:
+                v = params[key]
+                t = v.grad if isinstance(v, torch.Tensor) else None
+            if t is None:
+                continue
+            t = t.detach().to(dev, torch.float32).contiguous()
+            if sub == "sigma_t.data":
+                dx, dy, dz = medium.dims
+                td = t.reshape(dz, dy, dx)
+            elif sub == "albedo.data" and medium.has_albedo_grid:
+                ax, ay, az = medium.albedo_dims
+                ta = t.reshape(az, ay, ax, 3)
+        f = sensor.film()
+        out = torch.zeros((f.height, f.width, 3), dtype=torch.float32, device=dev)
+        if td is None and ta is None:
+            return self._post(out)
+        self._drain_ticket(dev)  # the call overwrites the adjoint scratch and the gradient records
+        st = stream_handle(dev)
+        m = medium.prepare(st)
+        s = sensor.c_struct()
+        o = self.options()
+        with profiling.region("trace_forward", dev):
+            _lib.check(
+                _lib.load().rcv_render_forward_volume(
+                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp,
+                    td.data_ptr() if td is not None else None, ta.data_ptr() if ta is not None else None,
+                    out.data_ptr(), self.adjoint_scratch(dev, sensor, spp), self.counters_ptr(dev), st,
+                ),
+                "rcv_render_forward_volume",
+            )
+        return self._post(out)
 
     def _checked_medium(self, scene):
         raise NotImplementedError

@@ -32,6 +32,12 @@ class VolpathSimpleIntegrator(PRBVolpathIntegrator):
         self.use_drt_mis = bool(props.get("use_drt_mis", True))
         self._vps_scratch: dict[torch.device, torch.Tensor] = {}
 
+    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0, tangents=None):
+        """The reference's sample() has a primal and an adjoint branch only
+        (plugins/volpathsimple.py:64): no forward mode."""
+        raise NotImplementedError("volpathsimple has no forward mode (plugins/volpathsimple.py:64); "
+                                  "use render_backward, or prbvolpath / twostateprbvolpath for forward mode")
+
     def prefetch_adjoint(self, scene, sensor=0, seed: int = 0, spp: int = 0):
         """The DRT adjoint is one launch per call: nothing to start ahead."""
         return None

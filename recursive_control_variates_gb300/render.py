@@ -36,6 +36,16 @@ class _RenderOp(torch.autograd.Function):
         return img
 
     @staticmethod
+    def jvp(ctx, _job_tangent, *tangents):
+        """Forward mode (torch.func.jvp / torch.autograd.forward_ad): the
+        image derivative along the parameter tangents, from
+        ``integrator.render_forward`` with the gradient seed and spp."""
+        job = ctx.job
+        tan = {k: t for k, t in zip(job.keys, tangents) if t is not None}
+        return job.integrator.render_forward(job.scene, job.params, job.sensor, job.seed_grad, job.spp_grad,
+                                             tangents=tan)
+
+    @staticmethod
     def backward(ctx, grad_img):
         job = ctx.job
         grads = job.integrator.render_backward(

@@ -530,3 +530,42 @@ def test_upsampling_schedule_step(cuda):
     assert tuple(g.shape) == (16, 16, 16, 1) and torch.isfinite(g).all() and float(g.abs().sum()) > 0
     H, F = integ.integrator.render_twostates(scene, 0, seed=7, spp=2)
     assert torch.equal(H, F)  # old = new right after the upsampling
+
+
+def test_forward_mode_matches_oracle_and_adjoint(cuda, oracle):
+    """render_forward (plugins/cv_integrator.py:79-85): the image derivative
+    along density and albedo tangents against the oracle (2e-5 relative L2)
+    and against the adjoint of the same paths (<w, J t> = <J^T w, t>); and
+    torch forward-mode AD through rcv.render."""
+    from torch.autograd import forward_ad
+
+    scene, med, grids = make_scene(cuda, res=24, albedo_grid=True)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
+    rng = np.random.default_rng(3)
+    delta = rng.normal(0, 1, (16, 16, 16, 1)).astype(np.float32)
+    dalb = rng.normal(0, 1, (16, 16, 16, 3)).astype(np.float32)
+    tan = {scenes.DENSITY_KEY: torch.from_numpy(delta).to(cuda), scenes.ALBEDO_KEY: torch.from_numpy(dalb).to(cuda)}
+    fw = integ.render_forward(scene, params, 0, seed=13, spp=4, tangents=tan)
+    osc = oracle_scene(oracle, scene, grids, 8, True)
+    ofw = oracle.forward(osc, seed=13, spp=4, tangent_density=delta[..., 0], tangent_albedo=dalb).astype(np.float64)
+    f = fw.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(ofw) > 0
+    assert np.linalg.norm(f - ofw) <= 2e-5 * np.linalg.norm(ofw)
+    w = rng.normal(0, 1, (24, 24, 3)).astype(np.float32)
+    g = integ.render_backward(scene, params, torch.from_numpy(w).to(cuda), 0, seed=13, spp=4)
+    lhs = float((w.astype(np.float64) * f).sum())
+    rhs = float((g[scenes.DENSITY_KEY].cpu().double().numpy() * delta).sum()
+                + (g[scenes.ALBEDO_KEY].cpu().double().numpy() * dalb).sum())
+    assert abs(lhs - rhs) <= 1e-4 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    # forward-mode AD: a dual density tensor through rcv.render
+    with forward_ad.dual_level():
+        primal = params[scenes.DENSITY_KEY].detach().clone()
+        params[scenes.DENSITY_KEY] = forward_ad.make_dual(primal, tan[scenes.DENSITY_KEY])
+        params.update()
+        img = rcv.render(scene, params, integrator=integ, seed=5, spp=4)
+        jvp = forward_ad.unpack_dual(img).tangent
+    direct = integ.render_forward(scene, params, 0, seed=rcv.default_seed_grad(5), spp=4,
+                                  tangents={scenes.DENSITY_KEY: tan[scenes.DENSITY_KEY]})
+    assert jvp is not None
+    assert float((jvp - direct).norm()) <= 1e-5 * float(direct.norm())

@@ -207,6 +207,38 @@ def test_albedo_grid_with_own_resolution(oracle):
     np.testing.assert_allclose(totals[2], totals[1], rtol=1e-6)
 
 
+def test_forward_mode_is_the_adjoint_transposed(oracle):
+    """Forward mode (render_forward) and the adjoint replay the same paths
+    and events: <w, J delta> equals <J^T w, delta> for the same seed, up to
+    rounding; and the forward derivative matches central differences."""
+    cam = oracle.camera_basis(16, 16)
+    theta = blob_density(8, 4)[..., 0] * 0.5
+    alb = np.full((8, 8, 8, 3), 0.6, np.float32) + 0.1 * np.random.default_rng(0).random((8, 8, 8, 3)).astype(np.float32)
+    sc = oracle.Scene(cam, theta, theta, albedo_old=alb, albedo_new=alb, max_depth=6)
+    rng = np.random.default_rng(1)
+    w = rng.normal(0, 1, (16, 16, 3)).astype(np.float32)
+    delta = rng.normal(0, 1, theta.shape).astype(np.float32)
+    dalb = rng.normal(0, 1, alb.shape).astype(np.float32)
+    fw = oracle.forward(sc, seed=21, spp=8, tangent_density=delta, tangent_albedo=dalb).astype(np.float64)
+    gd, ga = oracle.backward(sc, seed=21, spp=8, grad_img=w)
+    lhs = float((w.astype(np.float64) * fw).sum())
+    rhs = float((gd * delta).sum() + (ga * dalb).sum())
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    # statistical agreement with central differences (density only)
+    delta = theta / theta.max()
+    fws = [oracle.forward(sc, seed=100 + s, spp=32, tangent_density=delta).astype(np.float64) for s in range(12)]
+    proj = np.array([(f * w).sum() for f in fws])
+    h = 0.02
+    s2 = oracle.Scene(cam, theta - h * delta, theta + h * delta, albedo_old=alb, albedo_new=alb, max_depth=6)
+    est = []
+    for seed in range(12):
+        H, F = oracle.render_twostates(s2, seed=7 + seed, spp=64)
+        est.append(float(((F.astype(np.float64) - H) * w).sum() / (2 * h)))
+    fd, fd_sem = np.mean(est), np.std(est) / np.sqrt(len(est))
+    fwd, fwd_sem = proj.mean(), proj.std() / np.sqrt(len(proj))
+    assert abs(fd - fwd) < 4 * np.hypot(fd_sem, fwd_sem) + 1e-4, (fwd, fwd_sem, fd, fd_sem)
+
+
 def test_cv_welford_golden(oracle, golden_cv):
     """The numpy restatement reproduces the reference's own CVIntegrator /
     MetaIntegrator / StatisticsEstimator code bit for bit."""
