@@ -348,6 +348,16 @@ int rcv_render_backward_surface(const rcv_surface_scene* scene, const rcv_sensor
                                 const float* grad_img, float* grad_texture, void* workspace,
                                 uint64_t* counters, void* stream);
 
+/* Forward-mode derivative of the surface render on `new` along a texture
+ * tangent ([tex_height][tex_width][3], device): dimg ([height][width][3],
+ * overwritten) by path replay, as rcv_render_forward_volume.  The scene's
+ * texture gradient record is overwritten.  Replaces the render_forward of
+ * the surface integrator behind cv / meta (plugins/cv_integrator.py:79-85). */
+int rcv_render_forward_surface(const rcv_surface_scene* scene, const rcv_sensor* sensor,
+                               const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
+                               const float* tangent_texture, float* dimg, void* workspace,
+                               uint64_t* counters, void* stream);
+
 /* ------------------------------------------------- control variate state */
 /* Per-element state of the recursive control variate; every array holds
  * `n` float32 device values (n = height*width*3), zero-initialised. */

@@ -134,6 +134,17 @@ def surface_backward(scene: SurfaceScene, seed: int, spp: int, grad_img, threads
     return out
 
 
+def surface_forward(scene: SurfaceScene, seed: int, spp: int, tangent, threads: int | None = None):
+    """Forward-mode derivative image of the surface render along a texture
+    tangent [tex_h][tex_w][3]."""
+    t = np.ascontiguousarray(tangent, np.float32)
+    out = np.zeros((scene.height, scene.width, 3), np.float32)
+    if lib().oracle_surface_forward(C.byref(scene.c), seed & 0xFFFFFFFF, spp, t.ctypes.data, out.ctypes.data,
+                                    threads or default_threads()):
+        raise ValueError("oracle_surface_forward: invalid arguments")
+    return out
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -151,6 +162,8 @@ def lib():
         L.oracle_surface_render.argtypes = [C.POINTER(OracleSurface), C.c_int, C.c_uint32, C.c_int, vp, vp, C.c_int]
         L.oracle_surface_render.restype = C.c_int
         L.oracle_surface_backward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int]
+        L.oracle_surface_forward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int]
+        L.oracle_surface_forward.restype = C.c_int
         L.oracle_surface_backward.restype = C.c_int
         L.oracle_sample_tea_32.argtypes = [C.c_uint32, C.c_uint32]
         L.oracle_sample_tea_32.restype = C.c_uint32

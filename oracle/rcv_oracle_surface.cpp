@@ -124,6 +124,9 @@ struct Surf {
   int mode;  // 0 two-state, 1 new only
   std::vector<double>* grad = nullptr;
   V dL{0, 0, 0}, Lrem{0, 0, 0};
+  // forward mode: texture tangent [tex_h][tex_w][3] gathered into acc
+  const float* tan = nullptr;
+  double acc[3] = {0.0, 0.0, 0.0};
 
   float light_area() const { return (2.0f * S.light_h[0]) * (2.0f * S.light_h[1]); }
 
@@ -272,6 +275,17 @@ struct Surf {
       }
       const float cos_i = dot(n, wi);
       const bool active_next = depth + 1 < S.max_depth;
+      if (tan && id == 0 && active_next) {
+        const int idx[4] = {tl.i00, tl.i10, tl.i01, tl.i11};
+        const float gx = 1.0f - tl.fx, gy = 1.0f - tl.fy;
+        const float ws[4] = {gx * gy, tl.fx * gy, gx * tl.fy, tl.fx * tl.fy};
+        const float an_c[3] = {an.x, an.y, an.z}, lr[3] = {Lrem.x, Lrem.y, Lrem.z};
+        for (int c = 0; c < 3; ++c) {
+          double t = 0.0;
+          for (int k = 0; k < 4; ++k) t += (double)ws[k] * tan[idx[k] * 3 + c];
+          acc[c] += (double)lr[c] * t / std::fmax(an_c[c], 1e-8f);
+        }
+      }
       if (grad && id == 0 && active_next) {
         const V g{(dL.x * Lrem.x) / std::fmax(an.x, 1e-8f), (dL.y * Lrem.y) / std::fmax(an.y, 1e-8f),
                   (dL.z * Lrem.z) / std::fmax(an.z, 1e-8f)};
@@ -407,6 +421,32 @@ int oracle_surface_render(const oracle_surface* S, int mode, uint32_t seed, int 
         out_old[pix * 3 + 1] = ao.y / fs;
         out_old[pix * 3 + 2] = ao.z / fs;
       }
+    }
+  });
+  return 0;
+}
+
+// Forward-mode derivative image [height][width][3] of the render on `new`
+// along a texture tangent [tex_h][tex_w][3].
+int oracle_surface_forward(const oracle_surface* S, uint32_t seed, int spp, const float* tangent, float* out,
+                           int threads) {
+  if (!S || spp <= 0 || !tangent || !out) return -1;
+  const int nt = std::max(1, threads);
+  for_rows(S->height, nt, [&](int, int py) {
+    for (int px = 0; px < S->width; ++px) {
+      const int pix = py * S->width + px;
+      double d[3] = {0.0, 0.0, 0.0};
+      for (int s = 0; s < spp; ++s) {
+        const uint32_t lane = (uint32_t)((int64_t)pix * spp + s);
+        Surf primal{*S, 1};
+        V Lo, Ln;
+        primal.trace(seed, lane, px, py, Lo, Ln);
+        Surf fw{*S, 1, nullptr, V{0, 0, 0}, Ln};
+        fw.tan = tangent;
+        fw.trace(seed, lane, px, py, Lo, Ln);
+        for (int c = 0; c < 3; ++c) d[c] += fw.acc[c];
+      }
+      for (int c = 0; c < 3; ++c) out[pix * 3 + c] = (float)(d[c] / spp);
     }
   });
   return 0;

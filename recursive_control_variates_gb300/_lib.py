@@ -248,6 +248,9 @@ SIGNATURES = {
     "rcv_render_backward_surface": (
         C.c_int, [P(SurfaceScene), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp]
     ),
+    "rcv_render_forward_surface": (
+        C.c_int, [P(SurfaceScene), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, vp, vp]
+    ),
     "rcv_cv_step": (
         C.c_int,
         [P(CvState), C.c_int64, vp, vp, C.c_int32, C.c_int32, P(C.c_int32), C.c_float, C.c_float, C.c_int32, vp],

@@ -126,16 +126,23 @@ static int make_surf_job(const rcv_surface_scene* sc, const rcv_sensor* s, const
   return RCV_OK;
 }
 
+__global__ void pack_texture_tangent_kernel(int64_t n, const float* __restrict__ t, float4* __restrict__ out) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = make_float4(t[i * 3 + 0], t[i * 3 + 1], t[i * 3 + 2], 0.0f);
+}
+
 static int surf_resident_blocks(int mode) {
   static std::once_flag once;
-  static int blocks[3] = {1, 1, 1};
+  static int blocks[4] = {1, 1, 1, 1};
   std::call_once(once, [] {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_surface_kernel<kTwoState>, kSurfBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_surface_kernel<kSingle>, kSurfBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_surface_kernel<kAdjoint>, kSurfBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], trace_surface_kernel<kForward>, kSurfBlock, 0);
     for (int& b : blocks) b = b < 1 ? 1 : b;
   });
-  return blocks[mode];
+  return blocks[mode == kForward ? 3 : mode];
 }
 
 static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o, void* workspace,
@@ -148,7 +155,8 @@ static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o,
   Queue Q;
   std::memset(&Q, 0, sizeof(Q));
   Q.counter = reinterpret_cast<unsigned long long*>(ws + L.counter);
-  Q.path_out = mode == kAdjoint ? nullptr : reinterpret_cast<float4*>(ws + L.path_out);
+  const bool adj = mode == kAdjoint || mode == kForward;
+  Q.path_out = adj ? nullptr : reinterpret_cast<float4*>(ws + L.path_out);
   Q.counters = reinterpret_cast<unsigned long long*>(counters);
   Q.total = S.path_count;
   Q.batch = (o != nullptr && o->batch > 0) ? o->batch : 64;
@@ -166,10 +174,11 @@ static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o,
   switch (mode) {
     case kTwoState: trace_surface_kernel<kTwoState><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
     case kSingle: trace_surface_kernel<kSingle><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+    case kForward: trace_surface_kernel<kForward><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
     default: trace_surface_kernel<kAdjoint><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
   }
   int rc = launched("trace_surface launch");
-  if (rc || mode == kAdjoint) return rc;
+  if (rc || adj) return rc;
   return launch_reduce(mode == kTwoState, reinterpret_cast<const float4*>(ws + L.path_out), 0, npix, S.spp,
                        img_new, img_old, st);
 }
@@ -236,4 +245,30 @@ extern "C" int rcv_render_backward_surface(const rcv_surface_scene* sc, const rc
   fold_texture_kernel<<<grid_for(n, block), block, 0, st>>>(n, reinterpret_cast<const float4*>(ws + L.grad),
                                                            grad_texture);
   return launched("fold_texture launch");
+}
+
+// Forward mode of the surface path replay along a texture tangent
+// ([tex_h][tex_w][3], device): dimg ([height][width][3], overwritten).
+extern "C" int rcv_render_forward_surface(const rcv_surface_scene* sc, const rcv_sensor* s,
+                                          const rcv_volpath_options* o, uint32_t seed, int32_t spp,
+                                          const float* tangent_texture, float* dimg, void* workspace,
+                                          uint64_t* counters, void* stream) {
+  SurfJob S;
+  int rc = make_surf_job(sc, s, o, seed, spp, &S);
+  if (rc) return rc;
+  RCV_REQUIRE(tangent_texture != nullptr && dimg != nullptr, "tangent / output buffers are NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const SurfLayout L = surf_layout(sc->tex_width, sc->tex_height);
+  char* ws = static_cast<char*>(sc->workspace);
+  const int64_t n = int64_t(sc->tex_width) * sc->tex_height;
+  // the texture gradient record holds the tangent during the call
+  const int block = 256;
+  pack_texture_tangent_kernel<<<grid_for(n, block), block, 0, st>>>(n, tangent_texture,
+                                                                   reinterpret_cast<float4*>(ws + L.grad));
+  rc = launched("pack_texture_tangent launch");
+  if (rc) return rc;
+  RCV_TRY_CUDA(cudaMemsetAsync(dimg, 0, size_t(S.width) * S.height * 3 * sizeof(float), st), "derivative reset");
+  S.grad_tex = reinterpret_cast<float4*>(ws + L.grad);
+  S.out_img = dimg;
+  return run_surface(kForward, S, o, workspace, counters, nullptr, nullptr, st);
 }

@@ -43,7 +43,8 @@ struct SurfJob {
   float light_hx, light_hz, light_area;
   V3 light_le;
   const float* grad_img;
-  float4* grad_tex;  // [tex_h * tex_w] rgb + pad
+  float4* grad_tex;  // [tex_h * tex_w] rgb + pad (forward mode: the texture tangent)
+  float* out_img;    // forward mode: image derivative
   int64_t path_count;
 };
 
@@ -169,6 +170,14 @@ __device__ __forceinline__ void tex_scatter(const SurfJob& S, const TexLookup& l
   atomicAdd(S.grad_tex + l.i11, make_float4(g.x * w11, g.y * w11, g.z * w11, 0.0f));
 }
 
+// Forward mode: bilinear tangent of the texture (grad_tex holds it).
+__device__ __forceinline__ V3 tex_tangent(const SurfJob& S, const TexLookup& l) {
+  const float4 a = __ldg(S.grad_tex + l.i00), b = __ldg(S.grad_tex + l.i10);
+  const float4 c = __ldg(S.grad_tex + l.i01), d = __ldg(S.grad_tex + l.i11);
+  const V3 lo = lerp3(a, b, l.fx), hi = lerp3(c, d, l.fx);
+  return V3{lerpf(lo.x, hi.x, l.fy), lerpf(lo.y, hi.y, l.fy), lerpf(lo.z, hi.z, l.fy)};
+}
+
 __device__ __forceinline__ float mis_power(float a, float b) {
   const float a2 = a * a, b2 = b * b;
   const float w = a2 / (a2 + b2);
@@ -250,11 +259,15 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
       prev_pdf = 1.0f;
       prev_delta = true;
       depth = 0;
-      if (kMode == kAdjoint) {
+      if (kMode == kAdjoint || kMode == kForward) {
         if (pass == 0) {
-          const float fs = (float)S.spp;
-          const float* g = S.grad_img + (int64_t)pix * 3;
-          dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
+          if (kMode == kAdjoint) {
+            const float fs = (float)S.spp;
+            const float* g = S.grad_img + (int64_t)pix * 3;
+            dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
+          } else {
+            dL = V3{0.0f, 0.0f, 0.0f};  // forward mode: the path's image derivative
+          }
         }
         Lrem = Ltot;
       }
@@ -285,7 +298,7 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
           if (kMode == kTwoState)
             Lo = V3{Lo.x + (bo.x * mis) * S.light_le.x, Lo.y + (bo.y * mis) * S.light_le.y,
                     Lo.z + (bo.z * mis) * S.light_le.z};
-          if (kMode == kAdjoint) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
+          if (kMode == kAdjoint || kMode == kForward) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
         }
         // reflectance of both states at p
         V3 an, ao;
@@ -310,6 +323,12 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
           const V3 g{(dL.x * Lrem.x) / fmaxf(an.x, 1e-8f), (dL.y * Lrem.y) / fmaxf(an.y, 1e-8f),
                      (dL.z * Lrem.z) / fmaxf(an.z, 1e-8f)};
           tex_scatter(S, tl, g);
+          ++cnt.grad_events;
+        }
+        if (kMode == kForward && pass == 1 && id == kPlane && S.grad_tex != nullptr && active_next) {
+          const V3 tt = tex_tangent(S, tl);
+          dL = V3{dL.x + Lrem.x * (tt.x / fmaxf(an.x, 1e-8f)), dL.y + Lrem.y * (tt.y / fmaxf(an.y, 1e-8f)),
+                  dL.z + Lrem.z * (tt.z / fmaxf(an.z, 1e-8f))};
           ++cnt.grad_events;
         }
         // ----- emitter sampling (plugins/twostatepath.py:294-312)
@@ -341,7 +360,7 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
                 Lo = V3{Lo.x + ((bo.x * mis) * vo.x) * ew.x, Lo.y + ((bo.y * mis) * vo.y) * ew.y,
                         Lo.z + ((bo.z * mis) * vo.z) * ew.z};
               }
-              if (kMode == kAdjoint) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
+              if (kMode == kAdjoint || kMode == kForward) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
             }
           }
         }
@@ -396,12 +415,19 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
     }
 
     if (finished) {
-      if (kMode == kAdjoint && pass == 0) {
+      if ((kMode == kAdjoint || kMode == kForward) && pass == 0) {
         Ltot = Ln;
         pass = 1;
         phase = kSStart;
       } else {
-        if (kMode != kAdjoint) {
+        if (kMode == kForward && (dL.x != 0.0f || dL.y != 0.0f || dL.z != 0.0f)) {
+          const float fs = (float)S.spp;
+          float* o = S.out_img + (int64_t)pix * 3;
+          atomicAdd(o + 0, dL.x / fs);
+          atomicAdd(o + 1, dL.y / fs);
+          atomicAdd(o + 2, dL.z / fs);
+        }
+        if (kMode == kTwoState || kMode == kSingle) {
           float4* out = Q.path_out + path * (kMode == kTwoState ? 2 : 1);
           out[0] = make_float4(Ln.x, Ln.y, Ln.z, 0.0f);
           if (kMode == kTwoState) out[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);

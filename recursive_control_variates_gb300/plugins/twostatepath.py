@@ -162,8 +162,40 @@ class TwoStatePRBIntegrator:
                 out[key] = gt
         return out
 
-    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0):
-        raise NotImplementedError("forward-mode derivatives are not provided; use render_backward")
+    def render_forward(self, scene, params, sensor=0, seed: int = 0, spp: int = 0, tangents=None):
+        """Forward-mode derivative of the render of the current texture: the
+        (H, W, 3) image derivative along the tangent of the textured BSDF's
+        ``reflectance.data`` (``tangents[key]``, by default the parameter
+        tensor's ``.grad``), by path replay (rcv_render_forward_surface)."""
+        v = self.view(scene)
+        sensor = self.sensor_of(scene, sensor)
+        spp = self.resolve_spp(sensor, spp)
+        f = sensor.film()
+        out = torch.zeros((f.height, f.width, 3), dtype=torch.float32, device=v.device)
+        tex = None
+        for key in (params.keys() if params is not None else []):
+            owner, sub = params.owner_of(key)
+            if owner is v.bsdf and sub == "reflectance.data":
+                if tangents is not None:
+                    tex = tangents.get(key)
+                else:
+                    p = params[key]
+                    tex = p.grad if isinstance(p, torch.Tensor) else None
+        if tex is None:
+            return out
+        t = tex.detach().to(v.device, torch.float32).contiguous().reshape(v.bsdf.new.texture.data.shape)
+        st = stream_handle(v.device)
+        s = v.prepare(st)
+        cam, o = sensor.c_struct(), self.options()
+        with profiling.region("trace_surface_forward", v.device):
+            _lib.check(
+                _lib.load().rcv_render_forward_surface(
+                    C.byref(s), C.byref(cam), C.byref(o), seed & 0xFFFFFFFF, spp, t.data_ptr(), out.data_ptr(),
+                    self.scratch(v.device, sensor, spp, _lib.MODE_ADJOINT), self.counters(v.device).data_ptr(), st,
+                ),
+                "rcv_render_forward_surface",
+            )
+        return out
 
     def to_string(self):
         return f"TwoStatePRBIntegrator[max_depth = {self.max_depth}]"

@@ -133,3 +133,33 @@ def test_surface_cv_optimisation(cuda):
         opt.step()
     err = float(np.abs(opt[scenes.TEXTURE_KEY].detach().cpu().numpy() - target_tex).mean())
     assert err < 0.8 * err0, (err, err0)
+
+
+def test_surface_forward_is_the_adjoint_transposed(oracle):
+    """Surface forward mode (oracle): <w, J t> = <J^T w, t> for the same seed."""
+    res, T = 24, 16
+    tex = np.random.default_rng(4).uniform(0.2, 0.9, (T, T, 3)).astype(np.float32)
+    sc = oracle_surface(oracle, tex, tex, res)
+    rng = np.random.default_rng(5)
+    w = rng.normal(0, 1, (res, res, 3)).astype(np.float32)
+    t = rng.normal(0, 1, (T, T, 3)).astype(np.float32)
+    fw = oracle.surface_forward(sc, seed=9, spp=8, tangent=t).astype(np.float64)
+    g = oracle.surface_backward(sc, seed=9, spp=8, grad_img=w)
+    lhs, rhs = float((w * fw).sum()), float((g * t).sum())
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+@pytest.mark.gpu
+def test_surface_forward_matches_oracle(cuda, oracle):
+    res, T = 32, 16
+    tex = np.random.default_rng(6).uniform(0.2, 0.9, (T, T, 3)).astype(np.float32)
+    scene = gpu_scene(cuda, tex, tex, res)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "twostateprb", "max_depth": 6, "rr_depth": 3})
+    t = np.random.default_rng(7).normal(0, 1, (T, T, 3)).astype(np.float32)
+    fw = integ.render_forward(scene, params, 0, seed=11, spp=8,
+                              tangents={scenes.TEXTURE_KEY: torch.from_numpy(t).to(cuda)})
+    ofw = oracle.surface_forward(oracle_surface(oracle, tex, tex, res), seed=11, spp=8, tangent=t).astype(np.float64)
+    f = fw.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(ofw) > 0
+    assert np.linalg.norm(f - ofw) <= 2e-5 * np.linalg.norm(ofw)
