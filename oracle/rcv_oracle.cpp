@@ -1,19 +1,23 @@
 // CPU oracle for the recursive-control-variate gradient step — TEST
 // INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file; the
-// tests, the smoke check and the CPU-baseline leg of bench.py load it as the
-// checker.
+// tests, the smoke check and the CPU-baseline leg of bench.py load it to
+// check results against.
 //
 // It restates, as plain sequential C++ (one path at a time, nested loops),
-// the per-path algorithm of the reference for the synthetic scene family
-// (unit-cube heterogeneous medium behind a null boundary, constant white
-// environment, isotropic phase function, box film):
+// the per-path algorithm of the reference for its grid-scene family
+// (heterogeneous medium in an axis-aligned box behind a null boundary,
+// constant white environment, isotropic phase function, box film, one
+// perspective sensor or a batch of them):
 //   plugins/twostatevolpath.py:141-385  TwoStatePRBVolpathIntegrator.sample_twostates
 //   plugins/twostatevolpath.py:387-479  sample_emitter_twostates
 //   plugins/twostatemedium.py:15-107    TwoStateMedium.sample_interaction_twostates
 //   plugins/twostatevolpath.py:80-138   render_twostates + develop (box filter)
 // plus the single-state estimator a two-state integrator renders on `new`
-// (plugins/twostatemedium.py:125-151) and its path-replay adjoint (the
-// default adjoint of the cv integrator, plugins/cv_integrator.py:87-94).
+// (plugins/twostatemedium.py:125-151), its path-replay adjoint (the default
+// adjoint of the cv integrator, plugins/cv_integrator.py:87-94) and forward
+// mode (cv_integrator.py:79-85), the majorant supergrid
+// (plugins/twostatemedium.py:25-70) and the volpathsimple integrator
+// (plugins/volpathsimple.py).
 // Mitsuba primitives the reference calls (sampler, gridvolume, warps) are
 // restated from their documented behaviour.
 //
