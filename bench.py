@@ -214,11 +214,13 @@ class Job:
         self.it = 0
         self.torch = torch
 
-    def step(self, target=None):
+    def step(self, target=None, before_loss=None):
         rcv = self.rcv
         self.params.update(self.opt)
         img = rcv.render(self.scene, self.params, integrator=self.integrator, seed=self.seed + self.it,
                          spp=self.cfg.spp, spp_grad=self.cfg.spp_grad)
+        if before_loss is not None:
+            before_loss()
         loss = rcv.l2_loss(img, self.target if target is None else target)
         loss.backward()
         self.opt.step()
@@ -329,10 +331,18 @@ def run_ours(args, cfg):
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
+        # each step copies its target from pinned host memory on a copy
+        # stream, overlapped with the render; the loss waits for the copy
+        copy_stream = torch.cuda.Stream(device)
+        tgt = torch.empty_like(job.target)
+        main = torch.cuda.current_stream(device)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            tgt = target_host.to(device, non_blocking=True)
-            loss = job.step(tgt)
+            with torch.cuda.stream(copy_stream):
+                tgt.copy_(target_host, non_blocking=True)
+                copied = torch.cuda.Event()
+                copied.record(copy_stream)
+            loss = job.step(tgt, before_loss=lambda: main.wait_event(copied))
             loss.item()
         torch.cuda.synchronize()
         el = reduce_max(time.perf_counter() - t0, dist, device)

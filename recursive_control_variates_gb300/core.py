@@ -89,7 +89,7 @@ def _device(props: Properties) -> torch.device:
 
 
 # -------------------------------------------------------------- transforms
-@dataclass
+@dataclass(frozen=True)
 class LookAt:
     origin: tuple
     target: tuple
@@ -209,7 +209,15 @@ class PerspectiveSensor:
 
     def frame(self, width: int, height: int) -> tuple:
         """(origin, forward, right * tan(fov/2), up * tan(fov/2) * h / w) as
-        float32 values, for a film of width x height."""
+        float32 values, for a film of width x height (memoised: every render
+        call asks for it)."""
+        key = (width, height, self.fov, self.to_world)
+        cache = self.__dict__.setdefault("_frames", {})
+        if key not in cache:
+            cache[key] = self._frame(width, height)
+        return cache[key]
+
+    def _frame(self, width: int, height: int) -> tuple:
         o = np.array(self.to_world.origin, np.float64)
         t = np.array(self.to_world.target, np.float64)
         up = np.array(self.to_world.up, np.float64)
@@ -220,7 +228,7 @@ class PerspectiveSensor:
         cam_up = np.cross(right, fwd)
         tx = math.tan(math.radians(self.fov) * 0.5)
         ty = tx * height / width
-        f32 = lambda v: [float(np.float32(x)) for x in v]  # noqa: E731
+        f32 = lambda v: tuple(float(np.float32(x)) for x in v)  # noqa: E731
         return f32(o), f32(fwd), f32(right * tx), f32(cam_up * ty)
 
     def c_struct(self) -> _lib.Sensor:
