@@ -90,6 +90,24 @@ RCV_HD void pcg_skip3(Pcg32& r) {
   r.state = r.state * A3 + r.inc * K3;
 }
 
+// State after n more draws, by the LCG jump-ahead of O'Neill 2014 (section
+// on pcg32_advance): n = sum of powers of two, each applied as
+// state <- A^(2^i) state + C_(2^i) inc with C_m = 1 + A + ... + A^(m-1).
+RCV_HD uint64_t pcg_jump(uint64_t state, uint64_t inc, uint32_t n) {
+  uint64_t acc_a = 1ull, acc_c = 0ull;
+  uint64_t a = 6364136223846793005ull, c = 1ull;
+  while (n != 0u) {
+    if (n & 1u) {
+      acc_a *= a;
+      acc_c = acc_c * a + c;
+    }
+    c *= a + 1ull;
+    a *= a;
+    n >>= 1u;
+  }
+  return acc_a * state + acc_c * inc;
+}
+
 RCV_HD float u32_to_unit(uint32_t v) {
   // 23 random mantissa bits -> [1, 2) -> [0, 1)
   union { uint32_t u; float f; } x;

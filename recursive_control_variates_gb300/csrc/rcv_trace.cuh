@@ -76,6 +76,166 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
   return Q.jobs[lo];
 }
 
+// Warps per tracer block (the cooperative walk keeps 3 x 32 floats per warp in
+// shared memory).
+constexpr int kTraceWarps = 4;
+
+// Cooperative walk of a warp's last paths.
+//
+// Once the path queue is empty a warp runs until its longest path ends, and
+// that path's free-flight steps form one chain of dependent lookups: at full
+// size the last paths of a launch (up to 64 scattering events, each with a
+// shadow walk) keep a few warps busy for 40 % of the launch time.  A run of
+// null collisions of the main walk, or of ratio-tracking steps of the shadow
+// walk, needs no result of one step to place the next except the position,
+// and the random numbers of step k are at a known offset in the path's stream
+// (3 draws per main step below the roulette depth: roulette, distance,
+// real/null; 1 per shadow step).  So a group of G lanes evaluates the next G
+// steps of one walking path at once: lane k jumps the stream to step k, takes
+// its distance, and looks the densities up at its tentative point, assuming
+// all earlier steps of the group were null (main) or did not end the shadow
+// walk.  The first step that is something else (a real collision, leaving the
+// segment, a zero throughput or transmittance) ends the run; the owner lane
+// takes the steps before it, and the regular step code then executes that
+// step itself.  Positions, remaining distances, null-collision weights and
+// transmittances are accumulated in step order with the operations of the
+// regular step, so a path gives the same bits whether it walks alone or with
+// helpers.  `m` holds the walking lanes (at most 8: G = 32 / 16 / 8 / 4 for
+// 1 / 2 / 3-4 / 5-8 paths); `org`, `dir`, `tmax` are the walk's ray and
+// remaining distance, `c1`, `c2` its throughputs (main: bn, bo) or
+// transmittances (shadow: trn, tro in .x); `s_t`, `s_w1`, `s_w2` are the
+// warp's 32-float shared arrays for the steps' distances and weights.
+// Returns the number of steps the calling lane's path took (0 for lanes that
+// own no walking path).
+template <int kMode>
+__device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJob* Jp, Pcg32& rng, float mu,
+                                         float inv_mu, float half_inv_mu, V3& org, const V3& dir, float& tmax,
+                                         V3& c1, V3& c2, float* s_t, float* s_w1, float* s_w2) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  const int n = __popc(m);
+  const int G = n == 1 ? 32 : (n == 2 ? 16 : (n <= 4 ? 8 : 4));
+  const int grp = (int)lane / G;
+  const int k = (int)lane & (G - 1);
+  const int base = grp * G;
+  const bool busy = grp < n;
+  // owner of this lane's group: the grp-th walking lane (lanes of idle groups
+  // read their own registers and touch no memory)
+  unsigned mm = m;
+  for (int i = 0; i < grp && mm != 0u; ++i) mm &= mm - 1u;
+  const int owner = mm != 0u ? __ffs(mm) - 1 : (int)lane;
+
+  const bool g_main = __shfl_sync(kFull, (int)main_walk, owner) != 0;
+  const VolJob* J = (const VolJob*)__shfl_sync(kFull, (unsigned long long)Jp, owner);
+  Pcg32 r;
+  r.state = __shfl_sync(kFull, (unsigned long long)rng.state, owner);
+  r.inc = __shfl_sync(kFull, (unsigned long long)rng.inc, owner);
+  const float g_mu = __shfl_sync(kFull, mu, owner);
+  const float g_inv = __shfl_sync(kFull, inv_mu, owner);
+  const float g_hinv = __shfl_sync(kFull, half_inv_mu, owner);
+  const V3 dv{__shfl_sync(kFull, dir.x, owner), __shfl_sync(kFull, dir.y, owner), __shfl_sync(kFull, dir.z, owner)};
+  float px = __shfl_sync(kFull, org.x, owner), py = __shfl_sync(kFull, org.y, owner);
+  float pz = __shfl_sync(kFull, org.z, owner), tr = __shfl_sync(kFull, tmax, owner);
+
+  // this lane's step: its draws, distance and real/null variable
+  r.state = pcg_jump(r.state, r.inc, (g_main ? 3u : 1u) * (uint32_t)k);
+  if (g_main) pcg_skip1(r);  // roulette draw, unused below the roulette depth
+  const float t = free_flight(next1d(r), g_mu, g_inv);
+  const float ur = g_main ? next1d(r) : 0.0f;
+  s_t[lane] = t;
+  __syncwarp();
+  // position and remaining distance before this lane's step, in step order
+#pragma unroll 4
+  for (int j = 0; j < k; ++j) {
+    const float tj = s_t[base + j];
+    px = fmaf(tj, dv.x, px);
+    py = fmaf(tj, dv.y, py);
+    pz = fmaf(tj, dv.z, pz);
+    tr = tr - tj;
+  }
+  const bool valid = busy && t <= tr;
+  const V3 x{fmaf(t, dv.x, px), fmaf(t, dv.y, py), fmaf(t, dv.z, pz)};
+  float st_o = 0.0f, st_n = 0.0f;
+  if (valid) {
+    const Lookup lk = locate(*J, x);
+    float rho_o = 0.0f, rho_n;
+    if (kMode == kTwoState)
+      density2(*J, lk, rho_o, rho_n);
+    else
+      rho_n = density_new(*J, lk);
+    st_o = J->scale * rho_o;
+    st_n = J->scale * rho_n;
+  }
+  bool term;
+  float w1 = 0.0f, w2 = 0.0f;  // main: null-collision weights (two-state); shadow: transmittance factors
+  if (g_main) {
+    const float prob = kMode == kTwoState ? (st_n + st_o) * g_hinv : st_n * g_inv;
+    term = !(valid && ur >= prob);
+    if (kMode == kTwoState) {
+      const float sn_o = g_mu - st_o, sn_n = g_mu - st_n;
+      w1 = (2.0f * sn_n) / (sn_n + sn_o);
+      w2 = 2.0f - w1;
+    }
+  } else {
+    term = !valid;
+    w1 = (g_mu - st_n) * g_inv;
+    if (kMode == kTwoState) w2 = (g_mu - st_o) * g_inv;
+  }
+  s_w1[lane] = w1;
+  s_w2[lane] = w2;
+  const unsigned tb_all = __ballot_sync(kFull, term);
+  __syncwarp();
+
+  // the owner takes the steps before the first one that is not a null step
+  // (main) or that ends the shadow walk, with its throughputs (main) or
+  // transmittances (shadow) multiplied in step order
+  const bool own = (m >> lane) & 1u;
+  int f = 0, src = (int)lane;
+  if (own) {
+    const int ob = __popc(m & ((1u << lane) - 1u)) * G;
+    const unsigned gmask = G == 32 ? kFull : ((1u << G) - 1u);
+    const unsigned tb = (tb_all >> ob) & gmask;
+    const int f0 = tb != 0u ? __ffs(tb) - 1 : G;
+    f = f0;
+    for (int j = 0; j < f0; ++j) {
+      const float x1 = s_w1[ob + j], x2 = s_w2[ob + j];
+      if (main_walk) {
+        // the regular step begins with the roulette's throughput test
+        bool alive = c1.x != 0.0f || c1.y != 0.0f || c1.z != 0.0f;
+        if (kMode == kTwoState) alive = alive || (c2.x != 0.0f || c2.y != 0.0f || c2.z != 0.0f);
+        if (!alive) {
+          f = j;
+          break;
+        }
+        if (kMode == kTwoState) {
+          c1 = V3{c1.x * x1, c1.y * x1, c1.z * x1};
+          c2 = V3{c2.x * x2, c2.y * x2, c2.z * x2};
+        }
+      } else {
+        const float n1 = c1.x * x1, n2 = c2.x * x2;
+        const bool done = kMode == kTwoState ? (n1 == 0.0f && n2 == 0.0f) : n1 == 0.0f;
+        if (done) {
+          f = j;  // the regular step takes this step and ends the walk
+          break;
+        }
+        c1.x = n1;
+        if (kMode == kTwoState) c2.x = n2;
+      }
+    }
+    if (f > 0) src = ob + f - 1;
+  }
+  // state after f steps: position, remaining distance and stream after step
+  // f - 1 of the group's lane that took it
+  const V3 xs{__shfl_sync(kFull, x.x, src), __shfl_sync(kFull, x.y, src), __shfl_sync(kFull, x.z, src)};
+  const float ts = __shfl_sync(kFull, tr - t, src);
+  const unsigned long long ss = __shfl_sync(kFull, (unsigned long long)r.state, src);
+  if (f == 0) return 0;
+  org = xs;
+  tmax = ts;
+  rng.state = ss;
+  return f;
+}
+
 // kSG: the launch may contain media with a majorant supergrid.  kCount: the
 // launch accumulates the RCV_COUNTER_* event counts (off, the counters cost
 // no registers).
@@ -89,6 +249,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   // replay tasks, scattering the image gradient (kReplay) or gathering a
   // tangent field (kForward)
   constexpr bool kRep = kMode == kReplay || kMode == kForward;
+  constexpr bool kCoop = kMode == kTwoState || kMode == kSingle || kMode == kAdjoint;
+  __shared__ float s_coop[kCoop ? kTraceWarps * 96 : 1];  // cooperative walk: distances, weights
   // replay: camera tasks [0, paths), then the checkpoints that were written
   const int64_t total =
       kRep ? Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap) : Q.total;
@@ -345,6 +507,50 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           } else {
             rng_nee = rng;  // whole-path replay: walk for the transmittance, then again
           }
+        }
+      }
+    }
+
+    // ------------------------- cooperative walk of the last paths (see above)
+    if (kCoop && queue_empty) {
+      bool elig = false;
+      if (!finished) {
+        if (phase == kNee) {
+          elig = true;
+        } else if (phase == kMain) {
+          bool alive = bn.x != 0.0f || bn.y != 0.0f || bn.z != 0.0f;
+          if (kMode == kTwoState) alive = alive || (bo.x != 0.0f || bo.y != 0.0f || bo.z != 0.0f);
+          elig = alive && depth <= Jp->rr_depth;
+        }
+        if (kSG && elig && Jp->sg[0] > 0) elig = false;
+      }
+      const unsigned m_coop = __ballot_sync(0xffffffffu, elig);
+      const int n_coop = __popc(m_coop);
+      if (n_coop >= 1 && n_coop <= 8) {
+        const bool mw = phase == kMain;
+        V3 org = mw ? p : q;
+        const V3 dir = mw ? d : w;
+        float tmax = mw ? t_rem : tr_rem;
+        V3 c1 = mw ? bn : V3{trn, 0.0f, 0.0f};
+        V3 c2 = mw ? bo : V3{tro, 0.0f, 0.0f};
+        float* s = s_coop + (threadIdx.x >> 5) * 96;
+        const int f = coop_walk<kMode>(m_coop, mw, Jp, rng, mu, inv_mu, half_inv_mu, org, dir, tmax, c1, c2, s,
+                                       s + 32, s + 64);
+        if (f > 0) {
+          if (mw) {
+            p = org;
+            t_rem = tmax;
+            bn = c1;
+            if (kMode == kTwoState) bo = c2;
+            if (kCount) cnt.lookups += (unsigned)f;
+          } else {
+            q = org;
+            tr_rem = tmax;
+            trn = c1.x;
+            if (kMode == kTwoState) tro = c2.x;
+            if (kCount) cnt.nee_lookups += (unsigned)f;
+          }
+          iter0 -= (uint32_t)f;  // the path's cost counts its steps
         }
       }
     }

@@ -14,7 +14,7 @@
 
 namespace rcv {
 
-constexpr int kTraceBlock = 128;
+constexpr int kTraceBlock = 32 * kTraceWarps;
 
 // ------------------------------------------------------------------ packing
 // One thread per cell / voxel / albedo voxel (na: albedo grid voxels).

@@ -20,7 +20,7 @@ import pytest
 import torch
 
 import recursive_control_variates_gb300 as rcv
-from recursive_control_variates_gb300 import _lib, batch, scenes
+from recursive_control_variates_gb300 import _lib, batch, scenes, serve
 
 
 # ------------------------------------------------------------------- CPU
@@ -281,31 +281,43 @@ def test_job_alone_and_in_mix_agree(cuda):
 
 @pytest.mark.gpu
 def test_gradient_variance_matched(cuda):
-    """Per-voxel variance of dL/dtheta over 8 seeds, batched vs plain: same
-    seeds give the same estimates, so the variances agree far inside 5 %."""
-    D, res, spp, depth = 12, 24, 4, 8
+    """Per-voxel variance of dL/dtheta over 16 seeds in the plain, batched and
+    served forms (matched variance: same spp, spp_grad, max_depth and seeds
+    in every form).  Same seeds give the same estimates up to float-atomic
+    reordering, so the variances agree far inside 5 %.  lr = 0, so Adam's
+    first moment after one step is (1 - beta1) * gradient."""
+    D, res, spp, depth, n_seeds = 12, 24, 4, 8, 16
     true = scenes.blob_density(D, 5)
     dens = (0.7 * true).astype(np.float32)
     ref_scene = rcv.load_dict(scenes.scene_dict(true, 0.8, res=res), device=cuda)
     target = rcv.load_dict({"type": "prbvolpath", "max_depth": depth, "rr_depth": depth}).render(
         ref_scene, 0, seed=3, spp=64)
     grads_plain, jobs = [], []
-    for s in range(8):
+    for s in range(n_seeds):
         scene, params, integ, opt = plain_setup(cuda, dens, 0.8, res, depth, 0.0, spp)
         jobs.append(batch.CVJob.from_scene(scene, params, integ, opt, target, spp=spp, seed=1000 + 31 * s))
         plain_step(scene, params, integ, opt, target, 1000 + 31 * s, spp)
         grads_plain.append(opt.state[scenes.DENSITY_KEY][1].reshape(D, D, D) / 0.1)
+    served = [j.clone() for j in jobs]
     b = batch.BatchedCV(jobs)
     b.step()
-    grads_batch = torch.stack([j.density_m / np.float32(0.1) for j in jobs])
+    server = serve.StepServer(8 * 2**30, device=cuda, max_jobs_per_tick=5, pipeline=2)
+    for jid in [server.add_job(j) for j in served]:
+        server.submit(jid)
+    server.drain()
+    server.close()
     gp = torch.stack(grads_plain)
-    vp, vb = gp.var(dim=0), grads_batch.var(dim=0)
-    assert float(vb.sum()) > 0
-    assert abs(float(vb.sum() / vp.sum()) - 1.0) < 0.05
+    vp = gp.var(dim=0)
     busy = vp > 1e-3 * vp.max()
-    assert float(((vb[busy] / vp[busy] - 1).abs() < 0.05).float().mean()) >= 0.99
-    # lr = 0: the parameters did not move
-    assert all(torch.equal(j.params(), j.density[(j.it + 1) & 1]) for j in jobs)
+    for form in (jobs, served):
+        assert all(j.it == 1 for j in form)
+        g = torch.stack([j.density_m / np.float32(0.1) for j in form])
+        v = g.var(dim=0)
+        assert float(v.sum()) > 0
+        assert abs(float(v.sum() / vp.sum()) - 1.0) < 0.05
+        assert float(((v[busy] / vp[busy] - 1).abs() < 0.05).float().mean()) >= 0.99
+        # lr = 0: the parameters did not move
+        assert all(torch.equal(j.params(), j.density[(j.it + 1) & 1]) for j in form)
     b.close()
 
 
