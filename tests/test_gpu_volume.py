@@ -175,6 +175,84 @@ def test_losses_and_adam(cuda, oracle):
         assert float(opt["p"].grad.abs().max()) == 0.0
 
 
+def _oracle_scene_opts(O, scene, grids, max_depth, rr_depth, hide, albedo_grid=True):
+    s = scene.sensors()[0].c_struct()
+    cam = O.Camera(s.width, s.height, tuple(s.origin), tuple(s.forward), tuple(s.right), tuple(s.up))
+    old, new, ao, an = grids
+    return O.Scene(cam, old[..., 0], new[..., 0], albedo_old=ao if albedo_grid else None,
+                   albedo_new=an if albedo_grid else None, albedo_const=0.8, max_depth=max_depth,
+                   rr_depth=rr_depth, hide_emitters=hide)
+
+
+@pytest.mark.parametrize("max_depth,rr_depth,hide", [(16, 2, False), (0, 0, False), (2, 1, True), (-1, 3, False)])
+def test_depth_roulette_and_emitter_options_match_oracle(cuda, oracle, max_depth, rr_depth, hide):
+    """Russian roulette below max_depth (the plugins' default is max_depth 6,
+    rr_depth 5), max_depth 0 and 2, unlimited depth (-1, ended by the
+    roulette) and hidden emitters: two-state, single-state and adjoint
+    against the oracle.  The cooperative walk of the last paths only runs
+    below the roulette depth, so these cases also cover its hand-over."""
+    scene, med, grids = make_scene(cuda, albedo_grid=True, res=32)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": max_depth, "rr_depth": rr_depth,
+                           "hide_emitters": hide})
+    H, F = integ.render_twostates(scene, 0, seed=21, spp=4)
+    S = integ.render(scene, 0, seed=22, spp=4)
+    osc = _oracle_scene_opts(oracle, scene, grids, max_depth, rr_depth, hide)
+    Ho, Fo = oracle.render_twostates(osc, seed=21, spp=4)
+    So = oracle.render(osc, seed=22, spp=4)
+    H, F, S = H.cpu().numpy(), F.cpu().numpy(), S.cpu().numpy()
+    for a, b in ((H, Ho), (F, Fo), (S, So)):
+        assert frac_equal(a, b) >= 0.999
+        np.testing.assert_allclose(a.mean(), b.mean(), rtol=1e-5)
+    if hide:
+        assert float(S.min()) == 0.0  # pixels whose rays miss the medium see nothing
+    rng = np.random.default_rng(max_depth + 10)
+    gimg = rng.normal(0, 1, (32, 32, 3)).astype(np.float32)
+    grads = integ.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=23, spp=4)
+    od, oa = oracle.backward(osc, seed=23, spp=4, grad_img=gimg)
+    gd = grads[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
+    ga = grads[scenes.ALBEDO_KEY].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(od) > 0
+    assert np.linalg.norm(gd - od) <= 2e-5 * np.linalg.norm(od)
+    if np.linalg.norm(oa) > 0:
+        assert np.linalg.norm(ga - oa) <= 2e-5 * np.linalg.norm(oa)
+    else:
+        assert float(np.abs(ga).max()) == 0.0  # max_depth 0: no scattering event
+
+
+def test_empty_medium(cuda, oracle):
+    """All-zero density (majorant 0): no collision, every path sees the
+    environment (radiance 1) unattenuated, and no gradient event happens."""
+    D = 8
+    zero = np.zeros((D, D, D, 1), np.float32)
+    scene = rcv.load_dict(scenes.scene_dict(zero, 0.8, res=16), device=cuda)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 8, "rr_depth": 8})
+    H, F = integ.render_twostates(scene, 0, seed=3, spp=4)
+    assert torch.equal(H, torch.ones_like(H)) and torch.equal(F, torch.ones_like(F))
+    osc = _oracle_scene_opts(oracle, scene, (zero, zero, None, None), 8, 8, False, albedo_grid=False)
+    Ho, Fo = oracle.render_twostates(osc, seed=3, spp=4)
+    assert np.array_equal(F.cpu().numpy(), Fo) and np.array_equal(H.cpu().numpy(), Ho)
+    g = integ.render_backward(scene, params, torch.ones((16, 16, 3), device=cuda), 0, seed=4, spp=4)
+    assert float(g[scenes.DENSITY_KEY].abs().max()) == 0.0
+
+
+def test_one_pixel_one_sample_matches_oracle(cuda, oracle):
+    """A 1 x 1 film at spp 1: one path per launch (one warp, one lane)."""
+    scene, med, grids = make_scene(cuda, res=1, albedo_grid=True)
+    params = rcv.traverse(scene)
+    integ = rcv.load_dict({"type": "twostateprbvolpath", "max_depth": 16, "rr_depth": 4})
+    osc = _oracle_scene_opts(oracle, scene, grids, 16, 4, False)
+    for seed in range(6):
+        H, F = integ.render_twostates(scene, 0, seed=seed, spp=1)
+        Ho, Fo = oracle.render_twostates(osc, seed=seed, spp=1)
+        assert np.array_equal(H.cpu().numpy(), Ho) and np.array_equal(F.cpu().numpy(), Fo)
+        grads = integ.render_backward(scene, params, torch.ones((1, 1, 3), device=cuda), 0, seed=seed, spp=1)
+        od, _ = oracle.backward(osc, seed=seed, spp=1, grad_img=np.ones((1, 1, 3), np.float32))
+        gd = grads[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
+        assert np.linalg.norm(gd - od) <= 2e-5 * max(np.linalg.norm(od), 1e-30)
+
+
 def test_autograd_render_matches_direct_backward(cuda):
     scene, med, grids = make_scene(cuda, seeds=(1, 1), res=24)
     params = rcv.traverse(scene)
