@@ -73,6 +73,38 @@ def test_vps_adjoint_albedo_grid_and_supergrid(cuda, oracle, factor):
     assert np.linalg.norm(ga - oa) <= 2e-5 * np.linalg.norm(oa)
 
 
+@pytest.mark.parametrize("flags", [{}, {"use_drt": False}])
+@pytest.mark.parametrize("max_depth,rr_depth", [(16, 2), (-1, 3), (0, 0)])
+def test_vps_roulette_and_depth_limits_match_oracle(cuda, oracle, flags, max_depth, rr_depth):
+    """Russian roulette below max_depth (plugins/volpathsimple.py:131),
+    unlimited depth ended by the roulette, and max_depth 0: primal and
+    adjoint against the oracle."""
+    from test_gpu_volume import _oracle_scene_opts
+
+    scene, med, grids = make_scene(cuda, res=32, albedo_grid=True)
+    params = rcv.traverse(scene)
+    d = {"type": "volpathsimple", "max_depth": max_depth, "rr_depth": rr_depth}
+    d.update(flags)
+    integ = rcv.load_dict(d)
+    osc = _oracle_scene_opts(oracle, scene, grids, max_depth, rr_depth, False)
+    img = integ.render(scene, 0, seed=13, spp=4).cpu().numpy()
+    ref = oracle.vps_render(osc, seed=13, spp=4, flags=flags)
+    assert frac_equal(img, ref) >= 0.999
+    np.testing.assert_allclose(img.mean(), ref.mean(), rtol=1e-5)
+    rng = np.random.default_rng(7)
+    gimg = rng.normal(0, 1, (32, 32, 3)).astype(np.float32)
+    grads = integ.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=14, spp=4)
+    od, oa = oracle.vps_backward(osc, seed=14, spp=4, grad_img=gimg, flags=flags)
+    gd = grads[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
+    ga = grads[scenes.ALBEDO_KEY].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(od) > 0
+    assert np.linalg.norm(gd - od) <= 2e-5 * np.linalg.norm(od)
+    if np.linalg.norm(oa) > 0:
+        assert np.linalg.norm(ga - oa) <= 2e-5 * np.linalg.norm(oa)
+    else:
+        assert float(np.abs(ga).max()) == 0.0
+
+
 def test_cv_with_volpathsimple_adjoint(cuda):
     """The grid experiments' pairing (experiments.py:131,245,364): a `cv`
     integrator over the two-state tracer whose gradients come from
