@@ -97,15 +97,35 @@ __device__ __forceinline__ void reduce_pixel(const float4* __restrict__ path_out
   out_old = V3{ox / fs, oy / fs, oz / fs};
 }
 
-// Warp-wide max of the voxel densities into maxbits[0] (old), [1] (new);
-// every lane of the warp must call it.
+// Block-wide max of the voxel densities into maxbits[0] (old), [1] (new);
+// every thread of the block must call it (blockDim a multiple of 32).
+// Non-negative floats order like their bits.  One atomicMax per block and
+// state, skipped when the word already holds at least the block's value:
+// every value it ever holds is the maximum of some voxels, so a smaller one
+// cannot change the result, and a stale read only costs an unneeded atomic.
+// (Per-warp atomics on the same two words serialised in one L2 slice and
+// took most of a 128^3 grid's packing time.)
 __device__ __forceinline__ void reduce_majorants(float mo, float mn, uint32_t* maxbits) {
+  __shared__ uint32_t s_max[2][32];
   uint32_t bo = __float_as_uint(fmaxf(mo, 0.0f)), bn = __float_as_uint(fmaxf(mn, 0.0f));
   bo = __reduce_max_sync(0xffffffffu, bo);
   bn = __reduce_max_sync(0xffffffffu, bn);
+  const unsigned w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    if (bo) atomicMax(maxbits + 0, bo);
-    if (bn) atomicMax(maxbits + 1, bn);
+    s_max[0][w] = bo;
+    s_max[1][w] = bn;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const unsigned nw = (blockDim.x + 31) >> 5;
+    bo = threadIdx.x < nw ? s_max[0][threadIdx.x] : 0u;
+    bn = threadIdx.x < nw ? s_max[1][threadIdx.x] : 0u;
+    bo = __reduce_max_sync(0xffffffffu, bo);
+    bn = __reduce_max_sync(0xffffffffu, bn);
+    if (threadIdx.x == 0) {
+      if (bo != 0u && bo > __ldcg(maxbits + 0)) atomicMax(maxbits + 0, bo);
+      if (bn != 0u && bn > __ldcg(maxbits + 1)) atomicMax(maxbits + 1, bn);
+    }
   }
 }
 
