@@ -332,19 +332,40 @@ def run_ours(args, cfg):
         if dist is not None:
             dist.barrier()
         # each step copies its target from pinned host memory on a copy
-        # stream, overlapped with the render; the loss waits for the copy
+        # stream, overlapped with the render (the loss waits for the copy),
+        # and copies its loss into pinned host memory; the host reads step
+        # i's loss while step i+1 runs, as a training loop that logs its loss
+        # does, so the launches of a step are issued during the previous one
         copy_stream = torch.cuda.Stream(device)
-        tgt = torch.empty_like(job.target)
+        tgts = [torch.empty_like(job.target) for _ in range(2)]
+        consumed = [None, None]  # main-stream event after the loss read tgts[k]
+        loss_host = torch.empty(args.steps, dtype=torch.float32).pin_memory()
+        losses = []
         main = torch.cuda.current_stream(device)
+        pending = None  # (step, event after its loss copy)
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for i in range(args.steps):
+            k = i & 1
             with torch.cuda.stream(copy_stream):
-                tgt.copy_(target_host, non_blocking=True)
+                if consumed[k] is not None:
+                    copy_stream.wait_event(consumed[k])
+                tgts[k].copy_(target_host, non_blocking=True)
                 copied = torch.cuda.Event()
                 copied.record(copy_stream)
-            loss = job.step(tgt, before_loss=lambda: main.wait_event(copied))
-            loss.item()
+            loss = job.step(tgts[k], before_loss=lambda: main.wait_event(copied))
+            consumed[k] = torch.cuda.Event()
+            consumed[k].record(main)
+            loss_host[i].copy_(loss.detach(), non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(main)
+            if pending is not None:
+                pending[1].synchronize()
+                losses.append(float(loss_host[pending[0]]))
+            pending = (i, done)
+        pending[1].synchronize()
+        losses.append(float(loss_host[pending[0]]))
         torch.cuda.synchronize()
+        assert len(losses) == args.steps and all(math.isfinite(v) for v in losses)
         el = reduce_max(time.perf_counter() - t0, dist, device)
         e2e = {"value": paths * world * args.steps / el, "unit": UNIT,
                "h2d_bytes_per_step": int(target_host.numel() * 4), "d2h_bytes_per_step": 4,
