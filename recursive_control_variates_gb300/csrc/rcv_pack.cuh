@@ -129,38 +129,41 @@ __device__ __forceinline__ void reduce_majorants(float mo, float mn, uint32_t* m
   }
 }
 
-__device__ __forceinline__ int fold_candidates(int i, int D, int* cell, int* bit) {
-  int n = 0;
-  for (int c = i; c <= i + 1 && c <= D; ++c)
-    for (int b = 0; b < 2; ++b) {
-      const int v = clampi(c - 1 + b, D - 1);
-      if (v == i) {
-        cell[n] = c;
-        bit[n] = b;
-        ++n;
-      }
-    }
-  return n;
+// Whether cell c of an axis of D voxels uses voxel v as its corner `bit`
+// (corner 0 is voxel clamp(c - 1), corner 1 voxel clamp(c)).  Only cells v
+// and v + 1 can, so a voxel has at most 4 (cell, bit) pairs per axis.
+__device__ __forceinline__ bool fold_uses(int c, int bit, int v, int D) {
+  return c <= D && clampi(c - 1 + bit, D - 1) == v;
 }
 
-// Gradient of voxel i: the sum of its corner entries in every cell that uses it.
+// Gradient of voxel i: the sum of its corner entries in every cell that uses
+// it, in the order z, y, x candidate, each by cell and then corner bit.  The
+// candidate slots are fixed (cell v or v + 1, bit 0 or 1) and unrolled, so
+// everything stays in registers.
 __device__ __forceinline__ float fold_voxel(int64_t i, int dx, int dy, int dz, const float* __restrict__ gcells) {
   // 32-bit index arithmetic (the voxel count is below the cell count, < 2^30)
   const uint32_t row = (uint32_t)i / (uint32_t)dx;
   const int x = int((uint32_t)i - row * (uint32_t)dx);
   const uint32_t z_u = row / (uint32_t)dy;
   const int y = int(row - z_u * (uint32_t)dy), z = int(z_u);
-  int cxs[4], bxs[4], cys[4], bys[4], czs[4], bzs[4];
-  const int nx = fold_candidates(x, dx, cxs, bxs);
-  const int ny = fold_candidates(y, dy, cys, bys);
-  const int nz = fold_candidates(z, dz, czs, bzs);
   float g = 0.0f;
-  for (int a = 0; a < nz; ++a)
-    for (int b = 0; b < ny; ++b)
-      for (int c = 0; c < nx; ++c) {
-        const int64_t cell = (int64_t(czs[a]) * (dy + 1) + cys[b]) * (dx + 1) + cxs[c];
-        g += gcells[cell * 8 + bxs[c] + 2 * bys[b] + 4 * bzs[a]];
+#pragma unroll
+  for (int kz = 0; kz < 4; ++kz) {
+    const int cz = z + (kz >> 1), bz = kz & 1;
+    if (!fold_uses(cz, bz, z, dz)) continue;
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+      const int cy = y + (ky >> 1), by = ky & 1;
+      if (!fold_uses(cy, by, y, dy)) continue;
+#pragma unroll
+      for (int kx = 0; kx < 4; ++kx) {
+        const int cx = x + (kx >> 1), bx = kx & 1;
+        if (!fold_uses(cx, bx, x, dx)) continue;
+        const int64_t cell = (int64_t(cz) * (dy + 1) + cy) * (dx + 1) + cx;
+        g += gcells[cell * 8 + bx + 2 * by + 4 * bz];
       }
+    }
+  }
   return g;
 }
 
