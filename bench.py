@@ -656,18 +656,33 @@ def served_form(args, device):
     t0 = time.perf_counter()
     reqs = server.run_arrivals(arrivals)
     wall = time.perf_counter() - t0
-    server.close()
     lat = serve.latency_summary(reqs)
     paths = server.stats.paths
+    # The configured 2000 req/s offers several times what the GPU serves, so
+    # the latencies above grow with the number of requests (queueing).  The
+    # same mix at 80 % of the measured throughput shows the serving latency.
+    mean_paths = float(np.mean([j.paths_per_step() for j in jobs]))
+    rate = 0.8 * (paths / wall) / mean_paths
+    stats = server.stats  # of the configured run
+    server.stats = serve.ServerStats()
+    t1 = time.perf_counter()
+    reqs80 = server.run_arrivals(serve.poisson_arrivals(rate, args.served_requests, ids, seed=12))
+    wall80 = time.perf_counter() - t1
+    lat80 = serve.latency_summary(reqs80)
+    at80 = {"rate_req_s": round(rate, 1), "requests": len(reqs80), "value": server.stats.paths / wall80,
+            "p50_ms": lat80["p50_ms"], "p99_ms": lat80["p99_ms"], "mean_ms": lat80["mean_ms"],
+            "mean_jobs_per_tick": float(np.mean(server.stats.jobs_per_tick))}
+    server.close()
     return {
         "workload": "cfg5: Poisson 2000 req/s over 64 cfg4-mix jobs + 8 jobs (256^3, 1024^2, spp 16, depth 32), "
                     "continuous batching, 120 GB HBM budget",
         "requests": len(reqs), "value": paths / wall, "unit": UNIT, "wall_s": wall,
         "p50_ms": lat["p50_ms"], "p99_ms": lat["p99_ms"], "mean_ms": lat["mean_ms"],
-        "ticks": server.stats.ticks, "mean_jobs_per_tick": float(np.mean(server.stats.jobs_per_tick)),
-        "plan_reuses": server.stats.plan_reuses, "resident_jobs": int(resident),
+        "ticks": stats.ticks, "mean_jobs_per_tick": float(np.mean(stats.jobs_per_tick)),
+        "plan_reuses": stats.plan_reuses, "resident_jobs": int(resident),
         "resident_gb": round(server.resident_bytes() / 1e9, 2),
-        "offered_paths_per_s": 2000.0 * float(np.mean([j.paths_per_step() for j in jobs])),
+        "offered_paths_per_s": 2000.0 * mean_paths,
+        "at_80pct_of_served": at80,
     }
 
 
