@@ -347,8 +347,9 @@ def test_three_sigma_against_4096_spp(cuda):
     """Per-pixel means over 64 independent spp-64 renders lie within 3 sigma
     of a 4096-spp render (config-1 medium; sigma from the renders' spread, so
     that rare events at the cube's silhouette are represented in it); the
-    image mean of the 4096-spp render agrees with an FP64 host accumulation
-    of 16 x 256-spp passes within their statistical error."""
+    image mean of the 4096-spp render (float32 film sums) agrees with an FP64
+    host accumulation of 16 x 256-spp passes within 4 standard errors of
+    their difference; the test prints both means and the error."""
     cfg = scenes.CONFIGS["cfg1"]
     dens, alb = scenes.config_grids(cfg)
     scene = rcv.load_dict(scenes.scene_dict(dens, alb, res=cfg.res), device=cuda)
@@ -368,8 +369,15 @@ def test_three_sigma_against_4096_spp(cuda):
     nz = zz[sigma.cpu().numpy() > 0]
     assert float(np.median(nz)) < 0.8, float(np.median(nz))
     mean_err = abs(float(ref.mean()) - float(ref64.mean()))
-    stat = float(sigma.mean()) * np.sqrt(4 / 4096.0) / np.sqrt(ref.numel())
-    assert mean_err < 6 * stat + 1e-5, (mean_err, stat)
+    # statistical error of the difference of two independent 4096-sample
+    # image means: the spread of the 64 spp-64 renders' image means (which
+    # keeps the correlation of a path's three channels), / 8 for 4096 spp,
+    # times sqrt(2) for the difference
+    stat = float(imgs.mean(dim=(1, 2, 3)).std()) / 8.0 * np.sqrt(2.0)
+    print(f"image mean {float(ref.mean()):.7f} (4096 spp, float32 film) vs {float(ref64.mean()):.7f} "
+          f"(FP64 accumulation of 16 x 256 spp): error {mean_err:.3e}, statistical error {stat:.3e}; "
+          f"pixels within 3 sigma {float(np.mean(zz < 3)):.4f}, median |z| {float(np.median(nz)):.3f}")
+    assert mean_err < 4 * stat, (mean_err, stat)
 
 
 def test_cv_optimisation_reduces_loss(cuda):
