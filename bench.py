@@ -606,8 +606,12 @@ def batched_form(args, device, flush):
     value = paths * len(ms) / total
     plain_value = plain_ms = plain_wall = None
     if plains is not None:
-        # plain single-job form: the same jobs through the single-job API
-        plain_mix_step(plains)
+        # plain single-job form: the same jobs through the single-job API.
+        # Three untimed rounds: the first two steps of the first job pay
+        # one-time host costs (kernels loaded on first launch) that the events
+        # around a round would count when the form runs on its own.
+        for _ in range(3):
+            plain_mix_step(plains)
         torch.cuda.synchronize()
         rounds = args.plain_rounds
         a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
