@@ -604,7 +604,7 @@ def batched_form(args, device, flush):
     bc.close()
     total = sum(ms) / 1e3
     value = paths * len(ms) / total
-    plain_value = plain_ms = plain_wall = None
+    plain_value = plain_ms = plain_wall = plain_by_film = None
     if plains is not None:
         # plain single-job form: the same jobs through the single-job API.
         # Three untimed rounds: the first two steps of the first job pay
@@ -624,6 +624,22 @@ def batched_form(args, device, flush):
         plain_wall = (time.perf_counter() - t0) / rounds * 1e3
         plain_ms = a.elapsed_time(e) / rounds
         plain_value = paths / (plain_ms / 1e3)
+        # one more round timed job by job: where the batched form's lead
+        # comes from (small films cannot fill the GPU in a single-job launch)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in plains]
+        for p, (pa, pe) in zip(plains, ev):
+            pa.record(stream)
+            plain_mix_step([p])
+            pe.record(stream)
+        torch.cuda.synchronize()
+        by_film = {}
+        for m, job, (pa, pe) in zip(mix, jobs, ev):
+            g = by_film.setdefault(int(m["res"]), {"jobs": 0, "paths_per_step": 0, "ms": 0.0})
+            g["jobs"] += 1
+            g["paths_per_step"] += int(job.paths_per_step())
+            g["ms"] += pa.elapsed_time(pe)
+        plain_by_film = {f"{r}x{r}": dict(g, ms=round(g["ms"], 3), paths_per_s=g["paths_per_step"] / (g["ms"] / 1e3))
+                         for r, g in sorted(by_film.items())}
     return {
         "workload": f"cfg4: {len(jobs)} cv_ps jobs, grids {{16,32,64,128}}^3, films {{64..512}}^2, spp {{4,8,16}}, "
                     "depth 32, constant albedo 0.8, one persistent launch per tracer pass, CUDA graph",
@@ -633,6 +649,7 @@ def batched_form(args, device, flush):
         "gpu_launches_per_step": b.kernels_per_step,
         "plain_value": plain_value, "plain_ms_per_round": plain_ms, "plain_wall_ms_per_round": plain_wall,
         "speedup_vs_plain": value / plain_value if plain_value else None,
+        "plain_by_film": plain_by_film,
         "lookups_per_path": float((dc[0][1] + dc[0][2] + dc[1][1] + dc[1][2]) / max(dc[0][0] + dc[1][0], 1.0)),
         "l2": "flushed between timed steps (512 MB write)",
     }
