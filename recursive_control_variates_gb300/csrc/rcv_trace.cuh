@@ -280,7 +280,9 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   uint64_t ck_state = 0;
   bool ck_lost = false;  // a checkpoint of this path did not fit
   // replay
-  V3 Ltot{0, 0, 0}, cn_task{0, 0, 0};
+  // replay: radiance the path gathers after its current point,
+  // L_rem = L - (radiance gathered so far), kept instead of L and the sum so far
+  V3 Lrem{0, 0, 0}, cn_task{0, 0, 0};
   float s_nee = 0.0f;
   int task = kTaskSegment;
   bool own_event = false;  // checkpoint task: its scattering event is still to be processed
@@ -371,7 +373,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           dL = V3{0.0f, 0.0f, 0.0f};
         }
         const float4 lt = Q.path_ltot[path];
-        Ltot = V3{lt.x, lt.y, lt.z};
+        Lrem = V3{lt.x, lt.y, lt.z};
         task = resume ? kTaskCheckpoint : (lt.w != 0.0f ? kTaskWhole : kTaskSegment);
       }
       if (resume) {
@@ -383,6 +385,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           p = V3{r1.x, r1.y, r1.z};
           bn = V3{r1.w, r2.x, r2.y};
           Ln = V3{r2.z, r2.w, r3.x};
+          Lrem = V3{Lrem.x - Ln.x, Lrem.y - Ln.y, Lrem.z - Ln.z};
           cn_task = V3{r3.y, r3.z, r3.w};
           sc_n = J.scale * density_new(J, locate(J, p));
           own_event = true;
@@ -444,7 +447,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         } else {
           if (kMode == kReplay) {
             // d log(sigma_s) / d density and d log(albedo) / d albedo at the event
-            const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+            const V3 Lr = Lrem;
             const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
             scatter_density(J, lk, (J.scale * sd) / st_n);
             if (kCount) ++cnt.grad_events;
@@ -457,7 +460,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           } else if (kMode == kForward) {
             // the same terms applied to the tangent field: L_rem times
             // d log(sigma_s) along the tangent, per channel
-            const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+            const V3 Lr = Lrem;
             const float f = (J.scale * tangent_density(J, lk)) / st_n;
             dL = V3{dL.x + Lr.x * f, dL.y + Lr.y * f, dL.z + Lr.z * f};
             if (kCount) ++cnt.grad_events;
@@ -501,7 +504,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             // NEE contribution known from the radiance pass: one shadow walk
             // on the main stream scatters its gradient (gathers the tangent)
             if (kMode == kReplay) s_nee = (dL.x * cn_task.x + dL.y * cn_task.y) + dL.z * cn_task.z;
-            Ln = V3{Ln.x + cn_task.x, Ln.y + cn_task.y, Ln.z + cn_task.z};
+            Lrem = V3{Lrem.x - cn_task.x, Lrem.y - cn_task.y, Lrem.z - cn_task.z};
             own_event = false;
             phase = kNeeAdj;
           } else {
@@ -561,7 +564,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       bool alive = true;
       V3 org, dir;
       float tmax;
-      Pcg32* r = &rng;
+      // whole-path replay: the second shadow walk draws from the saved stream
+      // (chosen by value, not through a pointer, which would put both
+      // streams in local memory)
+      bool nee_stream = false;
       if (phase == kMain) {
         alive = roulette<kMode>(J, rng, depth, bn, bo);
         org = p;
@@ -571,7 +577,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         org = q;
         dir = w;
         tmax = tr_rem;
-        if (kRep && phase == kNeeAdj && task == kTaskWhole) r = &rng_nee;
+        nee_stream = kRep && phase == kNeeAdj && task == kTaskWhole;
       }
       if (!alive) {
         finished = true;
@@ -580,12 +586,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         float mu_c = mu, inv_c = inv_mu, hinv_c = half_inv_mu;
         float t;
         if (kSG && J.sg[0] > 0) {
-          const float tau = -log_unit(1.0f - next1d(*r));
+          const float tau = -log_unit(1.0f - (nee_stream ? next1d(rng_nee) : next1d(rng)));
           t = supergrid_flight(J, kMode == kTwoState ? J.sg_two : J.sg_new, org, dir, tmax, tau, mu_c);
           inv_c = 1.0f / mu_c;
           hinv_c = 0.5f * inv_c;
         } else {
-          t = free_flight(next1d(*r), mu, inv_mu);
+          t = free_flight(nee_stream ? next1d(rng_nee) : next1d(rng), mu, inv_mu);
         }
         const bool valid = t <= tmax;
         Lookup lk;
@@ -629,13 +635,13 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
               } else if (kMode == kReplay) {
                 const float sn = mu_c - st_n;
-                const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+                const V3 Lr = Lrem;
                 const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
                 scatter_density(J, lk, -(J.scale * sd) / sn);
                 if (kCount) ++cnt.grad_events;
               } else if (kMode == kForward) {
                 const float sn = mu_c - st_n;
-                const V3 Lr{Ltot.x - Ln.x, Ltot.y - Ln.y, Ltot.z - Ln.z};
+                const V3 Lr = Lrem;
                 const float f = -(J.scale * tangent_density(J, lk)) / sn;
                 dL = V3{dL.x + Lr.x * f, dL.y + Lr.y * f, dL.z + Lr.z * f};
                 if (kCount) ++cnt.grad_events;
@@ -687,6 +693,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 ck_lost = true;
             }
             Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
+            if (kRep) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
             if (kMode == kTwoState) {
               const float eo = emit_weight * tro;
               Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
