@@ -117,6 +117,14 @@ RCV_HD float u32_to_unit(uint32_t v) {
 
 RCV_HD float next1d(Pcg32& r) { return u32_to_unit(pcg_next(r)); }
 
+// next1d of the stream (state, inc), advancing the state in place.
+RCV_HD float next1d_state(uint64_t& state, uint64_t inc) {
+  Pcg32 r{state, inc};
+  const float u = next1d(r);
+  state = r.state;
+  return u;
+}
+
 // ------------------------------------------------------------- float math --
 struct V3 {
   float x, y, z;

@@ -265,7 +265,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   uint32_t sid = 0;  // sample index within the job: pixel * spp + sample
   V3 dL{0.0f, 0.0f, 0.0f};  // kReplay: dLoss/dL of the pixel; kForward: the task's image derivative
 
-  Pcg32 rng, rng_nee;  // rng_nee: whole-path replay, stream of the second shadow walk
+  Pcg32 rng;
+  // whole-path replay: state of the stream of the second shadow walk (its
+  // increment is rng.inc)
+  uint64_t nee_state = 0;
   // main path state
   V3 p, d;
   float t_rem = 0.0f;
@@ -283,6 +286,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   // replay: radiance the path gathers after its current point,
   // L_rem = L - (radiance gathered so far), kept instead of L and the sum so far
   V3 Lrem{0, 0, 0}, cn_task{0, 0, 0};
+  uint32_t ck_slot = 0;  // replay checkpoint task: its record (the NEE contribution is re-read there)
   float s_nee = 0.0f;
   int task = kTaskSegment;
   bool own_event = false;  // checkpoint task: its scattering event is still to be processed
@@ -335,6 +339,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       const bool resume = kRep && path >= Q.total;
       float4 r0, r1, r2, r3;
       if (resume) {
+        ck_slot = (uint32_t)(path - Q.total);
         const float4* rec = Q.ckpt + (path - Q.total) * 4;
         r0 = rec[0];
         r1 = rec[1];
@@ -386,7 +391,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           bn = V3{r1.w, r2.x, r2.y};
           Ln = V3{r2.z, r2.w, r3.x};
           Lrem = V3{Lrem.x - Ln.x, Lrem.y - Ln.y, Lrem.z - Ln.z};
-          cn_task = V3{r3.y, r3.z, r3.w};
+          if (kMode == kForward) cn_task = V3{r3.y, r3.z, r3.w};
           sc_n = J.scale * density_new(J, locate(J, p));
           own_event = true;
           phase = kScatter;
@@ -503,12 +508,17 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           if (task == kTaskCheckpoint) {
             // NEE contribution known from the radiance pass: one shadow walk
             // on the main stream scatters its gradient (gathers the tangent)
-            if (kMode == kReplay) s_nee = (dL.x * cn_task.x + dL.y * cn_task.y) + dL.z * cn_task.z;
-            Lrem = V3{Lrem.x - cn_task.x, Lrem.y - cn_task.y, Lrem.z - cn_task.z};
+            V3 cn = cn_task;
+            if (kMode == kReplay) {
+              const float4 r3 = Q.ckpt[(int64_t)ck_slot * 4 + 3];
+              cn = V3{r3.y, r3.z, r3.w};
+              s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
+            }
+            Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
             own_event = false;
             phase = kNeeAdj;
           } else {
-            rng_nee = rng;  // whole-path replay: walk for the transmittance, then again
+            nee_state = rng.state;  // whole-path replay: walk for the transmittance, then again
           }
         }
       }
@@ -586,12 +596,12 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         float mu_c = mu, inv_c = inv_mu, hinv_c = half_inv_mu;
         float t;
         if (kSG && J.sg[0] > 0) {
-          const float tau = -log_unit(1.0f - (nee_stream ? next1d(rng_nee) : next1d(rng)));
+          const float tau = -log_unit(1.0f - (nee_stream ? next1d_state(nee_state, rng.inc) : next1d(rng)));
           t = supergrid_flight(J, kMode == kTwoState ? J.sg_two : J.sg_new, org, dir, tmax, tau, mu_c);
           inv_c = 1.0f / mu_c;
           hinv_c = 0.5f * inv_c;
         } else {
-          t = free_flight(nee_stream ? next1d(rng_nee) : next1d(rng), mu, inv_mu);
+          t = free_flight(nee_stream ? next1d_state(nee_state, rng.inc) : next1d(rng), mu, inv_mu);
         }
         const bool valid = t <= tmax;
         Lookup lk;
