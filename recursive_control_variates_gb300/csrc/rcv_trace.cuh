@@ -236,6 +236,14 @@ __device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJo
   return f;
 }
 
+// dLoss/dL of one path of pixel `pix` (the pixel value is the mean of its
+// samples), as the replay uses it.
+__device__ __forceinline__ V3 pixel_dL(const VolJob& J, int pix) {
+  const float* g = J.grad_img + (int64_t)pix * 3;
+  const float fs = (float)J.spp;
+  return V3{g[0] / fs, g[1] / fs, g[2] / fs};
+}
+
 // kSG: the launch may contain media with a majorant supergrid.  kCount: the
 // launch accumulates the RCV_COUNTER_* event counts (off, the counters cost
 // no registers).
@@ -263,7 +271,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   float mu = 0.0f, inv_mu = 0.0f, half_inv_mu = 0.0f;
   int pix = 0;
   uint32_t sid = 0;  // sample index within the job: pixel * spp + sample
-  V3 dL{0.0f, 0.0f, 0.0f};  // kReplay: dLoss/dL of the pixel; kForward: the task's image derivative
+  V3 dL{0.0f, 0.0f, 0.0f};  // kForward: the task's image derivative
+  // kReplay: dL . L_rem with dL = dLoss/dL of the pixel; it changes only with
+  // L_rem, and dL itself is recomputed from the image gradient at the events
+  // that need it per channel (fewer registers live through the walk)
+  float s_main = 0.0f;
 
   Pcg32 rng;
   // whole-path replay: state of the stream of the second shadow walk (its
@@ -370,13 +382,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       depth = 0;
       if (kMode == kAdjoint) ck_lost = false;
       if (kRep) {
-        if (kMode == kReplay) {
-          const float* g = J.grad_img + (int64_t)pix * 3;
-          const float fs = (float)J.spp;
-          dL = V3{g[0] / fs, g[1] / fs, g[2] / fs};
-        } else {
-          dL = V3{0.0f, 0.0f, 0.0f};
-        }
+        if (kMode == kForward) dL = V3{0.0f, 0.0f, 0.0f};
         const float4 lt = Q.path_ltot[path];
         Lrem = V3{lt.x, lt.y, lt.z};
         task = resume ? kTaskCheckpoint : (lt.w != 0.0f ? kTaskWhole : kTaskSegment);
@@ -427,6 +433,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       }
     }
 
+    if (kMode == kReplay && run_start && iter0 == n_iter) {
+      const V3 g = pixel_dL(*Jp, pix);  // the task started in this iteration
+      s_main = (g.x * Lrem.x + g.y * Lrem.y) + g.z * Lrem.z;
+    }
+
     // ------------------------------------------------- real scattering event
     if (run_scat && phase == kScatter) {
       const VolJob& J = *Jp;
@@ -453,13 +464,14 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           if (kMode == kReplay) {
             // d log(sigma_s) / d density and d log(albedo) / d albedo at the event
             const V3 Lr = Lrem;
-            const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
+            const V3 g = pixel_dL(J, pix);
+            const float sd = s_main;  // (g . Lr)
             scatter_density(J, lk, (J.scale * sd) / st_n);
             if (kCount) ++cnt.grad_events;
             if (J.grad_albedo != nullptr) {
               if (kCount) ++cnt.albedo_events;
-              const V3 ga{(dL.x * Lr.x) / fmaxf(an.x, 1e-8f), (dL.y * Lr.y) / fmaxf(an.y, 1e-8f),
-                          (dL.z * Lr.z) / fmaxf(an.z, 1e-8f)};
+              const V3 ga{(g.x * Lr.x) / fmaxf(an.x, 1e-8f), (g.y * Lr.y) / fmaxf(an.y, 1e-8f),
+                          (g.z * Lr.z) / fmaxf(an.z, 1e-8f)};
               scatter_albedo(J, alk, ga);
             }
           } else if (kMode == kForward) {
@@ -512,9 +524,13 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             if (kMode == kReplay) {
               const float4 r3 = Q.ckpt[(int64_t)ck_slot * 4 + 3];
               cn = V3{r3.y, r3.z, r3.w};
-              s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
             }
             Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
+            if (kMode == kReplay) {
+              const V3 g = pixel_dL(J, pix);
+              s_nee = (g.x * cn.x + g.y * cn.y) + g.z * cn.z;
+              s_main = (g.x * Lrem.x + g.y * Lrem.y) + g.z * Lrem.z;
+            }
             own_event = false;
             phase = kNeeAdj;
           } else {
@@ -645,9 +661,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 bo = V3{bo.x * wo, bo.y * wo, bo.z * wo};
               } else if (kMode == kReplay) {
                 const float sn = mu_c - st_n;
-                const V3 Lr = Lrem;
-                const float sd = (dL.x * Lr.x + dL.y * Lr.y) + dL.z * Lr.z;
-                scatter_density(J, lk, -(J.scale * sd) / sn);
+                scatter_density(J, lk, -(J.scale * s_main) / sn);
                 if (kCount) ++cnt.grad_events;
               } else if (kMode == kForward) {
                 const float sn = mu_c - st_n;
@@ -712,10 +726,13 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             if (kRep) {
               // whole-path replay: walk the shadow ray again (saved stream) to
               // back-propagate through its transmittance
-              if (kMode == kReplay)
-                s_nee = (dL.x * cn.x + dL.y * cn.y) + dL.z * cn.z;
-              else
+              if (kMode == kReplay) {
+                const V3 g = pixel_dL(*Jp, pix);
+                s_nee = (g.x * cn.x + g.y * cn.y) + g.z * cn.z;
+                s_main = (g.x * Lrem.x + g.y * Lrem.y) + g.z * Lrem.z;
+              } else {
                 cn_task = cn;
+              }
               q = p;
               float a;
               slab(q, recip(w), a, tr_rem);
