@@ -268,7 +268,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   int64_t path = 0;
   const VolJob* Jp = &single;
   int phase = kIdle;
-  float mu = 0.0f, inv_mu = 0.0f, half_inv_mu = 0.0f;
+  float mu = 0.0f, inv_mu = 0.0f;  // half of inv_mu is recomputed where needed (one register less)
   int pix = 0;
   uint32_t sid = 0;  // sample index within the job: pixel * spp + sample
   V3 dL{0.0f, 0.0f, 0.0f};  // kForward: the task's image derivative
@@ -365,7 +365,6 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       const float mu_new = J.scale * bits_to_float(__ldg(J.maxbits + 1));
       mu = (kMode == kTwoState) ? fmaxf(mu_old, mu_new) : mu_new;
       inv_mu = 1.0f / mu;
-      half_inv_mu = 0.5f * inv_mu;
       // k-th pixel of the job's hand-out order, sample s of that pixel
       // 32-bit index arithmetic: a job has fewer than 2^32 paths
       const uint32_t local = (uint32_t)(path - J.path_begin);
@@ -563,7 +562,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         V3 c1 = mw ? bn : V3{trn, 0.0f, 0.0f};
         V3 c2 = mw ? bo : V3{tro, 0.0f, 0.0f};
         float* s = s_coop + (threadIdx.x >> 5) * 96;
-        const int f = coop_walk<kMode>(m_coop, mw, Jp, rng, mu, inv_mu, half_inv_mu, org, dir, tmax, c1, c2, s,
+        const int f = coop_walk<kMode>(m_coop, mw, Jp, rng, mu, inv_mu, 0.5f * inv_mu, org, dir, tmax, c1, c2, s,
                                        s + 32, s + 64);
         if (f > 0) {
           if (mw) {
@@ -609,7 +608,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         finished = true;
       } else {
         // majorant of this collision: global, or the supergrid cell it lies in
-        float mu_c = mu, inv_c = inv_mu, hinv_c = half_inv_mu;
+        float mu_c = mu, inv_c = inv_mu, hinv_c = 0.5f * inv_mu;
         float t;
         if (kSG && J.sg[0] > 0) {
           const float tau = -log_unit(1.0f - (nee_stream ? next1d_state(nee_state, rng.inc) : next1d(rng)));
