@@ -125,6 +125,16 @@ RCV_HD float next1d_state(uint64_t& state, uint64_t inc) {
   return u;
 }
 
+#ifdef __CUDACC__
+// Vector reduction without a returned value (red.global.add.v4.f32): the
+// float4 atomicAdd overload returns the old value, which the L1 must wait
+// for and write back even when it is unused.
+__device__ __forceinline__ void red_add_v4(float4* dst, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+#endif
+
 // ------------------------------------------------------------- float math --
 struct V3 {
   float x, y, z;

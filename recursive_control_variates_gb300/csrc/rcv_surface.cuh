@@ -164,10 +164,10 @@ __device__ __forceinline__ V3 tex_eval(const SurfJob& S, const TexLookup& l, int
 __device__ __forceinline__ void tex_scatter(const SurfJob& S, const TexLookup& l, const V3& g) {
   const float gx = 1.0f - l.fx, gy = 1.0f - l.fy;
   const float w00 = gx * gy, w10 = l.fx * gy, w01 = gx * l.fy, w11 = l.fx * l.fy;
-  atomicAdd(S.grad_tex + l.i00, make_float4(g.x * w00, g.y * w00, g.z * w00, 0.0f));
-  atomicAdd(S.grad_tex + l.i10, make_float4(g.x * w10, g.y * w10, g.z * w10, 0.0f));
-  atomicAdd(S.grad_tex + l.i01, make_float4(g.x * w01, g.y * w01, g.z * w01, 0.0f));
-  atomicAdd(S.grad_tex + l.i11, make_float4(g.x * w11, g.y * w11, g.z * w11, 0.0f));
+  red_add_v4(S.grad_tex + l.i00, g.x * w00, g.y * w00, g.z * w00, 0.0f);
+  red_add_v4(S.grad_tex + l.i10, g.x * w10, g.y * w10, g.z * w10, 0.0f);
+  red_add_v4(S.grad_tex + l.i01, g.x * w01, g.y * w01, g.z * w01, 0.0f);
+  red_add_v4(S.grad_tex + l.i11, g.x * w11, g.y * w11, g.z * w11, 0.0f);
 }
 
 // Forward mode: bilinear tangent of the texture (grad_tex holds it).

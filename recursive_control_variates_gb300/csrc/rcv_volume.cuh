@@ -311,8 +311,8 @@ __device__ __forceinline__ void scatter_density(const VolJob& J, const Lookup& l
   const float a = g * gz0, b = g * fz;
   const float a0 = a * gy0, a1 = a * fy, b0 = b * gy0, b1 = b * fy;
   float4* dst = J.grad_cells + l.cell * 2;
-  atomicAdd(dst + 0, make_float4(a0 * gx0, a0 * fx, a1 * gx0, a1 * fx));
-  atomicAdd(dst + 1, make_float4(b0 * gx0, b0 * fx, b1 * gx0, b1 * fx));
+  red_add_v4(dst + 0, a0 * gx0, a0 * fx, a1 * gx0, a1 * fx);
+  red_add_v4(dst + 1, b0 * gx0, b0 * fx, b1 * gx0, b1 * fx);
 }
 
 __device__ __forceinline__ void scatter_albedo(const VolJob& J, const AlbedoLookup& l, const V3& g) {
@@ -327,7 +327,7 @@ __device__ __forceinline__ void scatter_albedo(const VolJob& J, const AlbedoLook
     const int i = k & 1, j = (k >> 1) & 1, m = k >> 2;
     const float w = (wz[m] * wy[j]) * wx[i];
     float4* dst = J.grad_albedo + ((int64_t)zs[m] * J.ady + ys[j]) * J.adx + xs[i];
-    atomicAdd(dst, make_float4(g.x * w, g.y * w, g.z * w, 0.0f));
+    red_add_v4(dst, g.x * w, g.y * w, g.z * w, 0.0f);
   }
 }
 
