@@ -133,6 +133,10 @@ __device__ __forceinline__ void red_add_v4(float4* dst, float a, float b, float 
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(a), "f"(b), "f"(c), "f"(d)
                : "memory");
 }
+
+__device__ __forceinline__ void red_add_u32(uint32_t* dst, uint32_t v) {
+  asm volatile("red.global.add.u32 [%0], %1;" ::"l"(dst), "r"(v) : "memory");
+}
 #endif
 
 // ------------------------------------------------------------- float math --

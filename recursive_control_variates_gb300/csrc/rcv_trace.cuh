@@ -786,7 +786,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         atomicAdd(o + 2, dL.z / fs);
       }
       if (kCount && !kRep) ++cnt.paths;
-      if (Jp->pixel_cost != nullptr) atomicAdd(Jp->pixel_cost + pix, n_iter - iter0);
+      if (Jp->pixel_cost != nullptr) red_add_u32(Jp->pixel_cost + pix, n_iter - iter0);
       phase = kIdle;
     }
   }
