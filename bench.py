@@ -94,14 +94,28 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def ncu_traffic(kernel: str):
-    """dram bytes per launch recorded from an ncu capture in profiles/
-    (a line `traffic_bytes_per_launch[<kernel>]: <bytes>`), else None."""
+def profile_figures(kernel: str) -> dict:
+    """Per-launch figures of `kernel` recorded from ncu captures in
+    profiles/*.md (lines `<figure>[<kernel>]: <value>`, e.g.
+    traffic_bytes_per_launch, l1_throughput_pct, threads_per_inst).  A file
+    counts only if its `source_digest:` line matches the digest of the
+    current CUDA sources; otherwise its figures are stale and left out."""
+    from recursive_control_variates_gb300 import _build
+
+    cur = _build.source_digest()
+    figures, stale = {}, []
     for f in sorted((ROOT / "profiles").glob("*.md")):
-        m = re.search(rf"traffic_bytes_per_launch\[{re.escape(kernel)}\]:\s*([0-9.eE+]+)", f.read_text())
-        if m:
-            return float(m.group(1))
-    return None
+        txt = f.read_text()
+        found = re.findall(rf"^(\w+)\[{re.escape(kernel)}\]:\s*([0-9.eE+-]+)\s*$", txt, re.M)
+        if not found:
+            continue
+        m = re.search(r"^source_digest:\s*([0-9a-f]+)\s*$", txt, re.M)
+        if m is None or m.group(1) != cur:
+            stale.append(f"{f.name} ({m.group(1) if m else 'no digest'})")
+            continue
+        for k, v in found:
+            figures.setdefault(k, float(v))
+    return {"figures": figures, "source_digest": cur, "stale": stale}
 
 
 class ClockSampler:
@@ -315,12 +329,20 @@ def run_ours(args, cfg):
     peaks = measured_peaks()
     dur_s = kern_serial[dom]["mean_ms"] / 1e3
     achieved = algo[dom] / dur_s / 1e9
-    traffic = ncu_traffic(dom)
+    prof = profile_figures(dom)
+    fig = prof["figures"]
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
             "peak_source": peaks["source"], "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
-            "traffic": traffic, "algorithmic_bytes_per_launch": algo[dom],
+            "traffic": fig.get("traffic_bytes_per_launch"), "algorithmic_bytes_per_launch": algo[dom],
             "mean_launch_ms": round(kern_serial[dom]["mean_ms"], 4),
-            "timing": "launches timed alone (3 steps without the side-stream overlap)"}
+            "timing": "launches timed alone (3 steps without the side-stream overlap)",
+            # the ceiling the tracer launches actually meet (grids are L2-resident):
+            # L1 throughput and lanes per warp instruction from the same capture
+            "l1_throughput_pct": fig.get("l1_throughput_pct"), "threads_per_inst": fig.get("threads_per_inst"),
+            "profile_source_digest": prof["source_digest"]}
+    if not fig:
+        roof["profile_note"] = ("no ncu summary in profiles/ was captured from the current CUDA sources"
+                                + (f"; stale: {', '.join(prof['stale'])}" if prof["stale"] else ""))
 
     # --------------------------------------------------- end-to-end (API)
     e2e = None
@@ -378,6 +400,16 @@ def run_ours(args, cfg):
     if args.majorant_factor > 0:
         supergrid = time_phase(args, cfg, device, dist, job.target, "late", world, flush,
                                majorant_factor=args.majorant_factor)
+    sparse = None
+    if args.majorant_factor > 0 and not args.no_sparse:
+        # a medium sparse enough for the supergrid: one blob in a 128^3 grid
+        from recursive_control_variates_gb300 import scenes as _sc
+
+        scfg = _sc.CONFIGS["sparse128"]
+        glob = time_phase(args, scfg, device, dist, None, "late", world, flush)
+        sg = time_phase(args, scfg, device, dist, None, "late", world, flush, majorant_factor=8)
+        sparse = {"workload": "sparse128: one Gaussian blob in a 128^3 grid, 512^2, spp 16, depth 64, albedo 0.8",
+                  "global": glob, "supergrid": sg, "supergrid_speedup": glob["ms_per_step"] / sg["ms_per_step"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -413,6 +445,7 @@ def run_ours(args, cfg):
         "phase": "late (density starts at 0.8 x the true grid)",
         "early_phase": early,
         "supergrid": supergrid,
+        "supergrid_sparse": sparse,
         "surface": surface,
         "batched": batched,
         "served": served,
@@ -604,6 +637,27 @@ def batched_form(args, device, flush):
     bc.close()
     total = sum(ms) / 1e3
     value = paths * len(ms) / total
+    # the batched form per film size: the jobs of one film size in a batch of
+    # their own (same launch options), so that its lead over the plain API
+    # shows per size
+    batched_by_film = {}
+    for r in sorted({int(m["res"]) for m in mix}):
+        sel = [j for m, j in zip(mix, jobs) if int(m["res"]) == r]
+        bf = batch.BatchedCV(sel, options=best, use_graph=True)
+        bf.step(2)
+        torch.cuda.synchronize()
+        evf = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        for i, (a, e) in enumerate(evf):
+            flush.fill_(float(i))
+            a.record(stream)
+            bf.step()
+            e.record(stream)
+        torch.cuda.synchronize()
+        fms = sum(a.elapsed_time(e) for a, e in evf) / len(evf)
+        pp = sum(int(j.paths_per_step()) for j in sel)
+        batched_by_film[f"{r}x{r}"] = {"jobs": len(sel), "paths_per_step": pp, "ms": round(fms, 3),
+                                       "paths_per_s": pp / (fms / 1e3)}
+        bf.close()
     plain_value = plain_ms = plain_wall = plain_by_film = None
     if plains is not None:
         # plain single-job form: the same jobs through the single-job API.
@@ -650,6 +704,9 @@ def batched_form(args, device, flush):
         "plain_value": plain_value, "plain_ms_per_round": plain_ms, "plain_wall_ms_per_round": plain_wall,
         "speedup_vs_plain": value / plain_value if plain_value else None,
         "plain_by_film": plain_by_film,
+        "batched_by_film": batched_by_film,
+        "lead_by_film": ({k: round(v["paths_per_s"] / plain_by_film[k]["paths_per_s"], 3)
+                          for k, v in batched_by_film.items() if k in plain_by_film} if plain_by_film else None),
         "lookups_per_path": float((dc[0][1] + dc[0][2] + dc[1][1] + dc[1][2]) / max(dc[0][0] + dc[1][0], 1.0)),
         "l2": "flushed between timed steps (512 MB write)",
     }
@@ -764,8 +821,14 @@ def cpu_baseline(cfg, job, target_seconds: float = 15.0):
     return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"every {rows[2]}th row ({len(range(*rows))} rows) x {cfg.res} px x (spp {cfg.spp} + spp_grad "
                       f"{cfg.spp_grad}) of {cfg.name} at the job's current state, one CPU gradient step ({n} paths, "
-                      f"{dt:.1f} s), C++ restatement, {threads} threads",
-            "cpu": cpu_model()}
+                      f"{dt:.1f} s), C++ restatement built with `{oracle_flags()}`, {threads} threads",
+            "cpu": cpu_model(), "flags": oracle_flags()}
+
+
+def oracle_flags() -> str:
+    from oracle import build as oracle_build
+
+    return oracle_build.flags_text()
 
 
 def cpu_model() -> str:
@@ -828,9 +891,10 @@ def run_reference(args, cfg):
         "p50_ms": ts[len(ts) // 2] * 1e3, "p99_ms": ts[-1] * 1e3,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(range(*band))} rows x {cfg.res} px x (spp {cfg.spp} + spp_grad "
-                                   f"{cfg.spp_grad}) per step; C++ restatement of the reference's path (its "
-                                   f"llvm_ad_rgb path needs Mitsuba 3 / Dr.Jit, not installable offline)",
-                         "cpu": cpu_model()},
+                                   f"{cfg.spp_grad}) per step; C++ restatement of the reference's path built "
+                                   f"with `{oracle_flags()}` (its llvm_ad_rgb path needs Mitsuba 3 / Dr.Jit, not "
+                                   f"installable offline)",
+                         "cpu": cpu_model(), "flags": oracle_flags()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -856,6 +920,7 @@ def main(argv=None):
                     help="all: the headline line (plain cfg2) with the batched and served forms; batched / served: "
                          "only that form, printed as its own JSON object (profiling runs)")
     ap.add_argument("--batched-jobs", type=int, default=32)
+    ap.add_argument("--no-sparse", action="store_true", help="skip the sparse-medium supergrid comparison")
     ap.add_argument("--majorant-factor", type=int, default=8,
                     help="also time the headline step with a majorant supergrid of this factor (0 = skip)")
     ap.add_argument("--no-autotune", action="store_true")

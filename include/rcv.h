@@ -202,11 +202,16 @@ int rcv_render_volume(const rcv_medium* medium, const rcv_sensor* sensor,
  * a fixed memory pool and gives this library only its inputs and outputs.
  * Its scratch (work-queue counter, pixel order, per-path radiance) is a
  * file-scope static __device__ array of 16 MiB that every GPU loading the
- * library holds until exit, so width * height * spp is limited to about
- * 16 MiB / (16 B per path + 4 B per pixel); larger requests return
+ * library holds until exit.  A call needs 16 B per path and 8 B per pixel
+ * (pixel order and pixel cost) plus under 2 KB of counters, buckets and
+ * alignment; exactly, rcv_render_workspace_bytes(width, height, spp,
+ * RCV_MODE_SINGLE) must not exceed 16 MiB.  Larger requests return
  * RCV_ERR_INVALID with the needed size.  It calls no allocator.  The first
  * call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any
+ * stream capture.  The kept address belongs to the device's current primary
+ * context: after cudaDeviceReset on a device, this entry point must not be
+ * called again on that device in the same process.
  * All calls on one device share that device's copy of the array and find
  * the previous call's contents in it (the call resets what must start at
  * zero): calls that can overlap on the GPU, e.g. issued on two streams,

@@ -108,28 +108,32 @@ class SurfaceScene:
         self.width, self.height = cam.width, cam.height
 
 
-def surface_render_twostates(scene: SurfaceScene, seed: int, spp: int, threads: int | None = None):
+def surface_render_twostates(scene: SurfaceScene, seed: int, spp: int, threads: int | None = None,
+                             rows: tuple = (0, 0, 1)):
+    """(H, F); ``rows`` = (first, end[, stride]) rows to render (end 0 = all)."""
     H = np.zeros((scene.height, scene.width, 3), np.float32)
     F = np.zeros_like(H)
     if lib().oracle_surface_render(C.byref(scene.c), 0, seed & 0xFFFFFFFF, spp, H.ctypes.data, F.ctypes.data,
-                                   threads or default_threads()):
+                                   threads or default_threads(), *_rows(rows)):
         raise ValueError("oracle_surface_render: invalid arguments")
     return H, F
 
 
-def surface_render(scene: SurfaceScene, seed: int, spp: int, threads: int | None = None):
+def surface_render(scene: SurfaceScene, seed: int, spp: int, threads: int | None = None, rows: tuple = (0, 0, 1)):
     img = np.zeros((scene.height, scene.width, 3), np.float32)
     if lib().oracle_surface_render(C.byref(scene.c), 1, seed & 0xFFFFFFFF, spp, None, img.ctypes.data,
-                                   threads or default_threads()):
+                                   threads or default_threads(), *_rows(rows)):
         raise ValueError("oracle_surface_render: invalid arguments")
     return img
 
 
-def surface_backward(scene: SurfaceScene, seed: int, spp: int, grad_img, threads: int | None = None):
+def surface_backward(scene: SurfaceScene, seed: int, spp: int, grad_img, threads: int | None = None,
+                     rows: tuple = (0, 0, 1)):
+    """dLoss/dtexture (float64) from the paths of the selected rows."""
     g = np.ascontiguousarray(grad_img, np.float32)
     out = np.zeros(scene.tex_new.shape, np.float64)
     if lib().oracle_surface_backward(C.byref(scene.c), seed & 0xFFFFFFFF, spp, g.ctypes.data, out.ctypes.data,
-                                     threads or default_threads()):
+                                     threads or default_threads(), *_rows(rows)):
         raise ValueError("oracle_surface_backward: invalid arguments")
     return out
 
@@ -159,9 +163,11 @@ def lib():
         L.oracle_backward.restype = C.c_int
         L.oracle_forward.argtypes = [C.POINTER(OracleScene), C.c_uint32, C.c_int, vp, vp, vp, C.c_int]
         L.oracle_forward.restype = C.c_int
-        L.oracle_surface_render.argtypes = [C.POINTER(OracleSurface), C.c_int, C.c_uint32, C.c_int, vp, vp, C.c_int]
+        L.oracle_surface_render.argtypes = [C.POINTER(OracleSurface), C.c_int, C.c_uint32, C.c_int, vp, vp, C.c_int,
+                                            C.c_int, C.c_int, C.c_int]
         L.oracle_surface_render.restype = C.c_int
-        L.oracle_surface_backward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int]
+        L.oracle_surface_backward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int, C.c_int,
+                                              C.c_int, C.c_int]
         L.oracle_surface_forward.argtypes = [C.POINTER(OracleSurface), C.c_uint32, C.c_int, vp, vp, C.c_int]
         L.oracle_surface_forward.restype = C.c_int
         L.oracle_surface_backward.restype = C.c_int
@@ -457,6 +463,40 @@ class CVOracle:
         if self.it > 0 and not self.pre_update:
             self.stats.update(H, F)
         self.it += 1
+        return self.img
+
+
+class MetaOracle:
+    """MetaIntegrator.render (plugins/metaintegrator.py:57-130) around a
+    nested integrator given as two callables: ``render_twostates(seed)`` ->
+    (H, F) and ``render(seed)`` -> image.  Methods ``baseline``, ``cv_ps``,
+    ``cv_pss``; ``pre_update``; ``force_baseline`` (denoising is not
+    restated)."""
+
+    def __init__(self, method="baseline", warmup=1, beta1=0.9, beta2=0.999, pre_update=False,
+                 force_baseline=False):
+        self.method = method
+        self.force_baseline = force_baseline
+        self.cv = CVOracle(warmup, beta1, beta2, pre_update) if "cv" in method else None
+        self.H = f32(0.0)  # cv_pss: the previous step's render with this step's seed
+        self.img = f32(0.0)
+
+    def render(self, render_twostates, render, seed):
+        img_noisy = None
+        if self.method == "cv_ps":
+            H, F = render_twostates(seed)
+        else:
+            img_noisy = render(seed)
+        if self.method == "cv_pss":
+            H, F = self.H, img_noisy
+        if self.cv is not None:
+            self.img = self.cv.step(H, F)
+        else:
+            self.img = img_noisy
+        if self.method == "cv_pss":
+            self.H = render(seed + 1)  # re-rendered with the next step's seed
+        if self.force_baseline:
+            return img_noisy if self.method != "cv_ps" else render(seed)
         return self.img
 
 

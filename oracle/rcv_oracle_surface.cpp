@@ -381,13 +381,17 @@ struct Surf {
   }
 };
 
+// Rows row0, row0 + stride, ... < row1 (row1 <= 0: the image's height)
+// split over `threads` workers; f(worker, row).
 template <class F>
-void for_rows(int h, int threads, F&& f) {
+void for_rows(int h, int threads, F&& f, int row0 = 0, int row1 = 0, int stride = 1) {
   const int nt = std::max(1, threads);
+  const int end = row1 > 0 ? std::min(row1, h) : h;
+  const int st = std::max(1, stride);
   std::vector<std::thread> pool;
   for (int k = 0; k < nt; ++k)
     pool.emplace_back([&, k] {
-      for (int y = k; y < h; y += nt) f(k, y);
+      for (int y = row0 + k * st; y < end; y += nt * st) f(k, y);
     });
   for (auto& t : pool) t.join();
 }
@@ -397,10 +401,12 @@ void for_rows(int h, int threads, F&& f) {
 extern "C" {
 
 // mode 0: two-state (out_old = H, out_new = F); 1: single state (out_new).
-// Samples of a pixel are summed in sample order.
+// Samples of a pixel are summed in sample order.  Only rows row0, row0 +
+// stride, ... < row1 are rendered (row1 <= 0: all rows); other pixels of
+// the outputs are left untouched.
 int oracle_surface_render(const oracle_surface* S, int mode, uint32_t seed, int spp, float* out_old,
-                          float* out_new, int threads) {
-  if (!S || spp <= 0 || S->nspheres < 0 || S->nspheres > 8) return -1;
+                          float* out_new, int threads, int row0, int row1, int row_stride) {
+  if (!S || spp <= 0 || S->nspheres < 0 || S->nspheres > 8 || row0 < 0 || row1 > S->height) return -1;
   for_rows(S->height, threads, [&](int, int py) {
     Surf tr{*S, mode};
     for (int px = 0; px < S->width; ++px) {
@@ -422,7 +428,7 @@ int oracle_surface_render(const oracle_surface* S, int mode, uint32_t seed, int 
         out_old[pix * 3 + 2] = ao.z / fs;
       }
     }
-  });
+  }, row0, row1, row_stride);
   return 0;
 }
 
@@ -452,10 +458,11 @@ int oracle_surface_forward(const oracle_surface* S, uint32_t seed, int spp, cons
   return 0;
 }
 
-// Path-replay adjoint on `new`: ADDS dLoss/dtexture (double) to grad_tex.
+// Path-replay adjoint on `new`: ADDS dLoss/dtexture (double) to grad_tex,
+// from the paths of rows row0, row0 + stride, ... < row1 (row1 <= 0: all).
 int oracle_surface_backward(const oracle_surface* S, uint32_t seed, int spp, const float* grad_img,
-                            double* grad_tex, int threads) {
-  if (!S || spp <= 0 || !grad_img || !grad_tex) return -1;
+                            double* grad_tex, int threads, int row0, int row1, int row_stride) {
+  if (!S || spp <= 0 || !grad_img || !grad_tex || row0 < 0 || row1 > S->height) return -1;
   const int nt = std::max(1, threads);
   const size_t n = (size_t)S->tex_w * S->tex_h * 3;
   std::vector<std::vector<double>> sinks(nt, std::vector<double>(n, 0.0));
@@ -473,7 +480,7 @@ int oracle_surface_backward(const oracle_surface* S, uint32_t seed, int spp, con
         adj.trace(seed, lane, px, py, Lo, Ln);
       }
     }
-  });
+  }, row0, row1, row_stride);
   for (auto& s : sinks)
     for (size_t i = 0; i < n; ++i) grad_tex[i] += s[i];
   return 0;

@@ -58,6 +58,18 @@ def _digest() -> str:
     return h.hexdigest()
 
 
+def source_digest() -> str:
+    """Digest of the CUDA sources and the C header only (the same on every
+    machine): profile summaries record it, so that a figure captured from
+    other sources is recognised as stale."""
+    h = hashlib.sha256()
+    for p in sorted(list(CSRC.glob("*")) + [INCLUDE / "rcv.h"]):
+        if p.is_file():
+            h.update(p.name.encode())
+            h.update(p.read_bytes())
+    return h.hexdigest()[:16]
+
+
 def lib_path() -> Path:
     return BUILD_DIR / LIB_NAME
 

@@ -67,7 +67,7 @@ static JobLayout job_layout(const rcv_batch_job& j) {
   L.header = off;
   off = align256(off + sizeof(JobHeader));
   L.medium = off;
-  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr ? uint64_t(j.dims[0]) * j.dims[1] * j.dims[2] : 0u, j.majorant_factor).total);
+  off = align256(off + medium_layout(j.dims, j.albedo[0] != nullptr ? j.dims : nullptr, j.majorant_factor).total);
   L.buckets = off;
   off = align256(off + kRenderOrderBuckets * sizeof(uint32_t));
   L.order = off;
@@ -88,7 +88,7 @@ struct BatchEntry {
   float4* albedo;  // packed (old, new) pairs or null
   uint32_t* maxbits;
   float4* grad_cells;
-  float4* grad_albedo;  // or null
+  float4* grad_albedo;  // albedo cell records (6 float4 per cell) or null
   float* grad_img;
   uint32_t* buckets;  // 256 order buckets
   uint32_t* order;    // pixel hand-out order
@@ -179,12 +179,16 @@ __global__ void batch_pack_kernel(const BatchEntry* __restrict__ E, const int32_
     pack_cell(i, dx, dy, dz, od, nd, B.cells);
     B.grad_cells[i * 2 + 0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     B.grad_cells[i * 2 + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (B.opt_albedo) {
+      // the albedo grid has the density's resolution: one 6-float4 record per cell
+#pragma unroll
+      for (int q = 0; q < 6; ++q) B.grad_albedo[i * 6 + q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
   }
   if (i < B.nv) {
     mo = od[i];
     mn = nd[i];
     if (B.has_albedo) pack_albedo(i, B.d.albedo[cur ^ 1], B.d.albedo[cur], B.albedo);
-    if (B.opt_albedo) B.grad_albedo[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   reduce_majorants(mo, mn, B.maxbits);
 }
@@ -311,7 +315,8 @@ __global__ void batch_update_kernel(const BatchEntry* __restrict__ E, const int3
     B.d.density_v[i] = v;
   }
   if (B.opt_albedo) {
-    const float4 ga = B.grad_albedo[i];
+    const V3 ga = fold_voxel_rgb(i, B.d.dims[0], B.d.dims[1], B.d.dims[2],
+                                 reinterpret_cast<const float*>(B.grad_albedo));
     const float gs[3] = {0.0f + ga.x, 0.0f + ga.y, 0.0f + ga.z};
     const float* pin = B.d.albedo[cur];
     float* pout = B.d.albedo[cur ^ 1];
@@ -570,7 +575,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     std::memset(&e, 0, sizeof(e));
     e.d = d;
     e.hdr = reinterpret_cast<JobHeader*>(ws + L.header);
-    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr ? uint64_t(d.dims[0]) * d.dims[1] * d.dims[2] : 0u, d.majorant_factor);
+    const MediumLayout M = medium_layout(d.dims, d.albedo[0] != nullptr ? d.dims : nullptr, d.majorant_factor);
     char* mw = ws + L.medium;
     e.cells = reinterpret_cast<float4*>(mw + M.cells);
     e.has_albedo = d.albedo[0] != nullptr;

@@ -57,11 +57,15 @@ struct MediumLayout {
   uint64_t cells, albedo, maxbits, grad_cells, grad_albedo, sg_two, sg_new, total;
 };
 
-// albedo_voxels: voxels of the albedo grid (0 = no albedo grid).
-inline MediumLayout medium_layout(const int32_t dims[3], uint64_t albedo_voxels, int majorant_factor) {
+// albedo_dims: resolution of the albedo grid (null = no albedo grid).  The
+// albedo gradient is kept per albedo lookup cell like the density's: 8
+// corners x RGB = 24 floats (96 B, six 16-byte vector reductions per event).
+inline MediumLayout medium_layout(const int32_t dims[3], const int32_t* albedo_dims, int majorant_factor) {
   const uint64_t nc = uint64_t(dims[0] + 1) * uint64_t(dims[1] + 1) * uint64_t(dims[2] + 1);
-  const uint64_t nv = albedo_voxels;
-  const bool has_albedo = nv > 0;
+  const bool has_albedo = albedo_dims != nullptr;
+  const uint64_t nv = has_albedo ? uint64_t(albedo_dims[0]) * uint64_t(albedo_dims[1]) * uint64_t(albedo_dims[2]) : 0u;
+  const uint64_t nca =
+      has_albedo ? uint64_t(albedo_dims[0] + 1) * uint64_t(albedo_dims[1] + 1) * uint64_t(albedo_dims[2] + 1) : 0u;
   const uint64_t ns = uint64_t(supergrid_cells(dims[0], majorant_factor)) *
                       uint64_t(supergrid_cells(dims[1], majorant_factor)) *
                       uint64_t(supergrid_cells(dims[2], majorant_factor));
@@ -70,19 +74,25 @@ inline MediumLayout medium_layout(const int32_t dims[3], uint64_t albedo_voxels,
   l.cells = off;
   off = align256(off + nc * 64u);
   l.albedo = off;
-  off = align256(off + (has_albedo ? nv * 32u : 0u));
+  off = align256(off + nv * 32u);
   l.maxbits = off;
   off = align256(off + 16u);
   l.grad_cells = off;
   off = align256(off + nc * 32u);
   l.grad_albedo = off;
-  off = align256(off + (has_albedo ? nv * 16u : 0u));
+  off = align256(off + nca * 96u);
   l.sg_two = off;
   off = align256(off + ns * 4u);
   l.sg_new = off;
   off = align256(off + ns * 4u);
   l.total = off;
   return l;
+}
+
+// Bytes of the albedo gradient records of an albedo grid of the given
+// resolution: one 96-byte record per lookup cell.
+inline uint64_t albedo_grad_bytes(const int32_t ad[3]) {
+  return uint64_t(ad[0] + 1) * uint64_t(ad[1] + 1) * uint64_t(ad[2] + 1) * 96u;
 }
 
 // Albedo grid resolution of a medium: its own when set, else the density's.
@@ -99,7 +109,9 @@ inline uint64_t albedo_voxels_of(const rcv_medium* m) {
 }
 
 inline MediumLayout medium_layout(const rcv_medium* m) {
-  return medium_layout(m->dims, albedo_voxels_of(m), m->majorant_factor);
+  int32_t ad[3];
+  albedo_dims_of(m, ad);
+  return medium_layout(m->dims, m->albedo_old != nullptr ? ad : nullptr, m->majorant_factor);
 }
 
 // Scratch layout of one tracer call (all offsets 256-byte aligned):

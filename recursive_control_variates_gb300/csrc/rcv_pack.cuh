@@ -167,4 +167,34 @@ __device__ __forceinline__ float fold_voxel(int64_t i, int dx, int dy, int dz, c
   return g;
 }
 
+// RGB gradient of albedo voxel i from the albedo cell records (24 floats per
+// cell: corner k = bx + 2 by + 4 bz, then R, G, B), summed in the order of
+// fold_voxel.
+__device__ __forceinline__ V3 fold_voxel_rgb(int64_t i, int dx, int dy, int dz, const float* __restrict__ gcells) {
+  const uint32_t row = (uint32_t)i / (uint32_t)dx;
+  const int x = int((uint32_t)i - row * (uint32_t)dx);
+  const uint32_t z_u = row / (uint32_t)dy;
+  const int y = int(row - z_u * (uint32_t)dy), z = int(z_u);
+  V3 g{0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int kz = 0; kz < 4; ++kz) {
+    const int cz = z + (kz >> 1), bz = kz & 1;
+    if (!fold_uses(cz, bz, z, dz)) continue;
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+      const int cy = y + (ky >> 1), by = ky & 1;
+      if (!fold_uses(cy, by, y, dy)) continue;
+#pragma unroll
+      for (int kx = 0; kx < 4; ++kx) {
+        const int cx = x + (kx >> 1), bx = kx & 1;
+        if (!fold_uses(cx, bx, x, dx)) continue;
+        const int64_t cell = (int64_t(cz) * (dy + 1) + cy) * (dx + 1) + cx;
+        const float* r = gcells + cell * 24 + (bx + 2 * by + 4 * bz) * 3;
+        g = V3{g.x + r[0], g.y + r[1], g.z + r[2]};
+      }
+    }
+  }
+  return g;
+}
+
 }  // namespace rcv

@@ -166,11 +166,12 @@ __global__ void fold_density_kernel(int dx, int dy, int dz, const float* __restr
   grad[i] += fold_voxel(i, dx, dy, dz, gcells);
 }
 
-__global__ void fold_albedo_kernel(int64_t nv, const float4* __restrict__ ga,
+__global__ void fold_albedo_kernel(int adx, int ady, int adz, const float* __restrict__ gcells,
                                    float* __restrict__ grad) {
+  const int64_t nv = int64_t(adx) * ady * adz;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= nv) return;
-  const float4 g = ga[i];
+  const V3 g = fold_voxel_rgb(i, adx, ady, adz, gcells);
   grad[i * 3 + 0] += g.x;
   grad[i * 3 + 1] += g.y;
   grad[i * 3 + 2] += g.z;
@@ -412,9 +413,11 @@ int launch_fold(const rcv_medium* m, float* grad_density, float* grad_albedo, cu
   int rc = launched("fold_density launch");
   if (rc) return rc;
   if (grad_albedo != nullptr && m->albedo_old != nullptr) {
+    int32_t ad[3];
+    albedo_dims_of(m, ad);
     const int64_t na = (int64_t)albedo_voxels_of(m);
     fold_albedo_kernel<<<grid_for(na, block), block, 0, st>>>(
-        na, reinterpret_cast<const float4*>(ws + L.grad_albedo), grad_albedo);
+        ad[0], ad[1], ad[2], reinterpret_cast<const float*>(ws + L.grad_albedo), grad_albedo);
     rc = launched("fold_albedo launch");
   }
   return rc;
@@ -424,9 +427,12 @@ int reset_gradients(const rcv_medium* m, bool albedo, cudaStream_t st) {
   const MediumLayout L = medium_layout(m);
   char* ws = static_cast<char*>(m->workspace);
   const int64_t nc = int64_t(m->dims[0] + 1) * (m->dims[1] + 1) * (m->dims[2] + 1);
-  const int64_t na = (int64_t)albedo_voxels_of(m);
   RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_cells, 0, nc * 32, st), "gradient reset");
-  if (albedo) RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_albedo, 0, na * 16, st), "gradient reset");
+  if (albedo && m->albedo_old != nullptr) {
+    int32_t ad[3];
+    albedo_dims_of(m, ad);
+    RCV_TRY_CUDA(cudaMemsetAsync(ws + L.grad_albedo, 0, albedo_grad_bytes(ad), st), "gradient reset");
+  }
   return RCV_OK;
 }
 
@@ -437,8 +443,7 @@ using namespace rcv;
 extern "C" uint64_t rcv_medium_workspace_bytes(const int32_t dims[3], int32_t has_albedo_grid,
                                                int32_t majorant_factor) {
   if (dims == nullptr || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0 || majorant_factor < 0) return 0;
-  const uint64_t nv = has_albedo_grid ? uint64_t(dims[0]) * uint64_t(dims[1]) * uint64_t(dims[2]) : 0u;
-  return medium_layout(dims, nv, majorant_factor).total;
+  return medium_layout(dims, has_albedo_grid ? dims : nullptr, majorant_factor).total;
 }
 
 extern "C" uint64_t rcv_medium_workspace_bytes_for(const rcv_medium* m) {
@@ -656,7 +661,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 // Device address of g_noalloc_scratch on the current device.  In host code the
 // symbol is only a host-side stand-in, so the address is looked up once per
-// device (with that device current) and cached.
+// device (with that device current) and cached.  The cached address belongs to
+// the device's primary context; a cudaDeviceReset ends its validity, which is
+// why callers may not use the entry point on that device afterwards.
 static int noalloc_scratch(void** out) {
   static std::mutex mu;
   static void* addr[kNoAllocMaxDevices] = {};

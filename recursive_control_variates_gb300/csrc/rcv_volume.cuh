@@ -70,7 +70,9 @@ struct VolJob {
   // field, out_img receives the image derivative)
   const float* grad_img;
   float4* grad_cells;   // (dz+1)(dy+1)(dx+1) * 2
-  float4* grad_albedo;  // adz*ady*adx (rgb + pad) or null
+  // albedo cell records ((adz+1)(ady+1)(adx+1) x 6 float4: 8 corners x RGB),
+  // or in forward mode the tangent as one float4 per albedo voxel; or null
+  float4* grad_albedo;
   float* out_img;
   int64_t path_begin;   // first global path index of this job (batched launches)
   int64_t path_count;   // width*height*spp
@@ -315,19 +317,27 @@ __device__ __forceinline__ void scatter_density(const VolJob& J, const Lookup& l
   red_add_v4(dst + 1, b0 * gx0, b0 * fx, b1 * gx0, b1 * fx);
 }
 
+// Scatters g (RGB) * (trilinear weight of each corner) into the albedo
+// cell's gradient record (8 corners x RGB = 24 floats, 96 bytes): six vector
+// reductions of consecutive floats, none of them padding.  The fold resolves
+// the clamping of edge cells to voxels.
 __device__ __forceinline__ void scatter_albedo(const VolJob& J, const AlbedoLookup& l, const V3& g) {
-  const int x0 = clampi(l.ax.cell - 1, J.adx - 1), x1 = clampi(l.ax.cell, J.adx - 1);
-  const int y0 = clampi(l.ay.cell - 1, J.ady - 1), y1 = clampi(l.ay.cell, J.ady - 1);
-  const int z0 = clampi(l.az.cell - 1, J.adz - 1), z1 = clampi(l.az.cell, J.adz - 1);
   const float fx = l.ax.f, fy = l.ay.f, fz = l.az.f;
-  const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
-  const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+  const float gx0 = 1.0f - fx, gy0 = 1.0f - fy, gz0 = 1.0f - fz;
+  const float w0 = gz0 * gy0, w1 = gz0 * fy, w2 = fz * gy0, w3 = fz * fy;
+  const float w[8] = {w0 * gx0, w0 * fx, w1 * gx0, w1 * fx, w2 * gx0, w2 * fx, w3 * gx0, w3 * fx};
+  const int64_t cell = ((int64_t)l.az.cell * (J.ady + 1) + l.ay.cell) * (J.adx + 1) + l.ax.cell;
+  float4* dst = J.grad_albedo + cell * 6;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int i = k & 1, j = (k >> 1) & 1, m = k >> 2;
-    const float w = (wz[m] * wy[j]) * wx[i];
-    float4* dst = J.grad_albedo + ((int64_t)zs[m] * J.ady + ys[j]) * J.adx + xs[i];
-    red_add_v4(dst, g.x * w, g.y * w, g.z * w, 0.0f);
+  for (int q = 0; q < 6; ++q) {
+    float v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int f = q * 4 + e;  // corner f / 3, channel f % 3
+      const int c = f % 3;
+      v[e] = (c == 0 ? g.x : (c == 1 ? g.y : g.z)) * w[f / 3];
+    }
+    red_add_v4(dst + q, v[0], v[1], v[2], v[3]);
   }
 }
 

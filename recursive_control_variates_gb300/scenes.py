@@ -65,6 +65,7 @@ class VolumeConfig:
     init: float = 1.0
     seed: int = 0
     clamp: tuple = (0.0, 250.0)
+    blobs: int = 8  # Gaussian blobs of the density
     extra: dict = field(default_factory=dict)
 
     @property
@@ -82,6 +83,9 @@ CONFIGS = {
     "cfg2": VolumeConfig("cfg2", grid=64, res=512, spp=16, max_depth=64, steps=200, albedo=None),
     # profiling case: the cfg2 medium at 128^2 (one launch = 262 144 paths)
     "cfg2s": VolumeConfig("cfg2s", grid=64, res=128, spp=16, max_depth=64, steps=200, albedo=None),
+    # a sparse medium for the majorant supergrid: one Gaussian blob in a 128^3
+    # grid (mostly empty space), 512^2, spp 16, depth 64
+    "sparse128": VolumeConfig("sparse128", grid=128, res=512, spp=16, max_depth=64, steps=200, blobs=1),
 }
 
 
@@ -163,7 +167,7 @@ def orbit_views(box, n: int, distance: float = 2.0, height: float = 0.0, phase: 
 def config_grids(cfg: VolumeConfig, seed: int | None = None):
     """True density / albedo of a configuration (albedo is a float when constant)."""
     s = cfg.seed if seed is None else seed
-    dens = blob_density(cfg.grid, s)
+    dens = blob_density(cfg.grid, s, n_blobs=cfg.blobs)
     alb = cfg.albedo if cfg.albedo is not None else albedo_grid(cfg.grid, s)
     return dens, alb
 

@@ -10,10 +10,21 @@ integer sample count becomes a scalar whose `beta ** n` is the float32-rounded
 power of the float32 beta, and every other Mitsuba symbol the modules touch
 at import time is an inert placeholder.  Only the blend / statistics code
 paths run; the nested tracer is replaced by a stub returning the recorded
-(H, F) inputs.
+(H, F) inputs (``render_twostates``) or recorded single-state images
+(``render``), and logging the seed of every call.
 
-Usage (needs the reference checkout; the output is committed):
-    python tests/golden/make_cv_golden.py /root/reference
+Cases:
+  * ``cases``: CVIntegrator / MetaIntegrator ``cv_ps`` blend sequences
+    (plugins/cv_integrator.py:47-77, plugins/metaintegrator.py:57-130);
+  * ``meta_cases``: MetaIntegrator sequences with the nested integrator's
+    calls recorded: ``cv_pss`` (F = render(seed), H = the previous step's
+    render(seed + 1), plugins/metaintegrator.py:87-91,117-119), the
+    ``force_baseline`` returns of ``cv_pss`` and ``cv_ps``
+    (plugins/metaintegrator.py:124-128) and the ``baseline`` method.
+
+Usage (needs a checkout of the reference; the output is committed):
+    python tests/golden/make_cv_golden.py <reference checkout>
+or with the checkout in the environment variable RCV_REFERENCE.
 """
 from __future__ import annotations
 
@@ -154,6 +165,71 @@ def run_cv(cls, tsv, Hs, Fs, props):
     return {k: np.asarray(v) for k, v in outs.items()}
 
 
+class CallLog:
+    """Nested-integrator stub: hands out recorded images in call order and
+    logs (kind, seed) of every call (kind 0 = render_twostates, 1 = render)."""
+
+    def __init__(self, twostate=(), single=()):
+        self.twostate = iter(twostate)
+        self.single = iter(single)
+        self.calls = []
+
+    def render_twostates(self, scene, sensor, seed, spp):
+        self.calls.append((0, int(seed)))
+        return next(self.twostate)
+
+    def render(self, scene, sensor, seed, spp, develop=True, evaluate=True):
+        self.calls.append((1, int(seed)))
+        return next(self.single)
+
+
+def run_meta(meta, tsv, props, steps, n, rng, seed0=5):
+    """Drives the reference's MetaIntegrator with recorded nested renders.
+
+    The nested renders form the sequences of consecutive iterates of
+    ``sequence``: at step i the render with seed i of theta_i is F_i and the
+    render with seed i + 1 of theta_i is H_{i+1} (the two-state pair of the
+    next step)."""
+    Hs, Fs = sequence(rng, steps + 1, n, "normal")
+    method = props["method"]
+    if method == "cv_ps":
+        twostate = list(zip(Hs[:steps], Fs[:steps]))
+        single = [(F + rng.normal(0.0, 0.05, n)).astype(f32) for F in Fs[:steps]]  # fresh baseline renders
+    elif method == "cv_pss":
+        twostate = []
+        single = []
+        for i in range(steps):
+            single.append(Fs[i])
+            single.append(Hs[i + 1])
+    else:
+        twostate = []
+        single = [F.copy() for F in Fs[:steps]]
+    inner = tsv.TwoStatePRBVolpathIntegrator(Props())
+    log = CallLog(twostate, single)
+    inner.render_twostates = log.render_twostates
+    inner.render = log.render
+    p = Props(props)
+    p["integrator"] = inner
+    integ = meta.MetaIntegrator(p)
+    outs = {k: [] for k in ("out", "img", "w_s", "v_n", "var_x", "var_y", "cov", "n")}
+    for i in range(steps):
+        out = integ.render(None, 0, seed0 + i, 4)
+        outs["out"].append(np.broadcast_to(np.asarray(out, f32), (n,)).copy())
+        outs["img"].append(np.broadcast_to(np.asarray(integ.img, f32), (n,)).copy())
+        if "cv" in method:
+            outs["w_s"].append(np.broadcast_to(np.asarray(integ.w_s, f32), (n,)).copy())
+            outs["v_n"].append(np.broadcast_to(np.asarray(integ.v_n, f32), (n,)).copy())
+            for k in ("var_x", "var_y", "cov"):
+                outs[k].append(np.broadcast_to(np.asarray(getattr(integ.stats, k), f32), (n,)).copy())
+            outs["n"].append(int(integ.stats.n))
+    res = {k: np.asarray(v) for k, v in outs.items() if len(v)}
+    res["twostate_feed"] = np.asarray([np.stack(hf) for hf in twostate], f32).reshape(-1, 2, n)
+    res["single_feed"] = np.asarray(single, f32).reshape(-1, n)
+    res["calls"] = np.asarray(log.calls, np.int64).reshape(-1, 2)
+    res["seed0"] = np.int64(seed0)
+    return res
+
+
 def main(ref_root: str):
     warnings.simplefilter("ignore")
     cvi, meta, tsv, welford = import_reference(Path(ref_root))
@@ -196,10 +272,31 @@ def main(ref_root: str):
     arrays["welford1/var"] = np.asarray(variances)
     arrays["welford1/get"] = np.asarray(gets)
     arrays["cases"] = np.array([c[0] for c in specs])
+    # MetaIntegrator with its nested calls recorded (cv_pss, force_baseline)
+    meta_specs = [
+        ("meta_cv_pss", {"method": "cv_pss"}),
+        ("meta_cv_pss_pre_update", {"method": "cv_pss", "pre_update": True}),
+        ("meta_cv_pss_force", {"method": "cv_pss", "force_baseline": True}),
+        ("meta_cv_ps_force", {"method": "cv_ps", "force_baseline": True}),
+        ("meta_baseline", {"method": "baseline"}),
+    ]
+    for name, props in meta_specs:
+        out = run_meta(meta, tsv, props, 10, 64, rng)
+        arrays[f"{name}/method"] = np.array(props["method"])
+        arrays[f"{name}/pre_update"] = np.int32(bool(props.get("pre_update", False)))
+        arrays[f"{name}/force_baseline"] = np.int32(bool(props.get("force_baseline", False)))
+        for k, v in out.items():
+            arrays[f"{name}/{k}"] = v
+    arrays["meta_cases"] = np.array([c[0] for c in meta_specs])
     out_path = Path(__file__).with_name("cv_welford.npz")
     np.savez_compressed(out_path, **arrays)
     print(f"wrote {out_path} ({out_path.stat().st_size} bytes)")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RCV_REFERENCE")
+    if not root:
+        sys.exit("usage: make_cv_golden.py <reference checkout>  (or set RCV_REFERENCE)")
+    main(root)

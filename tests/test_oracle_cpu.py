@@ -260,6 +260,92 @@ def test_cv_welford_golden(oracle, golden_cv):
             assert cv.stats.n == int(g[f"{name}/n"][i])
 
 
+def _meta_feeds(g, name):
+    """Nested-render callables over the recorded feeds of a meta case, with a
+    call log of (kind, seed) like the generator's stub."""
+    two = iter(g[f"{name}/twostate_feed"])
+    single = iter(g[f"{name}/single_feed"])
+    calls = []
+
+    def render_twostates(seed):
+        calls.append((0, int(seed)))
+        hf = next(two)
+        return hf[0], hf[1]
+
+    def render(seed):
+        calls.append((1, int(seed)))
+        return next(single)
+
+    return render_twostates, render, calls
+
+
+def test_meta_cv_pss_and_force_baseline_golden(oracle, golden_cv):
+    """MetaIntegrator's cv_pss (F = render(seed), H = the previous step's
+    render(seed + 1), H = 0 at the first step), force_baseline and baseline
+    returns: the numpy restatement reproduces the reference's own
+    plugins/metaintegrator.py:57-130 bit for bit, with the same nested calls
+    and seeds in the same order."""
+    g = golden_cv
+    for name in g["meta_cases"]:
+        method = str(g[f"{name}/method"])
+        m = oracle.MetaOracle(method, pre_update=bool(g[f"{name}/pre_update"]),
+                              force_baseline=bool(g[f"{name}/force_baseline"]))
+        r2, r1, calls = _meta_feeds(g, name)
+        seed0 = int(g[f"{name}/seed0"])
+        for i in range(len(g[f"{name}/out"])):
+            with np.errstate(all="ignore"):
+                out = m.render(r2, r1, seed0 + i)
+            np.testing.assert_array_equal(out, g[f"{name}/out"][i], err_msg=f"{name} step {i}")
+            np.testing.assert_array_equal(np.broadcast_to(m.img, out.shape), g[f"{name}/img"][i])
+            if m.cv is not None:
+                np.testing.assert_array_equal(np.broadcast_to(m.cv.w_s, out.shape), g[f"{name}/w_s"][i])
+                np.testing.assert_array_equal(np.broadcast_to(m.cv.stats.cov, out.shape), g[f"{name}/cov"][i])
+                assert m.cv.stats.n == int(g[f"{name}/n"][i])
+        assert calls == [tuple(c) for c in g[f"{name}/calls"].tolist()], name
+    # force_baseline returns the noisy (cv_pss) or a fresh single-state
+    # (cv_ps) render while the control variate advances as without it
+    for force, method in (("meta_cv_pss_force", "cv_pss"), ("meta_cv_ps_force", "cv_ps")):
+        m = oracle.MetaOracle(method)
+        r2, r1, _ = _meta_feeds(g, force)
+        if method == "cv_ps":
+            r1 = lambda seed: None  # noqa: E731  (no single-state render without force_baseline)
+        for i in range(len(g[f"{force}/out"])):
+            with np.errstate(all="ignore"):
+                img = m.render(r2, r1, int(g[f"{force}/seed0"]) + i)
+            np.testing.assert_array_equal(img, g[f"{force}/img"][i])
+    np.testing.assert_array_equal(g["meta_cv_pss_force/out"], g["meta_cv_pss_force/single_feed"][0::2])
+    np.testing.assert_array_equal(g["meta_cv_ps_force/out"], g["meta_cv_ps_force/single_feed"])
+    assert not np.array_equal(g["meta_cv_ps_force/out"], g["meta_cv_ps_force/img"])
+
+
+def test_steady_state_anchor(oracle):
+    """Static scene, H == F (figures/steady_state/generate_data.py:56-79):
+    the statistics of H and F are then bitwise equal, the control weight
+    follows the analytic running-mean weight j/(j+1), and the image error
+    falls like 1/j as the running mean's does (the recursion drops the
+    first two renders and estimates its weights, so its error stays within
+    a constant factor of the running mean's)."""
+    rng = np.random.default_rng(5)
+    n = 20000
+    mu = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    cv = oracle.CVOracle()
+    acc = np.zeros(n)
+    mse = {}
+    for j in range(40):
+        F = (mu * rng.gamma(2.0, 0.5, n)).astype(np.float32)
+        with np.errstate(all="ignore"):
+            img = cv.step(F, F)
+        np.testing.assert_array_equal(cv.stats.var_x, cv.stats.cov)
+        np.testing.assert_array_equal(cv.stats.var_y, cv.stats.cov)
+        acc += F
+        mse[j] = (np.mean((img - mu) ** 2), np.mean((acc / (j + 1) - mu) ** 2))
+        if j >= 5:
+            if j >= 6:
+                assert abs(float(np.median(cv.w_s)) - j / (j + 1)) < 0.03, j
+            assert 0.9 < mse[j][0] / mse[j][1] < 2.0, (j, mse[j])
+    assert mse[39][0] < 0.25 * mse[5][0]
+
+
 def test_welford1_golden(oracle, golden_cv):
     g = golden_cv
     est = oracle.WelfordOracle()
