@@ -338,7 +338,11 @@ def run_ours(args, cfg):
             "timing": "launches timed alone (3 steps without the side-stream overlap)",
             # the ceiling the tracer launches actually meet (grids are L2-resident):
             # L1 throughput and lanes per warp instruction from the same capture
-            "l1_throughput_pct": fig.get("l1_throughput_pct"), "threads_per_inst": fig.get("threads_per_inst"),
+            "threads_per_inst": fig.get("threads_per_inst"),
+            "l1_throughput_pct_128px": fig.get("l1_throughput_pct_128px"),
+            "profile_note": ("traffic and threads_per_inst: 1-pass ncu metrics of this launch size; "
+                             "l1_throughput_pct_128px: the same medium at a 128^2 film (a multi-pass metric, "
+                             "captured on the small case only)"),
             "profile_source_digest": prof["source_digest"]}
     if not fig:
         roof["profile_note"] = ("no ncu summary in profiles/ was captured from the current CUDA sources"

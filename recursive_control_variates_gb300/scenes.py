@@ -81,8 +81,10 @@ CONFIGS = {
     "cfg1": VolumeConfig("cfg1", grid=32, res=128, spp=4, max_depth=16, steps=50),
     # 64^3 density + 64^3 RGB albedo, 512^2, spp 16, depth 64, 200 steps
     "cfg2": VolumeConfig("cfg2", grid=64, res=512, spp=16, max_depth=64, steps=200, albedo=None),
-    # profiling case: the cfg2 medium at 128^2 (one launch = 262 144 paths)
+    # profiling cases: the cfg2 medium at 128^2 and 256^2 (one launch = 262 144
+    # and 1 048 576 paths)
     "cfg2s": VolumeConfig("cfg2s", grid=64, res=128, spp=16, max_depth=64, steps=200, albedo=None),
+    "cfg2m": VolumeConfig("cfg2m", grid=64, res=256, spp=16, max_depth=64, steps=200, albedo=None),
     # a sparse medium for the majorant supergrid: one Gaussian blob in a 128^3
     # grid (mostly empty space), 512^2, spp 16, depth 64
     "sparse128": VolumeConfig("sparse128", grid=128, res=512, spp=16, max_depth=64, steps=200, blobs=1),
