@@ -106,6 +106,33 @@ typedef struct rcv_medium {
   int32_t pad;
 } rcv_medium;
 
+/* Environment map (the reference's `envmap` emitter of its grid scenes,
+ * experiments.py:81-85,195-199,315-319): a latitude-longitude RGB image of
+ * linear radiance, times `scale`.  Row 0 is the +y pole, column u covers
+ * azimuth 2 pi u: a world direction (x, y, z) has
+ *   u = atan2(x, -z) / (2 pi) (wrapped into [0, 1)),  v = acos(y) / pi,
+ * and the radiance is the bilinear interpolation of the texel centres
+ * ((j + 1/2) / width, (i + 1/2) / height), wrapping in u and clamping in v.
+ * Directions are importance-sampled from a piecewise-constant density over
+ * the texels, proportional to luminance x sin(theta) of the texel's row
+ * centre, whose solid-angle pdf is p(u, v) / (2 pi^2 sin(theta)).
+ * rcv_envmap_prepare fills the workspace (texels with their sampling
+ * weights, conditional and marginal CDFs) once after the texels change. */
+typedef struct rcv_envmap {
+  int32_t width, height;
+  float scale;
+  int32_t pad;
+  const float* texels; /* device, [height][width][3] RGB                      */
+  void* workspace;     /* device, rcv_envmap_workspace_bytes(), 256-B aligned  */
+} rcv_envmap;
+
+uint64_t rcv_envmap_workspace_bytes(int32_t width, int32_t height);
+/* Builds the sampling tables of an environment map in its workspace (one
+ * thread per row sums its texels in double, in order; one thread the rows).
+ * No counterpart call in the reference: Mitsuba builds its envmap's
+ * distribution when the plugin loads. */
+int rcv_envmap_prepare(const rcv_envmap* envmap, void* stream);
+
 typedef struct rcv_volpath_options {
   int32_t max_depth;     /* path length limit (real scattering events), -1 = none */
   int32_t rr_depth;      /* Russian roulette applies when depth > this            */
@@ -118,6 +145,11 @@ typedef struct rcv_volpath_options {
   int32_t count_events;  /* batched launches: accumulate the RCV_COUNTER_* totals
                             behind rcv_batch_counters (single-job calls count when
                             their `counters` argument is non-NULL)               */
+  /* Environment emitter of the two-state, single-state and adjoint volume
+   * tracers: a prepared environment map, or NULL for the constant white
+   * environment (radiance 1).  volpathsimple and the batched engine take the
+   * constant environment only. */
+  const rcv_envmap* envmap;
 } rcv_volpath_options;
 
 /* Pixel hand-out orders of the persistent tracers.  Results do not depend on

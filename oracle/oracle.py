@@ -54,6 +54,10 @@ class OracleScene(C.Structure):
         ("adx", C.c_int32),
         ("ady", C.c_int32),
         ("adz", C.c_int32),
+        ("env_w", C.c_int32),
+        ("env_h", C.c_int32),
+        ("env_scale", C.c_float),
+        ("env_texels", C.c_void_p),
     ]
 
 
@@ -190,6 +194,14 @@ def lib():
         L.oracle_vps_render.restype = C.c_int
         L.oracle_vps_backward.argtypes = [C.POINTER(OracleScene), vp, C.c_uint32, C.c_int, vp, vp, vp, C.c_int]
         L.oracle_vps_backward.restype = C.c_int
+        L.oracle_env_uv.argtypes = [vp, C.c_int, vp]
+        L.oracle_env_uv.restype = None
+        L.oracle_atan2.argtypes = [C.c_float, C.c_float]
+        L.oracle_atan2.restype = C.c_float
+        L.oracle_env_sample.argtypes = [C.POINTER(OracleScene), vp, C.c_int, vp, vp, vp]
+        L.oracle_env_sample.restype = C.c_int
+        L.oracle_env_eval.argtypes = [C.POINTER(OracleScene), vp, C.c_int, vp, vp]
+        L.oracle_env_eval.restype = C.c_int
         _lib = L
     return _lib
 
@@ -234,7 +246,7 @@ class Scene:
 
     def __init__(self, cam, dens_old, dens_new, albedo_old=None, albedo_new=None, albedo_const=0.8,
                  max_depth=16, rr_depth=None, hide_emitters=False, scale=1.0, majorant_factor=0,
-                 box_min=(0.0, 0.0, 0.0), box_size=(1.0, 1.0, 1.0)):
+                 box_min=(0.0, 0.0, 0.0), box_size=(1.0, 1.0, 1.0), envmap=None, envmap_scale=1.0):
         cams = list(cam) if isinstance(cam, (list, tuple)) else [cam]
         if not 1 <= len(cams) <= 16 or any((c.width, c.height) != (cams[0].width, cams[0].height) for c in cams):
             raise ValueError("a batch film takes 1..16 sub-sensors of one film size")
@@ -267,6 +279,12 @@ class Scene:
         s.n_cams = len(cams)
         for k, c in enumerate(cams[1:]):
             s.cams[k][:] = [*c.origin, *c.forward, *c.right, *c.up]
+        # environment map [H][W][3] (None: the constant white environment)
+        self.envmap = None if envmap is None else np.ascontiguousarray(envmap, np.float32)
+        if self.envmap is not None:
+            s.env_h, s.env_w = self.envmap.shape[:2]
+            s.env_scale = float(envmap_scale)
+            s.env_texels = self.envmap.ctypes.data
         self.c = s
         self.width, self.height = cam.width, cam.height
 
@@ -554,3 +572,36 @@ def vps_alt_seed(seed: int) -> int:
 
 def exp_nonpos(x: float) -> float:
     return float(lib().oracle_exp_nonpos(float(x)))
+
+
+# ------------------------------------------------------- environment map
+def env_uv(dirs) -> np.ndarray:
+    """(u, v, sin theta) of unit world directions [n][3]."""
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros((d.shape[0], 3), np.float32)
+    lib().oracle_env_uv(d.ctypes.data, d.shape[0], out.ctypes.data)
+    return out
+
+
+def atan2(y: float, x: float) -> float:
+    return float(lib().oracle_atan2(float(y), float(x)))
+
+
+def env_sample(scene: Scene, u) -> tuple:
+    """Directions [n][3], radiance [n][3] and pdf [n] sampled from uniforms [n][2]."""
+    u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+    n = u.shape[0]
+    d, le, pdf = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32), np.zeros(n, np.float32)
+    if lib().oracle_env_sample(C.byref(scene.c), u.ctypes.data, n, d.ctypes.data, le.ctypes.data, pdf.ctypes.data):
+        raise ValueError("oracle_env_sample: the scene has no environment map")
+    return d, le, pdf
+
+
+def env_eval(scene: Scene, dirs) -> tuple:
+    """Radiance [n][3] and sampling pdf [n] of the map along unit directions."""
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    n = d.shape[0]
+    le, pdf = np.zeros((n, 3), np.float32), np.zeros(n, np.float32)
+    if lib().oracle_env_eval(C.byref(scene.c), d.ctypes.data, n, le.ctypes.data, pdf.ctypes.data):
+        raise ValueError("oracle_env_eval: the scene has no environment map")
+    return le, pdf

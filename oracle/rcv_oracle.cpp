@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <thread>
 #include <vector>
 
@@ -189,6 +190,11 @@ struct oracle_scene {
   float cams[15][12];
   // albedo grid resolution when it differs from the density's (0 = same)
   int32_t adx, ady, adz;
+  // environment map (env_w = 0: the constant white environment): RGB texels
+  // [env_h][env_w][3], row 0 at the +y pole, radiance times env_scale
+  int32_t env_w, env_h;
+  float env_scale;
+  const float* env_texels;
 };
 }
 
@@ -485,6 +491,184 @@ struct GradSink {
 
 enum Mode { kTwoState = 0, kSingle = 1 };
 
+// ------------------------------------------------------ environment map
+// The `envmap` emitter of the reference's grid scenes (experiments.py:81-85):
+// latitude-longitude radiance, bilinear between texel centres (wrap in u,
+// clamp in v), importance-sampled from a piecewise-constant density
+// proportional to luminance x sin(theta) of the row centre (Pharr, Jakob &
+// Humphreys, PBR, infinite area lights).  Direction (x, y, z) <-> (u, v):
+// u = atan2(x, -z) / (2 pi) in [0, 1), v = acos(y) / pi.  atan2 by octant
+// reduction, a pi/4 shift above tan(pi/8) and the arctangent series through
+// x^19; sin / cos by sincos_2pi.
+constexpr float kEnvInvTwoPi = 0.159154943091895335769f;
+constexpr float kEnvInvPi = 0.318309886183790671538f;
+constexpr float kEnvInv2PiSq = 0.0506605918211688965f;
+constexpr float kEnvPi = 3.14159265358979323846f;
+constexpr float kEnvQuarterPi = 0.785398163397448309616f;
+
+float arctan01(float a) {
+  const bool big = a > 0.414213562373095f;
+  const float x = big ? (a - 1.0f) / (a + 1.0f) : a;
+  const float x2 = x * x;
+  // (-1)^k / (2k + 1), k = 9 .. 1, Horner in x^2
+  static const float c[9] = {-1.0f / 19.0f, 1.0f / 17.0f, -1.0f / 15.0f, 1.0f / 13.0f, -1.0f / 11.0f,
+                             1.0f / 9.0f,   -1.0f / 7.0f, 1.0f / 5.0f,   -1.0f / 3.0f};
+  float p = std::fmaf(x2, c[0], c[1]);
+  for (int k = 2; k < 9; ++k) p = std::fmaf(x2, p, c[k]);
+  const float r = std::fmaf(x * x2, p, x);
+  return big ? r + kEnvQuarterPi : r;
+}
+
+float arctan2(float y, float x) {
+  const float ax = std::fabs(x), ay = std::fabs(y);
+  const float mx = std::fmax(ax, ay), mn = std::fmin(ax, ay);
+  const float a = mx > 0.0f ? mn / mx : 0.0f;
+  float r = arctan01(a);
+  if (ay > ax) r = 2.0f * kEnvQuarterPi - r;
+  if (x < 0.0f) r = kEnvPi - r;
+  return y < 0.0f ? -r : r;
+}
+
+struct Env {
+  int w = 0, h = 0;
+  float scale = 1.0f, inv_w = 0.0f, inv_h = 0.0f, inv_norm = 0.0f;
+  bool sample = false;
+  std::vector<float> rgb, f, cond, marg;  // texels, weights, CDFs
+
+  explicit Env(const oracle_scene& S) {
+    if (S.env_w <= 0 || S.env_h <= 0 || S.env_texels == nullptr) return;
+    w = S.env_w;
+    h = S.env_h;
+    scale = S.env_scale;
+    inv_w = 1.0f / (float)w;
+    inv_h = 1.0f / (float)h;
+    rgb.assign(S.env_texels, S.env_texels + (size_t)w * h * 3);
+    f.resize((size_t)w * h);
+    cond.resize((size_t)(w + 1) * h);
+    marg.resize((size_t)h + 1);
+    std::vector<double> rows(h);
+    for (int i = 0; i < h; ++i) {
+      float s_, c_;
+      sincos_2pi((((float)i + 0.5f) * inv_h) * 0.5f, s_, c_);
+      double sum = 0.0;
+      for (int j = 0; j < w; ++j) {
+        const float* t = &rgb[((size_t)i * w + j) * 3];
+        const float lum = (0.2126f * t[0] + 0.7152f * t[1]) + 0.0722f * t[2];
+        f[(size_t)i * w + j] = lum * s_;
+        sum += (double)f[(size_t)i * w + j];
+      }
+      rows[i] = sum;
+      double acc = 0.0;
+      for (int j = 0; j < w; ++j) {
+        cond[(size_t)i * (w + 1) + j] = sum > 0.0 ? (float)(acc / sum) : (float)((double)j / (double)w);
+        acc += (double)f[(size_t)i * w + j];
+      }
+      cond[(size_t)i * (w + 1) + w] = 1.0f;
+    }
+    double total = 0.0;
+    for (int i = 0; i < h; ++i) total += rows[i];
+    double acc = 0.0;
+    for (int i = 0; i < h; ++i) {
+      marg[i] = total > 0.0 ? (float)(acc / total) : (float)((double)i / (double)h);
+      acc += rows[i];
+    }
+    marg[h] = 1.0f;
+    inv_norm = total > 0.0 ? (float)((double)w * (double)h / total) : 0.0f;
+    sample = total > 0.0;
+  }
+
+  bool valid() const { return w > 0; }
+
+  static void uv(const V3& d, float& u, float& v, float& sin_t) {
+    u = arctan2(d.x, -d.z) * kEnvInvTwoPi;
+    if (u < 0.0f) u = u + 1.0f;
+    if (!(u < 1.0f)) u = 0.0f;
+    sin_t = std::sqrt(std::fmax(0.0f, std::fmaf(-d.y, d.y, 1.0f)));
+    v = arctan2(sin_t, d.y) * kEnvInvPi;
+  }
+
+  V3 eval(float u, float v) const {
+    const float fx = std::fmaf(u, (float)w, -0.5f), fy = std::fmaf(v, (float)h, -0.5f);
+    const float x0f = std::floor(fx), y0f = std::floor(fy);
+    const float tx = fx - x0f, ty = fy - y0f;
+    const int x0 = (int)std::fmax(std::fmin(x0f, (float)w), -1.0f);
+    const int y0 = (int)std::fmax(std::fmin(y0f, (float)h), -1.0f);
+    auto wrap = [&](int x) { const int r = x % w; return r < 0 ? r + w : r; };
+    auto clampy = [&](int y) { return y < 0 ? 0 : (y > h - 1 ? h - 1 : y); };
+    const int c0 = wrap(x0), c1 = wrap(x0 + 1), r0 = clampy(y0), r1 = clampy(y0 + 1);
+    float out[3];
+    for (int k = 0; k < 3; ++k) {
+      const float a = rgb[((size_t)r0 * w + c0) * 3 + k], b = rgb[((size_t)r0 * w + c1) * 3 + k];
+      const float c = rgb[((size_t)r1 * w + c0) * 3 + k], d = rgb[((size_t)r1 * w + c1) * 3 + k];
+      out[k] = lerp(lerp(a, b, tx), lerp(c, d, tx), ty) * scale;
+    }
+    return V3{out[0], out[1], out[2]};
+  }
+
+  float pdf(float u, float v, float sin_t) const {
+    if (!sample || !(sin_t > 0.0f)) return 0.0f;
+    int i = (int)(v * (float)h), j = (int)(u * (float)w);
+    i = std::min(std::max(i, 0), h - 1);
+    j = std::min(std::max(j, 0), w - 1);
+    return ((f[(size_t)i * w + j] * inv_norm) * kEnvInv2PiSq) / sin_t;
+  }
+
+  static int find(const float* cdf, int n, float x) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (cdf[mid] <= x)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    return lo;
+  }
+
+  // sampled unit world direction, its radiance and pdf
+  V3 sample_dir(float u0, float u1, V3& Le, float& p) const {
+    Le = V3{0.0f, 0.0f, 0.0f};
+    p = 0.0f;
+    if (!sample) return V3{0.0f, 1.0f, 0.0f};
+    const int i = find(marg.data(), h, u1);
+    const float dv = (u1 - marg[i]) / (marg[i + 1] - marg[i]);
+    const float* row = &cond[(size_t)i * (w + 1)];
+    const int j = find(row, w, u0);
+    const float du = (u0 - row[j]) / (row[j + 1] - row[j]);
+    const float u = ((float)j + du) * inv_w, v = ((float)i + dv) * inv_h;
+    float st, ct, sp, cp;
+    sincos_2pi(v * 0.5f, st, ct);
+    sincos_2pi(u, sp, cp);
+    const V3 d{st * sp, ct, -(st * cp)};
+    if (st > 0.0f) {
+      p = ((f[(size_t)i * w + j] * inv_norm) * kEnvInv2PiSq) / st;
+      Le = eval(u, v);
+    }
+    return d;
+  }
+
+  // radiance along a box-space direction and the pdf of sampling it
+  V3 along(const oracle_scene& S, const V3& d, float& p) const {
+    const float bx = S.box_size[0] > 0.0f ? S.box_size[0] : 1.0f;
+    const float by = S.box_size[1] > 0.0f ? S.box_size[1] : 1.0f;
+    const float bz = S.box_size[2] > 0.0f ? S.box_size[2] : 1.0f;
+    V3 wd{d.x * bx, d.y * by, d.z * bz};
+    const float inv_len = 1.0f / std::sqrt(std::fmaf(wd.z, wd.z, std::fmaf(wd.y, wd.y, wd.x * wd.x)));
+    wd = V3{wd.x * inv_len, wd.y * inv_len, wd.z * inv_len};
+    float u, v, st;
+    uv(wd, u, v, st);
+    p = pdf(u, v, st);
+    return eval(u, v);
+  }
+};
+
+// Power heuristic (mitsuba.ad.common.mis_weight).
+float mis2(float a, float b) {
+  const float a2 = a * a, b2 = b * b;
+  const float s = a2 + b2;
+  return s > 0.0f ? a2 / s : 0.0f;
+}
+
 struct PathOut {
   V3 L_old{0, 0, 0}, L_new{0, 0, 0};
   uint64_t lookups = 0, nee_lookups = 0, scatters = 0;
@@ -498,6 +682,7 @@ struct Tracer {
   V3 dL{0, 0, 0};   // adjoint: dLoss/dL for this path
   V3 Ltot{0, 0, 0}; // adjoint: the path's total radiance (radiance pass)
   const Supergrid* sg = nullptr;  // majorant supergrid, if the medium has one
+  const Env* env = nullptr;       // environment map, if the scene has one
 
   // Radiance the path still gathers after the contributions in `got`:
   // L_rem = L - got, one rounding per channel.
@@ -592,8 +777,15 @@ struct Tracer {
     cube_hit(o, d, tn, tf);
     if (!(tn <= tf && tf > 0.0f)) {
       if (!S.hide_emitters) {
-        Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
-        if (mode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
+        if (env && env->valid()) {
+          float pe;
+          const V3 Le = env->along(S, d, pe);
+          Ln = V3{Ln.x + bn.x * Le.x, Ln.y + bn.y * Le.y, Ln.z + bn.z * Le.z};
+          if (mode == kTwoState) Lo = V3{Lo.x + bo.x * Le.x, Lo.y + bo.y * Le.y, Lo.z + bo.z * Le.z};
+        } else {
+          Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
+          if (mode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
+        }
       }
       return out;
     }
@@ -620,10 +812,21 @@ struct Tracer {
         rng.next1d();
         if (!roulette(rng, depth, bn, bo)) return out;
         if (!(S.hide_emitters && depth == 0)) {
-          const float k = depth == 0 ? 1.0f : mis;
-          const V3 cn{bn.x * k, bn.y * k, bn.z * k};
-          Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
-          if (mode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
+          if (env && env->valid()) {
+            // map hit after a phase sample: power heuristic against NEE
+            // (plugins/twostatevolpath.py:288-308)
+            float pe;
+            const V3 Le = env->along(S, d, pe);
+            const float k = depth == 0 ? 1.0f : mis2(kInvFourPi, pe);
+            Ln = V3{Ln.x + (bn.x * Le.x) * k, Ln.y + (bn.y * Le.y) * k, Ln.z + (bn.z * Le.z) * k};
+            if (mode == kTwoState)
+              Lo = V3{Lo.x + (bo.x * Le.x) * k, Lo.y + (bo.y * Le.y) * k, Lo.z + (bo.z * Le.z) * k};
+          } else {
+            const float k = depth == 0 ? 1.0f : mis;
+            const V3 cn{bn.x * k, bn.y * k, bn.z * k};
+            Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
+            if (mode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
+          }
         }
         return out;
       }
@@ -682,20 +885,42 @@ struct Tracer {
       rng.next1d();
       const float pu0 = rng.next1d(), pu1 = rng.next1d();
       const V3 wo = to_box(S, square_to_uniform_sphere(pu0, pu1));
-      // next event estimation towards the constant environment
+      // next event estimation towards the environment (constant, or the map
+      // by importance with a power-heuristic weight against the phase pdf,
+      // plugins/twostatevolpath.py:315-344)
       const float nu0 = rng.next1d(), nu1 = rng.next1d();
-      const V3 w = to_box(S, square_to_uniform_sphere(nu0, nu1));
+      V3 w, e{0.0f, 0.0f, 0.0f};
+      const bool use_env = env && env->valid();
+      if (use_env) {
+        V3 Le;
+        float pe;
+        w = to_box(S, env->sample_dir(nu0, nu1, Le, pe));
+        float k = 0.0f;
+        if (pe > 0.0f && pe < std::numeric_limits<float>::infinity()) k = (kInvFourPi * mis2(pe, kInvFourPi)) / pe;
+        e = V3{Le.x * k, Le.y * k, Le.z * k};
+      } else {
+        w = to_box(S, square_to_uniform_sphere(nu0, nu1));
+      }
       const Rng rng_before = rng;
       float tro, trn;
       transmittance(rng, x, w, tro, trn, out, nullptr);
-      const float en = emit_weight * trn;
-      const V3 cn{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
-                  ((bn.z * kInvFourPi) * mis) * en};
+      V3 cn;
+      if (use_env) {
+        cn = V3{(bn.x * e.x) * trn, (bn.y * e.y) * trn, (bn.z * e.z) * trn};
+      } else {
+        const float en = emit_weight * trn;
+        cn = V3{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
+                ((bn.z * kInvFourPi) * mis) * en};
+      }
       Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
       if (mode == kTwoState) {
-        const float eo = emit_weight * tro;
-        Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
-                Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
+        if (use_env) {
+          Lo = V3{Lo.x + (bo.x * e.x) * tro, Lo.y + (bo.y * e.y) * tro, Lo.z + (bo.z * e.z) * tro};
+        } else {
+          const float eo = emit_weight * tro;
+          Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
+                  Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
+        }
       }
       if (sink) {
         // replay the shadow walk with the same numbers to differentiate it
@@ -750,6 +975,48 @@ void parallel_rows(int row0, int row1, int stride, int threads, F&& f) {
 }  // namespace
 
 extern "C" {
+// Environment-map primitives for the tests: (u, v, sin theta) of unit
+// directions, the map's radiance and pdf there, and sampled directions with
+// their radiance and pdf.
+void oracle_env_uv(const float* d, int n, float* uvs) {
+  for (int i = 0; i < n; ++i) Env::uv(V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]}, uvs[3 * i], uvs[3 * i + 1], uvs[3 * i + 2]);
+}
+
+float oracle_atan2(float y, float x) { return arctan2(y, x); }
+
+int oracle_env_sample(const oracle_scene* S, const float* u, int n, float* dirs, float* le, float* pdf) {
+  if (!S || S->env_w <= 0) return -1;
+  const Env env(*S);
+  for (int i = 0; i < n; ++i) {
+    V3 L;
+    const V3 d = env.sample_dir(u[2 * i], u[2 * i + 1], L, pdf[i]);
+    dirs[3 * i] = d.x;
+    dirs[3 * i + 1] = d.y;
+    dirs[3 * i + 2] = d.z;
+    le[3 * i] = L.x;
+    le[3 * i + 1] = L.y;
+    le[3 * i + 2] = L.z;
+  }
+  return 0;
+}
+
+int oracle_env_eval(const oracle_scene* S, const float* d, int n, float* le, float* pdf) {
+  if (!S || S->env_w <= 0) return -1;
+  const Env env(*S);
+  for (int i = 0; i < n; ++i) {
+    float u, v, st;
+    Env::uv(V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]}, u, v, st);
+    const V3 L = env.eval(u, v);
+    le[3 * i] = L.x;
+    le[3 * i + 1] = L.y;
+    le[3 * i + 2] = L.z;
+    pdf[i] = env.pdf(u, v, st);
+  }
+  return 0;
+}
+}
+
+extern "C" {
 
 // Primal render.  mode 0 = two-state (out_old = H, out_new = F), 1 = single
 // state on `new` (out_new).  `chunk` = samples per GPU thread, which fixes the
@@ -767,11 +1034,13 @@ int oracle_render(const oracle_scene* S, int mode, uint32_t seed, int spp, int c
   const float mu = mode == kTwoState ? std::fmax(mu_o, mu_n) : mu_n;
   Supergrid sg;
   sg.build(*S);
+  const Env env(*S);
   const int T = spp / chunk;
   std::vector<uint64_t> cnt((size_t)std::max(threads, 1) * 4, 0);
   parallel_rows(row0, row1, row_stride, threads, [&](int k, int y0, int y1) {
     Tracer tr{*S, mode, mu, nullptr};
     tr.sg = &sg;
+    tr.env = &env;
     for (int py = y0; py < y1; ++py)
       for (int px = 0; px < S->width; ++px) {
         const int pix = py * S->width + px;
@@ -822,6 +1091,7 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
   const float mu = S->scale * grid_max(*S, S->dens_new);
   Supergrid sg;
   sg.build(*S);
+  const Env env(*S);
   const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
   int adx, ady, adz;
   albedo_dims(*S, adx, ady, adz);
@@ -843,9 +1113,11 @@ int oracle_backward(const oracle_scene* S, uint32_t seed, int spp, const float* 
           const uint32_t lane = (uint32_t)((int64_t)pix * spp + s);
           Tracer primal{*S, kSingle, mu, nullptr};
           primal.sg = &sg;
+          primal.env = &env;
           const PathOut o = primal.trace(seed, lane, px, py);
           Tracer adj{*S, kSingle, mu, &sinks[k], dL, o.L_new};
           adj.sg = &sg;
+          adj.env = &env;
           adj.trace(seed, lane, px, py);
         }
       }
@@ -868,6 +1140,7 @@ int oracle_forward(const oracle_scene* S, uint32_t seed, int spp, const float* t
   const float mu = S->scale * grid_max(*S, S->dens_new);
   Supergrid sg;
   sg.build(*S);
+  const Env env(*S);
   const float* ta = S->alb_new != nullptr ? tan_a : nullptr;
   parallel_rows(0, S->height, 1, threads, [&](int, int y0, int y1) {
     for (int py = y0; py < y1; ++py)
@@ -878,6 +1151,7 @@ int oracle_forward(const oracle_scene* S, uint32_t seed, int spp, const float* t
           const uint32_t lane = (uint32_t)((int64_t)pix * spp + s);
           Tracer primal{*S, kSingle, mu, nullptr};
           primal.sg = &sg;
+          primal.env = &env;
           const PathOut o = primal.trace(seed, lane, px, py);
           for (int k = 0; k < 3; ++k) {
             GradSink g;
@@ -886,6 +1160,7 @@ int oracle_forward(const oracle_scene* S, uint32_t seed, int spp, const float* t
             const V3 e{k == 0 ? 1.0f : 0.0f, k == 1 ? 1.0f : 0.0f, k == 2 ? 1.0f : 0.0f};
             Tracer adj{*S, kSingle, mu, &g, e, o.L_new};
             adj.sg = &sg;
+            adj.env = &env;
             adj.trace(seed, lane, px, py);
             d[k] += g.acc;
           }
@@ -1321,6 +1596,7 @@ int oracle_vps_render(const oracle_scene* S, const int32_t flags[4], uint32_t se
                       int row0, int row1, int row_stride) {
   if (S && row1 <= 0) row1 = S->height;
   if (!S || !flags || !out || spp <= 0 || row0 < 0 || row1 > S->height || row0 > row1) return -1;
+  if (S->env_w > 0) return -1;  // volpathsimple: constant environment only
   Supergrid sg;
   sg.build(*S);
   const Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, S->scale * grid_max(*S, S->dens_new), &sg};
@@ -1347,6 +1623,7 @@ int oracle_vps_render(const oracle_scene* S, const int32_t flags[4], uint32_t se
 int oracle_vps_backward(const oracle_scene* S, const int32_t flags[4], uint32_t seed, int spp, const float* grad_img,
                         double* grad_density, double* grad_albedo, int threads) {
   if (!S || !flags || spp <= 0 || !grad_img || !grad_density) return -1;
+  if (S->env_w > 0) return -1;  // volpathsimple: constant environment only
   Supergrid sg;
   sg.build(*S);
   const float mu = S->scale * grid_max(*S, S->dens_new);

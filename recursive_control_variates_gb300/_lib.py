@@ -80,6 +80,18 @@ class VolpathOptions(C.Structure):
         ("defer", C.c_int32),
         ("order", C.c_int32),
         ("count_events", C.c_int32),
+        ("envmap", C.c_void_p),  # const rcv_envmap* or NULL (constant environment)
+    ]
+
+
+class Envmap(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("scale", C.c_float),
+        ("pad", C.c_int32),
+        ("texels", C.c_void_p),
+        ("workspace", C.c_void_p),
     ]
 
 
@@ -203,6 +215,8 @@ SIGNATURES = {
     "rcv_medium_workspace_bytes": (C.c_uint64, [P(C.c_int32), C.c_int32, C.c_int32]),
     "rcv_medium_workspace_bytes_for": (C.c_uint64, [P(Medium)]),
     "rcv_medium_prepare": (C.c_int, [P(Medium), vp]),
+    "rcv_envmap_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32]),
+    "rcv_envmap_prepare": (C.c_int, [P(Envmap), vp]),
     "rcv_render_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "rcv_render_twostates_volume": (
         C.c_int,
@@ -301,6 +315,7 @@ STRUCTS = {
     "rcv_batch_job": BatchJob,
     "rcv_batch_job_status": BatchJobStatus,
     "rcv_volpathsimple_flags": VpsFlags,
+    "rcv_envmap": Envmap,
 }
 
 

@@ -205,6 +205,8 @@ class CVJob:
         medium = inner.medium_of(scene)
         if not isinstance(medium, TwoStateMedium):
             raise RuntimeError("No TwoStateMedium found in the scene!")
+        if hasattr(scene, "envmap") and scene.envmap() is not None:
+            raise ValueError("the batched engine renders under the constant environment only (the scene has an envmap)")
         keys = {}
         for key in opt.keys():
             owner, sub = params.owner_of(key)

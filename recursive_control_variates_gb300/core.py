@@ -288,6 +288,69 @@ class ConstantEmitter:
             raise ValueError("the constant emitter supports radiance 1.0 only")
 
 
+class EnvmapEmitter:
+    """``envmap`` (the reference's grid scenes light the medium with one,
+    experiments.py:81-85,195-199,315-319): a latitude-longitude RGB image of
+    linear radiance from ``filename`` (OpenEXR) or ``data`` ((H, W, 3)), times
+    ``scale``.  Row 0 is the +y pole; a direction (x, y, z) reads the image at
+    u = atan2(x, -z) / (2 pi), v = acos(y) / pi, bilinearly.  NEE samples
+    it by importance (luminance x sin(theta)).  Only the identity
+    ``to_world`` is supported."""
+
+    def __init__(self, props: Properties):
+        from . import io
+
+        if props.get("to_world") is not None:
+            raise ValueError("envmap: only the identity to_world is supported")
+        data = props.get("data")
+        if data is None:
+            fn = props.get("filename")
+            if fn is None:
+                raise ValueError("envmap: 'filename' or 'data' is required")
+            data = io.read_exr(fn)
+        arr = data if isinstance(data, torch.Tensor) else torch.as_tensor(np.asarray(data, np.float32))
+        if arr.dim() == 2:
+            arr = arr[..., None].expand(-1, -1, 3)
+        if arr.dim() != 3 or arr.shape[2] not in (1, 3, 4):
+            raise ValueError(f"envmap: expected an (H, W, 3) image, got shape {tuple(arr.shape)}")
+        if arr.shape[2] == 1:
+            arr = arr.expand(-1, -1, 3)
+        arr = arr[..., :3]
+        self.scale = float(props.get("scale", 1.0))
+        if not np.isfinite(self.scale) or self.scale < 0.0:
+            raise ValueError("envmap: scale must be finite and >= 0")
+        self.device = _device(props)
+        self.texels = arr.detach().to(device=self.device, dtype=torch.float32).contiguous().clone()
+        if not bool(torch.isfinite(self.texels).all()) or float(self.texels.min()) < 0.0:
+            raise ValueError("envmap: radiance must be finite and non-negative")
+        self.height, self.width = int(self.texels.shape[0]), int(self.texels.shape[1])
+        self._struct = None
+        self._ws = None
+        if self.device.type == "cuda":
+            self.prepare()
+
+    def prepare(self, stream=None):
+        """(Re)builds the sampling tables on the device after the texels change."""
+        from .utils import stream_handle
+
+        lib = _lib.load()
+        need = int(lib.rcv_envmap_workspace_bytes(self.width, self.height)) + 256
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        s = _lib.Envmap()
+        s.width, s.height, s.scale = self.width, self.height, self.scale
+        s.texels = self.texels.data_ptr()
+        s.workspace = (self._ws.data_ptr() + 255) & ~255
+        _lib.check(lib.rcv_envmap_prepare(C.byref(s), stream if stream is not None else stream_handle(self.device)),
+                   "rcv_envmap_prepare")
+        self._struct = s
+
+    def c_struct(self) -> "_lib.Envmap":
+        if self._struct is None:
+            raise RuntimeError("envmap: tables not prepared (a CUDA device is required)")
+        return self._struct
+
+
 # ------------------------------------------------------------------- media
 class Isotropic:
     def __init__(self, props: Properties):
@@ -651,7 +714,7 @@ class Scene:
                 continue
             if isinstance(v, (PerspectiveSensor, BatchSensor)):
                 self.sensors_.append(v)
-            elif isinstance(v, ConstantEmitter):
+            elif isinstance(v, (ConstantEmitter, EnvmapEmitter)):
                 self.emitters_.append(v)
             elif isinstance(v, CubeShape) or hasattr(v, "is_surface_shape"):
                 self.shapes_[k] = v
@@ -663,6 +726,15 @@ class Scene:
 
     def emitters(self):
         return self.emitters_
+
+    def envmap(self):
+        """The scene's environment map, or None (constant environment)."""
+        env = [e for e in self.emitters_ if isinstance(e, EnvmapEmitter)]
+        if len(env) > 1:
+            raise ValueError("a scene takes at most one envmap")
+        if env and any(isinstance(e, ConstantEmitter) for e in self.emitters_):
+            raise ValueError("a scene takes either a constant emitter or an envmap")
+        return env[0] if env else None
 
     def shapes(self):
         return list(self.shapes_.values())
@@ -771,6 +843,7 @@ for _name, _ctor, _kind in [
     ("box", BoxFilter, "rfilter"),
     ("independent", IndependentSampler, "sampler"),
     ("constant", ConstantEmitter, "emitter"),
+    ("envmap", EnvmapEmitter, "emitter"),
     ("gridvolume", GridVolume, "volume"),
     ("isotropic", Isotropic, "phase"),
     ("heterogeneous", HeterogeneousMedium, "medium"),

@@ -432,6 +432,7 @@ static rcv_volpath_options job_options(const rcv_batch_job& j, const rcv_volpath
   r.max_depth = j.max_depth;
   r.rr_depth = j.rr_depth;
   r.hide_emitters = j.hide_emitters;
+  r.envmap = nullptr;  // batched jobs see the constant environment
   return r;
 }
 
@@ -507,6 +508,8 @@ extern "C" uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t
 
 extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_volpath_options* opts,
                                 void* workspace, uint64_t workspace_bytes, rcv_batch** out, void* stream) {
+  RCV_REQUIRE(opts == nullptr || opts->envmap == nullptr,
+              "the batched engine renders under the constant environment only (no environment map)");
   RCV_REQUIRE(out != nullptr, "out is NULL");
   *out = nullptr;
   RCV_REQUIRE(jobs != nullptr && n >= 1 && n <= kMaxBatchJobs, "need 1..%d jobs", kMaxBatchJobs);

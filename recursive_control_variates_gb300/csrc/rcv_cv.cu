@@ -179,7 +179,7 @@ extern "C" uint64_t rcv_struct_size(const char* name) {
       {"rcv_sphere", sizeof(rcv_sphere)},             {"rcv_surface_scene", sizeof(rcv_surface_scene)},
       {"rcv_cv_state", sizeof(rcv_cv_state)},         {"rcv_batch_job", sizeof(rcv_batch_job)},
       {"rcv_batch_job_status", sizeof(rcv_batch_job_status)},
-      {"rcv_volpathsimple_flags", sizeof(rcv_volpathsimple_flags)},
+      {"rcv_volpathsimple_flags", sizeof(rcv_volpathsimple_flags)}, {"rcv_envmap", sizeof(rcv_envmap)},
   };
   for (const Entry& e : table)
     if (std::strcmp(e.name, name) == 0) return e.size;

@@ -244,10 +244,25 @@ __device__ __forceinline__ V3 pixel_dL(const VolJob& J, int pix) {
   return V3{g[0] / fs, g[1] / fs, g[2] / fs};
 }
 
+// Environment map seen along the box direction d (made a unit world
+// direction first): radiance, and the pdf of sampling that direction for NEE.
+__device__ __forceinline__ V3 env_radiance_dir(const VolJob& J, const V3& d, float& pdf) {
+  V3 wd{d.x * J.box.x, d.y * J.box.y, d.z * J.box.z};
+  const float inv_len = 1.0f / sqrtf(fmaf(wd.z, wd.z, fmaf(wd.y, wd.y, wd.x * wd.x)));
+  wd = V3{wd.x * inv_len, wd.y * inv_len, wd.z * inv_len};
+  float u, v, st;
+  env_uv(wd, u, v, st);
+  pdf = env_pdf(J.env, u, v, st);
+  return env_eval_uv(J.env, u, v);
+}
+
 // kSG: the launch may contain media with a majorant supergrid.  kCount: the
 // launch accumulates the RCV_COUNTER_* event counts (off, the counters cost
 // no registers).
-template <int kMode, bool kSG, bool kCount>
+// kEnv: the launch's job has an environment map (else the constant white
+// environment; the two are separate kernels so that the constant one carries
+// none of the map's code).
+template <int kMode, bool kSG, bool kCount, bool kEnv>
 __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& cnt) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -259,6 +274,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   constexpr bool kRep = kMode == kReplay || kMode == kForward;
   constexpr bool kCoop = kMode == kTwoState || kMode == kSingle || kMode == kAdjoint;
   __shared__ float s_coop[kCoop ? kTraceWarps * 96 : 1];  // cooperative walk: distances, weights
+  // environment map: each lane's NEE weight e = Le / pdf * phase * MIS of its
+  // pending shadow ray, kept here from the scattering event to the end of the
+  // walk instead of in registers
+  __shared__ float s_env[kEnv ? kTraceWarps * 32 * 3 : 1];
+  float* env_e = s_env + (kEnv ? threadIdx.x * 3 : 0);
   // replay: camera tasks [0, paths), then the checkpoints that were written
   const int64_t total =
       kRep ? Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap) : Q.total;
@@ -416,8 +436,15 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           if (!(tn <= tf && tf > 0.0f)) {
             // camera ray misses the cube: environment seen directly
             if (!J.hide_emitters) {
-              Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
-              if (kMode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
+              if (kEnv) {
+                float pdf;
+                const V3 Le = env_radiance_dir(J, d, pdf);
+                Ln = V3{Ln.x + bn.x * Le.x, Ln.y + bn.y * Le.y, Ln.z + bn.z * Le.z};
+                if (kMode == kTwoState) Lo = V3{Lo.x + bo.x * Le.x, Lo.y + bo.y * Le.y, Lo.z + bo.z * Le.z};
+              } else {
+                Ln = V3{Ln.x + bn.x, Ln.y + bn.y, Ln.z + bn.z};
+                if (kMode == kTwoState) Lo = V3{Lo.x + bo.x, Lo.y + bo.y, Lo.z + bo.z};
+              }
             }
             finished = true;
           } else {
@@ -506,7 +533,21 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         }
         // NEE towards the environment, then ratio tracking
         const float nu0 = next1d(rng), nu1 = next1d(rng);
-        w = to_box(J, uniform_sphere(nu0, nu1));
+        if (kEnv) {
+          // NEE towards the environment map (plugins/twostatevolpath.py:315-344):
+          // importance-sampled direction, power-heuristic weight against the
+          // phase function's pdf
+          V3 Le;
+          float pdf;
+          w = to_box(J, env_sample(J.env, nu0, nu1, Le, pdf));
+          float k = 0.0f;
+          if (pdf > 0.0f && pdf < kInf) k = (kInvFourPi * env_mis(pdf, kInvFourPi)) / pdf;
+          env_e[0] = Le.x * k;
+          env_e[1] = Le.y * k;
+          env_e[2] = Le.z * k;
+        } else {
+          w = to_box(J, uniform_sphere(nu0, nu1));
+        }
         q = p;
         {
           float a;
@@ -688,9 +729,20 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             // leaves the cube: null BSDF sample, outside iteration RR, environment
             pcg_skip3(rng);
             if (roulette<kMode>(J, rng, depth, bn, bo) && !(J.hide_emitters && depth == 0)) {
-              const float k = depth == 0 ? 1.0f : mis;
-              Ln = V3{Ln.x + bn.x * k, Ln.y + bn.y * k, Ln.z + bn.z * k};
-              if (kMode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
+              if (kEnv) {
+                // environment map hit after a phase sample: power heuristic
+                // against NEE (plugins/twostatevolpath.py:288-308)
+                float pdf;
+                const V3 Le = env_radiance_dir(J, d, pdf);
+                const float k = depth == 0 ? 1.0f : env_mis(kInvFourPi, pdf);
+                Ln = V3{Ln.x + (bn.x * Le.x) * k, Ln.y + (bn.y * Le.y) * k, Ln.z + (bn.z * Le.z) * k};
+                if (kMode == kTwoState)
+                  Lo = V3{Lo.x + (bo.x * Le.x) * k, Lo.y + (bo.y * Le.y) * k, Lo.z + (bo.z * Le.z) * k};
+              } else {
+                const float k = depth == 0 ? 1.0f : mis;
+                Ln = V3{Ln.x + bn.x * k, Ln.y + bn.y * k, Ln.z + bn.z * k};
+                if (kMode == kTwoState) Lo = V3{Lo.x + bo.x * k, Lo.y + bo.y * k, Lo.z + bo.z * k};
+              }
             }
             finished = true;
           }
@@ -705,9 +757,14 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             done = (kMode == kTwoState) ? (trn == 0.0f && tro == 0.0f) : (trn == 0.0f);
           }
           if (done) {
-            const float en = emit_weight * trn;
-            const V3 cn{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
-                        ((bn.z * kInvFourPi) * mis) * en};
+            V3 cn;
+            if (kEnv) {
+              cn = V3{(bn.x * env_e[0]) * trn, (bn.y * env_e[1]) * trn, (bn.z * env_e[2]) * trn};
+            } else {
+              const float en = emit_weight * trn;
+              cn = V3{((bn.x * kInvFourPi) * mis) * en, ((bn.y * kInvFourPi) * mis) * en,
+                      ((bn.z * kInvFourPi) * mis) * en};
+            }
             if (kMode == kAdjoint && !ck_lost) {
               const unsigned long long slot = atomicAdd(Q.ckpt_count, 1ull);
               if ((int64_t)slot < Q.ckpt_cap)
@@ -718,9 +775,14 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
             if (kRep) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
             if (kMode == kTwoState) {
-              const float eo = emit_weight * tro;
-              Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
-                      Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
+              if (kEnv) {
+                Lo = V3{Lo.x + (bo.x * env_e[0]) * tro, Lo.y + (bo.y * env_e[1]) * tro,
+                        Lo.z + (bo.z * env_e[2]) * tro};
+              } else {
+                const float eo = emit_weight * tro;
+                Lo = V3{Lo.x + ((bo.x * kInvFourPi) * mis) * eo, Lo.y + ((bo.y * kInvFourPi) * mis) * eo,
+                        Lo.z + ((bo.z * kInvFourPi) * mis) * eo};
+              }
             }
             if (kRep) {
               // whole-path replay: walk the shadow ray again (saved stream) to

@@ -55,29 +55,34 @@ __device__ __forceinline__ void add_counts(unsigned long long* counters, const C
   }
 }
 
-template <int kMode, bool kSG, bool kCount>
+template <int kMode, bool kSG, bool kCount, bool kEnv>
 __global__ void __launch_bounds__(kTraceBlock, 5) trace_kernel(const __grid_constant__ VolJob J,
                                                             const __grid_constant__ Queue Q) {
   Counts cnt{0, 0, 0, 0, 0, 0};
-  trace_persistent<kMode, kSG, kCount>(J, Q, cnt);
+  trace_persistent<kMode, kSG, kCount, kEnv>(J, Q, cnt);
   if (kCount) add_counts(Q.counters, cnt);
 }
 
-// Tracer variants by index mode + kTraceModes * (supergrid + 2 * counting).
+// Tracer variants by index mode + kTraceModes * (supergrid + 2 * counting +
+// 4 * environment map).
 using TraceKernel = void (*)(VolJob, Queue);
-template <bool kSG, bool kCount>
+template <bool kSG, bool kCount, bool kEnv>
 struct TraceVariants {
   static constexpr TraceKernel k[kTraceModes] = {
-      trace_kernel<kTwoState, kSG, kCount>, trace_kernel<kSingle, kSG, kCount>,
-      trace_kernel<kAdjoint, kSG, kCount>, trace_kernel<kReplay, kSG, kCount>,
-      trace_kernel<kForward, kSG, kCount>};
+      trace_kernel<kTwoState, kSG, kCount, kEnv>, trace_kernel<kSingle, kSG, kCount, kEnv>,
+      trace_kernel<kAdjoint, kSG, kCount, kEnv>, trace_kernel<kReplay, kSG, kCount, kEnv>,
+      trace_kernel<kForward, kSG, kCount, kEnv>};
 };
-static const TraceKernel* const kTraceTables[4] = {
-    TraceVariants<false, false>::k, TraceVariants<true, false>::k, TraceVariants<false, true>::k,
-    TraceVariants<true, true>::k};
-constexpr int kTraceVariants = 4 * kTraceModes;
+static const TraceKernel* const kTraceTables[8] = {
+    TraceVariants<false, false, false>::k, TraceVariants<true, false, false>::k,
+    TraceVariants<false, true, false>::k,  TraceVariants<true, true, false>::k,
+    TraceVariants<false, false, true>::k,  TraceVariants<true, false, true>::k,
+    TraceVariants<false, true, true>::k,   TraceVariants<true, true, true>::k};
+constexpr int kTraceVariants = 8 * kTraceModes;
 
-static int trace_variant(int mode, bool sg, bool count) { return mode + kTraceModes * ((sg ? 1 : 0) + (count ? 2 : 0)); }
+static int trace_variant(int mode, bool sg, bool count, bool env) {
+  return mode + kTraceModes * ((sg ? 1 : 0) + (count ? 2 : 0) + (env ? 4 : 0));
+}
 static TraceKernel trace_kernel_of(int variant) { return kTraceTables[variant / kTraceModes][variant % kTraceModes]; }
 
 // Majorant supergrid of a medium (both states' cells and the new state's).
@@ -250,6 +255,27 @@ int make_volume_job(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_
   J->spp = spp;
   J->n_cams = n_cams;
   J->inv_box = V3{inv_box[0], inv_box[1], inv_box[2]};
+  J->box = V3{m->box_size[0] > 0.0f ? m->box_size[0] : 1.0f, m->box_size[1] > 0.0f ? m->box_size[1] : 1.0f,
+              m->box_size[2] > 0.0f ? m->box_size[2] : 1.0f};
+  if (o->envmap != nullptr) {
+    const rcv_envmap* e = o->envmap;
+    RCV_REQUIRE(e->width > 0 && e->height > 0 && e->workspace != nullptr &&
+                    (reinterpret_cast<uintptr_t>(e->workspace) & 255u) == 0,
+                "environment map: positive size and a 256-byte aligned workspace are required");
+    RCV_REQUIRE(std::isfinite(e->scale) && e->scale >= 0.0f, "environment map scale must be finite and >= 0");
+    const EnvLayout EL = env_layout(e->width, e->height);
+    const char* ew = static_cast<const char*>(e->workspace);
+    J->env.valid = 1;
+    J->env.w = e->width;
+    J->env.h = e->height;
+    J->env.inv_w = 1.0f / (float)e->width;
+    J->env.inv_h = 1.0f / (float)e->height;
+    J->env.scale = e->scale;
+    J->env.tex = reinterpret_cast<const float4*>(ew + EL.tex);
+    J->env.cond = reinterpret_cast<const float*>(ew + EL.cond);
+    J->env.marg = reinterpret_cast<const float*>(ew + EL.marg);
+    J->env.hdr = reinterpret_cast<const float*>(ew + EL.hdr);
+  }
   for (int k = 0; k < n_cams; ++k) {
     const float* o = k == 0 ? s->origin : s->more[k - 1].origin;
     const float* f = k == 0 ? s->forward : s->more[k - 1].forward;
@@ -375,7 +401,8 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   RCV_REQUIRE(Q.defer <= 32, "defer must be in [1, 32]");
   RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
   const bool sg = supergrid || (jobs == nullptr && J.sg[0] > 0);
-  const int variant = trace_variant(mode, sg, counters != nullptr);
+  // an environment map belongs to a single job (batched tables take the constant environment)
+  const int variant = trace_variant(mode, sg, counters != nullptr, jobs == nullptr && J.env.valid != 0);
   int per_sm = resident_blocks(variant);
   if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
   // replay: the checkpoint tasks come on top of one camera task per path
@@ -451,6 +478,71 @@ extern "C" uint64_t rcv_medium_workspace_bytes_for(const rcv_medium* m) {
   for (int a = 0; a < 3; ++a)
     if (m->albedo_dims[a] < 0) return 0;
   return medium_layout(m).total;
+}
+
+// Environment-map tables: one thread per row packs its texels with their
+// sampling weight f = luminance * sin(theta of the row centre) and writes the
+// row's conditional CDF from double prefix sums taken in order; then one
+// thread writes the marginal CDF over the rows and the normalisation.
+__global__ void env_rows_kernel(int w, int h, float inv_h, const float* __restrict__ texels, float4* __restrict__ tex,
+                                float* __restrict__ cond, double* __restrict__ rows) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= h) return;
+  const float sin_i = env_row_sin(i, inv_h);
+  double sum = 0.0;
+  for (int j = 0; j < w; ++j) {
+    const float* t = texels + (int64_t(i) * w + j) * 3;
+    const float f = env_luminance(t[0], t[1], t[2]) * sin_i;
+    tex[int64_t(i) * w + j] = make_float4(t[0], t[1], t[2], f);
+    sum += (double)f;
+  }
+  rows[i] = sum;
+  float* c = cond + int64_t(i) * (w + 1);
+  double acc = 0.0;
+  for (int j = 0; j < w; ++j) {
+    c[j] = sum > 0.0 ? (float)(acc / sum) : (float)((double)j / (double)w);
+    acc += (double)tex[int64_t(i) * w + j].w;
+  }
+  c[w] = 1.0f;
+}
+
+__global__ void env_marginal_kernel(int w, int h, const double* __restrict__ rows, float* __restrict__ marg,
+                                    float* __restrict__ hdr) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double total = 0.0;
+  for (int i = 0; i < h; ++i) total += rows[i];
+  double acc = 0.0;
+  for (int i = 0; i < h; ++i) {
+    marg[i] = total > 0.0 ? (float)(acc / total) : (float)((double)i / (double)h);
+    acc += rows[i];
+  }
+  marg[h] = 1.0f;
+  hdr[0] = total > 0.0 ? (float)((double)w * (double)h / total) : 0.0f;
+  hdr[1] = total > 0.0 ? 1.0f : 0.0f;
+}
+
+extern "C" uint64_t rcv_envmap_workspace_bytes(int32_t width, int32_t height) {
+  if (width <= 0 || height <= 0) return 0;
+  return env_layout(width, height).total;
+}
+
+extern "C" int rcv_envmap_prepare(const rcv_envmap* e, void* stream) {
+  RCV_REQUIRE(e != nullptr && e->texels != nullptr, "environment map or its texels are NULL");
+  RCV_REQUIRE(e->width > 0 && e->height > 0 && int64_t(e->width) * e->height < (int64_t(1) << 30),
+              "environment map size must be positive and below 2^30 texels");
+  RCV_REQUIRE(e->workspace != nullptr && (reinterpret_cast<uintptr_t>(e->workspace) & 255u) == 0,
+              "environment map workspace must be non-NULL and 256-byte aligned");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const EnvLayout L = env_layout(e->width, e->height);
+  char* ws = static_cast<char*>(e->workspace);
+  env_rows_kernel<<<grid_for(e->height, 128), 128, 0, st>>>(
+      e->width, e->height, 1.0f / (float)e->height, e->texels, reinterpret_cast<float4*>(ws + L.tex),
+      reinterpret_cast<float*>(ws + L.cond), reinterpret_cast<double*>(ws + L.rows));
+  int rc = launched("envmap rows launch");
+  if (rc) return rc;
+  env_marginal_kernel<<<1, 1, 0, st>>>(e->width, e->height, reinterpret_cast<const double*>(ws + L.rows),
+                                       reinterpret_cast<float*>(ws + L.marg), reinterpret_cast<float*>(ws + L.hdr));
+  return launched("envmap marginal launch");
 }
 
 extern "C" uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp,

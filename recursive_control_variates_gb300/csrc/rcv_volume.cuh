@@ -33,6 +33,7 @@
 #pragma once
 #include "../../include/rcv.h"
 #include "rcv_device.cuh"
+#include "rcv_env.cuh"
 
 namespace rcv {
 
@@ -84,6 +85,11 @@ struct VolJob {
   float sg_inv[3];  // 1 / sg (host-computed)
   const float* sg_two;
   const float* sg_new;
+  // environment: a prepared map, or env.valid = 0 for the constant white
+  // environment; box = the world size of the medium box (to turn a box
+  // direction back into a world direction for the map)
+  EnvMap env;
+  V3 box;
 };
 
 // Work queue of a (possibly multi-job) persistent launch.

@@ -377,6 +377,8 @@ static uint32_t vps_alt_seed(uint32_t seed) {
 
 static int vps_setup(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o,
                      const rcv_volpathsimple_flags* f, uint32_t seed, int spp, VolJob* J, VpsParams* P) {
+  RCV_REQUIRE(o == nullptr || o->envmap == nullptr,
+              "volpathsimple renders under the constant environment only (no environment map)");
   int rc = make_volume_job(m, s, o, seed, spp, J);
   if (rc) return rc;
   std::memset(P, 0, sizeof(*P));

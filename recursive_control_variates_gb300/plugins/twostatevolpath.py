@@ -56,7 +56,9 @@ class _VolumeIntegratorBase:
         self._ticket = None  # (key, done event) of an adjoint radiance pass started ahead
 
     # ------------------------------------------------------------- helpers
-    def options(self) -> _lib.VolpathOptions:
+    def options(self, scene=None) -> _lib.VolpathOptions:
+        """Tracer options; with a scene, also its environment map (None for
+        the constant environment)."""
         o = _lib.VolpathOptions()
         o.max_depth = self.max_depth
         o.rr_depth = self.rr_depth
@@ -65,6 +67,8 @@ class _VolumeIntegratorBase:
         o.blocks_per_sm = self.blocks_per_sm
         o.defer = self.defer
         o.order = self.order
+        env = scene.envmap() if scene is not None and hasattr(scene, "envmap") else None
+        o.envmap = C.addressof(env.c_struct()) if env is not None else None
         return o
 
     def counters_ptr(self, device):
@@ -109,8 +113,8 @@ class _VolumeIntegratorBase:
         if t is not None:
             torch.cuda.current_stream(device).wait_event(t[1])
 
-    def _adjoint_key(self, medium, sensor, seed: int, spp: int):
-        o = self.options()
+    def _adjoint_key(self, scene, medium, sensor, seed: int, spp: int):
+        o = self.options(scene)
         return (id(medium), medium.version, id(sensor), seed & 0xFFFFFFFF, int(spp),
                 tuple(getattr(o, f) for f, _ in o._fields_))
 
@@ -130,11 +134,11 @@ class _VolumeIntegratorBase:
         main = torch.cuda.current_stream(dev)
         m = medium.prepare(main.cuda_stream)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         ws = self.adjoint_scratch(dev, sensor, spp)
         packed = torch.cuda.Event()
         packed.record(main)
-        key = self._adjoint_key(medium, sensor, seed, spp)
+        key = self._adjoint_key(scene, medium, sensor, seed, spp)
         side = self._side.get(dev)
         if side is None:
             side = self._side[dev] = torch.cuda.Stream(dev)
@@ -198,7 +202,7 @@ class _VolumeIntegratorBase:
         st = stream_handle(medium.device)
         m = medium.prepare(st)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         img = self._image(sensor, medium.device)
         with profiling.region("trace_single", medium.device):
             _lib.check(
@@ -229,12 +233,12 @@ class _VolumeIntegratorBase:
         dev = medium.device
         ticket, key = self._ticket, None
         if ticket is not None:
-            key = self._adjoint_key(medium, sensor, seed, spp)
+            key = self._adjoint_key(scene, medium, sensor, seed, spp)
         self._drain_ticket(dev)  # orders this stream after a radiance pass started ahead
         st = stream_handle(dev)
         m = medium.prepare(st)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         dx, dy, dz = medium.dims
         gd = torch.zeros((dz, dy, dx, 1), dtype=torch.float32, device=dev)
         ga = medium.albedo_grad_buffer()
@@ -304,7 +308,7 @@ class _VolumeIntegratorBase:
         st = stream_handle(dev)
         m = medium.prepare(st)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         with profiling.region("trace_forward", dev):
             _lib.check(
                 _lib.load().rcv_render_forward_volume(
@@ -347,7 +351,7 @@ class TwoStatePRBVolpathIntegrator(_VolumeIntegratorBase):
         st = stream_handle(medium.device)
         m = medium.prepare(st)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         H = self._image(sensor, medium.device)
         F = self._image(sensor, medium.device)
         with profiling.region("trace_twostate", medium.device):

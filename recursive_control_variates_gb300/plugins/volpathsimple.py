@@ -24,6 +24,11 @@ class VolpathSimpleIntegrator(PRBVolpathIntegrator):
     """``volpathsimple``: delta tracking to real interactions, NEE towards the
     environment with MIS, and an adjoint with DRT for the in-scattering term."""
 
+    def _checked_medium(self, scene):
+        if hasattr(scene, "envmap") and scene.envmap() is not None:
+            raise ValueError("volpathsimple renders under the constant environment only (the scene has an envmap)")
+        return super()._checked_medium(scene)
+
     def __init__(self, props):
         super().__init__(props)
         self.use_nee = bool(props.get("use_nee", True))
