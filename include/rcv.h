@@ -145,10 +145,9 @@ typedef struct rcv_volpath_options {
   int32_t count_events;  /* batched launches: accumulate the RCV_COUNTER_* totals
                             behind rcv_batch_counters (single-job calls count when
                             their `counters` argument is non-NULL)               */
-  /* Environment emitter of the two-state, single-state and adjoint volume
-   * tracers: a prepared environment map, or NULL for the constant white
-   * environment (radiance 1).  volpathsimple and the batched engine take the
-   * constant environment only. */
+  /* Environment emitter of the volume tracers and volpathsimple: a prepared
+   * environment map, or NULL for the constant white environment (radiance
+   * 1).  The batched engine takes the constant environment only. */
   const rcv_envmap* envmap;
 } rcv_volpath_options;
 

@@ -1279,6 +1279,9 @@ struct Vps {
   float mu;  // majorant of `new`
   const Supergrid* sg;
   GradSink* sink = nullptr;
+  const Env* env = nullptr;  // environment map, if the scene has one
+
+  bool use_env() const { return env != nullptr && env->valid(); }
 
   float flight(Rng& r, const V3& o, const V3& d, float tmax, float& m) const {
     const float tau = -log_unit(1.0f - r.next1d());
@@ -1338,14 +1341,29 @@ struct Vps {
   V3 nee(Rng& r, const V3& x, const V3& thr, const V3* dL) const {
     Rng replay = r;
     const float u0 = r.next1d(), u1 = r.next1d();
-    const V3 w = to_box(S, square_to_uniform_sphere(u0, u1));
+    V3 w, e{0.0f, 0.0f, 0.0f};
+    if (use_env()) {
+      V3 Le;
+      float pe;
+      w = to_box(S, env->sample_dir(u0, u1, Le, pe));
+      float k = 0.0f;
+      if (pe > 0.0f && pe < std::numeric_limits<float>::infinity()) k = (kInvFourPi * mis2(pe, kInvFourPi)) / pe;
+      e = V3{Le.x * k, Le.y * k, Le.z * k};
+    } else {
+      w = to_box(S, square_to_uniform_sphere(u0, u1));
+    }
     float tn, tf;
     cube_hit(x, w, tn, tf);
     const float tr = transmittance(r, x, w, tf, nullptr);
-    const float mis = 0.5f;
-    const float en = (1.0f / kInvFourPi) * tr;
-    const V3 c{((thr.x * kInvFourPi) * mis) * en, ((thr.y * kInvFourPi) * mis) * en,
-               ((thr.z * kInvFourPi) * mis) * en};
+    V3 c;
+    if (use_env()) {
+      c = V3{(thr.x * e.x) * tr, (thr.y * e.y) * tr, (thr.z * e.z) * tr};
+    } else {
+      const float mis = 0.5f;
+      const float en = (1.0f / kInvFourPi) * tr;
+      c = V3{((thr.x * kInvFourPi) * mis) * en, ((thr.y * kInvFourPi) * mis) * en,
+             ((thr.z * kInvFourPi) * mis) * en};
+    }
     if (dL != nullptr) {
       // replay the shadow walk with the same numbers (:412-422)
       const V3 adj{dL->x * c.x, dL->y * c.y, dL->z * c.z};
@@ -1397,8 +1415,15 @@ struct Vps {
       seg.tmax = tf;
     }
     if (escaped && !(depth <= 0 && S.hide_emitters)) {
-      const float k = (F.use_nee && has_scattered) ? 0.5f : 1.0f;
-      L = V3{L.x + thr.x * k, L.y + thr.y * k, L.z + thr.z * k};
+      if (use_env()) {
+        float pe;
+        const V3 Le = env->along(S, seg.d, pe);
+        const float k = (F.use_nee && has_scattered) ? mis2(kInvFourPi, pe) : 1.0f;
+        L = V3{L.x + (thr.x * Le.x) * k, L.y + (thr.y * Le.y) * k, L.z + (thr.z * Le.z) * k};
+      } else {
+        const float k = (F.use_nee && has_scattered) ? 0.5f : 1.0f;
+        L = V3{L.x + thr.x * k, L.y + thr.y * k, L.z + thr.z * k};
+      }
     }
     return L;
   }
@@ -1424,8 +1449,12 @@ struct Vps {
     V3 o, d;
     VpsSegment seg;
     if (!camera(r, px, py, o, d, seg)) {
-      const float k = S.hide_emitters ? 0.0f : 1.0f;
-      return V3{k, k, k};
+      if (S.hide_emitters) return V3{0.0f, 0.0f, 0.0f};
+      if (use_env()) {
+        float pe;
+        return env->along(S, d, pe);
+      }
+      return V3{1.0f, 1.0f, 1.0f};
     }
     r.next1d();  // seeds the adjoint's second stream
     return primal_from(r, seg, 0, false, true);
@@ -1596,10 +1625,11 @@ int oracle_vps_render(const oracle_scene* S, const int32_t flags[4], uint32_t se
                       int row0, int row1, int row_stride) {
   if (S && row1 <= 0) row1 = S->height;
   if (!S || !flags || !out || spp <= 0 || row0 < 0 || row1 > S->height || row0 > row1) return -1;
-  if (S->env_w > 0) return -1;  // volpathsimple: constant environment only
   Supergrid sg;
   sg.build(*S);
-  const Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, S->scale * grid_max(*S, S->dens_new), &sg};
+  const Env env(*S);
+  Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, S->scale * grid_max(*S, S->dens_new), &sg};
+  vps.env = &env;
   parallel_rows(row0, row1, row_stride, threads, [&](int, int y0, int y1) {
     for (int py = y0; py < y1; ++py)
       for (int px = 0; px < S->width; ++px) {
@@ -1623,9 +1653,9 @@ int oracle_vps_render(const oracle_scene* S, const int32_t flags[4], uint32_t se
 int oracle_vps_backward(const oracle_scene* S, const int32_t flags[4], uint32_t seed, int spp, const float* grad_img,
                         double* grad_density, double* grad_albedo, int threads) {
   if (!S || !flags || spp <= 0 || !grad_img || !grad_density) return -1;
-  if (S->env_w > 0) return -1;  // volpathsimple: constant environment only
   Supergrid sg;
   sg.build(*S);
+  const Env env(*S);
   const float mu = S->scale * grid_max(*S, S->dens_new);
   const uint32_t alt_seed = vps_alt_seed(seed);
   const int64_t nv = (int64_t)S->dx * S->dy * S->dz;
@@ -1642,6 +1672,7 @@ int oracle_vps_backward(const oracle_scene* S, const int32_t flags[4], uint32_t 
   parallel_rows(0, S->height, 1, threads, [&](int k, int y0, int y1) {
     Vps vps{*S, VpsFlags{flags[0], flags[1], flags[2], flags[3]}, mu, &sg};
     vps.sink = &sinks[k];
+    vps.env = &env;
     for (int py = y0; py < y1; ++py)
       for (int px = 0; px < S->width; ++px) {
         const int pix = py * S->width + px;

@@ -54,6 +54,8 @@ struct VpsSeg {
   float tmax;
 };
 
+// kEnv: the job has an environment map (else the constant white environment).
+template <bool kEnv>
 struct Vps {
   const VolJob& J;
   const VpsParams& P;
@@ -119,16 +121,34 @@ struct Vps {
     return tf;
   }
 
+  // NEE towards the environment (sample_emitter_for_nee, :393-417): the
+  // constant one sampled uniformly (MIS 1/2 against the phase function), a
+  // map by importance with the power heuristic.
   __device__ V3 nee(Pcg32& r, const V3& x, const V3& thr, const V3* dL) const {
     Pcg32 replay = r;
     const float u0 = next1d(r), u1 = next1d(r);
-    const V3 w = to_box(J, uniform_sphere(u0, u1));
+    V3 w, e{0.0f, 0.0f, 0.0f};
+    if (kEnv) {
+      V3 Le;
+      float pdf;
+      w = to_box(J, env_sample(J.env, u0, u1, Le, pdf));
+      float k = 0.0f;
+      if (pdf > 0.0f && pdf < kInf) k = (kInvFourPi * env_mis(pdf, kInvFourPi)) / pdf;
+      e = V3{Le.x * k, Le.y * k, Le.z * k};
+    } else {
+      w = to_box(J, uniform_sphere(u0, u1));
+    }
     const float tf = exit_distance(x, w);
     const float tr = transmittance(r, x, w, tf, nullptr);
-    const float mis = 0.5f;
-    const float en = (1.0f / kInvFourPi) * tr;
-    const V3 c{((thr.x * kInvFourPi) * mis) * en, ((thr.y * kInvFourPi) * mis) * en,
-               ((thr.z * kInvFourPi) * mis) * en};
+    V3 c;
+    if (kEnv) {
+      c = V3{(thr.x * e.x) * tr, (thr.y * e.y) * tr, (thr.z * e.z) * tr};
+    } else {
+      const float mis = 0.5f;
+      const float en = (1.0f / kInvFourPi) * tr;
+      c = V3{((thr.x * kInvFourPi) * mis) * en, ((thr.y * kInvFourPi) * mis) * en,
+             ((thr.z * kInvFourPi) * mis) * en};
+    }
     if (dL != nullptr) {
       const V3 adj{dL->x * c.x, dL->y * c.y, dL->z * c.z};
       pcg_skip1(replay);
@@ -176,16 +196,37 @@ struct Vps {
       seg.tmax = tf;
     }
     if (escaped && !(depth <= 0 && J.hide_emitters)) {
-      const float k = (P.use_nee && has_scattered) ? 0.5f : 1.0f;
-      L = V3{L.x + thr.x * k, L.y + thr.y * k, L.z + thr.z * k};
+      if (kEnv) {
+        // map hit: power heuristic against NEE after a scattering event (:280-298)
+        float pdf;
+        const V3 Le = env_along(seg.d, pdf);
+        const float k = (P.use_nee && has_scattered) ? env_mis(kInvFourPi, pdf) : 1.0f;
+        L = V3{L.x + (thr.x * Le.x) * k, L.y + (thr.y * Le.y) * k, L.z + (thr.z * Le.z) * k};
+      } else {
+        const float k = (P.use_nee && has_scattered) ? 0.5f : 1.0f;
+        L = V3{L.x + thr.x * k, L.y + thr.y * k, L.z + thr.z * k};
+      }
     }
     return L;
   }
 
-  // Camera ray, colour-channel draw, medium entry (reach_medium, :329-346).
-  __device__ bool camera(Pcg32& r, int pix, VpsSeg& seg) const {
+  // Radiance of the environment map along a box direction and the pdf of
+  // sampling it (the direction made a unit world direction first).
+  __device__ V3 env_along(const V3& d, float& pdf) const {
+    V3 wd{d.x * J.box.x, d.y * J.box.y, d.z * J.box.z};
+    const float inv_len = 1.0f / sqrtf(fmaf(wd.z, wd.z, fmaf(wd.y, wd.y, wd.x * wd.x)));
+    wd = V3{wd.x * inv_len, wd.y * inv_len, wd.z * inv_len};
+    float u, v, st;
+    env_uv(wd, u, v, st);
+    pdf = env_pdf(J.env, u, v, st);
+    return env_eval_uv(J.env, u, v);
+  }
+
+  // Camera ray, colour-channel draw, medium entry (reach_medium, :329-346);
+  // `d` is the camera ray (for the environment when it misses the medium).
+  __device__ bool camera(Pcg32& r, int pix, VpsSeg& seg, V3& d) const {
     const float u0 = next1d(r), u1 = next1d(r);
-    V3 o, d;
+    V3 o;
     camera_ray(J, pix % J.width, pix / J.width, u0, u1, o, d);
     pcg_skip1(r);
     const V3 inv_d = recip(d);
@@ -203,9 +244,14 @@ struct Vps {
     Pcg32 r;
     seed_lane(r, J.seed, sid);
     VpsSeg seg;
-    if (!camera(r, pix, seg)) {
-      const float k = J.hide_emitters ? 0.0f : 1.0f;
-      return V3{k, k, k};
+    V3 d;
+    if (!camera(r, pix, seg, d)) {
+      if (J.hide_emitters) return V3{0.0f, 0.0f, 0.0f};
+      if (kEnv) {
+        float pdf;
+        return env_along(d, pdf);
+      }
+      return V3{1.0f, 1.0f, 1.0f};
     }
     pcg_skip1(r);  // seeds the adjoint's second stream
     return primal_from(r, seg, 0, false, true);
@@ -250,7 +296,8 @@ struct Vps {
     seed_lane(r, J.seed, sid);
     seed_lane(alt, P.alt_seed, sid);
     VpsSeg seg;
-    if (!camera(r, pix, seg)) return;
+    V3 d;
+    if (!camera(r, pix, seg, d)) return;
     pcg_skip1(r);
     V3 res = Ltot, thr{1, 1, 1};
     int depth = 0;
@@ -340,11 +387,11 @@ struct Vps {
   }
 };
 
-template <bool kAdj>
+template <bool kAdj, bool kEnv>
 __global__ void __launch_bounds__(128) vps_kernel(const __grid_constant__ VolJob J,
                                                   const __grid_constant__ VpsParams P) {
   const float mu = J.scale * bits_to_float(__ldg(J.maxbits + 1));
-  const Vps v{J, P, mu, 1.0f / mu};
+  const Vps<kEnv> v{J, P, mu, 1.0f / mu};
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   for (int64_t path = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; path < J.path_count; path += stride) {
     const int pix = (int)(path / J.spp);
@@ -377,8 +424,6 @@ static uint32_t vps_alt_seed(uint32_t seed) {
 
 static int vps_setup(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o,
                      const rcv_volpathsimple_flags* f, uint32_t seed, int spp, VolJob* J, VpsParams* P) {
-  RCV_REQUIRE(o == nullptr || o->envmap == nullptr,
-              "volpathsimple renders under the constant environment only (no environment map)");
   int rc = make_volume_job(m, s, o, seed, spp, J);
   if (rc) return rc;
   std::memset(P, 0, sizeof(*P));
@@ -427,7 +472,10 @@ extern "C" int rcv_render_volpathsimple(const rcv_medium* m, const rcv_sensor* s
   int rc = vps_setup(m, s, o, f, seed, spp, &J, &P);
   if (rc) return rc;
   P.path_out = static_cast<float4*>(workspace);
-  vps_kernel<false><<<vps_grid(J.path_count), 128, 0, st>>>(J, P);
+  if (J.env.valid)
+    vps_kernel<false, true><<<vps_grid(J.path_count), 128, 0, st>>>(J, P);
+  else
+    vps_kernel<false, false><<<vps_grid(J.path_count), 128, 0, st>>>(J, P);
   rc = launched("volpathsimple launch");
   if (rc) return rc;
   return launch_reduce(false, P.path_out, 0, int64_t(J.width) * J.height, J.spp, img, nullptr, st);
@@ -448,7 +496,10 @@ extern "C" int rcv_render_backward_volpathsimple(const rcv_medium* m, const rcv_
   if (rc) return rc;
   if (!want_albedo) J.grad_albedo = nullptr;
   J.grad_img = grad_img;
-  vps_kernel<true><<<vps_grid(J.path_count), 128, 0, st>>>(J, P);
+  if (J.env.valid)
+    vps_kernel<true, true><<<vps_grid(J.path_count), 128, 0, st>>>(J, P);
+  else
+    vps_kernel<true, false><<<vps_grid(J.path_count), 128, 0, st>>>(J, P);
   rc = launched("volpathsimple adjoint launch");
   if (rc) return rc;
   return launch_fold(m, grad_density, want_albedo ? grad_albedo : nullptr, st);

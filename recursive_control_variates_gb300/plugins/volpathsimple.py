@@ -24,11 +24,6 @@ class VolpathSimpleIntegrator(PRBVolpathIntegrator):
     """``volpathsimple``: delta tracking to real interactions, NEE towards the
     environment with MIS, and an adjoint with DRT for the in-scattering term."""
 
-    def _checked_medium(self, scene):
-        if hasattr(scene, "envmap") and scene.envmap() is not None:
-            raise ValueError("volpathsimple renders under the constant environment only (the scene has an envmap)")
-        return super()._checked_medium(scene)
-
     def __init__(self, props):
         super().__init__(props)
         self.use_nee = bool(props.get("use_nee", True))
@@ -74,7 +69,7 @@ class VolpathSimpleIntegrator(PRBVolpathIntegrator):
         st = stream_handle(medium.device)
         m = medium.prepare(st)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         fl = self.flags()
         img = self._image(sensor, medium.device)
         with profiling.region("vps_primal", medium.device):
@@ -102,7 +97,7 @@ class VolpathSimpleIntegrator(PRBVolpathIntegrator):
         st = stream_handle(medium.device)
         m = medium.prepare(st)
         s = sensor.c_struct()
-        o = self.options()
+        o = self.options(scene)
         fl = self.flags()
         dx, dy, dz = medium.dims
         gd = torch.zeros((dz, dy, dx, 1), dtype=torch.float32, device=medium.device)

@@ -137,6 +137,37 @@ def test_envmap_adjoint_matches_finite_differences(oracle):
     assert abs(adj) > 3 * adj_se
 
 
+def test_envmap_volpathsimple_adjoint_and_primal(oracle):
+    """volpathsimple under a peaked map: its primal image has the two-state
+    tracer's expectation (other sampling), and its adjoint (NEE with map
+    importance sampling and MIS, DRT, transmittance terms) matches central
+    differences of the two-state tracer."""
+    res, D = 12, 8
+    cam = oracle.camera_basis(res, res)
+    env = random_map()
+    theta = scenes.blob_density(D, 4)[..., 0] * 0.5
+    sc = oracle.Scene(cam, theta, theta, albedo_const=0.8, max_depth=6, envmap=env)
+    a = np.stack([oracle.vps_render(sc, seed=s, spp=256) for s in range(6)]).astype(np.float64)
+    b = np.stack([oracle.render(sc, seed=50 + s, spp=256) for s in range(6)]).astype(np.float64)
+    ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
+    se = np.hypot(ma.std(ddof=1), mb.std(ddof=1)) / np.sqrt(6)
+    assert abs(ma.mean() - mb.mean()) < 4 * se + 1e-4, (ma.mean(), mb.mean(), se)
+    w = np.random.default_rng(0).normal(0, 1, (res, res, 3)).astype(np.float32) + 0.5
+    runs = np.array([oracle.vps_backward(sc, seed=100 + s, spp=32, grad_img=w)[0] for s in range(16)])
+    delta = theta / theta.max()
+    h = 0.02
+    s2 = oracle.Scene(cam, theta - h * delta, theta + h * delta, albedo_const=0.8, max_depth=6, envmap=env)
+    est = []
+    for seed in range(12):
+        H, F = oracle.render_twostates(s2, seed=7 + seed, spp=64)
+        est.append(float(((F.astype(np.float64) - H) * w).sum() / (2 * h)))
+    fd, fd_se = np.mean(est), np.std(est) / np.sqrt(len(est))
+    proj = (runs * delta).sum(axis=(1, 2, 3))
+    adj, adj_se = proj.mean(), proj.std() / np.sqrt(len(proj))
+    assert abs(fd - adj) < 4 * np.hypot(fd_se, adj_se) + 1e-4, (fd, fd_se, adj, adj_se)
+    assert abs(fd) > 4 * fd_se
+
+
 def test_envmap_plugin_on_the_host(tmp_path):
     from recursive_control_variates_gb300 import io
 
@@ -153,9 +184,6 @@ def test_envmap_plugin_on_the_host(tmp_path):
     d["emitter"] = {"type": "envmap", "data": env}
     sc = rcv.load_dict(d, device="cpu")
     assert sc.envmap() is not None
-    vps = rcv.load_dict({"type": "volpathsimple"})
-    with pytest.raises(ValueError, match="constant environment"):
-        vps._checked_medium(sc)
     d["sky"] = {"type": "constant"}
     with pytest.raises(ValueError):
         rcv.load_dict(d, device="cpu").envmap()
@@ -248,13 +276,34 @@ def test_envmap_forward_mode_and_file(cuda, oracle, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("flags", [{}, {"use_drt_subsampling": False}, {"use_nee": False}])
+def test_envmap_volpathsimple_matches_oracle(cuda, oracle, flags):
+    env, scale = random_map(seed=3), 1.3
+    scene, grids = gpu_env_scene(cuda, env, scale, res=24)
+    osc = oracle_env_scene(oracle, scene, grids, env, scale)
+    vps = rcv.load_dict({"type": "volpathsimple", "max_depth": 8, "rr_depth": 8, **flags})
+    img = vps.render(scene, 0, seed=3, spp=4).cpu().numpy()
+    assert frac_equal(img, oracle.vps_render(osc, seed=3, spp=4, flags=flags)) >= 0.999
+    params = rcv.traverse(scene)
+    gimg = np.random.default_rng(5).normal(0, 1, (24, 24, 3)).astype(np.float32)
+    g = vps.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=4, spp=4)
+    od, oa = oracle.vps_backward(osc, seed=4, spp=4, grad_img=gimg, flags=flags)
+    gd = g[scenes.DENSITY_KEY].cpu().numpy()[..., 0].astype(np.float64)
+    ga = g[scenes.ALBEDO_KEY].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(gd - od) <= 2e-5 * np.linalg.norm(od)
+    assert np.linalg.norm(ga - oa) <= 2e-5 * np.linalg.norm(oa)
+
+
+@pytest.mark.gpu
 def test_envmap_cv_step_and_rejections(cuda):
-    """A cv_ps step (render + adjoint) under an envmap through the public
-    API; volpathsimple and the batched engine refuse the map."""
+    """A cv step (two-state render, volpathsimple adjoint as in the grid
+    experiments, experiments.py:131) under an envmap through the public API;
+    the batched engine refuses the map."""
     env = random_map()
     scene, grids = gpu_env_scene(cuda, env, 1.0, res=24, albedo_grid=False)
     params = rcv.traverse(scene)
-    integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath", "max_depth": 8}})
+    integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath", "max_depth": 8},
+                           "adjoint_integrator": {"type": "volpathsimple", "max_depth": 8}})
     opt = rcv.ad.Adam(lr=0.02)
     opt[scenes.DENSITY_KEY] = params[scenes.DENSITY_KEY]
     params.update(opt)
@@ -267,9 +316,6 @@ def test_envmap_cv_step_and_rejections(cuda):
         assert torch.isfinite(opt[scenes.DENSITY_KEY].grad).all()
         opt.step()
     assert np.isfinite(loss.item())
-    vps = rcv.load_dict({"type": "volpathsimple"})
-    with pytest.raises(ValueError, match="constant environment"):
-        vps.render(scene, 0, seed=1, spp=2)
     from recursive_control_variates_gb300 import batch
 
     with pytest.raises(ValueError, match="constant environment"):
