@@ -94,12 +94,13 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profile_figures(kernel: str) -> dict:
+def profile_figures(kernel: str, workload: str = "cfg2") -> dict:
     """Per-launch figures of `kernel` recorded from ncu captures in
     profiles/*.md (lines `<figure>[<kernel>]: <value>`, e.g.
-    traffic_bytes_per_launch, l1_throughput_pct, threads_per_inst).  A file
-    counts only if its `source_digest:` line matches the digest of the
-    current CUDA sources; otherwise its figures are stale and left out."""
+    traffic_bytes_per_launch, l1_throughput_pct_128px, threads_per_inst).  A
+    file counts only if its `workload:` line names the bench's workload and
+    its `source_digest:` line matches the digest of the current CUDA
+    sources; otherwise its figures are left out."""
     from recursive_control_variates_gb300 import _build
 
     cur = _build.source_digest()
@@ -108,6 +109,9 @@ def profile_figures(kernel: str) -> dict:
         txt = f.read_text()
         found = re.findall(rf"^(\w+)\[{re.escape(kernel)}\]:\s*([0-9.eE+-]+)\s*$", txt, re.M)
         if not found:
+            continue
+        w = re.search(r"^workload:\s*(\S+)\s*$", txt, re.M)
+        if w is None or w.group(1) != workload:
             continue
         m = re.search(r"^source_digest:\s*([0-9a-f]+)\s*$", txt, re.M)
         if m is None or m.group(1) != cur:
@@ -329,7 +333,7 @@ def run_ours(args, cfg):
     peaks = measured_peaks()
     dur_s = kern_serial[dom]["mean_ms"] / 1e3
     achieved = algo[dom] / dur_s / 1e9
-    prof = profile_figures(dom)
+    prof = profile_figures(dom, cfg.name)
     fig = prof["figures"]
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
             "peak_source": peaks["source"], "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
@@ -345,7 +349,7 @@ def run_ours(args, cfg):
                              "captured on the small case only)"),
             "profile_source_digest": prof["source_digest"]}
     if not fig:
-        roof["profile_note"] = ("no ncu summary in profiles/ was captured from the current CUDA sources"
+        roof["profile_note"] = (f"no ncu summary in profiles/ was captured for {cfg.name} from the current CUDA sources"
                                 + (f"; stale: {', '.join(prof['stale'])}" if prof["stale"] else ""))
 
     # --------------------------------------------------- end-to-end (API)
