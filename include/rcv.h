@@ -149,7 +149,21 @@ typedef struct rcv_volpath_options {
    * environment map, or NULL for the constant white environment (radiance
    * 1).  The batched engine takes the constant environment only. */
   const rcv_envmap* envmap;
+  /* Adjoint of the single-job volume tracer (rcv_render_backward_volume and
+   * the radiance / replay stages): RCV_ADJOINT_TAPE records every gradient
+   * event of the radiance pass on a tape and scatters the gradient from it in
+   * one flat pass; RCV_ADJOINT_REPLAY replays the paths' segments from
+   * scattering checkpoints.  Both give the same gradient (up to the order of
+   * float additions).  The tape needs the global majorant: with a supergrid,
+   * in forward mode and in batched launches the replay runs. */
+  int32_t adjoint;
+  /* Tape slots per path, 1..16 (0 = 16, the room the adjoint workspace
+   * holds): paths whose events do not fit are replayed whole. */
+  int32_t tape_events_per_path;
 } rcv_volpath_options;
+
+#define RCV_ADJOINT_TAPE 0
+#define RCV_ADJOINT_REPLAY 1
 
 /* Pixel hand-out orders of the persistent tracers.  Results do not depend on
  * the order; it only changes how evenly the work drains at the end.

@@ -81,6 +81,8 @@ class VolpathOptions(C.Structure):
         ("order", C.c_int32),
         ("count_events", C.c_int32),
         ("envmap", C.c_void_p),  # const rcv_envmap* or NULL (constant environment)
+        ("adjoint", C.c_int32),  # ADJOINT_TAPE / ADJOINT_REPLAY
+        ("tape_events_per_path", C.c_int32),  # 1..16, 0 = 16
     ]
 
 
@@ -113,6 +115,10 @@ ORDERS = {"cost": ORDER_COST, "row_major": ORDER_ROW_MAJOR, "longest_first": ORD
 MODE_TWOSTATE = 0
 MODE_SINGLE = 1
 MODE_ADJOINT = 2
+
+ADJOINT_TAPE = 0
+ADJOINT_REPLAY = 1
+ADJOINTS = {"tape": ADJOINT_TAPE, "replay": ADJOINT_REPLAY}
 
 
 class SphereDesc(C.Structure):

@@ -115,18 +115,31 @@ inline MediumLayout medium_layout(const rcv_medium* m) {
 }
 
 // Scratch layout of one tracer call (all offsets 256-byte aligned):
-// queue counter (+ checkpoint counter) | order bucket counts | pixel order |
-// per-pixel cost | per-path radiance (32 B per path for two-state, 16 B
-// single-state) | adjoint: per-path total radiance | scatter checkpoints.
+// counters (queue, checkpoints / event records, tape slots, lost paths) |
+// order bucket counts | pixel order | per-pixel cost | per-path radiance (32 B
+// per path for two-state, 16 B single-state) | adjoint: per-path total
+// radiance | scatter checkpoints (tape: event records, then their weights) |
+// event tape | per-path camera-segment weight | lost-path list.
 constexpr int kRenderOrderBuckets = 256;
 
 struct RenderLayout {
-  uint64_t counter, buckets, order, cost, path_out, ltot, ckpt, total;
+  uint64_t counter, buckets, order, cost, path_out, ltot, ckpt, tape, cam_w, lost, total;
 };
 
 // Adjoint scatter checkpoints: 64 bytes each, room for 2 per path plus a
-// margin; paths whose checkpoints do not fit are replayed whole.
+// margin; paths whose checkpoints do not fit are replayed whole.  The tape
+// adjoint keeps its 32-byte event records in the first half of the same
+// buffer and their 32-byte weights in the second.
 inline int64_t ckpt_capacity(int64_t paths) { return 2 * paths + 65536; }
+
+// Event tape of the adjoint: 16 bytes per event, kTapeSlotsPerPath per path
+// (whole chunks of kTapeChunkSlots, the unit a warp claims).
+constexpr int64_t kTapeSlotsPerPath = 16;
+constexpr int64_t kTapeChunkSlots = 256;
+inline int64_t tape_capacity(int64_t paths, int per_path) {
+  const int64_t slots = paths * (int64_t)per_path;
+  return (slots + kTapeChunkSlots - 1) / kTapeChunkSlots * kTapeChunkSlots;
+}
 
 inline uint64_t path_out_bytes(int64_t paths, int mode) {
   return mode == RCV_MODE_ADJOINT ? 0u : uint64_t(paths) * (mode == RCV_MODE_TWOSTATE ? 32u : 16u);
@@ -142,7 +155,10 @@ inline RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
   const bool adj = mode == RCV_MODE_ADJOINT;
   L.ltot = align256(L.path_out + path_out_bytes(paths, mode));
   L.ckpt = align256(L.ltot + (adj ? uint64_t(paths) * 16u : 0u));
-  L.total = align256(L.ckpt + (adj ? uint64_t(ckpt_capacity(paths)) * 64u : 0u));
+  L.tape = align256(L.ckpt + (adj ? uint64_t(ckpt_capacity(paths)) * 64u : 0u));
+  L.cam_w = align256(L.tape + (adj ? uint64_t(tape_capacity(paths, kTapeSlotsPerPath)) * 16u : 0u));
+  L.lost = align256(L.cam_w + (adj ? uint64_t(paths) * 4u : 0u));
+  L.total = align256(L.lost + (adj ? uint64_t(paths) * 4u : 0u));
   return L;
 }
 

@@ -1,0 +1,154 @@
+// Gradient of the adjoint from the event tape of the kTape radiance pass.
+//
+// Path replay backpropagation (Vicini et al. 2021) scatters, at every event of
+// a path, dL . L_rem times a factor of the event into the grid gradient, with
+// L_rem = L - (radiance gathered before the event).  The replay tasks of
+// kReplay retrace every segment to find the events again.  The kTape radiance
+// pass instead records each event as it happens (its position and a
+// reference), and this file turns the tape into the gradient in two flat
+// launches, the same arithmetic as the replay event by event
+// (plugins/twostatevolpath.py:141-479 for the events; the adjoint
+// semantics of Mitsuba's prb_volpath):
+//   tape_weights_kernel  per event record and per path, dL . L_rem of every
+//                        kind of event that refers to it, once dL is known;
+//   tape_scatter_kernel  per tape slot: the density (and at scattering
+//                        events the albedo) at the event from the medium,
+//                        the event's factor, and the gradient scatter:
+//                          null collision   -scale * (dL . L_rem) / sigma_n
+//                          scattering event  scale * (dL . L_rem) / sigma_t,
+//                                            albedo: dL * L_rem / albedo
+//                          shadow-walk step -scale * (dL . c_nee) / sigma_n
+//                                            (where sigma_n > 0)
+// Events of a path that lost an event or a record are skipped; kReplay
+// replays that path whole.
+#include "rcv_common.h"
+#include "rcv_volume.cuh"
+
+namespace rcv {
+
+// Pixel of a path of the job (the hand-out order maps the k-th pixel slot).
+__device__ __forceinline__ int tape_pixel(const VolJob& J, uint32_t path) {
+  const uint32_t k = (path - (uint32_t)J.path_begin) / (uint32_t)J.spp;
+  return J.pixel_order != nullptr ? (int)__ldg(J.pixel_order + k) : (int)k;
+}
+
+__device__ __forceinline__ V3 tape_dL(const VolJob& J, int pix) {
+  const float* g = J.grad_img + (int64_t)pix * 3;
+  const float fs = (float)J.spp;
+  return V3{g[0] / fs, g[1] / fs, g[2] / fs};
+}
+
+// Record k (2 float4: [path, radiance gathered before the event's NEE
+// contribution] [NEE contribution]) -> weights [dL . L_rem after the NEE
+// contribution (the next segment), dL . c_nee (the shadow walk), dL . L_rem
+// (the event), skip] [dL * L_rem per channel (the event's albedo)].  Path p ->
+// dL . L (its camera segment), or NaN when the path is replayed instead.
+__global__ void tape_weights_kernel(const __grid_constant__ VolJob J, const float4* __restrict__ rec,
+                                    const unsigned long long* __restrict__ rec_count, int64_t rec_cap,
+                                    float4* __restrict__ w, const float4* __restrict__ ltot, float* __restrict__ cam_w,
+                                    int64_t paths) {
+  const int64_t nrec = min((int64_t)*rec_count, rec_cap);
+  const int64_t n = max(nrec, paths);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    if (i < nrec) {
+      const float4 r0 = rec[2 * i], r1 = rec[2 * i + 1];
+      const uint32_t path = __float_as_uint(r0.x);
+      const float4 lt = ltot[path];
+      if (lt.w != 0.0f) {
+        w[2 * i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+      } else {
+        const V3 g = tape_dL(J, tape_pixel(J, path));
+        const V3 lr{lt.x - r0.y, lt.y - r0.z, lt.z - r0.w};
+        const V3 ls{lr.x - r1.x, lr.y - r1.y, lr.z - r1.z};
+        const float s_event = (g.x * lr.x + g.y * lr.y) + g.z * lr.z;
+        const float s_next = (g.x * ls.x + g.y * ls.y) + g.z * ls.z;
+        const float s_nee = (g.x * r1.x + g.y * r1.y) + g.z * r1.z;
+        w[2 * i] = make_float4(s_next, s_nee, s_event, 0.0f);
+        w[2 * i + 1] = make_float4(g.x * lr.x, g.y * lr.y, g.z * lr.z, 0.0f);
+      }
+    }
+    if (i < paths) {
+      const float4 lt = ltot[i];
+      float s = __int_as_float(0x7fc00000);  // NaN: skip
+      if (lt.w == 0.0f) {
+        const V3 g = tape_dL(J, tape_pixel(J, (uint32_t)i));
+        s = (g.x * lt.x + g.y * lt.y) + g.z * lt.z;
+      }
+      cam_w[i] = s;
+    }
+  }
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant__ VolJob J,
+                                                           const float4* __restrict__ tape,
+                                                           const unsigned long long* __restrict__ tape_count,
+                                                           int64_t tape_cap, const float4* __restrict__ w,
+                                                           const float* __restrict__ cam_w,
+                                                           unsigned long long* counters) {
+  const int64_t n = min((int64_t)*tape_count, tape_cap);
+  const float mu = J.scale * bits_to_float(__ldg(J.maxbits + 1));
+  uint32_t ge = 0, ae = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const float4 ev = __ldcs(tape + i);
+    const uint32_t ref = __float_as_uint(ev.w);
+    if (ref == kTapeEmpty) continue;
+    const uint32_t kind = ref >> 30, idx = ref & kTapeIndexMask;
+    float s;
+    if (kind == kEvCamera) {
+      s = __ldg(cam_w + idx);
+      if (s != s) continue;
+    } else {
+      const float4 wr = __ldg(w + 2 * (int64_t)idx);
+      if (wr.w != 0.0f) continue;
+      s = kind == kEvSegment ? wr.x : (kind == kEvShadow ? wr.y : wr.z);
+    }
+    const V3 x{ev.x, ev.y, ev.z};
+    const Lookup lk = locate(J, x);
+    const float st_n = J.scale * density_new(J, lk);
+    if (kind == kEvScatter) {
+      scatter_density(J, lk, (J.scale * s) / st_n);
+      if (kCount) ++ge;
+      if (J.grad_albedo != nullptr) {
+        const AlbedoLookup alk = albedo_lookup(J, lk, x);
+        const V3 an = albedo_at(J, alk, 1);
+        const float4 ga = __ldg(w + 2 * (int64_t)idx + 1);
+        scatter_albedo(J, alk,
+                       V3{ga.x / fmaxf(an.x, 1e-8f), ga.y / fmaxf(an.y, 1e-8f), ga.z / fmaxf(an.z, 1e-8f)});
+        if (kCount) ++ae;
+      }
+    } else {
+      const float sn = mu - st_n;
+      if (kind != kEvShadow || sn > 0.0f) {
+        scatter_density(J, lk, -(J.scale * s) / sn);
+        if (kCount) ++ge;
+      }
+    }
+  }
+  if (kCount && counters != nullptr) {
+    ge = __reduce_add_sync(0xffffffffu, ge);
+    ae = __reduce_add_sync(0xffffffffu, ae);
+    if ((threadIdx.x & 31) == 0) {
+      if (ge) atomicAdd(counters + RCV_COUNTER_GRAD_EVENTS, (unsigned long long)ge);
+      if (ae) atomicAdd(counters + RCV_COUNTER_ALBEDO_EVENTS, (unsigned long long)ae);
+    }
+  }
+}
+
+int launch_tape_gradient(const VolJob& J, const AdjBuffers& A, float4* weights, float* cam_w, int64_t paths,
+                         uint64_t* counters, int sms, cudaStream_t st) {
+  const int block = 256;
+  tape_weights_kernel<<<grid_for(A.ckpt_cap > paths ? A.ckpt_cap : paths, block), block, 0, st>>>(
+      J, A.ckpt, A.ckpt_count, A.ckpt_cap, weights, A.path_ltot, cam_w, paths);
+  int rc = launched("tape_weights launch");
+  if (rc) return rc;
+  const unsigned grid = (unsigned)(sms > 0 ? sms : 1) * 8u;
+  unsigned long long* c = reinterpret_cast<unsigned long long*>(counters);
+  if (counters != nullptr)
+    tape_scatter_kernel<true><<<grid, block, 0, st>>>(J, A.tape, A.tape_count, A.tape_cap, weights, cam_w, c);
+  else
+    tape_scatter_kernel<false><<<grid, block, 0, st>>>(J, A.tape, A.tape_count, A.tape_cap, weights, cam_w, c);
+  return launched("tape_scatter launch");
+}
+
+}  // namespace rcv

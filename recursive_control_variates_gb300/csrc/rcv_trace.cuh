@@ -40,6 +40,15 @@
 //             pixel at the end of the task.
 // Replaying segments instead of whole paths keeps every task short, so the
 // launch does not end on a few paths that scatter dozens of times.
+//   kTape     the radiance pass without checkpoints: it records every
+//             gradient event of the path (main-walk null collisions, real
+//             scattering events, shadow-walk steps) on a tape, as its
+//             position and a reference to the path or to the record of its
+//             scattering event (radiance gathered before it, NEE
+//             contribution).  The gradient is then one flat pass over the
+//             tape (rcv_tape.cu), which recomputes each event's factor from
+//             the medium; paths whose events did not fit are replayed whole
+//             by kReplay over the lost list.
 #pragma once
 #include "rcv_volume.cuh"
 
@@ -80,6 +89,50 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
 // shared memory).
 constexpr int kTraceWarps = 4;
 
+// Slots [cur, end) of the tape chunk a warp fills (warp-uniform).
+struct TapeCursor {
+  uint32_t cur, end;
+};
+
+// Appends the events of the lanes with `has` to the warp's tape chunk (one
+// event per lane, in lane order), claiming a new chunk of kTapeChunk slots
+// when the current one runs out; a chunk is only claimed whole inside the
+// capacity.  Called by the whole warp.  Returns false on the lanes whose
+// event did not fit (their path is then replayed instead).
+__device__ __forceinline__ bool tape_append(const Queue& Q, TapeCursor& tc, bool has, const V3& x, uint32_t ref) {
+  const unsigned m = __ballot_sync(0xffffffffu, has);
+  if (m == 0u) return true;
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t n = (uint32_t)__popc(m), q = (uint32_t)__popc(m & ((1u << lane) - 1u));
+  const uint32_t rem = tc.end - tc.cur;
+  uint32_t nb = 0xffffffffu;  // start of the newly claimed chunk, if any
+  if (n > rem) {
+    unsigned long long b = 0;
+    if (lane == 0) b = atomicAdd(Q.tape_count, (unsigned long long)kTapeChunk);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (b + kTapeChunk <= (unsigned long long)Q.tape_cap) nb = (uint32_t)b;
+  }
+  bool ok = true;
+  if (has) {
+    if (q < rem) {
+      Q.tape[tc.cur + q] = make_float4(x.x, x.y, x.z, __uint_as_float(ref));
+    } else if (nb != 0xffffffffu) {
+      Q.tape[nb + (q - rem)] = make_float4(x.x, x.y, x.z, __uint_as_float(ref));
+    } else {
+      ok = false;
+    }
+  }
+  if (n <= rem) {
+    tc.cur += n;
+  } else if (nb != 0xffffffffu) {
+    tc.cur = nb + (n - rem);
+    tc.end = nb + kTapeChunk;
+  } else {
+    tc.cur = tc.end;  // the tape is full: later events of this warp do not fit either
+  }
+  return ok;
+}
+
 // Cooperative walk of a warp's last paths.
 //
 // Once the path queue is empty a warp runs until its longest path ends, and
@@ -106,11 +159,14 @@ constexpr int kTraceWarps = 4;
 // transmittances (shadow: trn, tro in .x); `s_t`, `s_w1`, `s_w2` are the
 // warp's 32-float shared arrays for the steps' distances and weights.
 // Returns the number of steps the calling lane's path took (0 for lanes that
-// own no walking path).
+// own no walking path).  kTape: every step taken is a gradient event, which
+// the lane that evaluated it appends to the tape with the owner's reference
+// `ref`; `lost` is set on an owner whose events did not fit.
 template <int kMode>
 __device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJob* Jp, Pcg32& rng, float mu,
                                          float inv_mu, float half_inv_mu, V3& org, const V3& dir, float& tmax,
-                                         V3& c1, V3& c2, float* s_t, float* s_w1, float* s_w2) {
+                                         V3& c1, V3& c2, float* s_t, float* s_w1, float* s_w2, const Queue& Q,
+                                         TapeCursor& tc, uint32_t ref, bool& lost) {
   constexpr unsigned kFull = 0xffffffffu;
   const unsigned lane = threadIdx.x & 31u;
   const int n = __popc(m);
@@ -191,9 +247,9 @@ __device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJo
   // transmittances (shadow) multiplied in step order
   const bool own = (m >> lane) & 1u;
   int f = 0, src = (int)lane;
+  const int ob = __popc(m & ((1u << lane) - 1u)) * G;
+  const unsigned gmask = G == 32 ? kFull : ((1u << G) - 1u);
   if (own) {
-    const int ob = __popc(m & ((1u << lane) - 1u)) * G;
-    const unsigned gmask = G == 32 ? kFull : ((1u << G) - 1u);
     const unsigned tb = (tb_all >> ob) & gmask;
     const int f0 = tb != 0u ? __ffs(tb) - 1 : G;
     f = f0;
@@ -229,6 +285,14 @@ __device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJo
   const V3 xs{__shfl_sync(kFull, x.x, src), __shfl_sync(kFull, x.y, src), __shfl_sync(kFull, x.z, src)};
   const float ts = __shfl_sync(kFull, tr - t, src);
   const unsigned long long ss = __shfl_sync(kFull, (unsigned long long)r.state, src);
+  if (kMode == kTape) {
+    // the group's steps before the first that ends the run are events
+    const int fg = __shfl_sync(kFull, f, owner);
+    const uint32_t rg = __shfl_sync(kFull, ref, owner);
+    const bool ok = tape_append(Q, tc, busy && k < fg, x, rg);
+    const unsigned bad = __ballot_sync(kFull, !ok);
+    if (own && ((bad >> ob) & gmask) != 0u) lost = true;
+  }
   if (f == 0) return 0;
   org = xs;
   tmax = ts;
@@ -272,16 +336,20 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   // replay tasks, scattering the image gradient (kReplay) or gathering a
   // tangent field (kForward)
   constexpr bool kRep = kMode == kReplay || kMode == kForward;
-  constexpr bool kCoop = kMode == kTwoState || kMode == kSingle || kMode == kAdjoint;
+  // radiance passes of the adjoint (checkpoints or tape)
+  constexpr bool kRad = kMode == kAdjoint || kMode == kTape;
+  constexpr bool kCoop = kMode == kTwoState || kMode == kSingle || kRad;
   __shared__ float s_coop[kCoop ? kTraceWarps * 96 : 1];  // cooperative walk: distances, weights
   // environment map: each lane's NEE weight e = Le / pdf * phase * MIS of its
   // pending shadow ray, kept here from the scattering event to the end of the
   // walk instead of in registers
   __shared__ float s_env[kEnv ? kTraceWarps * 32 * 3 : 1];
   float* env_e = s_env + (kEnv ? threadIdx.x * 3 : 0);
-  // replay: camera tasks [0, paths), then the checkpoints that were written
-  const int64_t total =
-      kRep ? Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap) : Q.total;
+  // replay: camera tasks [0, paths) (after a tape pass: the paths on the lost
+  // list), then the checkpoints that were written
+  const int64_t total = !kRep ? Q.total
+                              : (Q.lost_list != nullptr ? (int64_t)*Q.lost_count
+                                                        : Q.total + min((int64_t)*Q.ckpt_count, Q.ckpt_cap));
 
   int64_t batch_next = 0, batch_end = 0;
   bool queue_empty = false;
@@ -313,7 +381,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
   V3 wo_next;
   // adjoint radiance pass: random-number state at the pending scattering event
   uint64_t ck_state = 0;
-  bool ck_lost = false;  // a checkpoint of this path did not fit
+  bool ck_lost = false;  // a checkpoint (kTape: an event or event record) of this path did not fit
+  // kTape: reference of the path's next events (kind << 30 | path or event
+  // record), and the warp's tape chunk
+  uint32_t tref = 0;
+  TapeCursor tc{0u, 0u};
   // replay
   // replay: radiance the path gathers after its current point,
   // L_rem = L - (radiance gathered so far), kept instead of L and the sum so far
@@ -368,7 +440,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     if (run_start && phase == kStart) {
       iter0 = n_iter;
       // replay: a checkpoint task resumes at its scattering event
-      const bool resume = kRep && path >= Q.total;
+      const bool resume = kRep && Q.lost_list == nullptr && path >= Q.total;
       float4 r0, r1, r2, r3;
       if (resume) {
         ck_slot = (uint32_t)(path - Q.total);
@@ -378,6 +450,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         r2 = rec[2];
         r3 = rec[3];
         path = (int64_t)__float_as_uint(r0.x);
+      } else if (kRep && Q.lost_list != nullptr) {
+        path = (int64_t)Q.lost_list[path];  // a path the tape could not hold
       }
       Jp = &job_of(single, Q, path);
       const VolJob& J = *Jp;
@@ -399,7 +473,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       Lo = V3{0, 0, 0};
       Ln = V3{0, 0, 0};
       depth = 0;
-      if (kMode == kAdjoint) ck_lost = false;
+      if (kRad) ck_lost = false;
+      if (kMode == kTape) tref = (kEvCamera << 30) | (uint32_t)path;
       if (kRep) {
         if (kMode == kForward) dL = V3{0.0f, 0.0f, 0.0f};
         const float4 lt = Q.path_ltot[path];
@@ -521,6 +596,17 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           }
         }
         if (kMode == kAdjoint) ck_state = rng.state;
+        if (kMode == kTape && !ck_lost) {
+          // the event's record, written when its shadow walk ends; the walk's
+          // steps refer to it (a path without one is replayed instead)
+          const unsigned long long k = atomicAdd(Q.ckpt_count, 1ull);
+          if ((int64_t)k < Q.ckpt_cap) {
+            tref = (kEvShadow << 30) | (uint32_t)k;
+          } else {
+            ck_lost = true;
+            tref = (kEvCamera << 30) | (uint32_t)path;
+          }
+        }
         // isotropic phase sample (1D unused + 2D), plugins/twostatevolpath.py:275
         pcg_skip1(rng);
         const float pu0 = next1d(rng), pu1 = next1d(rng);
@@ -604,7 +690,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         V3 c2 = mw ? bo : V3{tro, 0.0f, 0.0f};
         float* s = s_coop + (threadIdx.x >> 5) * 96;
         const int f = coop_walk<kMode>(m_coop, mw, Jp, rng, mu, inv_mu, 0.5f * inv_mu, org, dir, tmax, c1, c2, s,
-                                       s + 32, s + 64);
+                                       s + 32, s + 64, Q, tc, tref, ck_lost);
         if (f > 0) {
           if (mw) {
             p = org;
@@ -624,6 +710,13 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       }
     }
 
+    // kTape: this iteration's events, appended below where the warp has
+    // reconverged: a walk step (1: null collision at p, 2: shadow-walk step
+    // at q) with its reference, and the scattering event at p whose shadow
+    // walk ended
+    int ev_kind = 0;
+    uint32_t ev_ref = 0;
+    bool ev_scat = false;
     // --------------------------------------------------- free-flight step
     if (phase == kMain || phase == kNee || phase == kNeeAdj) {
       const VolJob& J = *Jp;
@@ -712,6 +805,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               }
               p = x;
               t_rem = t_rem - t;
+              if (kMode == kTape) {
+                ev_kind = 1;
+                ev_ref = tref;
+              }
             } else {
               // real scattering event (plugins/twostatevolpath.py:249-253)
               depth += 1;
@@ -754,6 +851,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             if (kMode == kTwoState) tro = tro * ((mu_c - st_o) * inv_c);
             q = x;
             tr_rem = tr_rem - t;
+            if (kMode == kTape) {
+              ev_kind = 2;
+              ev_ref = tref;
+            }
             done = (kMode == kTwoState) ? (trn == 0.0f && tro == 0.0f) : (trn == 0.0f);
           }
           if (done) {
@@ -771,6 +872,18 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
                 write_checkpoint(Q.ckpt + slot * 4, (uint32_t)path, depth, ck_state, p, bn, Ln, cn);
               else
                 ck_lost = true;
+            }
+            if (kMode == kTape && (tref >> 30) == kEvShadow) {
+              // the scattering event's record: its path, the radiance gathered
+              // before its NEE contribution, and that contribution; the event
+              // itself goes on the tape, and the next segment's null
+              // collisions refer to the record too
+              const uint32_t k = tref & kTapeIndexMask;
+              float4* rec = Q.ckpt + (int64_t)k * 2;
+              rec[0] = make_float4(__uint_as_float((uint32_t)path), Ln.x, Ln.y, Ln.z);
+              rec[1] = make_float4(cn.x, cn.y, cn.z, 0.0f);
+              ev_scat = true;
+              tref = (kEvSegment << 30) | k;
             }
             Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
             if (kRep) Lrem = V3{Lrem.x - cn.x, Lrem.y - cn.y, Lrem.z - cn.z};
@@ -830,6 +943,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       }
     }
 
+    if (kMode == kTape) {
+      if (!tape_append(Q, tc, ev_kind != 0 && !ck_lost, ev_kind == 2 ? q : p, ev_ref)) ck_lost = true;
+      if (!tape_append(Q, tc, ev_scat && !ck_lost, p, (kEvScatter << 30) | (tref & kTapeIndexMask))) ck_lost = true;
+    }
+
     // -------------------------------------------------------------- path end
     if (finished) {
       if (kMode == kTwoState || kMode == kSingle) {
@@ -837,7 +955,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
         o[0] = make_float4(Ln.x, Ln.y, Ln.z, 0.0f);
         if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
       }
-      if (kMode == kAdjoint) Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f);
+      if (kRad) Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f);
+      if (kMode == kTape && ck_lost) Q.lost_list[atomicAdd(Q.lost_count, 1ull)] = (uint32_t)path;
       if (kMode == kForward && (dL.x != 0.0f || dL.y != 0.0f || dL.z != 0.0f)) {
         // the task's share of its pixel's derivative (the pixel value is the
         // mean of its samples)
@@ -851,6 +970,11 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       if (Jp->pixel_cost != nullptr) red_add_u32(Jp->pixel_cost + pix, n_iter - iter0);
       phase = kIdle;
     }
+  }
+  if (kMode == kTape) {
+    // the unused slots of the warp's last chunk
+    for (uint32_t i = tc.cur + lane; i < tc.end; i += 32u)
+      Q.tape[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTapeEmpty));
   }
 }
 

@@ -71,7 +71,9 @@ struct TraceVariants {
   static constexpr TraceKernel k[kTraceModes] = {
       trace_kernel<kTwoState, kSG, kCount, kEnv>, trace_kernel<kSingle, kSG, kCount, kEnv>,
       trace_kernel<kAdjoint, kSG, kCount, kEnv>, trace_kernel<kReplay, kSG, kCount, kEnv>,
-      trace_kernel<kForward, kSG, kCount, kEnv>};
+      trace_kernel<kForward, kSG, kCount, kEnv>,
+      // the tape pass needs the global majorant (supergrid launches replay)
+      trace_kernel<kSG ? kAdjoint : kTape, kSG, kCount, kEnv>};
 };
 static const TraceKernel* const kTraceTables[8] = {
     TraceVariants<false, false, false>::k, TraceVariants<true, false, false>::k,
@@ -357,6 +359,7 @@ void warm_launch_config() {
 }
 
 static_assert(kOrderBuckets == kRenderOrderBuckets, "order bucket count mismatch");
+static_assert(int64_t(kTapeChunk) == kTapeChunkSlots, "tape chunk mismatch");
 
 // Fills `order` with the job's pixels, longest expected path first.
 int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, uint32_t* cost, cudaStream_t st) {
@@ -383,14 +386,28 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   std::memset(&Q, 0, sizeof(Q));
   Q.counter = queue_counter;
   Q.path_out = (mode == kTwoState || mode == kSingle) ? path_out : nullptr;
-  if (mode == kAdjoint || mode == kReplay || mode == kForward) {
+  if (mode == kAdjoint || mode == kReplay || mode == kForward || mode == kTape) {
     RCV_REQUIRE(adj != nullptr && adj->ckpt && adj->ckpt_count && adj->path_ltot, "adjoint buffers missing");
     RCV_REQUIRE(total < (int64_t(1) << 32), "an adjoint launch must have fewer than 2^32 paths");
     Q.ckpt = adj->ckpt;
     Q.ckpt_count = adj->ckpt_count;
     Q.ckpt_cap = adj->ckpt_cap;
     Q.path_ltot = adj->path_ltot;
+    if (adj->tape != nullptr) {
+      // tape pass, or the replay of the paths it lost
+      RCV_REQUIRE(mode == kTape || mode == kReplay, "the tape serves the gradient only");
+      RCV_REQUIRE(total < (int64_t(1) << 30) && adj->ckpt_cap < (int64_t(1) << 30) &&
+                      adj->tape_cap <= (int64_t(1) << 32) - int64_t(kTapeChunk),
+                  "too many paths for the tape adjoint");
+      RCV_REQUIRE(!supergrid && jobs == nullptr && J.sg[0] == 0, "the tape adjoint needs one job and the global majorant");
+      Q.tape = adj->tape;
+      Q.tape_count = adj->tape_count;
+      Q.tape_cap = adj->tape_cap;
+      Q.lost_list = adj->lost_list;
+      Q.lost_count = adj->lost_count;
+    }
   }
+  RCV_REQUIRE(mode != kTape || Q.tape != nullptr, "the tape pass needs a tape");
   Q.counters = reinterpret_cast<unsigned long long*>(counters);
   Q.jobs = jobs;
   Q.njobs = njobs;
@@ -613,14 +630,40 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
   unsigned long long* qc = reinterpret_cast<unsigned long long*>(ws + L.counter);
   if (mode == kAdjoint) {
     AdjBuffers A;
+    std::memset(&A, 0, sizeof(A));
     A.ckpt = reinterpret_cast<float4*>(ws + L.ckpt);
     A.ckpt_count = qc + 1;
     A.ckpt_cap = ckpt_capacity(J.path_count);
     A.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
+    const int adjoint = o == nullptr ? RCV_ADJOINT_TAPE : o->adjoint;
+    const int per_path = (o == nullptr || o->tape_events_per_path == 0) ? int(kTapeSlotsPerPath)
+                                                                      : o->tape_events_per_path;
+    RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
+    RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
+                int(kTapeSlotsPerPath));
+    // the tape serves the gradient of single jobs with the global majorant;
+    // forward mode gathers along replayed segments
+    const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward && J.sg[0] == 0;
+    if (tape) {
+      A.tape = reinterpret_cast<float4*>(ws + L.tape);
+      A.tape_count = qc + 2;
+      A.tape_cap = tape_capacity(J.path_count, per_path);
+      A.lost_list = reinterpret_cast<uint32_t*>(ws + L.lost);
+      A.lost_count = qc + 3;
+    }
     if (stage != kAdjReplay) {
-      RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, sizeof(unsigned long long), st), "checkpoint reset");
-      rc = launch_persistent(kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters, st, false);
+      RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, 3 * sizeof(unsigned long long), st), "adjoint counters reset");
+      rc = launch_persistent(tape ? kTape : kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters,
+                             st, false);
       if (rc || stage == kAdjRadiance) return rc;
+    }
+    if (tape) {
+      // weights of the event records: the second half of the checkpoint buffer
+      float4* weights = reinterpret_cast<float4*>(ws + L.ckpt + uint64_t(A.ckpt_cap) * 32u);
+      rc = launch_tape_gradient(J, A, weights, reinterpret_cast<float*>(ws + L.cam_w), J.path_count, counters,
+                                sm_count(), st);
+      if (rc) return rc;
+      // the paths whose events did not fit, replayed whole
     }
     return launch_persistent(stage == kAdjForward ? kForward : kReplay, J, nullptr, 0, J.path_count, o, qc,
                              nullptr, &A, counters, st, false);

@@ -104,18 +104,43 @@ struct Queue {
   int32_t defer;                 // lanes that must wait before a deferred branch runs
   int32_t pad;
   // adjoint: scatter checkpoints (4 float4 each), how many were claimed (may
-  // exceed the capacity) and per-path (total radiance, checkpoint-lost flag)
+  // exceed the capacity) and per-path (total radiance, lost flag)
   float4* ckpt;
   unsigned long long* ckpt_count;
   int64_t ckpt_cap;
   float4* path_ltot;
+  // kTape: the gradient-event tape (one float4 per event: position, reference)
+  // with its claimed slots (whole chunks; may exceed the capacity), the
+  // event records (2 float4 each, in the checkpoint buffer, counted by
+  // ckpt_count) and the paths whose events did not fit.  kReplay with a lost
+  // list replays only the paths on it.
+  float4* tape;
+  unsigned long long* tape_count;
+  int64_t tape_cap;
+  uint32_t* lost_list;
+  unsigned long long* lost_count;
 };
 
 // kForward: the replay tasks of kReplay, gathering a tangent field at every
 // gradient event (forward-mode derivative of the image) instead of
 // scattering the image gradient into the grids.
-enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2, kReplay = 3, kForward = 4 };
-constexpr int kTraceModes = 5;
+// kTape: the radiance pass of kAdjoint that, instead of checkpoints, records
+// every gradient event of the path (main-walk null collisions, real
+// scattering events, shadow-walk steps) on a tape; the gradient then comes
+// from one flat pass over the tape (rcv_tape.cu) instead of replay tasks.
+enum TraceMode { kTwoState = 0, kSingle = 1, kAdjoint = 2, kReplay = 3, kForward = 4, kTape = 5 };
+constexpr int kTraceModes = 6;
+
+// Tape events: float4 (x, y, z, ref) with ref = kind << 30 | index.  The
+// index is the path (kEvCamera: null collisions before the first scattering
+// event) or the event record of the last scattering event (kEvSegment: null
+// collisions after its shadow walk; kEvScatter: the event itself; kEvShadow:
+// steps of its shadow walk).  Event record (2 float4): [path, radiance
+// gathered before the event's NEE contribution] [NEE contribution, 0].
+enum TapeEvent : uint32_t { kEvCamera = 0, kEvSegment = 1, kEvScatter = 2, kEvShadow = 3 };
+constexpr uint32_t kTapeIndexMask = 0x3fffffffu;
+constexpr uint32_t kTapeEmpty = 0xffffffffu;  // unused slot at the end of a warp's last chunk
+constexpr uint32_t kTapeChunk = 256;          // slots a warp claims at a time
 
 // Buffers of the two adjoint launches.
 struct AdjBuffers {
@@ -123,6 +148,11 @@ struct AdjBuffers {
   unsigned long long* ckpt_count;
   int64_t ckpt_cap;
   float4* path_ltot;
+  float4* tape;  // null: checkpoints and replay tasks
+  unsigned long long* tape_count;
+  int64_t tape_cap;
+  uint32_t* lost_list;
+  unsigned long long* lost_count;
 };
 
 struct Counts {
@@ -453,5 +483,10 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
 // Queries the occupancy and SM count the launchers cache, so that later
 // launches (e.g. under stream capture) make no device queries.
 void warm_launch_config();
+// Gradient from a kTape radiance pass (rcv_tape.cu): the per-record and
+// per-path weights (`weights`: 2 float4 per record, `cam_w`: one float per
+// path) and the scatter of every tape event into J's gradient records.
+int launch_tape_gradient(const VolJob& J, const AdjBuffers& A, float4* weights, float* cam_w, int64_t paths,
+                         uint64_t* counters, int sms, cudaStream_t st);
 
 }  // namespace rcv

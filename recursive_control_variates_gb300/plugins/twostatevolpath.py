@@ -45,6 +45,15 @@ class _VolumeIntegratorBase:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         # run the adjoint's radiance pass beside the primal render (rcv.render)
         self.overlap_adjoint = bool(props.get("overlap_adjoint", True))
+        # gradient from an event tape of the radiance pass ("tape") or from
+        # replayed path segments ("replay"); the same gradient either way
+        adjoint = props.get("adjoint", "tape")
+        if adjoint not in _lib.ADJOINTS:
+            raise ValueError(f"unknown adjoint {adjoint!r}")
+        self.adjoint = _lib.ADJOINTS[adjoint]
+        self.tape_events_per_path = int(props.get("tape_events_per_path", 0))
+        if not 0 <= self.tape_events_per_path <= 16:
+            raise ValueError("tape_events_per_path must be in [0, 16]")
         # accumulate the RCV_COUNTER_* event counts into counters() (the
         # counting tracer variants hold the counts in registers)
         self.count_events = bool(props.get("count_events", False))
@@ -67,6 +76,8 @@ class _VolumeIntegratorBase:
         o.blocks_per_sm = self.blocks_per_sm
         o.defer = self.defer
         o.order = self.order
+        o.adjoint = self.adjoint
+        o.tape_events_per_path = self.tape_events_per_path
         env = scene.envmap() if scene is not None and hasattr(scene, "envmap") else None
         o.envmap = C.addressof(env.c_struct()) if env is not None else None
         return o
