@@ -252,17 +252,27 @@ class Job:
         return self.cfg.paths_per_step()
 
 
-def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj) -> dict:
+def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj, tape: bool = True) -> dict:
     """Algorithmic bytes per launch of the two tracer kernels from the device
-    counters (lookups, scatters, gradient events) of one step."""
+    counters (lookups, scatters, gradient events) of one step.
+
+    Two-state pass: 64 B per density lookup (8 corners x 2 states), 192 B of
+    albedo per real scattering event, 24 B of film per pixel.  Adjoint: 32 B
+    per density lookup of its passes, 32 B per gradient reduction (8 corners),
+    96 B of albedo read and 96 B reduced per scattering event, 12 B of dL per
+    pixel.  With the tape the gradient pass re-reads the density at each
+    gradient event (32 B; the replay's lookups are counted as lookups) and
+    moves the event through the tape (16 B written, 16 B read)."""
     lookups2 = float(c_two[1] + c_two[2])
     scat2 = float(c_two[3])
     npix = cfg.res * cfg.res
     two = 64.0 * lookups2 + (192.0 * scat2 if has_albedo else 0.0) + 24.0 * npix
     lookups_a = float(c_adj[1] + c_adj[2])
     scat_a = float(c_adj[3])
-    adj = (32.0 * lookups_a + 32.0 * float(c_adj[4]) + (96.0 * scat_a + 96.0 * float(c_adj[5]) if has_albedo else 0.0)
-           + 12.0 * npix)
+    ge, ae = float(c_adj[4]), float(c_adj[5])
+    per_event = 32.0 + (32.0 + 32.0 if tape else 0.0)
+    albedo = 96.0 * scat_a + (96.0 + 96.0 if tape else 96.0) * ae
+    adj = 32.0 * lookups_a + per_event * ge + (albedo if has_albedo else 0.0) + 12.0 * npix
     return {"trace_twostate": two, "trace_adjoint": adj}
 
 
@@ -328,7 +338,7 @@ def run_ours(args, cfg):
     # the counters mix both tracers; split with a separate 1-step measurement
     c_two, c_adj = split_counters(job)
     delta = (c_two + c_adj).astype(np.float64)  # event counts of one step (counted separately)
-    algo = algorithmic_bytes(cfg, job.has_albedo, c_two, c_adj)
+    algo = algorithmic_bytes(cfg, job.has_albedo, c_two, c_adj, tape=job.integrator.integrator.adjoint == 0)
     dom = max(("trace_twostate", "trace_adjoint"), key=lambda k: kern_serial.get(k, {}).get("total_ms", 0.0))
     peaks = measured_peaks()
     dur_s = kern_serial[dom]["mean_ms"] / 1e3

@@ -313,6 +313,8 @@ class LaunchOptions:
     defer: int = 8           # lanes that must wait before a deferred branch runs
     order: str = "cost"      # pixel hand-out order: cost | longest_first | row_major
     count_events: bool = False  # accumulate the tracer event counts (counters())
+    adjoint: str = "tape"    # gradient from the event tape | replayed segments ("replay")
+    tape_events_per_path: int = 0  # tape slots per path, 0 = 16 (testing: fewer, paths are replayed)
 
     def c_struct(self) -> _lib.VolpathOptions:
         o = _lib.VolpathOptions()
@@ -321,6 +323,10 @@ class LaunchOptions:
         if self.order not in _lib.ORDERS:
             raise ValueError(f"unknown pixel order {self.order!r}")
         o.order = _lib.ORDERS[self.order]
+        if self.adjoint not in _lib.ADJOINTS:
+            raise ValueError(f"unknown adjoint {self.adjoint!r}")
+        o.adjoint = _lib.ADJOINTS[self.adjoint]
+        o.tape_events_per_path = self.tape_events_per_path
         return o
 
 

@@ -374,11 +374,13 @@ static int validate_job(const rcv_batch_job* j, int idx) {
 }
 
 // Plan workspace: entries | two-state jobs | adjoint jobs | block prefixes |
-// queue counters (two-state, adjoint radiance, replay, checkpoints) | tracer
-// counters | per-path radiance | adjoint per-path total radiance |
-// scatter checkpoints.
+// queue counters (two-state, adjoint radiance, replay, checkpoints / event
+// records, tape slots, lost paths) | tracer counters | per-path radiance |
+// adjoint per-path total radiance | scatter checkpoints (tape: event records
+// and their weights) | event tape | per-path camera-segment weights |
+// lost-path list.
 struct PlanLayout {
-  uint64_t entries, two, adj, prefix, queue, counters, path_out, ltot, ckpt, total;
+  uint64_t entries, two, adj, prefix, queue, counters, path_out, ltot, ckpt, tape, cam_w, lost, total;
 };
 
 static PlanLayout plan_layout(int n, int64_t total_two_paths, int64_t total_adj_paths) {
@@ -393,7 +395,7 @@ static PlanLayout plan_layout(int n, int64_t total_two_paths, int64_t total_adj_
   L.prefix = off;
   off = align256(off + 4u * uint64_t(n + 1) * sizeof(int32_t));
   L.queue = off;
-  off = align256(off + 4u * sizeof(unsigned long long));
+  off = align256(off + 8u * sizeof(unsigned long long));
   L.counters = off;
   off = align256(off + 2u * RCV_COUNTER_COUNT * sizeof(uint64_t));
   L.path_out = off;
@@ -402,6 +404,12 @@ static PlanLayout plan_layout(int n, int64_t total_two_paths, int64_t total_adj_
   off = align256(off + uint64_t(total_adj_paths) * 16u);
   L.ckpt = off;
   off = align256(off + uint64_t(ckpt_capacity(total_adj_paths)) * 64u);
+  L.tape = off;
+  off = align256(off + uint64_t(tape_capacity(total_adj_paths, kTapeSlotsPerPath)) * 16u);
+  L.cam_w = off;
+  off = align256(off + uint64_t(total_adj_paths) * 8u);
+  L.lost = off;
+  off = align256(off + uint64_t(total_adj_paths) * 4u);
   L.total = off;
   return L;
 }
@@ -452,6 +460,9 @@ struct rcv_batch {
   uint64_t* counters = nullptr;
   float4* path_out = nullptr;
   AdjBuffers adjbuf{};
+  bool tape = false;  // gradient from the event tape (else replay tasks)
+  float4* tape_weights = nullptr;
+  float2* cam_w = nullptr;
   int64_t total_two = 0, total_adj = 0;
   int32_t pack_blocks = 0, pix_blocks = 0, vox_blocks = 0, sg_blocks = 0;
   // host copies of the tables (kept until destroy: the upload reads them)
@@ -524,6 +535,10 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     RCV_REQUIRE(opts->batch >= 0 && opts->batch <= (1 << 20), "batch must be in [0, 2^20]");
     RCV_REQUIRE(opts->defer >= 0 && opts->defer <= 32, "defer must be in [0, 32]");
     RCV_REQUIRE(opts->blocks_per_sm >= 0, "blocks_per_sm must be >= 0");
+    RCV_REQUIRE(opts->adjoint == RCV_ADJOINT_TAPE || opts->adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d",
+                opts->adjoint);
+    RCV_REQUIRE(opts->tape_events_per_path >= 0 && opts->tape_events_per_path <= kTapeSlotsPerPath,
+                "tape_events_per_path must be in [0, %d]", int(kTapeSlotsPerPath));
   }
   const uint64_t need = rcv_batch_workspace_bytes(jobs, n);
   RCV_REQUIRE(need > 0 && workspace_bytes >= need, "batch workspace too small: %llu bytes, need %llu",
@@ -640,6 +655,18 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->adjbuf.ckpt_count = b->queue + 3;
   b->adjbuf.ckpt_cap = ckpt_capacity(adj_total);
   b->adjbuf.path_ltot = reinterpret_cast<float4*>(w + P.ltot);
+  // the tape needs every job on its global majorant
+  b->tape = b->opt.adjoint == RCV_ADJOINT_TAPE && sg_blocks == 0 && adj_total < (int64_t(1) << 29);
+  if (b->tape) {
+    const int per_path = b->opt.tape_events_per_path > 0 ? b->opt.tape_events_per_path : int(kTapeSlotsPerPath);
+    b->adjbuf.tape = reinterpret_cast<float4*>(w + P.tape);
+    b->adjbuf.tape_count = b->queue + 4;
+    b->adjbuf.tape_cap = tape_capacity(adj_total, per_path);
+    b->adjbuf.lost_list = reinterpret_cast<uint32_t*>(w + P.lost);
+    b->adjbuf.lost_count = b->queue + 5;
+    b->tape_weights = reinterpret_cast<float4*>(w + P.ckpt + uint64_t(b->adjbuf.ckpt_cap) * 32u);
+    b->cam_w = reinterpret_cast<float2*>(w + P.cam_w);
+  }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemcpyAsync(b->entries, b->h_entries.data(), sizeof(BatchEntry) * n, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
@@ -701,11 +728,13 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   // stream beside the two-state pass and the image kernel
   RCV_TRY_CUDA(cudaEventRecord(b->fork, st), "fork record");
   RCV_TRY_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "fork wait");
-  RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, sizeof(unsigned long long), b->side), "checkpoint reset");
+  // checkpoint / event-record, tape-slot and lost-path counters
+  RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, 3 * sizeof(unsigned long long), b->side),
+               "adjoint counters reset");
   // event counts only when asked for: the counting tracers hold the counts in registers
   uint64_t* cnt = b->opt.count_events ? b->counters : nullptr;
-  rc = launch_persistent(kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr, &b->adjbuf,
-                         cnt ? cnt + RCV_COUNTER_COUNT : nullptr, b->side, sg);
+  rc = launch_persistent(b->tape ? kTape : kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr,
+                         &b->adjbuf, cnt ? cnt + RCV_COUNTER_COUNT : nullptr, b->side, sg);
   if (rc) return rc;
   RCV_TRY_CUDA(cudaEventRecord(b->join, b->side), "join record");
   rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr,
@@ -715,6 +744,12 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   rc = launched("batch image launch");
   if (rc) return rc;
   RCV_TRY_CUDA(cudaStreamWaitEvent(st, b->join, 0), "join wait");
+  if (b->tape) {
+    // the gradient from the tape; the replay then takes only the lost paths
+    rc = launch_tape_gradient(none, b->adj, n, b->adjbuf, b->tape_weights, b->cam_w, b->total_adj,
+                              cnt ? cnt + RCV_COUNTER_COUNT : nullptr, tracer_sm_count(), st);
+    if (rc) return rc;
+  }
   rc = launch_persistent(kReplay, none, b->adj, n, b->total_adj, &b->opt, b->queue + 2, nullptr, &b->adjbuf,
                          cnt ? cnt + RCV_COUNTER_COUNT : nullptr, st, sg);
   if (rc) return rc;
@@ -758,7 +793,7 @@ extern "C" uint64_t* rcv_batch_counters(rcv_batch* b) { return b != nullptr ? b-
 
 extern "C" int32_t rcv_batch_kernels_per_step(const rcv_batch* b) {
   if (b == nullptr) return RCV_ERR_INVALID;
-  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0) + (b->sg_blocks > 0 ? 1 : 0);
+  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0) + (b->sg_blocks > 0 ? 1 : 0) + (b->tape ? 2 : 0);
 }
 
 extern "C" int rcv_batch_destroy(rcv_batch* b) {

@@ -157,7 +157,7 @@ inline RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
   L.ckpt = align256(L.ltot + (adj ? uint64_t(paths) * 16u : 0u));
   L.tape = align256(L.ckpt + (adj ? uint64_t(ckpt_capacity(paths)) * 64u : 0u));
   L.cam_w = align256(L.tape + (adj ? uint64_t(tape_capacity(paths, kTapeSlotsPerPath)) * 16u : 0u));
-  L.lost = align256(L.cam_w + (adj ? uint64_t(paths) * 4u : 0u));
+  L.lost = align256(L.cam_w + (adj ? uint64_t(paths) * 8u : 0u));
   L.total = align256(L.lost + (adj ? uint64_t(paths) * 4u : 0u));
   return L;
 }

@@ -20,11 +20,27 @@
 //                          shadow-walk step -scale * (dL . c_nee) / sigma_n
 //                                            (where sigma_n > 0)
 // Events of a path that lost an event or a record are skipped; kReplay
-// replays that path whole.
+// replays that path whole.  Batched launches find each event's job through
+// its path (binary search in the job table, once per record and path).
 #include "rcv_common.h"
 #include "rcv_volume.cuh"
 
 namespace rcv {
+
+// Job of a global path index: the single job, or a binary search in the
+// launch's job table (batched launches).
+__device__ __forceinline__ int tape_job(const VolJob* jobs, int njobs, uint32_t path) {
+  if (jobs == nullptr) return 0;
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].path_begin <= (int64_t)path)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
 
 // Pixel of a path of the job (the hand-out order maps the k-th pixel slot).
 __device__ __forceinline__ int tape_pixel(const VolJob& J, uint32_t path) {
@@ -41,12 +57,14 @@ __device__ __forceinline__ V3 tape_dL(const VolJob& J, int pix) {
 // Record k (2 float4: [path, radiance gathered before the event's NEE
 // contribution] [NEE contribution]) -> weights [dL . L_rem after the NEE
 // contribution (the next segment), dL . c_nee (the shadow walk), dL . L_rem
-// (the event), skip] [dL * L_rem per channel (the event's albedo)].  Path p ->
-// dL . L (its camera segment), or NaN when the path is replayed instead.
-__global__ void tape_weights_kernel(const __grid_constant__ VolJob J, const float4* __restrict__ rec,
+// (the event), job] [dL * L_rem per channel (the event's albedo)].  Path p ->
+// [dL . L (its camera segment), job].  Job -1: the path is replayed instead
+// and its events are skipped.
+__global__ void tape_weights_kernel(const __grid_constant__ VolJob single, const VolJob* __restrict__ jobs,
+                                    int njobs, const float4* __restrict__ rec,
                                     const unsigned long long* __restrict__ rec_count, int64_t rec_cap,
-                                    float4* __restrict__ w, const float4* __restrict__ ltot, float* __restrict__ cam_w,
-                                    int64_t paths) {
+                                    float4* __restrict__ w, const float4* __restrict__ ltot,
+                                    float2* __restrict__ cam_w, int64_t paths) {
   const int64_t nrec = min((int64_t)*rec_count, rec_cap);
   const int64_t n = max(nrec, paths);
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
@@ -55,39 +73,43 @@ __global__ void tape_weights_kernel(const __grid_constant__ VolJob J, const floa
       const uint32_t path = __float_as_uint(r0.x);
       const float4 lt = ltot[path];
       if (lt.w != 0.0f) {
-        w[2 * i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        w[2 * i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
       } else {
+        const int j = tape_job(jobs, njobs, path);
+        const VolJob& J = jobs != nullptr ? jobs[j] : single;
         const V3 g = tape_dL(J, tape_pixel(J, path));
         const V3 lr{lt.x - r0.y, lt.y - r0.z, lt.z - r0.w};
         const V3 ls{lr.x - r1.x, lr.y - r1.y, lr.z - r1.z};
         const float s_event = (g.x * lr.x + g.y * lr.y) + g.z * lr.z;
         const float s_next = (g.x * ls.x + g.y * ls.y) + g.z * ls.z;
         const float s_nee = (g.x * r1.x + g.y * r1.y) + g.z * r1.z;
-        w[2 * i] = make_float4(s_next, s_nee, s_event, 0.0f);
+        w[2 * i] = make_float4(s_next, s_nee, s_event, __int_as_float(j));
         w[2 * i + 1] = make_float4(g.x * lr.x, g.y * lr.y, g.z * lr.z, 0.0f);
       }
     }
     if (i < paths) {
       const float4 lt = ltot[i];
-      float s = __int_as_float(0x7fc00000);  // NaN: skip
+      float2 c = make_float2(0.0f, __int_as_float(-1));
       if (lt.w == 0.0f) {
+        const int j = tape_job(jobs, njobs, (uint32_t)i);
+        const VolJob& J = jobs != nullptr ? jobs[j] : single;
         const V3 g = tape_dL(J, tape_pixel(J, (uint32_t)i));
-        s = (g.x * lt.x + g.y * lt.y) + g.z * lt.z;
+        c = make_float2((g.x * lt.x + g.y * lt.y) + g.z * lt.z, __int_as_float(j));
       }
-      cam_w[i] = s;
+      cam_w[i] = c;
     }
   }
 }
 
 template <bool kCount>
-__global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant__ VolJob J,
+__global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant__ VolJob single,
+                                                           const VolJob* __restrict__ jobs,
                                                            const float4* __restrict__ tape,
                                                            const unsigned long long* __restrict__ tape_count,
                                                            int64_t tape_cap, const float4* __restrict__ w,
-                                                           const float* __restrict__ cam_w,
+                                                           const float2* __restrict__ cam_w,
                                                            unsigned long long* counters) {
   const int64_t n = min((int64_t)*tape_count, tape_cap);
-  const float mu = J.scale * bits_to_float(__ldg(J.maxbits + 1));
   uint32_t ge = 0, ae = 0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const float4 ev = __ldcs(tape + i);
@@ -95,14 +117,18 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
     if (ref == kTapeEmpty) continue;
     const uint32_t kind = ref >> 30, idx = ref & kTapeIndexMask;
     float s;
+    int j;
     if (kind == kEvCamera) {
-      s = __ldg(cam_w + idx);
-      if (s != s) continue;
+      const float2 c = __ldg(cam_w + idx);
+      s = c.x;
+      j = __float_as_int(c.y);
     } else {
       const float4 wr = __ldg(w + 2 * (int64_t)idx);
-      if (wr.w != 0.0f) continue;
       s = kind == kEvSegment ? wr.x : (kind == kEvShadow ? wr.y : wr.z);
+      j = __float_as_int(wr.w);
     }
+    if (j < 0) continue;
+    const VolJob& J = jobs != nullptr ? jobs[j] : single;
     const V3 x{ev.x, ev.y, ev.z};
     const Lookup lk = locate(J, x);
     const float st_n = J.scale * density_new(J, lk);
@@ -118,7 +144,8 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
         if (kCount) ++ae;
       }
     } else {
-      const float sn = mu - st_n;
+      // the walk's majorant: the job's global one (tape launches have no supergrid)
+      const float sn = J.scale * bits_to_float(__ldg(J.maxbits + 1)) - st_n;
       if (kind != kEvShadow || sn > 0.0f) {
         scatter_density(J, lk, -(J.scale * s) / sn);
         if (kCount) ++ge;
@@ -135,19 +162,21 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
   }
 }
 
-int launch_tape_gradient(const VolJob& J, const AdjBuffers& A, float4* weights, float* cam_w, int64_t paths,
-                         uint64_t* counters, int sms, cudaStream_t st) {
+int launch_tape_gradient(const VolJob& single, const VolJob* jobs, int njobs, const AdjBuffers& A, float4* weights,
+                         float2* cam_w, int64_t paths, uint64_t* counters, int sms, cudaStream_t st) {
   const int block = 256;
   tape_weights_kernel<<<grid_for(A.ckpt_cap > paths ? A.ckpt_cap : paths, block), block, 0, st>>>(
-      J, A.ckpt, A.ckpt_count, A.ckpt_cap, weights, A.path_ltot, cam_w, paths);
+      single, jobs, njobs, A.ckpt, A.ckpt_count, A.ckpt_cap, weights, A.path_ltot, cam_w, paths);
   int rc = launched("tape_weights launch");
   if (rc) return rc;
   const unsigned grid = (unsigned)(sms > 0 ? sms : 1) * 8u;
   unsigned long long* c = reinterpret_cast<unsigned long long*>(counters);
   if (counters != nullptr)
-    tape_scatter_kernel<true><<<grid, block, 0, st>>>(J, A.tape, A.tape_count, A.tape_cap, weights, cam_w, c);
+    tape_scatter_kernel<true><<<grid, block, 0, st>>>(single, jobs, A.tape, A.tape_count, A.tape_cap, weights,
+                                                       cam_w, c);
   else
-    tape_scatter_kernel<false><<<grid, block, 0, st>>>(J, A.tape, A.tape_count, A.tape_cap, weights, cam_w, c);
+    tape_scatter_kernel<false><<<grid, block, 0, st>>>(single, jobs, A.tape, A.tape_count, A.tape_cap, weights,
+                                                        cam_w, c);
   return launched("tape_scatter launch");
 }
 

@@ -353,6 +353,8 @@ static int sm_count() {
   return n;
 }
 
+int tracer_sm_count() { return sm_count(); }
+
 void warm_launch_config() {
   (void)resident_blocks(0);
   (void)sm_count();
@@ -399,7 +401,7 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
       RCV_REQUIRE(total < (int64_t(1) << 30) && adj->ckpt_cap < (int64_t(1) << 30) &&
                       adj->tape_cap <= (int64_t(1) << 32) - int64_t(kTapeChunk),
                   "too many paths for the tape adjoint");
-      RCV_REQUIRE(!supergrid && jobs == nullptr && J.sg[0] == 0, "the tape adjoint needs one job and the global majorant");
+      RCV_REQUIRE(!supergrid && (jobs != nullptr || J.sg[0] == 0), "the tape adjoint needs the global majorant");
       Q.tape = adj->tape;
       Q.tape_count = adj->tape_count;
       Q.tape_cap = adj->tape_cap;
@@ -660,8 +662,8 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
     if (tape) {
       // weights of the event records: the second half of the checkpoint buffer
       float4* weights = reinterpret_cast<float4*>(ws + L.ckpt + uint64_t(A.ckpt_cap) * 32u);
-      rc = launch_tape_gradient(J, A, weights, reinterpret_cast<float*>(ws + L.cam_w), J.path_count, counters,
-                                sm_count(), st);
+      rc = launch_tape_gradient(J, nullptr, 0, A, weights, reinterpret_cast<float2*>(ws + L.cam_w), J.path_count,
+                                counters, sm_count(), st);
       if (rc) return rc;
       // the paths whose events did not fit, replayed whole
     }

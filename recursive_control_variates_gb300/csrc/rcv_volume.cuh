@@ -483,10 +483,12 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
 // Queries the occupancy and SM count the launchers cache, so that later
 // launches (e.g. under stream capture) make no device queries.
 void warm_launch_config();
-// Gradient from a kTape radiance pass (rcv_tape.cu): the per-record and
-// per-path weights (`weights`: 2 float4 per record, `cam_w`: one float per
-// path) and the scatter of every tape event into J's gradient records.
-int launch_tape_gradient(const VolJob& J, const AdjBuffers& A, float4* weights, float* cam_w, int64_t paths,
-                         uint64_t* counters, int sms, cudaStream_t st);
+// Gradient from a kTape radiance pass (rcv_tape.cu) of one job (jobs ==
+// NULL) or of a device job table: the per-record and per-path weights
+// (`weights`: 2 float4 per record, `cam_w`: one float2 per path) and the
+// scatter of every tape event into its job's gradient records.
+int launch_tape_gradient(const VolJob& single, const VolJob* jobs, int njobs, const AdjBuffers& A, float4* weights,
+                         float2* cam_w, int64_t paths, uint64_t* counters, int sms, cudaStream_t st);
+int tracer_sm_count();
 
 }  // namespace rcv

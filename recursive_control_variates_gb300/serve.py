@@ -90,13 +90,15 @@ class StepServer:
         self._last_ids: tuple = ()
 
     # ------------------------------------------------------------ memory
-    @staticmethod
-    def job_bytes(job: B.CVJob) -> int:
+    def job_bytes(self, job: B.CVJob) -> int:
         """Resident bytes of a job plus the per-path scratch it adds to a tick:
         32 bytes per primal path (radiance slots), 16 + 2 x 64 bytes per
-        gradient path (total radiance, scatter checkpoints)."""
+        gradient path (total radiance, scatter checkpoints or event records
+        and their weights), and with the tape adjoint 16 x 16 + 8 + 4 bytes
+        more (event slots, camera-segment weight, lost-path list)."""
         npix = job.width * job.height
-        return job.nbytes() + 32 * npix * job.spp + 144 * npix * job.spp_grad
+        per_grad = 144 + (268 if self.options.adjoint == "tape" else 0)
+        return job.nbytes() + 32 * npix * job.spp + per_grad * npix * job.spp_grad
 
     def resident_bytes(self) -> int:
         return sum(self.job_bytes(j) for j in self.jobs.values())

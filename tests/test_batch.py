@@ -131,11 +131,11 @@ def test_cfg4_mix_is_seeded_and_in_range():
 
 
 # ------------------------------------------------------------------- GPU
-def plain_setup(device, dens, alb, res, depth, lr, spp):
+def plain_setup(device, dens, alb, res, depth, lr, spp, adjoint="tape"):
     scene = rcv.load_dict(scenes.scene_dict(dens, alb, res=res, spp=spp), device=device)
     params = rcv.traverse(scene)
     integ = rcv.load_dict({"type": "cv", "integrator": {"type": "twostateprbvolpath", "max_depth": depth,
-                                                         "rr_depth": depth}})
+                                                         "rr_depth": depth, "adjoint": adjoint}})
     opt = rcv.ad.Adam(lr=lr)
     opt[scenes.DENSITY_KEY] = dens
     opt.set_bounds(scenes.DENSITY_KEY, 0.0, 250.0)
@@ -224,24 +224,25 @@ def test_batch_matches_plain_api(cuda, use_graph):
 @pytest.mark.gpu
 @pytest.mark.parametrize("use_graph", [False, True])
 def test_single_path_jobs_bitwise_over_many_steps(cuda, use_graph):
-    """With one path per step (1x1 film, spp 1) every gradient atomic of a job
-    comes from one thread in program order, so the whole optimisation is
-    deterministic: parameters, moments, weights, statistics and images of the
-    batched and the plain form stay bit-identical over many steps (this
-    exercises the device-side CV and Adam bias-correction tables, and the
-    batched supergrid of the third job)."""
+    """With one path per step (1x1 film, spp 1) and the replay adjoint every
+    gradient atomic of a job comes from one thread in program order, so the
+    whole optimisation is deterministic: parameters, moments, weights,
+    statistics and images of the batched and the plain form stay
+    bit-identical over many steps (this exercises the device-side CV and
+    Adam bias-correction tables, and the batched supergrid of the third
+    job).  The tape adjoint scatters a path's events from several threads."""
     pairs = []
     for k, (D, agrid, factor) in enumerate([(6, True, 0), (5, False, 0), (12, False, 4)]):
         true = scenes.blob_density(D, 60 + k)
         alb = scenes.albedo_grid(D, 60 + k) if agrid else 0.8
         target = torch.full((1, 1, 3), 0.3 + 0.1 * k, device=cuda)
         alb0 = np.full_like(alb, 0.5) if agrid else alb
-        plain = plain_setup(cuda, (0.5 * true).astype(np.float32), alb0, 1, 16, 0.05, 1)
+        plain = plain_setup(cuda, (0.5 * true).astype(np.float32), alb0, 1, 16, 0.05, 1, adjoint="replay")
         if factor:  # a majorant supergrid on the third job
             plain[0].named_shapes()["object"].interior_medium().set_majorant_resolution_factor(factor)
         job = batch.CVJob.from_scene(*plain, target, spp=1, seed=3 + k, keep_images=True)
         pairs.append((plain, job, target, 3 + k))
-    b = batch.BatchedCV([p[1] for p in pairs], use_graph=use_graph)
+    b = batch.BatchedCV([p[1] for p in pairs], batch.LaunchOptions(adjoint="replay"), use_graph=use_graph)
     for it in range(8):
         b.step()
         for (scene, params, integ, opt), job, target, seed in pairs:
@@ -256,6 +257,30 @@ def test_single_path_jobs_bitwise_over_many_steps(cuda, use_graph):
             assert abs(job.status()["loss"] - loss) <= 1e-6 * max(abs(loss), 1e-30)
     assert pairs[0][1].status()["welford_count"] == 7
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("per_path", [0, 2])
+def test_batch_tape_matches_replay(cuda, per_path):
+    """One batched step with the tape adjoint and one with the replay tasks:
+    the same images, and first Adam moments (the gradients) within the
+    reordering of float atomics; with 2 tape slots per path most paths are
+    replayed whole."""
+    pairs = [build_pair(cuda, k) for k in range(len(JOBS))]
+    jobs_t = [p[1] for p in pairs]
+    jobs_r = [j.clone() for j in jobs_t]
+    bt = batch.BatchedCV(jobs_t, batch.LaunchOptions(tape_events_per_path=per_path), use_graph=False)
+    br = batch.BatchedCV(jobs_r, batch.LaunchOptions(adjoint="replay"), use_graph=False)
+    bt.step()
+    br.step()
+    torch.cuda.synchronize()
+    for a, b in zip(jobs_t, jobs_r):
+        assert torch.equal(a.image(), b.image())
+        assert rel_l2(a.density_m, b.density_m) <= 1e-5
+        if a.albedo_m is not None:
+            assert rel_l2(a.albedo_m, b.albedo_m) <= 1e-5
+    bt.close()
+    br.close()
 
 
 @pytest.mark.gpu

@@ -84,8 +84,14 @@ def fire_all():
 
 
 def test_admission_by_budget(fake_cuda):
-    s = serve.StepServer(1000, device="cpu", clock=lambda: fake_cuda.t)
-    a, b, c = FakeJob(400 - 176), FakeJob(400 - 176), FakeJob(400 - 176)  # 400 B each with scratch
+    s = serve.StepServer(2500, device="cpu", clock=lambda: fake_cuda.t)
+    # per-path scratch of a 1 x 1 x spp 1 job: 32 B primal, 144 B gradient
+    # (total radiance, records), 268 B of tape
+    scratch = s.job_bytes(FakeJob(0))
+    assert scratch == 32 + 144 + 268
+    replay = serve.StepServer(2500, device="cpu", options=serve.B.LaunchOptions(adjoint="replay"))
+    assert replay.job_bytes(FakeJob(0)) == 32 + 144
+    a, b, c = (FakeJob(1000 - scratch) for _ in range(3))  # 1000 B each with scratch
     ja, jb, jc = s.add_job(a), s.add_job(b), s.add_job(c)
     assert s.is_resident(ja) and s.is_resident(jb) and not s.is_resident(jc)
     with pytest.raises(ValueError):
