@@ -216,10 +216,13 @@ int rcv_medium_prepare(const rcv_medium* medium, void* stream);
 
 /* ------------------------------------------------------------- tracers  */
 /* Scratch a tracer call needs (work-queue counter, pixel order, per-pixel
- * cost and, for the primal tracers, one radiance slot per path): 256-B
- * aligned device memory of this size, passed as `workspace`.  The per-pixel
- * cost persists from call to call (RCV_ORDER_COST); pass the same workspace to
- * the calls of one image size.  mode = RCV_MODE_*. */
+ * cost and, for the primal tracers, one radiance slot per path; for the
+ * adjoint 412 B per path: total radiance, 2 scatter checkpoints or event
+ * records with their weights, 16 tape slots of 16 B, camera-segment weight,
+ * lost-path list): 256-B aligned device memory of this size, passed as
+ * `workspace`.  The per-pixel cost persists from call to call
+ * (RCV_ORDER_COST); pass the same workspace to the calls of one image size.
+ * mode = RCV_MODE_*. */
 uint64_t rcv_render_workspace_bytes(int32_t width, int32_t height, int32_t spp, int32_t mode);
 
 /* Two-state primal: renders the previous (img_old = H) and current
@@ -266,11 +269,15 @@ int rcv_render_volume_noalloc(const rcv_medium* medium, const rcv_sensor* sensor
                               const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
                               float* img, uint64_t* counters, void* stream);
 
-/* Seed-replay adjoint on the current parameters: traces `spp` paths per
- * pixel from `seed`, first to obtain each path's radiance and then again to
- * back-propagate grad_img (dLoss/dimage, [height][width][3]) into the density
- * grid (and the albedo grid when the medium has one).  Gradients are ADDED to
- * grad_density ([Dz][Dy][Dx]) and grad_albedo ([Dz][Dy][Dx][3] or NULL).
+/* Path-replay adjoint on the current parameters: traces `spp` paths per
+ * pixel from `seed` to obtain each path's radiance, then back-propagates
+ * grad_img (dLoss/dimage, [height][width][3]) into the density grid (and the
+ * albedo grid when the medium has one) at every event of the paths: from the
+ * event tape the radiance pass recorded (RCV_ADJOINT_TAPE, the default), or
+ * by tracing the paths' segments again from scatter checkpoints
+ * (RCV_ADJOINT_REPLAY, and always with a majorant supergrid).  Gradients are
+ * ADDED to grad_density ([Dz][Dy][Dx]) and grad_albedo ([Dz][Dy][Dx][3] or
+ * NULL).
  * Replaces CVIntegrator.render_backward / MetaIntegrator.render_backward
  * (plugins/cv_integrator.py:87-94, plugins/metaintegrator.py:140-147), i.e.
  * the path-replay adjoint of the wrapped two-state integrator. */
@@ -296,10 +303,10 @@ int rcv_render_forward_volume(const rcv_medium* medium, const rcv_sensor* sensor
                               void* workspace, uint64_t* counters, void* stream);
 
 /* rcv_render_backward_volume in two calls.  The first pass of the adjoint
- * (each path's radiance and its scatter checkpoints) does not depend on
- * grad_img, so it can run as soon as the parameters are known — e.g. on a
- * second stream beside the primal render — and the second call, given
- * grad_img, only replays.  The replay call must get the same medium state,
+ * (each path's radiance and its event tape or scatter checkpoints) does not
+ * depend on grad_img, so it can run as soon as the parameters are known — e.g.
+ * on a second stream beside the primal render — and the second call, given
+ * grad_img, only scatters the tape (or replays).  The replay call must get the same medium state,
  * sensor, options, seed, spp and workspace as the radiance call, and be
  * ordered after it; the pair gives the same gradients as
  * rcv_render_backward_volume. */
@@ -570,8 +577,11 @@ int rcv_batch_job_init(const rcv_batch_job* job, void* stream);
 
 typedef struct rcv_batch rcv_batch; /* opaque host handle of a batch plan */
 
-/* Shared device scratch of a batch: job tables and the per-path radiance of
- * the two-state launch (32 bytes per primal path of all jobs). */
+/* Shared device scratch of a batch: job tables, the per-path radiance of the
+ * two-state launch (32 bytes per primal path of all jobs) and the adjoint's
+ * per-path scratch (412 bytes per gradient path, as for
+ * rcv_render_workspace_bytes).  opts->adjoint selects the tape or the replay
+ * tasks for the whole batch; a batch with a majorant supergrid replays. */
 uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n);
 /* Plans a batch of n initialised jobs with launch options `opts` (batch,
  * blocks_per_sm, defer, order; max_depth / rr_depth / hide_emitters come from
