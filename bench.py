@@ -260,9 +260,10 @@ def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj, tape: bool = True) ->
     albedo per real scattering event, 24 B of film per pixel.  Adjoint: 32 B
     per density lookup of its passes, 32 B per gradient reduction (8 corners),
     96 B of albedo read and 96 B reduced per scattering event, 12 B of dL per
-    pixel.  With the tape the gradient pass re-reads the density at each
-    gradient event (32 B; the replay's lookups are counted as lookups) and
-    moves the event through the tape (16 B written, 16 B read)."""
+    pixel.  With the tape the gradient pass reads the density (and albedo) at
+    each gradient event again (the replay's lookups are counted as lookups);
+    the tape itself (16 B written and read per event) is intermediate
+    storage and not counted."""
     lookups2 = float(c_two[1] + c_two[2])
     scat2 = float(c_two[3])
     npix = cfg.res * cfg.res
@@ -270,7 +271,7 @@ def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj, tape: bool = True) ->
     lookups_a = float(c_adj[1] + c_adj[2])
     scat_a = float(c_adj[3])
     ge, ae = float(c_adj[4]), float(c_adj[5])
-    per_event = 32.0 + (32.0 + 32.0 if tape else 0.0)
+    per_event = 32.0 + (32.0 if tape else 0.0)
     albedo = 96.0 * scat_a + (96.0 + 96.0 if tape else 96.0) * ae
     adj = 32.0 * lookups_a + per_event * ge + (albedo if has_albedo else 0.0) + 12.0 * npix
     return {"trace_twostate": two, "trace_adjoint": adj}
