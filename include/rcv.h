@@ -399,7 +399,11 @@ int rcv_render_surface(const rcv_surface_scene* scene, const rcv_sensor* sensor,
 /* Path-replay adjoint of the surface render on `new`: ADDS dLoss/dtexture to
  * grad_texture ([tex_height][tex_width][3]); replaces
  * CVIntegrator.render_backward with a twostateprb integrator
- * (plugins/cv_integrator.py:87-94, Mitsuba PRBIntegrator.render_backward). */
+ * (plugins/cv_integrator.py:87-94, Mitsuba PRBIntegrator.render_backward).
+ * opts->adjoint: RCV_ADJOINT_TAPE traces each path once, recording its
+ * texture vertices (2 of the 16 tape slots per path each), and scatters them
+ * once L is known; RCV_ADJOINT_REPLAY traces each path a second time.
+ * Scratch: rcv_render_workspace_bytes(..., RCV_MODE_ADJOINT). */
 int rcv_render_backward_surface(const rcv_surface_scene* scene, const rcv_sensor* sensor,
                                 const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
                                 const float* grad_img, float* grad_texture, void* workspace,

@@ -132,17 +132,70 @@ __global__ void pack_texture_tangent_kernel(int64_t n, const float* __restrict__
   out[i] = make_float4(t[i * 3 + 0], t[i * 3 + 1], t[i * 3 + 2], 0.0f);
 }
 
+// Gradient from the surface tape: per recorded texture vertex (2 float4:
+// [x, z, path, 0] [radiance gathered before the vertex]),
+// dL * (L - gathered) / albedo scattered bilinearly into the texels, as the
+// replay pass of kAdjoint does at the same vertex.  Vertices of paths that
+// lost one are skipped (the replay takes those paths).
+__global__ void __launch_bounds__(256) surface_tape_scatter_kernel(const __grid_constant__ SurfJob S,
+                                                                   const float4* __restrict__ tape,
+                                                                   const unsigned long long* __restrict__ tape_count,
+                                                                   int64_t tape_cap,
+                                                                   const float4* __restrict__ ltot) {
+  const int64_t n = min((int64_t)*tape_count, tape_cap) / 2;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const float4 a = __ldcs(tape + 2 * i);
+    if (__float_as_uint(a.w) == kTapeEmpty) continue;
+    const float4 b = __ldcs(tape + 2 * i + 1);
+    const uint32_t path = __float_as_uint(a.z);
+    const float4 lt = __ldg(ltot + path);
+    if (lt.w != 0.0f) continue;
+    const int pix = (int)(path / (uint32_t)S.spp);
+    const float fs = (float)S.spp;
+    const float* g = S.grad_img + (int64_t)pix * 3;
+    const V3 dL{g[0] / fs, g[1] / fs, g[2] / fs};
+    const TexLookup tl = tex_locate(S, V3{a.x, 0.0f, a.y});
+    const V3 an = tex_eval(S, tl, 1);
+    const V3 lr{lt.x - b.x, lt.y - b.y, lt.z - b.z};
+    tex_scatter(S, tl,
+                V3{(dL.x * lr.x) / fmaxf(an.x, 1e-8f), (dL.y * lr.y) / fmaxf(an.y, 1e-8f),
+                   (dL.z * lr.z) / fmaxf(an.z, 1e-8f)});
+  }
+}
+
 static int surf_resident_blocks(int mode) {
   static std::once_flag once;
-  static int blocks[4] = {1, 1, 1, 1};
+  static int blocks[5] = {1, 1, 1, 1, 1};
   std::call_once(once, [] {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[0], trace_surface_kernel<kTwoState>, kSurfBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[1], trace_surface_kernel<kSingle>, kSurfBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[2], trace_surface_kernel<kAdjoint>, kSurfBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[3], trace_surface_kernel<kForward>, kSurfBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks[4], trace_surface_kernel<kTape>, kSurfBlock, 0);
     for (int& b : blocks) b = b < 1 ? 1 : b;
   });
-  return blocks[mode == kForward ? 3 : mode];
+  return blocks[mode == kForward ? 3 : (mode == kTape ? 4 : mode)];
+}
+
+static int launch_surface(int mode, const SurfJob& S, const Queue& Q, const rcv_volpath_options* o,
+                          cudaStream_t st) {
+  RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
+  int dev = 0, sms = 1;
+  RCV_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  RCV_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+  int per_sm = surf_resident_blocks(mode);
+  if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
+  int64_t blocks = ((S.path_count + Q.batch - 1) / Q.batch + (kSurfBlock / 32) - 1) / (kSurfBlock / 32);
+  if (blocks > int64_t(sms) * per_sm) blocks = int64_t(sms) * per_sm;
+  if (blocks < 1) blocks = 1;
+  switch (mode) {
+    case kTwoState: trace_surface_kernel<kTwoState><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+    case kSingle: trace_surface_kernel<kSingle><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+    case kForward: trace_surface_kernel<kForward><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+    case kTape: trace_surface_kernel<kTape><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+    default: trace_surface_kernel<kAdjoint><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+  }
+  return launched("trace_surface launch");
 }
 
 static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o, void* workspace,
@@ -162,22 +215,37 @@ static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o,
   Q.batch = (o != nullptr && o->batch > 0) ? o->batch : 64;
   RCV_REQUIRE(Q.batch <= (1 << 20), "batch must be <= 2^20");
   Q.defer = 1;
-  RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
-  int dev = 0, sms = 1;
-  RCV_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
-  RCV_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
-  int per_sm = surf_resident_blocks(mode);
-  if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
-  int64_t blocks = ((S.path_count + Q.batch - 1) / Q.batch + (kSurfBlock / 32) - 1) / (kSurfBlock / 32);
-  if (blocks > int64_t(sms) * per_sm) blocks = int64_t(sms) * per_sm;
-  if (blocks < 1) blocks = 1;
-  switch (mode) {
-    case kTwoState: trace_surface_kernel<kTwoState><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
-    case kSingle: trace_surface_kernel<kSingle><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
-    case kForward: trace_surface_kernel<kForward><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
-    default: trace_surface_kernel<kAdjoint><<<(unsigned)blocks, kSurfBlock, 0, st>>>(S, Q); break;
+  const int adjoint = o == nullptr ? RCV_ADJOINT_TAPE : o->adjoint;
+  RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
+  if (mode == kAdjoint && adjoint == RCV_ADJOINT_TAPE) {
+    // one pass records the texture vertices, one flat pass scatters them, and
+    // the replay takes the paths whose vertices did not fit (2 slots each)
+    const int per_path = (o == nullptr || o->tape_events_per_path == 0) ? int(kTapeSlotsPerPath)
+                                                                      : o->tape_events_per_path;
+    RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
+                int(kTapeSlotsPerPath));
+    RCV_REQUIRE(S.path_count < (int64_t(1) << 32), "the tape adjoint needs fewer than 2^32 paths");
+    unsigned long long* qc = Q.counter;
+    Q.tape = reinterpret_cast<float4*>(ws + L.tape);
+    Q.tape_count = qc + 2;
+    Q.tape_cap = tape_capacity(S.path_count, per_path) & ~int64_t(1);
+    Q.lost_list = reinterpret_cast<uint32_t*>(ws + L.lost);
+    Q.lost_count = qc + 3;
+    Q.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
+    RCV_TRY_CUDA(cudaMemsetAsync(qc + 2, 0, 2 * sizeof(unsigned long long), st), "tape counters reset");
+    int rc = launch_surface(kTape, S, Q, o, st);
+    if (rc) return rc;
+    const int block = 256;
+    int sms = 1, dev = 0;
+    RCV_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    RCV_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+    surface_tape_scatter_kernel<<<(unsigned)sms * 8u, block, 0, st>>>(S, Q.tape, Q.tape_count, Q.tape_cap,
+                                                                       Q.path_ltot);
+    rc = launched("surface_tape_scatter launch");
+    if (rc) return rc;
+    return launch_surface(kAdjoint, S, Q, o, st);  // the lost-path list only
   }
-  int rc = launched("trace_surface launch");
+  int rc = launch_surface(mode, S, Q, o, st);
   if (rc || adj) return rc;
   return launch_reduce(mode == kTwoState, reinterpret_cast<const float4*>(ws + L.path_out), 0, npix, S.spp,
                        img_new, img_old, st);

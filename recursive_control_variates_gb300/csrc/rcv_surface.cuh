@@ -12,8 +12,14 @@
 //   draw, probability min(max(beta_new), 0.95) once depth >= rr_depth.
 // Random numbers per path: film 2D, then per bounce NEE 2D, BSDF 1D + 2D,
 // RR 1D.  The adjoint (Mitsuba's PRBIntegrator.render_backward on `new`)
-// replays each path: at every texture vertex dL * L_rem / albedo is scattered
-// bilinearly into the four texels.
+// scatters at every texture vertex dL * L_rem / albedo bilinearly into the
+// four texels, L_rem = L - (radiance gathered before the vertex's
+// reflectance acts).  kAdjoint traces each path twice (L, then the replay);
+// kTape traces it once and records each texture vertex (its position, the
+// path and the radiance gathered so far) on a tape that
+// surface_tape_scatter_kernel (rcv_surface.cu) turns into the gradient once
+// L is known; paths whose vertices did not fit are replayed by kAdjoint over
+// the lost-path list.
 #pragma once
 #include "rcv_volume.cuh"
 
@@ -206,6 +212,11 @@ template <int kMode>
 __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
+  // kAdjoint after a tape pass: only the paths on the lost list
+  const bool lost_only = kMode == kAdjoint && Q.lost_list != nullptr;
+  const int64_t total = lost_only ? (int64_t)*Q.lost_count : Q.total;
+  TapeCursor tc{0u, 0u};  // kTape: the warp's tape chunk
+  bool lost = false;      // kTape: a vertex of this path did not fit
   int64_t batch_next = 0, batch_end = 0;
   bool queue_empty = false;
   int64_t path = 0;
@@ -224,18 +235,18 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
         unsigned long long b = 0;
         if (lane == 0) b = atomicAdd(Q.counter, (unsigned long long)Q.batch);
         b = __shfl_sync(0xffffffffu, b, 0);
-        if ((int64_t)b >= Q.total) {
+        if ((int64_t)b >= total) {
           queue_empty = true;
           break;
         }
         batch_next = (int64_t)b;
-        batch_end = min((int64_t)b + Q.batch, Q.total);
+        batch_end = min((int64_t)b + Q.batch, total);
       }
       const unsigned avail = (unsigned)(batch_end - batch_next);
       const unsigned take = min((unsigned)__popc(need), avail);
       const unsigned rank = (unsigned)__popc(need & lt_mask);
       if (((need >> lane) & 1u) && rank < take) {
-        path = batch_next + rank;
+        path = lost_only ? (int64_t)Q.lost_list[batch_next + rank] : batch_next + rank;
         phase = kSStart;
         pass = 0;
       }
@@ -243,10 +254,13 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
       need = __ballot_sync(0xffffffffu, phase == kSIdle);
     }
     if (queue_empty && __all_sync(0xffffffffu, phase == kSIdle)) break;
-    if (phase == kSIdle) continue;
+    // kTape: idle lanes stay for the warp-wide tape append below
+    if (kMode != kTape && phase == kSIdle) continue;
 
     const int pix = (int)(path / S.spp);
     bool finished = false;
+    bool ev = false;  // kTape: this bounce's texture vertex, recorded below
+    V3 ev_p{0.0f, 0.0f, 0.0f}, ev_l{0.0f, 0.0f, 0.0f};
     if (phase == kSStart) {
       seed_lane(rng, S.seed, (uint32_t)path);
       const float u0 = next1d(rng), u1 = next1d(rng);
@@ -259,6 +273,7 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
       prev_pdf = 1.0f;
       prev_delta = true;
       depth = 0;
+      lost = false;
       if (kMode == kAdjoint || kMode == kForward) {
         if (pass == 0) {
           if (kMode == kAdjoint) {
@@ -275,7 +290,7 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
     }
 
     // ------------------------------------------------------------ one bounce
-    {
+    if (kMode != kTape || phase == kSBounce) {
       ++cnt.bounces;
       float t;
       const int id = intersect(S, o, d, kInf, t);
@@ -323,6 +338,12 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
           const V3 g{(dL.x * Lrem.x) / fmaxf(an.x, 1e-8f), (dL.y * Lrem.y) / fmaxf(an.y, 1e-8f),
                      (dL.z * Lrem.z) / fmaxf(an.z, 1e-8f)};
           tex_scatter(S, tl, g);
+          ++cnt.grad_events;
+        }
+        if (kMode == kTape && id == kPlane && active_next) {
+          ev = true;
+          ev_p = p;
+          ev_l = Ln;  // radiance gathered before the vertex's reflectance acts
           ++cnt.grad_events;
         }
         if (kMode == kForward && pass == 1 && id == kPlane && S.grad_tex != nullptr && active_next) {
@@ -414,7 +435,17 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
       }
     }
 
+    if (kMode == kTape) {
+      const float4 a = make_float4(ev_p.x, ev_p.z, __uint_as_float((uint32_t)path), 0.0f);
+      const float4 b = make_float4(ev_l.x, ev_l.y, ev_l.z, 0.0f);
+      if (!tape_append_n<2>(Q, tc, ev && !lost, a, b)) lost = true;
+    }
+
     if (finished) {
+      if (kMode == kTape) {
+        Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, lost ? 1.0f : 0.0f);
+        if (lost) Q.lost_list[atomicAdd(Q.lost_count, 1ull)] = (uint32_t)path;
+      }
       if ((kMode == kAdjoint || kMode == kForward) && pass == 0) {
         Ltot = Ln;
         pass = 1;
@@ -437,6 +468,7 @@ __device__ void trace_surface(const SurfJob& S, const Queue& Q, SurfCounts& cnt)
       }
     }
   }
+  if (kMode == kTape) tape_close(Q, tc);  // the unused slots of the warp's last chunk
 }
 
 }  // namespace rcv

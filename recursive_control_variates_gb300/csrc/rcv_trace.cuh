@@ -89,50 +89,6 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
 // shared memory).
 constexpr int kTraceWarps = 4;
 
-// Slots [cur, end) of the tape chunk a warp fills (warp-uniform).
-struct TapeCursor {
-  uint32_t cur, end;
-};
-
-// Appends the events of the lanes with `has` to the warp's tape chunk (one
-// event per lane, in lane order), claiming a new chunk of kTapeChunk slots
-// when the current one runs out; a chunk is only claimed whole inside the
-// capacity.  Called by the whole warp.  Returns false on the lanes whose
-// event did not fit (their path is then replayed instead).
-__device__ __forceinline__ bool tape_append(const Queue& Q, TapeCursor& tc, bool has, const V3& x, uint32_t ref) {
-  const unsigned m = __ballot_sync(0xffffffffu, has);
-  if (m == 0u) return true;
-  const unsigned lane = threadIdx.x & 31u;
-  const uint32_t n = (uint32_t)__popc(m), q = (uint32_t)__popc(m & ((1u << lane) - 1u));
-  const uint32_t rem = tc.end - tc.cur;
-  uint32_t nb = 0xffffffffu;  // start of the newly claimed chunk, if any
-  if (n > rem) {
-    unsigned long long b = 0;
-    if (lane == 0) b = atomicAdd(Q.tape_count, (unsigned long long)kTapeChunk);
-    b = __shfl_sync(0xffffffffu, b, 0);
-    if (b + kTapeChunk <= (unsigned long long)Q.tape_cap) nb = (uint32_t)b;
-  }
-  bool ok = true;
-  if (has) {
-    if (q < rem) {
-      Q.tape[tc.cur + q] = make_float4(x.x, x.y, x.z, __uint_as_float(ref));
-    } else if (nb != 0xffffffffu) {
-      Q.tape[nb + (q - rem)] = make_float4(x.x, x.y, x.z, __uint_as_float(ref));
-    } else {
-      ok = false;
-    }
-  }
-  if (n <= rem) {
-    tc.cur += n;
-  } else if (nb != 0xffffffffu) {
-    tc.cur = nb + (n - rem);
-    tc.end = nb + kTapeChunk;
-  } else {
-    tc.cur = tc.end;  // the tape is full: later events of this warp do not fit either
-  }
-  return ok;
-}
-
 // Cooperative walk of a warp's last paths.
 //
 // Once the path queue is empty a warp runs until its longest path ends, and
@@ -971,11 +927,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       phase = kIdle;
     }
   }
-  if (kMode == kTape) {
-    // the unused slots of the warp's last chunk
-    for (uint32_t i = tc.cur + lane; i < tc.end; i += 32u)
-      Q.tape[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTapeEmpty));
-  }
+  if (kMode == kTape) tape_close(Q, tc);  // the unused slots of the warp's last chunk
 }
 
 }  // namespace rcv

@@ -142,6 +142,71 @@ constexpr uint32_t kTapeIndexMask = 0x3fffffffu;
 constexpr uint32_t kTapeEmpty = 0xffffffffu;  // unused slot at the end of a warp's last chunk
 constexpr uint32_t kTapeChunk = 256;          // slots a warp claims at a time
 
+// Slots [cur, end) of the tape chunk a warp fills (warp-uniform).
+struct TapeCursor {
+  uint32_t cur, end;
+};
+
+// Appends kWords consecutive float4 (a, then b) for each lane with `has` to
+// the warp's tape chunk, in lane order, claiming a new chunk of kTapeChunk
+// slots when the current one runs out; a chunk is only claimed whole inside
+// the capacity.  A tape holds events of one size only (so an event never
+// straddles two chunks).  Called by the whole warp.  Returns false on the
+// lanes whose event did not fit.
+template <int kWords>
+__device__ __forceinline__ bool tape_append_n(const Queue& Q, TapeCursor& tc, bool has, const float4& a,
+                                              const float4& b) {
+  const unsigned m = __ballot_sync(0xffffffffu, has);
+  if (m == 0u) return true;
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t n = (uint32_t)__popc(m) * kWords, q = (uint32_t)__popc(m & ((1u << lane) - 1u)) * kWords;
+  const uint32_t rem = tc.end - tc.cur;
+  uint32_t nb = 0xffffffffu;  // start of the newly claimed chunk, if any
+  if (n > rem) {
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(Q.tape_count, (unsigned long long)kTapeChunk);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c + kTapeChunk <= (unsigned long long)Q.tape_cap) nb = (uint32_t)c;
+  }
+  bool ok = true;
+  if (has) {
+    uint32_t slot = 0;
+    if (q < rem) {
+      slot = tc.cur + q;
+    } else if (nb != 0xffffffffu) {
+      slot = nb + (q - rem);
+    } else {
+      ok = false;
+    }
+    if (ok) {
+      Q.tape[slot] = a;
+      if (kWords == 2) Q.tape[slot + 1] = b;
+    }
+  }
+  if (n <= rem) {
+    tc.cur += n;
+  } else if (nb != 0xffffffffu) {
+    tc.cur = nb + (n - rem);
+    tc.end = nb + kTapeChunk;
+  } else {
+    tc.cur = tc.end;  // the tape is full: later events of this warp do not fit either
+  }
+  return ok;
+}
+
+// One-slot event (position, reference) of the volume tape.
+__device__ __forceinline__ bool tape_append(const Queue& Q, TapeCursor& tc, bool has, const V3& x, uint32_t ref) {
+  const float4 a = make_float4(x.x, x.y, x.z, __uint_as_float(ref));
+  return tape_append_n<1>(Q, tc, has, a, a);
+}
+
+// Marks the unused slots of the warp's last chunk empty (slot word .w =
+// kTapeEmpty).  Called by the whole warp at exit.
+__device__ __forceinline__ void tape_close(const Queue& Q, const TapeCursor& tc) {
+  for (uint32_t i = tc.cur + (threadIdx.x & 31u); i < tc.end; i += 32u)
+    Q.tape[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTapeEmpty));
+}
+
 // Buffers of the two adjoint launches.
 struct AdjBuffers {
   float4* ckpt;

@@ -34,6 +34,15 @@ class TwoStatePRBIntegrator:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         self.batch = int(props.get("batch", 0))
         self.blocks_per_sm = int(props.get("blocks_per_sm", 0))
+        # adjoint: texture vertices recorded on a tape ("tape") or the paths
+        # traced a second time ("replay"); the same gradient either way
+        adjoint = props.get("adjoint", "tape")
+        if adjoint not in _lib.ADJOINTS:
+            raise ValueError(f"unknown adjoint {adjoint!r}")
+        self.adjoint = _lib.ADJOINTS[adjoint]
+        self.tape_events_per_path = int(props.get("tape_events_per_path", 0))
+        if not 0 <= self.tape_events_per_path <= 16:
+            raise ValueError("tape_events_per_path must be in [0, 16]")
         self.is_checked = False
         self._counters: dict[torch.device, torch.Tensor] = {}
         self._scratch: dict[torch.device, torch.Tensor] = {}
@@ -44,6 +53,7 @@ class TwoStatePRBIntegrator:
         o.max_depth, o.rr_depth, o.hide_emitters = self.max_depth, self.rr_depth, int(self.hide_emitters)
         o.batch, o.blocks_per_sm = self.batch, self.blocks_per_sm
         o.order = _lib.ORDER_ROW_MAJOR
+        o.adjoint, o.tape_events_per_path = self.adjoint, self.tape_events_per_path
         return o
 
     def counters(self, device) -> torch.Tensor:

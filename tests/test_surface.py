@@ -96,17 +96,27 @@ def test_surface_two_state_matches_oracle(cuda, oracle, batch):
 
 
 @pytest.mark.gpu
-def test_surface_adjoint_matches_oracle(cuda, oracle):
+@pytest.mark.parametrize("adjoint,per_path", [("tape", 0), ("tape", 1), ("tape", 4), ("replay", 0)])
+def test_surface_adjoint_matches_oracle(cuda, oracle, adjoint, per_path):
+    """The texture gradient from the tape of texture vertices (16 slots per
+    path; 1 and 4: most paths lose vertices and are replayed) and from the
+    second tracing pass, against the oracle and against each other (the
+    same vertex terms; only the order of float additions differs)."""
     res = 32
     tex = scenes.value_noise(16, 3)
     scene = gpu_scene(cuda, tex, tex, res)
     params = rcv.traverse(scene)
-    integ = rcv.load_dict({"type": "twostateprb", "max_depth": 6, "rr_depth": 3})
     gimg = np.random.default_rng(2).normal(0, 1, (res, res, 3)).astype(np.float32)
-    g = integ.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=21, spp=16)
-    g = g[scenes.TEXTURE_KEY].cpu().numpy().astype(np.float64)
+    grads = {}
+    for mode, pp in ((adjoint, per_path), ("replay", 0)):
+        integ = rcv.load_dict({"type": "twostateprb", "max_depth": 6, "rr_depth": 3, "adjoint": mode,
+                               "tape_events_per_path": pp})
+        g = integ.render_backward(scene, params, torch.from_numpy(gimg).to(cuda), 0, seed=21, spp=16)
+        grads[mode] = g[scenes.TEXTURE_KEY].cpu().numpy().astype(np.float64)
+    g = grads[adjoint]
     go = oracle.surface_backward(oracle_surface(oracle, tex, tex, res), seed=21, spp=16, grad_img=gimg)
     assert np.linalg.norm(g - go) <= 2e-5 * np.linalg.norm(go)
+    assert np.linalg.norm(g - grads["replay"]) <= 1e-6 * np.linalg.norm(grads["replay"])
 
 
 @pytest.mark.gpu
