@@ -75,6 +75,24 @@ def test_unknown_plugin_and_unsupported_options():
         rcv.load_dict(bad, device="cpu")
 
 
+@pytest.mark.parametrize("kind", ["twostateprbvolpath", "prbvolpath", "twostateprb"])
+def test_adjoint_options(kind):
+    """The adjoint choice of the volume and surface integrators reaches the C
+    options: the event tape by default, the replay on request; unknown names
+    and tape sizes outside [0, 16] are rejected."""
+    from recursive_control_variates_gb300 import _lib
+    o = rcv.load_dict({"type": kind}).options()
+    assert o.adjoint == _lib.ADJOINT_TAPE and o.tape_events_per_path == 0
+    o = rcv.load_dict({"type": kind, "adjoint": "replay", "tape_events_per_path": 4}).options()
+    assert o.adjoint == _lib.ADJOINT_REPLAY and o.tape_events_per_path == 4
+    with pytest.raises(ValueError):
+        rcv.load_dict({"type": kind, "adjoint": "none"})
+    with pytest.raises(ValueError):
+        rcv.load_dict({"type": kind, "tape_events_per_path": 17})
+    with pytest.raises(ValueError):
+        rcv.load_dict({"type": kind, "tape_events_per_path": -1})
+
+
 def test_majorant_resolution_factor():
     """`majorant_resolution_factor` (experiments.py:70,187,306) is accepted on the
     heterogeneous media; the two-state medium reports and sets the factor of
