@@ -154,8 +154,9 @@ typedef struct rcv_volpath_options {
    * event of the radiance pass on a tape and scatters the gradient from it in
    * one flat pass; RCV_ADJOINT_REPLAY replays the paths' segments from
    * scattering checkpoints.  Both give the same gradient (up to the order of
-   * float additions).  The tape needs the global majorant: with a supergrid,
-   * in forward mode and in batched launches the replay runs. */
+   * float additions).  Under a majorant supergrid the tape keeps each
+   * event's majorant beside it (at most 12 events per path); forward mode
+   * always replays.  The batched engine takes the same choice. */
   int32_t adjoint;
   /* Tape slots per path, 1..16 (0 = 16, the room the adjoint workspace
    * holds): paths whose events do not fit are replayed whole. */
@@ -275,7 +276,7 @@ int rcv_render_volume_noalloc(const rcv_medium* medium, const rcv_sensor* sensor
  * albedo grid when the medium has one) at every event of the paths: from the
  * event tape the radiance pass recorded (RCV_ADJOINT_TAPE, the default), or
  * by tracing the paths' segments again from scatter checkpoints
- * (RCV_ADJOINT_REPLAY, and always with a majorant supergrid).  Gradients are
+ * (RCV_ADJOINT_REPLAY).  Gradients are
  * ADDED to grad_density ([Dz][Dy][Dx]) and grad_albedo ([Dz][Dy][Dx][3] or
  * NULL).
  * Replaces CVIntegrator.render_backward / MetaIntegrator.render_backward
@@ -585,7 +586,7 @@ typedef struct rcv_batch rcv_batch; /* opaque host handle of a batch plan */
  * two-state launch (32 bytes per primal path of all jobs) and the adjoint's
  * per-path scratch (412 bytes per gradient path, as for
  * rcv_render_workspace_bytes).  opts->adjoint selects the tape or the replay
- * tasks for the whole batch; a batch with a majorant supergrid replays. */
+ * tasks for the whole batch. */
 uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n);
 /* Plans a batch of n initialised jobs with launch options `opts` (batch,
  * blocks_per_sm, defer, order; max_depth / rr_depth / hide_emitters come from

@@ -655,8 +655,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->adjbuf.ckpt_count = b->queue + 3;
   b->adjbuf.ckpt_cap = ckpt_capacity(adj_total);
   b->adjbuf.path_ltot = reinterpret_cast<float4*>(w + P.ltot);
-  // the tape needs every job on its global majorant
-  b->tape = b->opt.adjoint == RCV_ADJOINT_TAPE && sg_blocks == 0 && adj_total < (int64_t(1) << 29);
+  b->tape = b->opt.adjoint == RCV_ADJOINT_TAPE && adj_total < (int64_t(1) << 29);
   if (b->tape) {
     const int per_path = b->opt.tape_events_per_path > 0 ? b->opt.tape_events_per_path : int(kTapeSlotsPerPath);
     b->adjbuf.tape = reinterpret_cast<float4*>(w + P.tape);
@@ -664,6 +663,8 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     b->adjbuf.tape_cap = tape_capacity(adj_total, per_path);
     b->adjbuf.lost_list = reinterpret_cast<uint32_t*>(w + P.lost);
     b->adjbuf.lost_count = b->queue + 5;
+    // a batch with a supergrid keeps every event's majorant beside the tape
+    if (sg_blocks > 0) tape_with_majorants(b->adjbuf, w + P.tape, adj_total, per_path);
     b->tape_weights = reinterpret_cast<float4*>(w + P.ckpt + uint64_t(b->adjbuf.ckpt_cap) * 32u);
     b->cam_w = reinterpret_cast<float2*>(w + P.cam_w);
   }

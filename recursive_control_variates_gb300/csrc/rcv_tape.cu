@@ -19,6 +19,8 @@
 //                                            albedo: dL * L_rem / albedo
 //                          shadow-walk step -scale * (dL . c_nee) / sigma_n
 //                                            (where sigma_n > 0)
+// with sigma_n = majorant - sigma_t: the job's global majorant, or under a
+// majorant supergrid the one the radiance pass recorded beside the event.
 // Events of a path that lost an event or a record are skipped; kReplay
 // replays that path whole.  Batched launches find each event's job through
 // its path (binary search in the job table, once per record and path).
@@ -108,6 +110,7 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
                                                            const unsigned long long* __restrict__ tape_count,
                                                            int64_t tape_cap, const float4* __restrict__ w,
                                                            const float2* __restrict__ cam_w,
+                                                           const float* __restrict__ tape_mu,
                                                            unsigned long long* counters) {
   const int64_t n = min((int64_t)*tape_count, tape_cap);
   uint32_t ge = 0, ae = 0;
@@ -144,8 +147,9 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
         if (kCount) ++ae;
       }
     } else {
-      // the walk's majorant: the job's global one (tape launches have no supergrid)
-      const float sn = J.scale * bits_to_float(__ldg(J.maxbits + 1)) - st_n;
+      // the majorant of the collision: recorded (supergrid launches) or the job's global one
+      const float mu = tape_mu != nullptr ? __ldg(tape_mu + i) : J.scale * bits_to_float(__ldg(J.maxbits + 1));
+      const float sn = mu - st_n;
       if (kind != kEvShadow || sn > 0.0f) {
         scatter_density(J, lk, -(J.scale * s) / sn);
         if (kCount) ++ge;
@@ -173,10 +177,10 @@ int launch_tape_gradient(const VolJob& single, const VolJob* jobs, int njobs, co
   unsigned long long* c = reinterpret_cast<unsigned long long*>(counters);
   if (counters != nullptr)
     tape_scatter_kernel<true><<<grid, block, 0, st>>>(single, jobs, A.tape, A.tape_count, A.tape_cap, weights,
-                                                       cam_w, c);
+                                                       cam_w, A.tape_mu, c);
   else
     tape_scatter_kernel<false><<<grid, block, 0, st>>>(single, jobs, A.tape, A.tape_count, A.tape_cap, weights,
-                                                        cam_w, c);
+                                                        cam_w, A.tape_mu, c);
   return launched("tape_scatter launch");
 }
 

@@ -245,7 +245,8 @@ __device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJo
     // the group's steps before the first that ends the run are events
     const int fg = __shfl_sync(kFull, f, owner);
     const uint32_t rg = __shfl_sync(kFull, ref, owner);
-    const bool ok = tape_append(Q, tc, busy && k < fg, x, rg);
+    // (the cooperative walk runs on the global majorant only)
+    const bool ok = tape_append(Q, tc, busy && k < fg, x, rg, g_mu);
     const unsigned bad = __ballot_sync(kFull, !ok);
     if (own && ((bad >> ob) & gmask) != 0u) lost = true;
   }
@@ -672,6 +673,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     // walk ended
     int ev_kind = 0;
     uint32_t ev_ref = 0;
+    float ev_mu = 0.0f;  // the majorant of the step's collision (supergrid launches)
     bool ev_scat = false;
     // --------------------------------------------------- free-flight step
     if (phase == kMain || phase == kNee || phase == kNeeAdj) {
@@ -764,6 +766,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               if (kMode == kTape) {
                 ev_kind = 1;
                 ev_ref = tref;
+                if (kSG) ev_mu = mu_c;
               }
             } else {
               // real scattering event (plugins/twostatevolpath.py:249-253)
@@ -810,6 +813,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             if (kMode == kTape) {
               ev_kind = 2;
               ev_ref = tref;
+              if (kSG) ev_mu = mu_c;
             }
             done = (kMode == kTwoState) ? (trn == 0.0f && tro == 0.0f) : (trn == 0.0f);
           }
@@ -900,8 +904,9 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     }
 
     if (kMode == kTape) {
-      if (!tape_append(Q, tc, ev_kind != 0 && !ck_lost, ev_kind == 2 ? q : p, ev_ref)) ck_lost = true;
-      if (!tape_append(Q, tc, ev_scat && !ck_lost, p, (kEvScatter << 30) | (tref & kTapeIndexMask))) ck_lost = true;
+      if (!tape_append(Q, tc, ev_kind != 0 && !ck_lost, ev_kind == 2 ? q : p, ev_ref, ev_mu)) ck_lost = true;
+      if (!tape_append(Q, tc, ev_scat && !ck_lost, p, (kEvScatter << 30) | (tref & kTapeIndexMask), 0.0f))
+        ck_lost = true;
     }
 
     // -------------------------------------------------------------- path end

@@ -71,9 +71,7 @@ struct TraceVariants {
   static constexpr TraceKernel k[kTraceModes] = {
       trace_kernel<kTwoState, kSG, kCount, kEnv>, trace_kernel<kSingle, kSG, kCount, kEnv>,
       trace_kernel<kAdjoint, kSG, kCount, kEnv>, trace_kernel<kReplay, kSG, kCount, kEnv>,
-      trace_kernel<kForward, kSG, kCount, kEnv>,
-      // the tape pass needs the global majorant (supergrid launches replay)
-      trace_kernel<kSG ? kAdjoint : kTape, kSG, kCount, kEnv>};
+      trace_kernel<kForward, kSG, kCount, kEnv>, trace_kernel<kTape, kSG, kCount, kEnv>};
 };
 static const TraceKernel* const kTraceTables[8] = {
     TraceVariants<false, false, false>::k, TraceVariants<true, false, false>::k,
@@ -401,8 +399,10 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
       RCV_REQUIRE(total < (int64_t(1) << 30) && adj->ckpt_cap < (int64_t(1) << 30) &&
                       adj->tape_cap <= (int64_t(1) << 32) - int64_t(kTapeChunk),
                   "too many paths for the tape adjoint");
-      RCV_REQUIRE(!supergrid && (jobs != nullptr || J.sg[0] == 0), "the tape adjoint needs the global majorant");
+      const bool sg_launch = supergrid || (jobs == nullptr && J.sg[0] > 0);
+      RCV_REQUIRE(!sg_launch || adj->tape_mu != nullptr, "a supergrid tape launch needs the event majorants");
       Q.tape = adj->tape;
+      Q.tape_mu = sg_launch ? adj->tape_mu : nullptr;
       Q.tape_count = adj->tape_count;
       Q.tape_cap = adj->tape_cap;
       Q.lost_list = adj->lost_list;
@@ -643,15 +643,15 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
     RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
     RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
                 int(kTapeSlotsPerPath));
-    // the tape serves the gradient of single jobs with the global majorant;
     // forward mode gathers along replayed segments
-    const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward && J.sg[0] == 0;
+    const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward;
     if (tape) {
       A.tape = reinterpret_cast<float4*>(ws + L.tape);
       A.tape_count = qc + 2;
       A.tape_cap = tape_capacity(J.path_count, per_path);
       A.lost_list = reinterpret_cast<uint32_t*>(ws + L.lost);
       A.lost_count = qc + 3;
+      if (J.sg[0] > 0) tape_with_majorants(A, ws + L.tape, J.path_count, per_path);
     }
     if (stage != kAdjReplay) {
       RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, 3 * sizeof(unsigned long long), st), "adjoint counters reset");

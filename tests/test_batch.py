@@ -265,8 +265,13 @@ def test_batch_tape_matches_replay(cuda, per_path):
     """One batched step with the tape adjoint and one with the replay tasks:
     the same images, and first Adam moments (the gradients) within the
     reordering of float atomics; with 2 tape slots per path most paths are
-    replayed whole."""
+    replayed whole, and the second job has a majorant supergrid (the tape
+    then keeps each event's majorant)."""
     pairs = [build_pair(cuda, k) for k in range(len(JOBS))]
+    if per_path == 2:  # a majorant supergrid on one job: the tape keeps every event's majorant
+        pairs[1][0][0].named_shapes()["object"].interior_medium().set_majorant_resolution_factor(4)
+        pairs[1] = (pairs[1][0], batch.CVJob.from_scene(*pairs[1][0], pairs[1][2], spp=pairs[1][3], seed=pairs[1][4],
+                                                        keep_images=True), pairs[1][2], pairs[1][3], pairs[1][4])
     jobs_t = [p[1] for p in pairs]
     jobs_r = [j.clone() for j in jobs_t]
     bt = batch.BatchedCV(jobs_t, batch.LaunchOptions(tape_events_per_path=per_path), use_graph=False)

@@ -70,6 +70,23 @@ def test_tape_depth_limits(cuda, oracle, max_depth):
     assert rel_l2(gd, od) <= 2e-5, rel_l2(gd, od)
 
 
+@pytest.mark.parametrize("factor,per_path", [(4, 0), (8, 0), (4, 3)])
+def test_tape_under_supergrid(cuda, oracle, factor, per_path):
+    """With a majorant supergrid the tape keeps each event's majorant (the
+    DDA cell's) beside it: the gradient equals the replay's and the
+    oracle's (per_path 3: most paths replayed whole)."""
+    scene, med, grids = make_scene(cuda, albedo_grid=True, D=24, res=32)
+    med.set_majorant_resolution_factor(factor)
+    gimg = np.random.default_rng(factor).normal(0, 1, (32, 32, 3)).astype(np.float32)
+    tape = grads_of(cuda, scene, gimg, 31, 4, tape_events_per_path=per_path)
+    replay = grads_of(cuda, scene, gimg, 31, 4, adjoint="replay")
+    od, oa = oracle.backward(oracle_scene(oracle, scene, grids, 8, True, factor), seed=31, spp=4, grad_img=gimg)
+    gd = tape[scenes.DENSITY_KEY][..., 0]
+    assert rel_l2(gd, replay[scenes.DENSITY_KEY][..., 0]) <= 1e-6
+    assert rel_l2(gd, od) <= 2e-5, rel_l2(gd, od)
+    assert rel_l2(tape[scenes.ALBEDO_KEY], oa) <= 2e-5
+
+
 def test_tape_counters_match_replay(cuda):
     """The tape's gradient scatter counts the same events as the replay."""
     scene, med, grids = make_scene(cuda, res=24, albedo_grid=True)
