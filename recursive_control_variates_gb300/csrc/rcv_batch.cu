@@ -655,7 +655,8 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->adjbuf.ckpt_count = b->queue + 3;
   b->adjbuf.ckpt_cap = ckpt_capacity(adj_total);
   b->adjbuf.path_ltot = reinterpret_cast<float4*>(w + P.ltot);
-  b->tape = b->opt.adjoint == RCV_ADJOINT_TAPE && adj_total < (int64_t(1) << 29);
+  // (tape slots are 32-bit indices: batches of 2^28 gradient paths or more replay)
+  b->tape = b->opt.adjoint == RCV_ADJOINT_TAPE && adj_total < (int64_t(1) << 28);
   if (b->tape) {
     const int per_path = b->opt.tape_events_per_path > 0 ? b->opt.tape_events_per_path : int(kTapeSlotsPerPath);
     b->adjbuf.tape = reinterpret_cast<float4*>(w + P.tape);

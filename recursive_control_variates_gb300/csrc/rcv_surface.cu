@@ -217,14 +217,13 @@ static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o,
   Q.defer = 1;
   const int adjoint = o == nullptr ? RCV_ADJOINT_TAPE : o->adjoint;
   RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
-  if (mode == kAdjoint && adjoint == RCV_ADJOINT_TAPE) {
+  if (mode == kAdjoint && adjoint == RCV_ADJOINT_TAPE && S.path_count < (int64_t(1) << 28)) {
     // one pass records the texture vertices, one flat pass scatters them, and
     // the replay takes the paths whose vertices did not fit (2 slots each)
     const int per_path = (o == nullptr || o->tape_events_per_path == 0) ? int(kTapeSlotsPerPath)
                                                                       : o->tape_events_per_path;
     RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
                 int(kTapeSlotsPerPath));
-    RCV_REQUIRE(S.path_count < (int64_t(1) << 32), "the tape adjoint needs fewer than 2^32 paths");
     unsigned long long* qc = Q.counter;
     Q.tape = reinterpret_cast<float4*>(ws + L.tape);
     Q.tape_count = qc + 2;

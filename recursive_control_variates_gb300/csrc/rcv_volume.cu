@@ -643,8 +643,9 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
     RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
     RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
                 int(kTapeSlotsPerPath));
-    // forward mode gathers along replayed segments
-    const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward;
+    // forward mode gathers along replayed segments; a job of 2^28 paths or
+    // more (tape slots are 32-bit indices) replays too
+    const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward && J.path_count < (int64_t(1) << 28);
     if (tape) {
       A.tape = reinterpret_cast<float4*>(ws + L.tape);
       A.tape_count = qc + 2;

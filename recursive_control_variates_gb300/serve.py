@@ -182,9 +182,13 @@ class StepServer:
         if ids == self._last_ids and self._last_plan is not None:
             plan = self._last_plan
             self.stats.plan_reuses += 1
+            # a plan that is stepped again is worth capturing as a CUDA graph
+            plan.use_graph = self.use_graph
         else:
             old = self._last_plan
-            plan = B.BatchedCV([self.jobs[j] for j in ids], options=self.options, use_graph=self.use_graph)
+            # most ticks form a new plan that runs once: its launches are
+            # enqueued directly, without the cost of capturing a graph
+            plan = B.BatchedCV([self.jobs[j] for j in ids], options=self.options, use_graph=False)
             self._last_plan, self._last_ids = plan, ids
             if old is not None and not any(t.plan is old for t in self.inflight):
                 old.close()
