@@ -156,7 +156,8 @@ typedef struct rcv_volpath_options {
    * scattering checkpoints.  Both give the same gradient (up to the order of
    * float additions).  Under a majorant supergrid the tape keeps each
    * event's majorant beside it (at most 12 events per path); forward mode
-   * always replays.  The batched engine takes the same choice. */
+   * and jobs (or batches) of 2^28 gradient paths or more always replay.  The
+   * batched engine takes the same choice. */
   int32_t adjoint;
   /* Tape slots per path, 1..16 (0 = 16, the room the adjoint workspace
    * holds): paths whose events do not fit are replayed whole. */
