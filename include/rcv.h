@@ -219,9 +219,9 @@ int rcv_medium_prepare(const rcv_medium* medium, void* stream);
 /* ------------------------------------------------------------- tracers  */
 /* Scratch a tracer call needs (work-queue counter, pixel order, per-pixel
  * cost and, for the primal tracers, one radiance slot per path; for the
- * adjoint 412 B per path: total radiance, 2 scatter checkpoints or event
- * records with their weights, 16 tape slots of 16 B, camera-segment weight,
- * lost-path list): 256-B aligned device memory of this size, passed as
+ * adjoint 476 B per path: total radiance, 2 scatter checkpoints or event
+ * records with their weights, 16 tape slots of 16 B each with a 4-B
+ * extinction term, camera-segment weight, lost-path list): 256-B aligned device memory of this size, passed as
  * `workspace`.  The per-pixel cost persists from call to call
  * (RCV_ORDER_COST); pass the same workspace to the calls of one image size.
  * mode = RCV_MODE_*. */
@@ -585,7 +585,7 @@ typedef struct rcv_batch rcv_batch; /* opaque host handle of a batch plan */
 
 /* Shared device scratch of a batch: job tables, the per-path radiance of the
  * two-state launch (32 bytes per primal path of all jobs) and the adjoint's
- * per-path scratch (412 bytes per gradient path, as for
+ * per-path scratch (476 bytes per gradient path, as for
  * rcv_render_workspace_bytes).  opts->adjoint selects the tape or the replay
  * tasks for the whole batch. */
 uint64_t rcv_batch_workspace_bytes(const rcv_batch_job* jobs, int32_t n);

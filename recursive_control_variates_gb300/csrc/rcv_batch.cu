@@ -405,7 +405,7 @@ static PlanLayout plan_layout(int n, int64_t total_two_paths, int64_t total_adj_
   L.ckpt = off;
   off = align256(off + uint64_t(ckpt_capacity(total_adj_paths)) * 64u);
   L.tape = off;
-  off = align256(off + uint64_t(tape_capacity(total_adj_paths, kTapeSlotsPerPath)) * 16u);
+  off = align256(off + uint64_t(tape_capacity(total_adj_paths, kTapeSlotsPerPath)) * 20u);
   L.cam_w = off;
   off = align256(off + uint64_t(total_adj_paths) * 8u);
   L.lost = off;
@@ -664,8 +664,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
     b->adjbuf.tape_cap = tape_capacity(adj_total, per_path);
     b->adjbuf.lost_list = reinterpret_cast<uint32_t*>(w + P.lost);
     b->adjbuf.lost_count = b->queue + 5;
-    // a batch with a supergrid keeps every event's majorant beside the tape
-    if (sg_blocks > 0) tape_with_majorants(b->adjbuf, w + P.tape, adj_total, per_path);
+    b->adjbuf.tape_f = tape_terms(w + P.tape, adj_total);
     b->tape_weights = reinterpret_cast<float4*>(w + P.ckpt + uint64_t(b->adjbuf.ckpt_cap) * 32u);
     b->cam_w = reinterpret_cast<float2*>(w + P.cam_w);
   }

@@ -133,7 +133,8 @@ struct RenderLayout {
 inline int64_t ckpt_capacity(int64_t paths) { return 2 * paths + 65536; }
 
 // Event tape of the adjoint: 16 bytes per event, kTapeSlotsPerPath per path
-// (whole chunks of kTapeChunkSlots, the unit a warp claims).
+// (whole chunks of kTapeChunkSlots, the unit a warp claims), followed by one
+// 4-byte extinction term per slot (volume tape).
 constexpr int64_t kTapeSlotsPerPath = 16;
 constexpr int64_t kTapeChunkSlots = 256;
 inline int64_t tape_capacity(int64_t paths, int per_path) {
@@ -156,7 +157,7 @@ inline RenderLayout render_layout(int64_t npix, int64_t paths, int mode) {
   L.ltot = align256(L.path_out + path_out_bytes(paths, mode));
   L.ckpt = align256(L.ltot + (adj ? uint64_t(paths) * 16u : 0u));
   L.tape = align256(L.ckpt + (adj ? uint64_t(ckpt_capacity(paths)) * 64u : 0u));
-  L.cam_w = align256(L.tape + (adj ? uint64_t(tape_capacity(paths, kTapeSlotsPerPath)) * 16u : 0u));
+  L.cam_w = align256(L.tape + (adj ? uint64_t(tape_capacity(paths, kTapeSlotsPerPath)) * 20u : 0u));
   L.lost = align256(L.cam_w + (adj ? uint64_t(paths) * 8u : 0u));
   L.total = align256(L.lost + (adj ? uint64_t(paths) * 4u : 0u));
   return L;

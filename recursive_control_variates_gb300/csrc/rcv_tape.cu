@@ -11,16 +11,18 @@
 // semantics of Mitsuba's prb_volpath):
 //   tape_weights_kernel  per event record and per path, dL . L_rem of every
 //                        kind of event that refers to it, once dL is known;
-//   tape_scatter_kernel  per tape slot: the density (and at scattering
-//                        events the albedo) at the event from the medium,
+//   tape_scatter_kernel  per tape slot: the event's extinction term that
+//                        the radiance pass kept beside it (and at
+//                        scattering events the albedo from the medium),
 //                        the event's factor, and the gradient scatter:
 //                          null collision   -scale * (dL . L_rem) / sigma_n
 //                          scattering event  scale * (dL . L_rem) / sigma_t,
 //                                            albedo: dL * L_rem / albedo
 //                          shadow-walk step -scale * (dL . c_nee) / sigma_n
 //                                            (where sigma_n > 0)
-// with sigma_n = majorant - sigma_t: the job's global majorant, or under a
-// majorant supergrid the one the radiance pass recorded beside the event.
+// with sigma_n = majorant - sigma_t (the collision's majorant: global or
+// the supergrid cell's) and sigma_t of the new state, both as the radiance
+// pass computed them.
 // Events of a path that lost an event or a record are skipped; kReplay
 // replays that path whole.  Batched launches find each event's job through
 // its path (binary search in the job table, once per record and path).
@@ -110,7 +112,7 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
                                                            const unsigned long long* __restrict__ tape_count,
                                                            int64_t tape_cap, const float4* __restrict__ w,
                                                            const float2* __restrict__ cam_w,
-                                                           const float* __restrict__ tape_mu,
+                                                           const float* __restrict__ tape_f,
                                                            unsigned long long* counters) {
   const int64_t n = min((int64_t)*tape_count, tape_cap);
   uint32_t ge = 0, ae = 0;
@@ -134,9 +136,9 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
     const VolJob& J = jobs != nullptr ? jobs[j] : single;
     const V3 x{ev.x, ev.y, ev.z};
     const Lookup lk = locate(J, x);
-    const float st_n = J.scale * density_new(J, lk);
+    const float f = __ldcs(tape_f + i);  // sigma_t (scattering event) or sigma_n
     if (kind == kEvScatter) {
-      scatter_density(J, lk, (J.scale * s) / st_n);
+      scatter_density(J, lk, (J.scale * s) / f);
       if (kCount) ++ge;
       if (J.grad_albedo != nullptr) {
         const AlbedoLookup alk = albedo_lookup(J, lk, x);
@@ -147,9 +149,7 @@ __global__ void __launch_bounds__(256) tape_scatter_kernel(const __grid_constant
         if (kCount) ++ae;
       }
     } else {
-      // the majorant of the collision: recorded (supergrid launches) or the job's global one
-      const float mu = tape_mu != nullptr ? __ldg(tape_mu + i) : J.scale * bits_to_float(__ldg(J.maxbits + 1));
-      const float sn = mu - st_n;
+      const float sn = f;
       if (kind != kEvShadow || sn > 0.0f) {
         scatter_density(J, lk, -(J.scale * s) / sn);
         if (kCount) ++ge;
@@ -177,10 +177,10 @@ int launch_tape_gradient(const VolJob& single, const VolJob* jobs, int njobs, co
   unsigned long long* c = reinterpret_cast<unsigned long long*>(counters);
   if (counters != nullptr)
     tape_scatter_kernel<true><<<grid, block, 0, st>>>(single, jobs, A.tape, A.tape_count, A.tape_cap, weights,
-                                                       cam_w, A.tape_mu, c);
+                                                       cam_w, A.tape_f, c);
   else
     tape_scatter_kernel<false><<<grid, block, 0, st>>>(single, jobs, A.tape, A.tape_count, A.tape_cap, weights,
-                                                        cam_w, A.tape_mu, c);
+                                                        cam_w, A.tape_f, c);
   return launched("tape_scatter launch");
 }
 

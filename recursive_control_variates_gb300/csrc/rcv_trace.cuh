@@ -245,8 +245,8 @@ __device__ __forceinline__ int coop_walk(unsigned m, bool main_walk, const VolJo
     // the group's steps before the first that ends the run are events
     const int fg = __shfl_sync(kFull, f, owner);
     const uint32_t rg = __shfl_sync(kFull, ref, owner);
-    // (the cooperative walk runs on the global majorant only)
-    const bool ok = tape_append(Q, tc, busy && k < fg, x, rg, g_mu);
+    // sigma_n of each step (the cooperative walk runs on the global majorant)
+    const bool ok = tape_append(Q, tc, busy && k < fg, x, rg, g_mu - st_n);
     const unsigned bad = __ballot_sync(kFull, !ok);
     if (own && ((bad >> ob) & gmask) != 0u) lost = true;
   }
@@ -392,6 +392,14 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     const bool run_scat = (unsigned)__popc(m_scat) >= need_lanes || (m_walk == 0u && m_scat != 0u);
 
     bool finished = false;  // the lane's current path (or task) ends this iteration
+    // kTape: this iteration's events, appended where the warp has
+    // reconverged: a walk step (1: null collision at p, 2: shadow-walk step
+    // at q) with its reference and sigma_n, and the scattering event at p
+    // processed in this iteration with its sigma_t
+    int ev_kind = 0;
+    uint32_t ev_ref = 0;
+    float ev_f = 0.0f, ev_sf = 0.0f;
+    bool ev_scat = false;
 
     // ------------------------------------------------------------ path start
     if (run_start && phase == kStart) {
@@ -559,6 +567,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
           const unsigned long long k = atomicAdd(Q.ckpt_count, 1ull);
           if ((int64_t)k < Q.ckpt_cap) {
             tref = (kEvShadow << 30) | (uint32_t)k;
+            ev_scat = true;  // the event itself
+            ev_sf = st_n;
           } else {
             ck_lost = true;
             tref = (kEvCamera << 30) | (uint32_t)path;
@@ -667,14 +677,6 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
       }
     }
 
-    // kTape: this iteration's events, appended below where the warp has
-    // reconverged: a walk step (1: null collision at p, 2: shadow-walk step
-    // at q) with its reference, and the scattering event at p whose shadow
-    // walk ended
-    int ev_kind = 0;
-    uint32_t ev_ref = 0;
-    float ev_mu = 0.0f;  // the majorant of the step's collision (supergrid launches)
-    bool ev_scat = false;
     // --------------------------------------------------- free-flight step
     if (phase == kMain || phase == kNee || phase == kNeeAdj) {
       const VolJob& J = *Jp;
@@ -766,7 +768,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               if (kMode == kTape) {
                 ev_kind = 1;
                 ev_ref = tref;
-                if (kSG) ev_mu = mu_c;
+                ev_f = mu_c - st_n;
               }
             } else {
               // real scattering event (plugins/twostatevolpath.py:249-253)
@@ -813,7 +815,7 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
             if (kMode == kTape) {
               ev_kind = 2;
               ev_ref = tref;
-              if (kSG) ev_mu = mu_c;
+              ev_f = mu_c - st_n;
             }
             done = (kMode == kTwoState) ? (trn == 0.0f && tro == 0.0f) : (trn == 0.0f);
           }
@@ -842,7 +844,6 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               float4* rec = Q.ckpt + (int64_t)k * 2;
               rec[0] = make_float4(__uint_as_float((uint32_t)path), Ln.x, Ln.y, Ln.z);
               rec[1] = make_float4(cn.x, cn.y, cn.z, 0.0f);
-              ev_scat = true;
               tref = (kEvSegment << 30) | k;
             }
             Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
@@ -904,8 +905,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     }
 
     if (kMode == kTape) {
-      if (!tape_append(Q, tc, ev_kind != 0 && !ck_lost, ev_kind == 2 ? q : p, ev_ref, ev_mu)) ck_lost = true;
-      if (!tape_append(Q, tc, ev_scat && !ck_lost, p, (kEvScatter << 30) | (tref & kTapeIndexMask), 0.0f))
+      if (!tape_append(Q, tc, ev_kind != 0 && !ck_lost, ev_kind == 2 ? q : p, ev_ref, ev_f)) ck_lost = true;
+      if (!tape_append(Q, tc, ev_scat && !ck_lost, p, (kEvScatter << 30) | (tref & kTapeIndexMask), ev_sf))
         ck_lost = true;
     }
 

@@ -399,10 +399,9 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
       RCV_REQUIRE(total < (int64_t(1) << 30) && adj->ckpt_cap < (int64_t(1) << 30) &&
                       adj->tape_cap <= (int64_t(1) << 32) - int64_t(kTapeChunk),
                   "too many paths for the tape adjoint");
-      const bool sg_launch = supergrid || (jobs == nullptr && J.sg[0] > 0);
-      RCV_REQUIRE(!sg_launch || adj->tape_mu != nullptr, "a supergrid tape launch needs the event majorants");
+      RCV_REQUIRE(adj->tape_f != nullptr, "the tape needs its extinction terms");
       Q.tape = adj->tape;
-      Q.tape_mu = sg_launch ? adj->tape_mu : nullptr;
+      Q.tape_f = adj->tape_f;
       Q.tape_count = adj->tape_count;
       Q.tape_cap = adj->tape_cap;
       Q.lost_list = adj->lost_list;
@@ -652,7 +651,7 @@ static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, voi
       A.tape_cap = tape_capacity(J.path_count, per_path);
       A.lost_list = reinterpret_cast<uint32_t*>(ws + L.lost);
       A.lost_count = qc + 3;
-      if (J.sg[0] > 0) tape_with_majorants(A, ws + L.tape, J.path_count, per_path);
+      A.tape_f = tape_terms(ws + L.tape, J.path_count);
     }
     if (stage != kAdjReplay) {
       RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, 3 * sizeof(unsigned long long), st), "adjoint counters reset");

@@ -120,9 +120,10 @@ struct Queue {
   int64_t tape_cap;
   uint32_t* lost_list;
   unsigned long long* lost_count;
-  // launches with a majorant supergrid: the majorant of each event's
-  // collision, one float per tape slot (null: each job's global majorant)
-  float* tape_mu;
+  // one float per tape slot: the event's sigma_n = majorant - sigma_t of
+  // the new state (null collisions, shadow-walk steps) or sigma_t
+  // (scattering events), so that the gradient pass needs no grid lookup
+  float* tape_f;
 };
 
 // kForward: the replay tasks of kReplay, gathering a tangent field at every
@@ -159,7 +160,7 @@ struct TapeCursor {
 // lanes whose event did not fit.
 template <int kWords>
 __device__ __forceinline__ bool tape_append_n(const Queue& Q, TapeCursor& tc, bool has, const float4& a,
-                                              const float4& b, float mu = 0.0f) {
+                                              const float4& b, float f = 0.0f) {
   const unsigned m = __ballot_sync(0xffffffffu, has);
   if (m == 0u) return true;
   const unsigned lane = threadIdx.x & 31u;
@@ -185,7 +186,7 @@ __device__ __forceinline__ bool tape_append_n(const Queue& Q, TapeCursor& tc, bo
     if (ok) {
       Q.tape[slot] = a;
       if (kWords == 2) Q.tape[slot + 1] = b;
-      if (kWords == 1 && Q.tape_mu != nullptr) Q.tape_mu[slot] = mu;
+      if (kWords == 1 && Q.tape_f != nullptr) Q.tape_f[slot] = f;
     }
   }
   if (n <= rem) {
@@ -199,12 +200,12 @@ __device__ __forceinline__ bool tape_append_n(const Queue& Q, TapeCursor& tc, bo
   return ok;
 }
 
-// One-slot event (position, reference) of the volume tape, with the majorant
-// of its collision where the launch keeps them (supergrid).
+// One-slot event (position, reference) of the volume tape, with its
+// extinction term (sigma_n, or sigma_t at a scattering event).
 __device__ __forceinline__ bool tape_append(const Queue& Q, TapeCursor& tc, bool has, const V3& x, uint32_t ref,
-                                            float mu) {
+                                            float f) {
   const float4 a = make_float4(x.x, x.y, x.z, __uint_as_float(ref));
-  return tape_append_n<1>(Q, tc, has, a, a, mu);
+  return tape_append_n<1>(Q, tc, has, a, a, f);
 }
 
 // Marks the unused slots of the warp's last chunk empty (slot word .w =
@@ -225,7 +226,7 @@ struct AdjBuffers {
   int64_t tape_cap;
   uint32_t* lost_list;
   unsigned long long* lost_count;
-  float* tape_mu;  // supergrid launches: each event's majorant
+  float* tape_f;  // each event's sigma_n (sigma_t at scattering events)
 };
 
 struct Counts {
@@ -556,17 +557,10 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
 // Queries the occupancy and SM count the launchers cache, so that later
 // launches (e.g. under stream capture) make no device queries.
 void warm_launch_config();
-// Supergrid launches keep each event's majorant beside the tape: at most 12
-// of the 16 slots per path of the tape region go to events, and the floats
-// follow them (20 bytes per event).  A region too small for one chunk leaves
-// no room: every path is then replayed.
-inline void tape_with_majorants(AdjBuffers& A, char* region, int64_t paths, int per_path) {
-  const int64_t bytes = tape_capacity(paths, kTapeSlotsPerPath) * 16;
-  int64_t cap = tape_capacity(paths, per_path < 12 ? per_path : 12);
-  const int64_t fit = bytes / 20 / kTapeChunkSlots * kTapeChunkSlots;
-  if (cap > fit) cap = fit;
-  A.tape_cap = cap;
-  A.tape_mu = reinterpret_cast<float*>(region + cap * 16);
+// The extinction terms follow the tape's slots in the tape region (16 B +
+// 4 B per slot).
+inline float* tape_terms(char* region, int64_t paths) {
+  return reinterpret_cast<float*>(region + tape_capacity(paths, kTapeSlotsPerPath) * 16);
 }
 
 // Gradient from a kTape radiance pass (rcv_tape.cu) of one job (jobs ==

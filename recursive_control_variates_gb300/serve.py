@@ -94,10 +94,11 @@ class StepServer:
         """Resident bytes of a job plus the per-path scratch it adds to a tick:
         32 bytes per primal path (radiance slots), 16 + 2 x 64 bytes per
         gradient path (total radiance, scatter checkpoints or event records
-        and their weights), and with the tape adjoint 16 x 16 + 8 + 4 bytes
-        more (event slots, camera-segment weight, lost-path list)."""
+        and their weights), and with the tape adjoint 16 x 20 + 8 + 4 bytes
+        more (event slots with their extinction terms, camera-segment weight,
+        lost-path list)."""
         npix = job.width * job.height
-        per_grad = 144 + (268 if self.options.adjoint == "tape" else 0)
+        per_grad = 144 + (332 if self.options.adjoint == "tape" else 0)
         return job.nbytes() + 32 * npix * job.spp + per_grad * npix * job.spp_grad
 
     def resident_bytes(self) -> int:

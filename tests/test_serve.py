@@ -86,9 +86,9 @@ def fire_all():
 def test_admission_by_budget(fake_cuda):
     s = serve.StepServer(2500, device="cpu", clock=lambda: fake_cuda.t)
     # per-path scratch of a 1 x 1 x spp 1 job: 32 B primal, 144 B gradient
-    # (total radiance, records), 268 B of tape
+    # (total radiance, records), 332 B of tape
     scratch = s.job_bytes(FakeJob(0))
-    assert scratch == 32 + 144 + 268
+    assert scratch == 32 + 144 + 332
     replay = serve.StepServer(2500, device="cpu", options=serve.B.LaunchOptions(adjoint="replay"))
     assert replay.job_bytes(FakeJob(0)) == 32 + 144
     a, b, c = (FakeJob(1000 - scratch) for _ in range(3))  # 1000 B each with scratch
