@@ -260,10 +260,11 @@ def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj, tape: bool = True) ->
     albedo per real scattering event, 24 B of film per pixel.  Adjoint: 32 B
     per density lookup of its passes, 32 B per gradient reduction (8 corners),
     96 B of albedo read and 96 B reduced per scattering event, 12 B of dL per
-    pixel.  With the tape the gradient pass reads the density (and albedo) at
-    each gradient event again (the replay's lookups are counted as lookups);
-    the tape itself (16 B written and read per event) is intermediate
-    storage and not counted."""
+    pixel.  Each gradient event counts a 32-B read and a 32-B reduction,
+    whether the gradient pass reads the grid again (the replay's lookups,
+    counted as lookups) or keeps the value beside the event (the tape); the
+    tape itself (20 B written and read per event) is intermediate storage
+    and not counted."""
     lookups2 = float(c_two[1] + c_two[2])
     scat2 = float(c_two[3])
     npix = cfg.res * cfg.res
