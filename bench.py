@@ -194,7 +194,8 @@ def initial_density(cfg, true_density, phase: str):
 class Job:
     """One optimisation job of the configuration, resident on the device."""
 
-    def __init__(self, cfg, device, seed: int, phase: str = "late", target=None, majorant_factor: int = 0):
+    def __init__(self, cfg, device, seed: int, phase: str = "late", target=None, majorant_factor: int = 0,
+                 pair: bool = True):
         import torch
 
         import recursive_control_variates_gb300 as rcv
@@ -218,7 +219,8 @@ class Job:
         self.params = rcv.traverse(self.scene)
         self.integrator = rcv.load_dict({
             "type": "cv",
-            "integrator": {"type": "twostateprbvolpath", "max_depth": cfg.max_depth, "rr_depth": cfg.max_depth},
+            "integrator": {"type": "twostateprbvolpath", "max_depth": cfg.max_depth, "rr_depth": cfg.max_depth,
+                           "pair_adjoint": pair},
         })
         self.opt = rcv.ad.Adam(lr=cfg.lr)
         self.opt[scenes.DENSITY_KEY] = self.init_density
@@ -289,7 +291,7 @@ def run_ours(args, cfg):
     device = torch.device("cuda", local)
     dist = init_dist("nccl")
     lib = rcv.load_library()
-    job = Job(cfg, device, seed=replica_seed(rank))
+    job = Job(cfg, device, seed=replica_seed(rank), pair=not args.no_pair)
     paths = job.paths_per_step()
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -452,7 +454,9 @@ def run_ours(args, cfg):
                    else f", albedo {cfg.albedo}") + f", {cfg.res}x{cfg.res}, spp={cfg.spp}, spp_grad={cfg.spp_grad}, "
                    f"max_depth={cfg.max_depth}, cv_ps + path-replay adjoint + Adam",
                    "paths_per_step": paths, "parallelism": f"replicas x{world}",
-                   "l2": "flushed between timed steps (512 MB write)"},
+                   "l2": "flushed between timed steps (512 MB write)",
+                   "tracers": ("two-state render and adjoint radiance pass in one persistent launch"
+                               if not args.no_pair else "two-state render and adjoint radiance pass on two streams")},
         "p50_ms": ms_sorted[len(ms_sorted) // 2],
         "p99_ms": ms_sorted[min(len(ms_sorted) - 1, int(math.ceil(0.99 * len(ms_sorted))) - 1)],
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
@@ -537,7 +541,7 @@ def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_fa
     import torch
 
     job = Job(cfg, device, seed=replica_seed(dist_info()[0]) + 77, phase=phase, target=target,
-              majorant_factor=majorant_factor)
+              majorant_factor=majorant_factor, pair=not args.no_pair)
     for _ in range(args.warmup):
         job.step()
     stream = torch.cuda.current_stream(device)
@@ -634,6 +638,7 @@ def batched_form(args, device, flush):
     plains = plain_mix_setup(mix, jobs, device) if args.plain_rounds > 0 else None
     t0 = time.perf_counter()
     best = batch.autotune(jobs, steps=2) if not args.no_autotune else batch.LaunchOptions()
+    best = dataclasses.replace(best, pair_tracers=not args.no_pair)
     tune_s = time.perf_counter() - t0
     b = batch.BatchedCV(jobs, options=best, use_graph=True)
     stream = torch.cuda.current_stream(device)
@@ -944,6 +949,8 @@ def main(argv=None):
     ap.add_argument("--majorant-factor", type=int, default=8,
                     help="also time the headline step with a majorant supergrid of this factor (0 = skip)")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-pair", action="store_true",
+                    help="run the adjoint's radiance pass on a side stream instead of in the two-state launch")
     ap.add_argument("--batched-steps", type=int, default=200)
     ap.add_argument("--plain-rounds", type=int, default=2)
     ap.add_argument("--served-requests", type=int, default=400)

@@ -162,6 +162,12 @@ typedef struct rcv_volpath_options {
   /* Tape slots per path, 1..16 (0 = 16, the room the adjoint workspace
    * holds): paths whose events do not fit are replayed whole. */
   int32_t tape_events_per_path;
+  /* The two-state pass and the adjoint's radiance pass of a step as two
+   * launches (1; the batched engine runs them on two streams) instead of one
+   * paired persistent launch (0, the default: the batched step, and
+   * rcv_render_twostates_volume_and_adjoint_radiance).  The results are the
+   * same either way. */
+  int32_t separate_tracers;
 } rcv_volpath_options;
 
 #define RCV_ADJOINT_TAPE 0
@@ -319,6 +325,28 @@ int rcv_render_backward_replay(const rcv_medium* medium, const rcv_sensor* senso
                                const rcv_volpath_options* opts, uint32_t seed, int32_t spp,
                                const float* grad_img, float* grad_density, float* grad_albedo,
                                void* workspace, uint64_t* counters, void* stream);
+
+/* One optimisation step's two gradient-independent tracers in one call: the
+ * two-state primal of (seed, spp) into img_old / img_new, exactly as
+ * rcv_render_twostates_volume with `workspace`, and the adjoint's radiance
+ * pass of (seed_grad, spp_grad), exactly as rcv_render_adjoint_radiance
+ * with `adjoint_workspace` (a separate buffer of RCV_MODE_ADJOINT size).
+ * rcv_render_backward_replay with (seed_grad, spp_grad, adjoint_workspace)
+ * then completes the gradient.  Both tracers run in one persistent launch,
+ * so that the longest paths of both start together instead of the second
+ * launch's starting only as the first one's blocks retire; with event
+ * counting (counters non-NULL), the replay adjoint or separate_tracers the
+ * two run as separate launches.  Images and gradients equal those of the separate
+ * calls.  Replaces the primal of the reference's cv_ps step
+ * (TwoStatePRBVolpathIntegrator.render_twostates,
+ * plugins/twostatevolpath.py:91-138) together with the primal phase that the
+ * path-replay adjoint runs before its backward phase (render_backward of
+ * the prb_volpath integrator it derives from). */
+int rcv_render_twostates_volume_and_adjoint_radiance(const rcv_medium* medium, const rcv_sensor* sensor,
+                                                     const rcv_volpath_options* opts, uint32_t seed,
+                                                     int32_t spp, float* img_old, float* img_new,
+                                                     void* workspace, uint32_t seed_grad, int32_t spp_grad,
+                                                     void* adjoint_workspace, uint64_t* counters, void* stream);
 
 /* ------------------------------------------------ volpathsimple integrator */
 /* Switches of VolpathSimpleIntegrator (plugins/volpathsimple.py:20-51):

@@ -83,6 +83,7 @@ class VolpathOptions(C.Structure):
         ("envmap", C.c_void_p),  # const rcv_envmap* or NULL (constant environment)
         ("adjoint", C.c_int32),  # ADJOINT_TAPE / ADJOINT_REPLAY
         ("tape_events_per_path", C.c_int32),  # 1..16, 0 = 16
+        ("separate_tracers", C.c_int32),  # 1: two-state and adjoint radiance passes as two launches
     ]
 
 
@@ -244,6 +245,11 @@ SIGNATURES = {
     ),
     "rcv_render_adjoint_radiance": (
         C.c_int, [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp]
+    ),
+    "rcv_render_twostates_volume_and_adjoint_radiance": (
+        C.c_int,
+        [P(Medium), P(Sensor), P(VolpathOptions), C.c_uint32, C.c_int32, vp, vp, vp, C.c_uint32, C.c_int32, vp, vp,
+         vp],
     ),
     "rcv_render_backward_replay": (
         C.c_int,

@@ -315,6 +315,7 @@ class LaunchOptions:
     count_events: bool = False  # accumulate the tracer event counts (counters())
     adjoint: str = "tape"    # gradient from the event tape | replayed segments ("replay")
     tape_events_per_path: int = 0  # tape slots per path, 0 = 16 (testing: fewer, paths are replayed)
+    pair_tracers: bool = True  # two-state and adjoint radiance passes in one launch (else two streams)
 
     def c_struct(self) -> _lib.VolpathOptions:
         o = _lib.VolpathOptions()
@@ -327,6 +328,7 @@ class LaunchOptions:
             raise ValueError(f"unknown adjoint {self.adjoint!r}")
         o.adjoint = _lib.ADJOINTS[self.adjoint]
         o.tape_events_per_path = self.tape_events_per_path
+        o.separate_tracers = 0 if self.pair_tracers else 1
         return o
 
 

@@ -6,10 +6,17 @@
 //   pack       medium packing of every job (old = theta_{it-1}, new =
 //              theta_it from the parameter double buffer), majorants, and
 //              zeroed gradient cells
-//   trace 2S   ONE persistent two-state launch over the paths of all jobs
+//   trace 2S   ONE persistent two-state launch over the paths of all jobs;
+//              with the tape adjoint the same launch runs the adjoint's
+//              radiance pass over the gradient paths of all jobs
+//              (rcv_pair.cu; separate_tracers: a second launch on a side
+//              stream)
 //   image      per pixel of every job: sample reduction (H, F), control
 //              variate blend + statistics, loss gradient and loss sum
-//   trace adj  ONE persistent adjoint launch over the gradient paths of all jobs
+//   trace adj  the adjoint's gradient: from the tape (weights + scatter),
+//              then ONE persistent replay launch over the paths the tape
+//              lost (or over all gradient paths, after a checkpoint
+//              radiance launch, with the replay adjoint)
 //   update     per voxel of every job: cell-gradient fold, Adam + clamp into
 //              the other half of the parameter double buffer
 //
@@ -461,6 +468,9 @@ struct rcv_batch {
   float4* path_out = nullptr;
   AdjBuffers adjbuf{};
   bool tape = false;  // gradient from the event tape (else replay tasks)
+  // the two-state and tape radiance passes in one launch (rcv_pair.cu), else
+  // two launches on two streams
+  bool paired = false;
   float4* tape_weights = nullptr;
   float2* cam_w = nullptr;
   int64_t total_two = 0, total_adj = 0;
@@ -539,6 +549,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
                 opts->adjoint);
     RCV_REQUIRE(opts->tape_events_per_path >= 0 && opts->tape_events_per_path <= kTapeSlotsPerPath,
                 "tape_events_per_path must be in [0, %d]", int(kTapeSlotsPerPath));
+    RCV_REQUIRE(opts->separate_tracers == 0 || opts->separate_tracers == 1, "separate_tracers must be 0 or 1");
   }
   const uint64_t need = rcv_batch_workspace_bytes(jobs, n);
   RCV_REQUIRE(need > 0 && workspace_bytes >= need, "batch workspace too small: %llu bytes, need %llu",
@@ -657,6 +668,7 @@ extern "C" int rcv_batch_create(const rcv_batch_job* jobs, int32_t n, const rcv_
   b->adjbuf.path_ltot = reinterpret_cast<float4*>(w + P.ltot);
   // (tape slots are 32-bit indices: batches of 2^28 gradient paths or more replay)
   b->tape = b->opt.adjoint == RCV_ADJOINT_TAPE && adj_total < (int64_t(1) << 28);
+  b->paired = b->tape && !b->opt.count_events && !b->opt.separate_tracers;
   if (b->tape) {
     const int per_path = b->opt.tape_events_per_path > 0 ? b->opt.tape_events_per_path : int(kTapeSlotsPerPath);
     b->adjbuf.tape = reinterpret_cast<float4*>(w + P.tape);
@@ -725,26 +737,42 @@ static int enqueue_step(rcv_batch* b, cudaStream_t st) {
   }
   VolJob none;
   std::memset(&none, 0, sizeof(none));
-  // the adjoint radiance pass needs no image gradient: it runs on the side
-  // stream beside the two-state pass and the image kernel
-  RCV_TRY_CUDA(cudaEventRecord(b->fork, st), "fork record");
-  RCV_TRY_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "fork wait");
-  // checkpoint / event-record, tape-slot and lost-path counters
-  RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, 3 * sizeof(unsigned long long), b->side),
-               "adjoint counters reset");
   // event counts only when asked for: the counting tracers hold the counts in registers
   uint64_t* cnt = b->opt.count_events ? b->counters : nullptr;
-  rc = launch_persistent(b->tape ? kTape : kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr,
-                         &b->adjbuf, cnt ? cnt + RCV_COUNTER_COUNT : nullptr, b->side, sg);
-  if (rc) return rc;
-  RCV_TRY_CUDA(cudaEventRecord(b->join, b->side), "join record");
-  rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr,
-                         cnt, st, sg);
-  if (rc) return rc;
-  batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
-  rc = launched("batch image launch");
-  if (rc) return rc;
-  RCV_TRY_CUDA(cudaStreamWaitEvent(st, b->join, 0), "join wait");
+  if (b->paired) {
+    // the adjoint radiance pass needs no image gradient: it runs in the
+    // launch of the two-state pass
+    RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, 3 * sizeof(unsigned long long), st),
+                 "adjoint counters reset");
+    Queue QA, QB;
+    rc = make_queue(kTwoState, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr, nullptr, st,
+                    &QA);
+    if (rc == RCV_OK)
+      rc = make_queue(kTape, b->adj, n, b->total_adj, &b->opt, b->queue + 1, nullptr, &b->adjbuf, nullptr, st, &QB);
+    if (rc == RCV_OK) rc = launch_pair(none, QA, none, QB, &b->opt, st, sg);
+    if (rc) return rc;
+    batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
+    rc = launched("batch image launch");
+    if (rc) return rc;
+  } else {
+    // ... or on the side stream beside the two-state pass and the image kernel
+    RCV_TRY_CUDA(cudaEventRecord(b->fork, st), "fork record");
+    RCV_TRY_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "fork wait");
+    // checkpoint / event-record, tape-slot and lost-path counters
+    RCV_TRY_CUDA(cudaMemsetAsync(b->adjbuf.ckpt_count, 0, 3 * sizeof(unsigned long long), b->side),
+                 "adjoint counters reset");
+    rc = launch_persistent(b->tape ? kTape : kAdjoint, none, b->adj, n, b->total_adj, &b->opt, b->queue + 1,
+                           nullptr, &b->adjbuf, cnt ? cnt + RCV_COUNTER_COUNT : nullptr, b->side, sg);
+    if (rc) return rc;
+    RCV_TRY_CUDA(cudaEventRecord(b->join, b->side), "join record");
+    rc = launch_persistent(kTwoState, none, b->two, n, b->total_two, &b->opt, b->queue + 0, b->path_out, nullptr,
+                           cnt, st, sg);
+    if (rc) return rc;
+    batch_image_kernel<<<(unsigned)b->pix_blocks, kBatchBlock, 0, st>>>(b->entries, pi, n, b->path_out);
+    rc = launched("batch image launch");
+    if (rc) return rc;
+    RCV_TRY_CUDA(cudaStreamWaitEvent(st, b->join, 0), "join wait");
+  }
   if (b->tape) {
     // the gradient from the tape; the replay then takes only the lost paths
     rc = launch_tape_gradient(none, b->adj, n, b->adjbuf, b->tape_weights, b->cam_w, b->total_adj,
@@ -794,7 +822,8 @@ extern "C" uint64_t* rcv_batch_counters(rcv_batch* b) { return b != nullptr ? b-
 
 extern "C" int32_t rcv_batch_kernels_per_step(const rcv_batch* b) {
   if (b == nullptr) return RCV_ERR_INVALID;
-  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0) + (b->sg_blocks > 0 ? 1 : 0) + (b->tape ? 2 : 0);
+  return kBatchKernels + (b->opt.order == RCV_ORDER_COST ? 3 : 0) + (b->sg_blocks > 0 ? 1 : 0) + (b->tape ? 2 : 0) -
+         (b->paired ? 1 : 0);
 }
 
 extern "C" int rcv_batch_destroy(rcv_batch* b) {

@@ -88,6 +88,7 @@ __device__ __forceinline__ const VolJob& job_of(const VolJob& single, const Queu
 // Warps per tracer block (the cooperative walk keeps 3 x 32 floats per warp in
 // shared memory).
 constexpr int kTraceWarps = 4;
+constexpr int kTraceBlock = 32 * kTraceWarps;
 
 // Cooperative walk of a warp's last paths.
 //
@@ -842,8 +843,8 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
               // collisions refer to the record too
               const uint32_t k = tref & kTapeIndexMask;
               float4* rec = Q.ckpt + (int64_t)k * 2;
-              rec[0] = make_float4(__uint_as_float((uint32_t)path), Ln.x, Ln.y, Ln.z);
-              rec[1] = make_float4(cn.x, cn.y, cn.z, 0.0f);
+              __stcs(rec, make_float4(__uint_as_float((uint32_t)path), Ln.x, Ln.y, Ln.z));
+              __stcs(rec + 1, make_float4(cn.x, cn.y, cn.z, 0.0f));
               tref = (kEvSegment << 30) | k;
             }
             Ln = V3{Ln.x + cn.x, Ln.y + cn.y, Ln.z + cn.z};
@@ -914,10 +915,10 @@ __device__ void trace_persistent(const VolJob& single, const Queue& Q, Counts& c
     if (finished) {
       if (kMode == kTwoState || kMode == kSingle) {
         float4* o = Q.path_out + (Jp->path_begin + sid) * (kMode == kTwoState ? 2 : 1);
-        o[0] = make_float4(Ln.x, Ln.y, Ln.z, 0.0f);
-        if (kMode == kTwoState) o[1] = make_float4(Lo.x, Lo.y, Lo.z, 0.0f);
+        __stcs(o, make_float4(Ln.x, Ln.y, Ln.z, 0.0f));
+        if (kMode == kTwoState) __stcs(o + 1, make_float4(Lo.x, Lo.y, Lo.z, 0.0f));
       }
-      if (kRad) Q.path_ltot[path] = make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f);
+      if (kRad) __stcs(Q.path_ltot + path, make_float4(Ln.x, Ln.y, Ln.z, ck_lost ? 1.0f : 0.0f));
       if (kMode == kTape && ck_lost) Q.lost_list[atomicAdd(Q.lost_count, 1ull)] = (uint32_t)path;
       if (kMode == kForward && (dL.x != 0.0f || dL.y != 0.0f || dL.z != 0.0f)) {
         // the task's share of its pixel's derivative (the pixel value is the

@@ -14,8 +14,6 @@
 
 namespace rcv {
 
-constexpr int kTraceBlock = 32 * kTraceWarps;
-
 // ------------------------------------------------------------------ packing
 // One thread per cell / voxel / albedo voxel (na: albedo grid voxels).
 __global__ void pack_medium_kernel(int dx, int dy, int dz, const float* __restrict__ old_d,
@@ -356,6 +354,7 @@ int tracer_sm_count() { return sm_count(); }
 void warm_launch_config() {
   (void)resident_blocks(0);
   (void)sm_count();
+  warm_pair_config();
 }
 
 static_assert(kOrderBuckets == kRenderOrderBuckets, "order bucket count mismatch");
@@ -376,13 +375,12 @@ int order_pixels(const VolJob& J, uint32_t* buckets, uint32_t* order, uint32_t* 
   return launched("order_place launch");
 }
 
-// Persistent launch over `total` paths of one job (jobs == null) or of a
-// device job table.
-int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
-                      const rcv_volpath_options* o, unsigned long long* queue_counter,
-                      float4* path_out, const AdjBuffers* adj, uint64_t* counters, cudaStream_t st,
-                      bool supergrid) {
-  Queue Q;
+// Work queue of a persistent launch over `total` paths of one job (jobs ==
+// null) or of a device job table; zeroes its hand-out counter on `st`.
+int make_queue(int mode, const VolJob* jobs, int njobs, int64_t total, const rcv_volpath_options* o,
+               unsigned long long* queue_counter, float4* path_out, const AdjBuffers* adj, uint64_t* counters,
+               cudaStream_t st, Queue* out) {
+  Queue& Q = *out;
   std::memset(&Q, 0, sizeof(Q));
   Q.counter = queue_counter;
   Q.path_out = (mode == kTwoState || mode == kSingle) ? path_out : nullptr;
@@ -418,6 +416,18 @@ int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, 
   Q.defer = (o != nullptr && o->defer > 0) ? o->defer : 8;
   RCV_REQUIRE(Q.defer <= 32, "defer must be in [1, 32]");
   RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
+  return RCV_OK;
+}
+
+// Persistent launch over `total` paths of one job (jobs == null) or of a
+// device job table.
+int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
+                      const rcv_volpath_options* o, unsigned long long* queue_counter,
+                      float4* path_out, const AdjBuffers* adj, uint64_t* counters, cudaStream_t st,
+                      bool supergrid) {
+  Queue Q;
+  int rc = make_queue(mode, jobs, njobs, total, o, queue_counter, path_out, adj, counters, st, &Q);
+  if (rc) return rc;
   const bool sg = supergrid || (jobs == nullptr && J.sg[0] > 0);
   // an environment map belongs to a single job (batched tables take the constant environment)
   const int variant = trace_variant(mode, sg, counters != nullptr, jobs == nullptr && J.env.valid != 0);
@@ -596,63 +606,88 @@ extern "C" int rcv_medium_prepare(const rcv_medium* m, void* stream) {
   return launched("supergrid launch");
 }
 
-// Orders the pixels, runs the persistent tracer of one job and, for the
-// primal tracers, reduces the per-path radiance into the output image(s).
 // Adjoint stages: both launches, the radiance pass alone, or the replay alone
 // (which reuses the pixel order, checkpoints and total radiance the radiance
 // pass left in the same workspace).
 enum AdjStage { kAdjBoth = 0, kAdjRadiance = 1, kAdjReplay = 2, kAdjForward = 3 };
 
-static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, void* workspace,
-                          uint64_t* counters, float* img_new, float* img_old, cudaStream_t st,
-                          int stage = kAdjBoth) {
+static int check_workspace(const void* workspace) {
   RCV_REQUIRE(workspace != nullptr && (reinterpret_cast<uintptr_t>(workspace) & 255u) == 0,
               "render workspace must be non-NULL and 256-byte aligned");
-  const int64_t npix = int64_t(J.width) * J.height;
-  const RenderLayout L = render_layout(npix, J.path_count, mode);
-  char* ws = static_cast<char*>(workspace);
-  int rc = RCV_OK;
+  return RCV_OK;
+}
+
+// Pixel hand-out order of a job (RCV_ORDER_*), in its workspace; `sort`
+// false reuses the order an earlier stage left there.
+static int order_job(VolJob& J, const rcv_volpath_options* o, char* ws, const RenderLayout& L, bool sort,
+                     cudaStream_t st) {
   J.pixel_order = nullptr;
   J.pixel_cost = nullptr;
   const int order = o == nullptr ? RCV_ORDER_COST : o->order;
   RCV_REQUIRE(order == RCV_ORDER_COST || order == RCV_ORDER_ROW_MAJOR || order == RCV_ORDER_LONGEST_FIRST,
               "unknown pixel order %d", order);
-  if (order != RCV_ORDER_ROW_MAJOR) {
-    uint32_t* cost = order == RCV_ORDER_COST ? reinterpret_cast<uint32_t*>(ws + L.cost) : nullptr;
-    if (stage != kAdjReplay) {
-      rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets), reinterpret_cast<uint32_t*>(ws + L.order),
-                        cost, st);
-      if (rc) return rc;
-    }
-    J.pixel_order = reinterpret_cast<const uint32_t*>(ws + L.order);
-    J.pixel_cost = cost;
+  if (order == RCV_ORDER_ROW_MAJOR) return RCV_OK;
+  uint32_t* cost = order == RCV_ORDER_COST ? reinterpret_cast<uint32_t*>(ws + L.cost) : nullptr;
+  if (sort) {
+    const int rc = order_pixels(J, reinterpret_cast<uint32_t*>(ws + L.buckets),
+                                reinterpret_cast<uint32_t*>(ws + L.order), cost, st);
+    if (rc) return rc;
   }
+  J.pixel_order = reinterpret_cast<const uint32_t*>(ws + L.order);
+  J.pixel_cost = cost;
+  return RCV_OK;
+}
+
+// Adjoint buffers of a job in its workspace (queue counters at qc: hand-out,
+// records, tape slots, lost paths).  *tape: the gradient comes from the
+// event tape (RCV_ADJOINT_TAPE, except in forward mode and for jobs of 2^28
+// paths or more, whose tape slots would not fit 32-bit indices).
+static int adjoint_buffers(const VolJob& J, const rcv_volpath_options* o, char* ws, const RenderLayout& L,
+                           unsigned long long* qc, int stage, AdjBuffers* out, bool* tape_out) {
+  AdjBuffers& A = *out;
+  std::memset(&A, 0, sizeof(A));
+  A.ckpt = reinterpret_cast<float4*>(ws + L.ckpt);
+  A.ckpt_count = qc + 1;
+  A.ckpt_cap = ckpt_capacity(J.path_count);
+  A.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
+  const int adjoint = o == nullptr ? RCV_ADJOINT_TAPE : o->adjoint;
+  const int per_path = (o == nullptr || o->tape_events_per_path == 0) ? int(kTapeSlotsPerPath)
+                                                                    : o->tape_events_per_path;
+  RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
+  RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
+              int(kTapeSlotsPerPath));
+  const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward && J.path_count < (int64_t(1) << 28);
+  if (tape) {
+    A.tape = reinterpret_cast<float4*>(ws + L.tape);
+    A.tape_count = qc + 2;
+    A.tape_cap = tape_capacity(J.path_count, per_path);
+    A.lost_list = reinterpret_cast<uint32_t*>(ws + L.lost);
+    A.lost_count = qc + 3;
+    A.tape_f = tape_terms(ws + L.tape, J.path_count);
+  }
+  *tape_out = tape;
+  return RCV_OK;
+}
+
+// Orders the pixels, runs the persistent tracer of one job and, for the
+// primal tracers, reduces the per-path radiance into the output image(s).
+static int run_single_job(int mode, VolJob& J, const rcv_volpath_options* o, void* workspace,
+                          uint64_t* counters, float* img_new, float* img_old, cudaStream_t st,
+                          int stage = kAdjBoth) {
+  int rc = check_workspace(workspace);
+  if (rc) return rc;
+  const int64_t npix = int64_t(J.width) * J.height;
+  const RenderLayout L = render_layout(npix, J.path_count, mode);
+  char* ws = static_cast<char*>(workspace);
+  rc = order_job(J, o, ws, L, stage != kAdjReplay, st);
+  if (rc) return rc;
   float4* po = reinterpret_cast<float4*>(ws + L.path_out);
   unsigned long long* qc = reinterpret_cast<unsigned long long*>(ws + L.counter);
   if (mode == kAdjoint) {
     AdjBuffers A;
-    std::memset(&A, 0, sizeof(A));
-    A.ckpt = reinterpret_cast<float4*>(ws + L.ckpt);
-    A.ckpt_count = qc + 1;
-    A.ckpt_cap = ckpt_capacity(J.path_count);
-    A.path_ltot = reinterpret_cast<float4*>(ws + L.ltot);
-    const int adjoint = o == nullptr ? RCV_ADJOINT_TAPE : o->adjoint;
-    const int per_path = (o == nullptr || o->tape_events_per_path == 0) ? int(kTapeSlotsPerPath)
-                                                                      : o->tape_events_per_path;
-    RCV_REQUIRE(adjoint == RCV_ADJOINT_TAPE || adjoint == RCV_ADJOINT_REPLAY, "unknown adjoint %d", adjoint);
-    RCV_REQUIRE(per_path >= 1 && per_path <= kTapeSlotsPerPath, "tape_events_per_path must be in [0, %d]",
-                int(kTapeSlotsPerPath));
-    // forward mode gathers along replayed segments; a job of 2^28 paths or
-    // more (tape slots are 32-bit indices) replays too
-    const bool tape = adjoint == RCV_ADJOINT_TAPE && stage != kAdjForward && J.path_count < (int64_t(1) << 28);
-    if (tape) {
-      A.tape = reinterpret_cast<float4*>(ws + L.tape);
-      A.tape_count = qc + 2;
-      A.tape_cap = tape_capacity(J.path_count, per_path);
-      A.lost_list = reinterpret_cast<uint32_t*>(ws + L.lost);
-      A.lost_count = qc + 3;
-      A.tape_f = tape_terms(ws + L.tape, J.path_count);
-    }
+    bool tape = false;
+    rc = adjoint_buffers(J, o, ws, L, qc, stage, &A, &tape);
+    if (rc) return rc;
     if (stage != kAdjReplay) {
       RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, 3 * sizeof(unsigned long long), st), "adjoint counters reset");
       rc = launch_persistent(tape ? kTape : kAdjoint, J, nullptr, 0, J.path_count, o, qc, nullptr, &A, counters,
@@ -695,6 +730,55 @@ extern "C" int rcv_render_volume(const rcv_medium* m, const rcv_sensor* s,
   if (rc) return rc;
   RCV_REQUIRE(img != nullptr, "output image is NULL");
   return run_single_job(kSingle, J, o, workspace, counters, img, nullptr, static_cast<cudaStream_t>(stream));
+}
+
+// The two-state primal of (seed, spp) and the adjoint's radiance pass of
+// (seed_grad, spp_grad) on the same medium: one persistent launch that runs
+// both (rcv_pair.cu), where the two launches in a row would each end on
+// their longest paths.  With event counting, the replay adjoint or
+// separate_tracers the two run as separate launches.
+extern "C" int rcv_render_twostates_volume_and_adjoint_radiance(
+    const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o, uint32_t seed, int32_t spp,
+    float* img_old, float* img_new, void* workspace, uint32_t seed_grad, int32_t spp_grad, void* adjoint_workspace,
+    uint64_t* counters, void* stream) {
+  VolJob JA, JB;
+  int rc = make_volume_job(m, s, o, seed, spp, &JA);
+  if (rc) return rc;
+  rc = make_volume_job(m, s, o, seed_grad, spp_grad, &JB);
+  if (rc) return rc;
+  RCV_REQUIRE(img_old != nullptr && img_new != nullptr, "output images are NULL");
+  RCV_REQUIRE(workspace != adjoint_workspace, "the render and the adjoint need separate workspaces");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = check_workspace(workspace);
+  if (rc == RCV_OK) rc = check_workspace(adjoint_workspace);
+  if (rc) return rc;
+  const int64_t npix = int64_t(JA.width) * JA.height;
+  const RenderLayout LA = render_layout(npix, JA.path_count, kTwoState);
+  const RenderLayout LB = render_layout(npix, JB.path_count, kAdjoint);
+  char* wa = static_cast<char*>(workspace);
+  char* wb = static_cast<char*>(adjoint_workspace);
+  unsigned long long* qa = reinterpret_cast<unsigned long long*>(wa + LA.counter);
+  unsigned long long* qb = reinterpret_cast<unsigned long long*>(wb + LB.counter);
+  AdjBuffers A;
+  bool tape = false;
+  rc = adjoint_buffers(JB, o, wb, LB, qb, kAdjRadiance, &A, &tape);
+  if (rc) return rc;
+  if (counters != nullptr || !tape || (o != nullptr && o->separate_tracers)) {
+    rc = run_single_job(kTwoState, JA, o, workspace, counters, img_new, img_old, st);
+    if (rc) return rc;
+    return run_single_job(kAdjoint, JB, o, adjoint_workspace, counters, nullptr, nullptr, st, kAdjRadiance);
+  }
+  rc = order_job(JA, o, wa, LA, true, st);
+  if (rc == RCV_OK) rc = order_job(JB, o, wb, LB, true, st);
+  if (rc) return rc;
+  RCV_TRY_CUDA(cudaMemsetAsync(A.ckpt_count, 0, 3 * sizeof(unsigned long long), st), "adjoint counters reset");
+  float4* po = reinterpret_cast<float4*>(wa + LA.path_out);
+  Queue QA, QB;
+  rc = make_queue(kTwoState, nullptr, 0, JA.path_count, o, qa, po, nullptr, nullptr, st, &QA);
+  if (rc == RCV_OK) rc = make_queue(kTape, nullptr, 0, JB.path_count, o, qb, nullptr, &A, nullptr, st, &QB);
+  if (rc == RCV_OK) rc = launch_pair(JA, QA, JB, QB, o, st, false);
+  if (rc) return rc;
+  return launch_reduce(true, po, 0, npix, JA.spp, img_new, img_old, st);
 }
 
 static int backward_volume(const rcv_medium* m, const rcv_sensor* s, const rcv_volpath_options* o, uint32_t seed,

@@ -184,9 +184,9 @@ __device__ __forceinline__ bool tape_append_n(const Queue& Q, TapeCursor& tc, bo
       ok = false;
     }
     if (ok) {
-      Q.tape[slot] = a;
-      if (kWords == 2) Q.tape[slot + 1] = b;
-      if (kWords == 1 && Q.tape_f != nullptr) Q.tape_f[slot] = f;
+      __stcs(Q.tape + slot, a);
+      if (kWords == 2) __stcs(Q.tape + slot + 1, b);
+      if (kWords == 1 && Q.tape_f != nullptr) __stcs(Q.tape_f + slot, f);
     }
   }
   if (n <= rem) {
@@ -212,7 +212,7 @@ __device__ __forceinline__ bool tape_append(const Queue& Q, TapeCursor& tc, bool
 // kTapeEmpty).  Called by the whole warp at exit.
 __device__ __forceinline__ void tape_close(const Queue& Q, const TapeCursor& tc) {
   for (uint32_t i = tc.cur + (threadIdx.x & 31u); i < tc.end; i += 32u)
-    Q.tape[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTapeEmpty));
+    __stcs(Q.tape + i, make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kTapeEmpty)));
 }
 
 // Buffers of the two adjoint launches.
@@ -554,6 +554,18 @@ __device__ __forceinline__ int cost_bucket(uint32_t c) {
 int launch_persistent(int mode, const VolJob& J, const VolJob* jobs, int njobs, int64_t total,
                       const rcv_volpath_options* o, unsigned long long* queue_counter, float4* path_out,
                       const AdjBuffers* adj, uint64_t* counters, cudaStream_t st, bool supergrid);
+// Work queue of a persistent tracer launch (the arguments of
+// launch_persistent); zeroes its hand-out counter on `st`.
+int make_queue(int mode, const VolJob* jobs, int njobs, int64_t total, const rcv_volpath_options* o,
+               unsigned long long* queue_counter, float4* path_out, const AdjBuffers* adj, uint64_t* counters,
+               cudaStream_t st, Queue* out);
+// One persistent launch of two tracers (rcv_pair.cu): the two-state primal
+// over QA and the tape radiance pass over QB, each of a single job (JA, JB:
+// the same medium and environment) or both of job tables (supergrid: some
+// job of the tables has a majorant supergrid).
+int launch_pair(const VolJob& JA, const Queue& QA, const VolJob& JB, const Queue& QB, const rcv_volpath_options* o,
+                cudaStream_t st, bool supergrid);
+void warm_pair_config();
 // Queries the occupancy and SM count the launchers cache, so that later
 // launches (e.g. under stream capture) make no device queries.
 void warm_launch_config();

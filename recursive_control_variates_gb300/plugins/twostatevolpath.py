@@ -45,6 +45,10 @@ class _VolumeIntegratorBase:
             raise ValueError("max_depth must be -1 (infinite) or non-negative")
         # run the adjoint's radiance pass beside the primal render (rcv.render)
         self.overlap_adjoint = bool(props.get("overlap_adjoint", True))
+        # ... in the same persistent launch as a two-state render
+        # (rcv_render_twostates_volume_and_adjoint_radiance) rather than on a
+        # side stream
+        self.pair_adjoint = bool(props.get("pair_adjoint", True))
         # gradient from an event tape of the radiance pass ("tape") or from
         # replayed path segments ("replay"); the same gradient either way
         adjoint = props.get("adjoint", "tape")
@@ -63,6 +67,8 @@ class _VolumeIntegratorBase:
         self._adj_scratch: dict[torch.device, torch.Tensor] = {}
         self._side: dict[torch.device, torch.cuda.Stream] = {}
         self._ticket = None  # (key, done event) of an adjoint radiance pass started ahead
+        self._pending = None  # a prepared radiance pass the next two-state render may run with it
+        self.last_primal_call = None
 
     # ------------------------------------------------------------- helpers
     def options(self, scene=None) -> _lib.VolpathOptions:
@@ -78,6 +84,7 @@ class _VolumeIntegratorBase:
         o.order = self.order
         o.adjoint = self.adjoint
         o.tape_events_per_path = self.tape_events_per_path
+        o.separate_tracers = 0 if self.pair_adjoint else 1
         env = scene.envmap() if scene is not None and hasattr(scene, "envmap") else None
         o.envmap = C.addressof(env.c_struct()) if env is not None else None
         return o
@@ -134,7 +141,10 @@ class _VolumeIntegratorBase:
         scatter checkpoints), which does not depend on the image gradient.
         Returns a function that enqueues it on a side stream, ordered after
         the medium's packing but not after the work enqueued in between (the
-        primal render), or None when there is nothing to overlap.
+        primal render), or None when there is nothing to overlap.  With
+        ``pair_adjoint`` (the default) a ``render_twostates`` of the same
+        medium state, sensor and options called before that function runs
+        the pass in its own launch instead, and the function does nothing.
         ``render_backward`` with the same arguments then only replays."""
         if not self.overlap_adjoint:
             return None
@@ -154,8 +164,14 @@ class _VolumeIntegratorBase:
         if side is None:
             side = self._side[dev] = torch.cuda.Stream(dev)
         counters = self.counters_ptr(dev)
+        pending = {"key": key, "seed": seed, "spp": spp, "ws": ws, "used": False}
+        self._pending = pending if self.pair_adjoint else None
 
         def launch():
+            if self._pending is pending:
+                self._pending = None
+            if pending["used"]:
+                return  # it ran in the launch of the two-state render
             self._drain_ticket(dev)
             side.wait_event(packed)
             with torch.cuda.stream(side), profiling.region("trace_adjoint_radiance", dev):
@@ -365,15 +381,35 @@ class TwoStatePRBVolpathIntegrator(_VolumeIntegratorBase):
         o = self.options(scene)
         H = self._image(sensor, medium.device)
         F = self._image(sensor, medium.device)
+        ws = self.scratch(medium.device, sensor, spp, _lib.MODE_TWOSTATE)
+        # an adjoint radiance pass prepared for this medium state, sensor and
+        # options runs in the same launch
+        pend, self._pending = self._pending, None
+        key = self._adjoint_key(scene, medium, sensor, 0, 0)
+        if pend is not None and (pend["key"][:3] != key[:3] or pend["key"][5:] != key[5:]):
+            pend = None
         with profiling.region("trace_twostate", medium.device):
-            _lib.check(
-                _lib.load().rcv_render_twostates_volume(
-                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, H.data_ptr(), F.data_ptr(),
-                    self.scratch(medium.device, sensor, spp, _lib.MODE_TWOSTATE),
+            if pend is None:
+                fn = "rcv_render_twostates_volume"
+                rc = _lib.load().rcv_render_twostates_volume(
+                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, H.data_ptr(), F.data_ptr(), ws,
                     self.counters_ptr(medium.device), st,
-                ),
-                "rcv_render_twostates_volume",
-            )
+                )
+            else:
+                fn = "rcv_render_twostates_volume_and_adjoint_radiance"
+                self._drain_ticket(medium.device)  # the call overwrites the adjoint scratch
+                rc = _lib.load().rcv_render_twostates_volume_and_adjoint_radiance(
+                    C.byref(m), C.byref(s), C.byref(o), seed & 0xFFFFFFFF, spp, H.data_ptr(), F.data_ptr(), ws,
+                    pend["seed"] & 0xFFFFFFFF, pend["spp"], pend["ws"], self.counters_ptr(medium.device), st,
+                )
+            _lib.check(rc, fn)
+        self.last_primal_call = fn
+        if pend is not None:
+            done = torch.cuda.Event()
+            done.record(torch.cuda.current_stream(medium.device))
+            medium.add_reader(done)
+            self._ticket = (pend["key"], done)
+            pend["used"] = True
         self.primal_image_old, self.primal_image_new = self._post(H), self._post(F)
         return self.primal_image_old, self.primal_image_new
 

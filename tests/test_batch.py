@@ -289,6 +289,39 @@ def test_batch_tape_matches_replay(cuda, per_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_paired_tracers_match_two_streams(cuda, use_graph):
+    """The two-state and tape radiance passes of all jobs in one paired
+    launch (the default) or as two launches on two streams: the same images
+    bit for bit, gradients (first Adam moments) within the reordering of
+    float atomics, over two steps (captured into a graph or not); one
+    kernel launch fewer per step when paired."""
+    pairs = [build_pair(cuda, k) for k in range(len(JOBS))]
+    jobs_p = [p[1] for p in pairs]
+    jobs_s = [j.clone() for j in jobs_p]
+    bp = batch.BatchedCV(jobs_p, batch.LaunchOptions(), use_graph=use_graph)
+    bs = batch.BatchedCV(jobs_s, batch.LaunchOptions(pair_tracers=False), use_graph=use_graph)
+    assert bp.kernels_per_step == bs.kernels_per_step - 1
+    for step in range(2):
+        bp.step()
+        bs.step()
+        torch.cuda.synchronize()
+        for a, b in zip(jobs_p, jobs_s):
+            if step == 0:  # later steps start from parameters that differ by the atomics' rounding
+                assert torch.equal(a.primal_images()[0], b.primal_images()[0])
+                assert torch.equal(a.primal_images()[1], b.primal_images()[1])
+                assert torch.equal(a.image(), b.image())
+            else:
+                assert rel_l2(a.image(), b.image()) <= 1e-3
+            tol = 1e-5 if step == 0 else 1e-3
+            assert rel_l2(a.density_m, b.density_m) <= tol
+            if a.albedo_m is not None:
+                assert rel_l2(a.albedo_m, b.albedo_m) <= tol
+    bp.close()
+    bs.close()
+
+
+@pytest.mark.gpu
 def test_job_alone_and_in_mix_agree(cuda):
     """The same job stepped alone and inside a mix of uneven jobs: first-step
     images bit-identical, later steps within the atomic-reordering tolerance."""
