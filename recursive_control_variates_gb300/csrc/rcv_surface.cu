@@ -180,9 +180,7 @@ static int surf_resident_blocks(int mode) {
 static int launch_surface(int mode, const SurfJob& S, const Queue& Q, const rcv_volpath_options* o,
                           cudaStream_t st) {
   RCV_TRY_CUDA(cudaMemsetAsync(Q.counter, 0, sizeof(unsigned long long), st), "queue reset");
-  int dev = 0, sms = 1;
-  RCV_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
-  RCV_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+  const int sms = tracer_sm_count();
   int per_sm = surf_resident_blocks(mode);
   if (o != nullptr && o->blocks_per_sm > 0 && o->blocks_per_sm < per_sm) per_sm = o->blocks_per_sm;
   int64_t blocks = ((S.path_count + Q.batch - 1) / Q.batch + (kSurfBlock / 32) - 1) / (kSurfBlock / 32);
@@ -235,9 +233,7 @@ static int run_surface(int mode, const SurfJob& S, const rcv_volpath_options* o,
     int rc = launch_surface(kTape, S, Q, o, st);
     if (rc) return rc;
     const int block = 256;
-    int sms = 1, dev = 0;
-    RCV_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
-    RCV_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+    const int sms = tracer_sm_count();
     surface_tape_scatter_kernel<<<(unsigned)sms * 8u, block, 0, st>>>(S, Q.tape, Q.tape_count, Q.tape_cap,
                                                                        Q.path_ltot);
     rc = launched("surface_tape_scatter launch");

@@ -748,6 +748,8 @@ extern "C" int rcv_render_twostates_volume_and_adjoint_radiance(
   if (rc) return rc;
   RCV_REQUIRE(img_old != nullptr && img_new != nullptr, "output images are NULL");
   RCV_REQUIRE(workspace != adjoint_workspace, "the render and the adjoint need separate workspaces");
+  RCV_REQUIRE(o == nullptr || o->separate_tracers == 0 || o->separate_tracers == 1,
+              "separate_tracers must be 0 or 1");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   rc = check_workspace(workspace);
   if (rc == RCV_OK) rc = check_workspace(adjoint_workspace);

@@ -7,12 +7,14 @@ the gradient that the replay call completes from the paired radiance pass
 must equal the one-call adjoint (float atomics in another order: 1e-6
 relative L2) and the oracle (2e-5).  Event counting and the replay adjoint
 take the two launches one after the other inside the same call."""
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
 
 import recursive_control_variates_gb300 as rcv
-from recursive_control_variates_gb300 import scenes
+from recursive_control_variates_gb300 import _lib, scenes
 
 from test_envmap import gpu_env_scene, oracle_env_scene, random_map
 from test_gpu_volume import make_scene, oracle_scene
@@ -115,6 +117,20 @@ def test_pairing_off_and_mismatched_requests(cuda):
     launch()
     on.render_backward(scene, params, g, 0, seed=5, spp=4)
     assert on.last_adjoint_call == "rcv_render_backward_volume"
+
+    # separate_tracers is 0 or 1
+    sensor = scene.sensors()[0]
+    o = on.options(scene)
+    o.separate_tracers = 2
+    m = med.prepare(torch.cuda.current_stream(cuda).cuda_stream)
+    H = torch.empty((24, 24, 3), device=cuda)
+    F = torch.empty_like(H)
+    rc = _lib.load().rcv_render_twostates_volume_and_adjoint_radiance(
+        C.byref(m), C.byref(sensor.c_struct()), C.byref(o), 9, 4, H.data_ptr(), F.data_ptr(),
+        on.scratch(cuda, sensor, 4, _lib.MODE_TWOSTATE), 5, 4, on.adjoint_scratch(cuda, sensor, 4), None,
+        torch.cuda.current_stream(cuda).cuda_stream)
+    assert rc == _lib.RCV_ERR_INVALID
+    assert b"separate_tracers" in _lib.load().rcv_last_error()
 
 
 def test_paired_step_through_the_public_api(cuda):
