@@ -254,6 +254,13 @@ class Job:
         return self.cfg.paths_per_step()
 
 
+def workload_name(cfg, has_albedo: bool) -> str:
+    """The workload string of both arms' JSON lines."""
+    alb = f" + {cfg.grid}^3 RGB albedo" if has_albedo else f", albedo {cfg.albedo}"
+    return (f"{cfg.name}: {cfg.grid}^3 density{alb}, {cfg.res}x{cfg.res}, spp={cfg.spp}, spp_grad={cfg.spp_grad}, "
+            f"max_depth={cfg.max_depth}, cv_ps + path-replay adjoint + Adam")
+
+
 def algorithmic_bytes(cfg, has_albedo: bool, c_two, c_adj, tape: bool = True) -> dict:
     """Algorithmic bytes per launch of the two tracer kernels from the device
     counters (lookups, scatters, gradient events) of one step.
@@ -450,10 +457,7 @@ def run_ours(args, cfg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian-blob medium; no public dataset)",
-        "config": {"workload": f"{cfg.name}: {cfg.grid}^3 density" + (f" + {cfg.grid}^3 RGB albedo" if has_albedo
-                   else f", albedo {cfg.albedo}") + f", {cfg.res}x{cfg.res}, spp={cfg.spp}, spp_grad={cfg.spp_grad}, "
-                   f"max_depth={cfg.max_depth}, cv_ps + path-replay adjoint + Adam",
-                   "paths_per_step": paths, "parallelism": f"replicas x{world}",
+        "config": {"workload": workload_name(cfg, has_albedo), "paths_per_step": paths, "parallelism": f"replicas x{world}",
                    "l2": "flushed between timed steps (512 MB write)",
                    "tracers": ("two-state render and adjoint radiance pass in one persistent launch"
                                if not args.no_pair else "two-state render and adjoint radiance pass on two streams")},
@@ -911,8 +915,8 @@ def run_reference(args, cfg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total * 1e3 / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded Gaussian-blob medium; no public dataset)", "impl": "reference",
-        "config": {"workload": f"{cfg.name} (CPU sample: every {band[2]}th row of {cfg.res})",
-                   "paths_per_step": npaths},
+        "config": {"workload": workload_name(cfg, has_alb), "paths_per_step": npaths,
+                   "sample": f"every {band[2]}th row of {cfg.res} (the CPU step's row sample)"},
         "p50_ms": ts[len(ts) // 2] * 1e3, "p99_ms": ts[-1] * 1e3,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(range(*band))} rows x {cfg.res} px x (spp {cfg.spp} + spp_grad "
