@@ -533,10 +533,15 @@ def surface_form(args, device, dist, world, flush):
     ms = sorted(a.elapsed_time(b) for a, b in ev)
     total = reduce_max(sum(ms) / 1e3, dist, device)
     paths = cfg.paths_per_step()
+    cpu = None
+    if dist_info()[0] == 0 and world == 1 and not args.no_cpu_baseline:
+        # the texture state of the last step on the CPU restatement
+        bsdf = scene.named_shapes()["plane"].bsdf
+        cpu = surface_cpu_baseline(cfg, bsdf.old.texture.data.cpu().numpy(), bsdf.new.texture.data.cpu().numpy())
     return {"workload": f"cfg3: {cfg.res}^2 two-state surface scene (plane + {cfg.tex_res}^2 RGB texture, 3 spheres, "
                         f"area light), spp={cfg.spp}, spp_grad={cfg.spp_grad}, max_depth={cfg.max_depth}, cv_ps",
             "value": paths * world * steps / total, "unit": UNIT, "ms_per_step": total * 1e3 / steps, "steps": steps,
-            "p50_ms": pctl(ms, 0.5), "p99_ms": pctl(ms, 0.99), "paths_per_step": paths}
+            "p50_ms": pctl(ms, 0.5), "p99_ms": pctl(ms, 0.99), "paths_per_step": paths, "cpu_baseline": cpu}
 
 
 def time_phase(args, cfg, device, dist, target, phase, world, flush, majorant_factor=0):
@@ -851,6 +856,35 @@ def cpu_baseline(cfg, job, target_seconds: float = 15.0):
             "sample": f"every {rows[2]}th row ({len(range(*rows))} rows) x {cfg.res} px x (spp {cfg.spp} + spp_grad "
                       f"{cfg.spp_grad}) of {cfg.name} at the job's current state, one CPU gradient step ({n} paths, "
                       f"{dt:.1f} s), C++ restatement built with `{oracle_flags()}`, {threads} threads",
+            "cpu": cpu_model(), "flags": oracle_flags()}
+
+
+def surface_cpu_baseline(cfg, tex_old, tex_new, target_seconds: float = 4.0):
+    """The surface oracle (two-state render + texture adjoint of the same
+    scene) timed on an every-k-th-row sample of the config-3 step."""
+    from oracle import oracle as O
+
+    from recursive_control_variates_gb300 import scenes
+
+    threads = O.default_threads()
+    cam = O.camera_basis(cfg.res, cfg.res, *scenes.SURFACE_CAMERA)
+    sc = O.SurfaceScene(cam, tex_old, tex_new, scenes.surface_spheres(cfg.seed), (0.0, 3.0, 0.0), (0.5, 0.5),
+                        (15.0, 15.0, 15.0), plane_half=2.0, max_depth=cfg.max_depth, rr_depth=cfg.rr_depth)
+    grad = np.random.default_rng(5).normal(0.0, 1.0, (cfg.res, cfg.res, 3)).astype(np.float32)
+
+    def step(seed, rows):
+        O.surface_render_twostates(sc, seed, cfg.spp, threads=threads, rows=rows)
+        O.surface_backward(sc, seed + 1, cfg.spp_grad, grad, threads=threads, rows=rows)
+        return len(range(*rows)) * cfg.res * (cfg.spp + cfg.spp_grad)
+
+    rows = row_sample(cfg.res, step, target_seconds)
+    t0 = time.perf_counter()
+    n = step(3, rows)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"every {rows[2]}th row ({len(range(*rows))} rows) x {cfg.res} px x (spp {cfg.spp} + spp_grad "
+                      f"{cfg.spp_grad}) of {cfg.name}: two-state render and texture adjoint ({n} paths, {dt:.1f} s), "
+                      f"C++ restatement built with `{oracle_flags()}`, {threads} threads",
             "cpu": cpu_model(), "flags": oracle_flags()}
 
 
